@@ -1,0 +1,329 @@
+#!/usr/bin/env python3
+"""Benchmark of the plain proliferation path: cell divisions per second.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--workload large|medium|small]
+    python bench.py --impl reference ...     # the CPU arm (see below)
+
+One step = one complete simulation of the workload (root sweep + every division sweep)
+from inputs already resident in HBM (`value`), and the same through the C ABI with host
+buffers, the upload and the histogram download inside the timed region (`e2e`). The
+default workload is the 1e7-cell configuration: 4096 bins, fluorescence log-uniform on
+[1, 1e6], Poisson(2500) cells per bin, five types (means U[30, 60], sd 0.3 x mean,
+Dirichlet ratios), t_max 336, phi 1; about 3.9e9 divisions per step.
+
+Under torchrun each rank runs its own instance (seed + rank) of the workload on its own
+GPU: weak scaling, no collective on the data path; value = all ranks' divisions / the
+slowest rank's time.
+
+The reference has no CPU implementation of this path (every step of it is a CUDA kernel),
+so `--impl reference` times the CPU restatement of the reference's algorithm (the oracle)
+on all host cores, over a bounded sample of the same workload's initial cells.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "cuda-pro-cell_gb300")
+sys.path.insert(0, PKG)
+
+METRIC = "cell divisions/s"
+UNIT = "divisions/s"
+ALG_BYTES_PER_NODE = 32  # 16-byte cell state written once and read once per tree node
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples (200 ms) while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+        top = max(sm)
+        loaded = [s for s in sm if s >= 0.5 * top] or sm
+        return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def workload(name):
+    import procell.configs as cfg
+    return cfg.by_name(name)
+
+
+def describe(w):
+    return (f"{w.name}: {len(w.bins)} bins, {w.roots} initial cells, {len(w.types)} types, "
+            f"t_max {w.t_max:g}, phi {w.phi:g}")
+
+
+def cpu_sample(w, target_s, nthreads, oracle):
+    """Oracle divisions/s on a prefix of the workload's initial cells sized to ~target_s."""
+    n = w.roots
+    probe = max(1, n // 2048)
+    t = time.perf_counter()
+    r = oracle.simulate(w.bins, w.types, w.t_max, w.phi, seed=w.seed, root_end=probe, nthreads=nthreads)
+    dt = max(time.perf_counter() - t, 1e-3)
+    rate_roots = probe / dt
+    m = int(min(n, max(probe, rate_roots * target_s)))
+    t = time.perf_counter()
+    r = oracle.simulate(w.bins, w.types, w.t_max, w.phi, seed=w.seed, root_end=m, nthreads=nthreads)
+    dt = time.perf_counter() - t
+    return r.stats["divisions"], dt, m
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build()
+    w = workload(args.workload)
+    cores = os.cpu_count() or 1
+    per_step = max(2.0, args.cpu_seconds / 2)
+    for _ in range(args.warmup):
+        cpu_sample(w, per_step / 4, cores, oracle)
+    divs, secs, samples = 0, 0.0, []
+    for _ in range(args.steps):
+        d, s, m = cpu_sample(w, per_step, cores, oracle)
+        divs += d
+        secs += s
+        samples.append(m)
+    value = divs / secs
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded generator, procell/configs.py)",
+        "config": {"workload": describe(w), "sample": "first %d of %d initial cells per step" % (min(samples), w.roots)},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": "oracle (CPU restatement of the reference algorithm) on the first "
+                                   "%d-%d of %d initial cells per step, %d threads"
+                                   % (min(samples), max(samples), w.roots, cores)},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    if rank == 0:
+        import build as pkg_build
+        pkg_build.build()
+    if world > 1:
+        torch.distributed.barrier()
+    from procell import Engine
+
+    w = workload(args.workload)
+    seed = w.seed + rank
+    eng = Engine(local)
+    stream = torch.cuda.current_stream()
+    eng.set_stream(stream.cuda_stream)
+    plan = eng.plan(w.bins, w.types, w.t_max, w.phi, seed)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    for _ in range(args.warmup):
+        plan.run()
+    barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    divisions = roots = sweeps = 0
+    divide_ms = device_ms = 0.0
+    e0.record(stream)
+    for _ in range(args.steps):
+        plan.run()
+        st = plan.stats()
+        divisions += st["divisions"]
+        roots += st["roots"]
+        sweeps += st["sweeps"]
+        divide_ms += st["divide_ms"]
+        device_ms += st["device_ms"]
+    e1.record(stream)
+    barrier()
+    elapsed_ms = e0.elapsed_time(e1)
+
+    # end to end through the C ABI: host inputs, upload, run, histogram download + merge
+    e2e_t = 0.0
+    h2d = d2h = 0
+    e2e_div = 0
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        res = eng.simulate(w.bins, w.types, w.t_max, w.phi, seed)
+        e2e_t += time.perf_counter() - t
+        h2d += res.stats["h2d_bytes"]
+        d2h += res.stats["d2h_bytes"]
+        e2e_div += res.stats["divisions"]
+    clk = clocks.stop()
+    barrier()
+
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([elapsed_ms, e2e_t], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        s = torch.tensor([divisions, e2e_div], dtype=torch.float64, device="cuda")
+        dist.all_reduce(s, op=dist.ReduceOp.SUM)
+        elapsed_ms, e2e_t = float(t[0]), float(t[1])
+        tot_div, tot_e2e_div = float(s[0]), float(s[1])
+    else:
+        tot_div, tot_e2e_div = float(divisions), float(e2e_div)
+    if rank != 0:
+        return 0
+
+    hbm, peak_kind = peaks()
+    # dominant kernel: the division sweep. Algorithmic bytes: each division creates two
+    # tree nodes, each node's 16-byte state written once and read once (32 B per node).
+    alg_bytes = 2 * ALG_BYTES_PER_NODE * divisions
+    launches = max(1, sweeps)
+    achieved = alg_bytes / (divide_ms * 1e-3) / 1e9 if divide_ms > 0 else None
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic_per_division.txt")
+    if os.path.exists(tpath):
+        try:
+            per_div = float(open(tpath).read().split()[0])
+            traffic = per_div * divisions / launches
+        except (ValueError, IndexError):
+            traffic = None
+    cpu = None
+    if not args.no_cpu_baseline and world == 1:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+        oracle.build()
+        cores = os.cpu_count() or 1
+        d, s, m = cpu_sample(w, args.cpu_seconds, cores, oracle)
+        cpu = {"value": d / s, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": "oracle on the first %d of %d initial cells (%.1f s, %d divisions)"
+                         % (m, w.roots, s, d)}
+    line = {
+        "metric": METRIC,
+        "value": tot_div / (elapsed_ms * 1e-3),
+        "unit": UNIT,
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": elapsed_ms / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded generator, procell/configs.py)",
+        "config": {"workload": describe(w), "divisions_per_step": divisions // args.steps,
+                   "nodes_per_step": (roots + 2 * divisions) // args.steps,
+                   "l2": "no flush: each step streams %.0f GB of level buffers, >> 129 MB L2"
+                         % (2 * 16 * divisions / args.steps / 1e9),
+                   "parallelism": f"one independent instance per GPU x{world}"},
+        "e2e": {"value": tot_e2e_div / e2e_t, "unit": UNIT,
+                "h2d_bytes_per_step": h2d // args.steps, "d2h_bytes_per_step": d2h // args.steps},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": (achieved / hbm) if achieved else None, "traffic": traffic,
+                     "peak_source": peak_kind,
+                     "kernel": "k_divide", "launches_per_step": sweeps / args.steps,
+                     "alg_bytes_per_launch": alg_bytes / launches,
+                     "note": "alg bytes = 64 B per division (two 16-B nodes written+read); the "
+                             "kernel stores only daughters that divide again"},
+        "gpu_launches": (sweeps + args.steps * 1),
+        "clocks": clk,
+        "device_ms_per_step": device_ms / args.steps,
+    }
+    if cpu:
+        line["cpu_baseline"] = cpu
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=["small", "medium", "large"], default="large")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        print("warning: --warmup < 3 violates the timing rules", file=sys.stderr)
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

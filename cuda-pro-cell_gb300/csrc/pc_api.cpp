@@ -1,0 +1,767 @@
+// Host side of libprocell: the C ABI of include/procell.h.
+//
+// pc_plan_create restates the host part of the reference's pipeline once per input:
+// the output value set and bin layout of io::load_fluorescences (src/io/parser.cu:68-154),
+// the type table of io::load_cell_types (parser.cu:156-185), and the per-bin "phi cap"
+// that the division test `fluorescence / 2 > threshold` (proliferation.cu:323) implies.
+// pc_plan_run replaces simulation::proliferate's host loop (proliferation.cu:26-215):
+// instead of allocating every tree level at full size and recursing on the device, it
+// runs one root sweep per chunk of initial cells and then one division sweep per
+// generation slice, depth-first over a stack of level buffers whose size is fixed by a
+// memory budget, so the peak footprint is bounded and independent of the tree shape.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/procell.h"
+#include "pc_engine.h"
+
+using namespace pc;
+
+struct LevelBuf {
+  ulonglong2* cells = nullptr;
+  unsigned long long* count = nullptr;
+  unsigned long long* prefix = nullptr;
+  uint32_t* ticket = nullptr;
+  bool busy = false;
+};
+
+struct pc_context {
+  int device = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  int sms = 0, root_bps = 0, div_bps = 0;
+  double opt_budget = 0.0;
+  uint64_t opt_max_slice = 0, opt_max_root_chunk = 0;
+  int opt_grid_blocks = 0;
+  ZigTables zig_host;
+  ZigTables* zig_dev = nullptr;
+  std::vector<LevelBuf> pool;
+  uint64_t pool_cells = 0;   // capacity of each pool buffer (cells)
+  uint32_t pool_segs = 0;    // segments each buffer's count/prefix arrays hold
+  unsigned long long* stats_dev = nullptr;  // [4]
+  uint32_t* error_dev = nullptr;
+  unsigned long long* pinned = nullptr;     // host staging for small reads
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  uint64_t free_at_start = 0;
+};
+
+struct pc_plan {
+  std::vector<double> bin_value;
+  std::vector<uint64_t> bin_start;
+  std::vector<uint32_t> bin_info;
+  std::vector<TypeDev> types;
+  std::vector<uint32_t> sorted_to_file;
+  uint32_t fallback = 0;
+  double t_max = 0.0, phi = 0.0;
+  uint64_t seed = 0;
+  std::vector<double> values;
+  std::vector<int64_t> vidx;  // [nbins][hist_gens]
+  uint32_t gmax = 0, hist_gens = 1, g_store_max = 0;
+  uint64_t roots_total = 0, root_begin = 0, root_end = 0, chunk = 1;
+  float t_hi = 0.f, t_lo = 0.f;
+  int est_ok = 0;
+  TypeDev* types_dev = nullptr;
+  uint32_t* bin_info_dev = nullptr;
+  uint64_t* bin_start_dev = nullptr;
+  uint32_t* root_rec_dev = nullptr;
+  unsigned long long* hist_dev = nullptr;
+  size_t hist_elems = 0;
+  pc_stats stats;
+  uint64_t upload_bytes = 0;
+  bool ran = false;
+};
+
+namespace {
+
+thread_local std::string g_create_error;
+
+int fail(pc_context* ctx, int code, const std::string& msg) {
+  if (ctx) ctx->err = msg;
+  return code;
+}
+
+#define PC_CUDA(ctx, call)                                                                    \
+  do {                                                                                        \
+    cudaError_t e__ = (call);                                                                 \
+    if (e__ != cudaSuccess)                                                                   \
+      return fail((ctx), e__ == cudaErrorMemoryAllocation ? PC_ERR_NOMEM : PC_ERR_CUDA,       \
+                  std::string(#call) + ": " + cudaGetErrorString(e__));                       \
+  } while (0)
+
+// Ziggurat tables for f(x) = exp(-x^2/2), 128 layers (Marsaglia & Tsang 2000): the layer
+// edges follow x_{i+1} = sqrt(-2 ln(v/x_i + f(x_i))) from x_1 = r; the base strip's
+// effective width is v/f(r).
+ZigTables build_zig_tables() {
+  const double r = kZigR, v = kZigV, scale = 2147483648.0;
+  double x[kZigLayers + 1];
+  x[1] = r;
+  for (int i = 1; i + 1 < kZigLayers; ++i) {
+    const double fx = std::exp(-0.5 * x[i] * x[i]);
+    x[i + 1] = std::sqrt(-2.0 * std::log(v / x[i] + fx));
+  }
+  x[kZigLayers] = 0.0;
+  const double base = v / std::exp(-0.5 * r * r);
+  ZigTables t;
+  t.k[0] = (uint32_t)std::floor(r / base * scale);
+  t.w[0] = (float)(base / scale);
+  t.f[0] = 0.0f;
+  for (int i = 1; i < kZigLayers; ++i) {
+    t.k[i] = (uint32_t)std::floor(x[i + 1] / x[i] * scale);
+    t.w[i] = (float)(x[i] / scale);
+    t.f[i] = (float)std::exp(-0.5 * x[i] * x[i]);
+  }
+  t.f[kZigLayers] = 1.0f;
+  return t;
+}
+
+// Smallest (sigma > 0) or largest (sigma < 0) FP32 z with fma(sigma, z, mu) > 0: the
+// truncation tau > 0 of determine_cell_timer (cell.cu:114-118) as an FP32 test on z.
+void truncation_bounds(double mu, double sigma, float& zlo, float& zhi) {
+  const float inf = INFINITY;
+  zlo = -inf;
+  zhi = inf;
+  if (sigma == 0.0) return;
+  auto ok = [&](float z) { return std::fma(sigma, (double)z, mu) > 0.0; };
+  float z = (float)(-mu / sigma);
+  if (std::isnan(z)) z = 0.0f;
+  if (sigma > 0.0) {
+    for (int i = 0; i < 4096 && std::isfinite(z) && ok(z); ++i) z = std::nextafter(z, -inf);
+    for (int i = 0; i < 4096 && !ok(z); ++i) z = std::nextafter(z, inf);
+    zlo = z;
+  } else {
+    for (int i = 0; i < 4096 && std::isfinite(z) && ok(z); ++i) z = std::nextafter(z, inf);
+    for (int i = 0; i < 4096 && !ok(z); ++i) z = std::nextafter(z, -inf);
+    zhi = z;
+  }
+}
+
+bool in_est_range(double x) { return x == 0.0 || (std::fabs(x) >= 1e-30 && std::fabs(x) <= 1e30); }
+
+void free_pool(pc_context* ctx) {
+  for (auto& b : ctx->pool) {
+    cudaFree(b.cells);
+    cudaFree(b.count);
+    cudaFree(b.prefix);
+    cudaFree(b.ticket);
+  }
+  ctx->pool.clear();
+  ctx->pool_cells = 0;
+  ctx->pool_segs = 0;
+}
+
+int acquire(pc_context* ctx, int* idx) {
+  for (size_t i = 0; i < ctx->pool.size(); ++i) {
+    if (!ctx->pool[i].busy) {
+      ctx->pool[i].busy = true;
+      *idx = (int)i;
+      return PC_OK;
+    }
+  }
+  LevelBuf b;
+  PC_CUDA(ctx, cudaMalloc(&b.cells, ctx->pool_cells * sizeof(ulonglong2)));
+  cudaError_t e = cudaMalloc(&b.count, ctx->pool_segs * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMalloc(&b.prefix, (ctx->pool_segs + 1) * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMalloc(&b.ticket, sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMemsetAsync(b.ticket, 0, sizeof(uint32_t), ctx->stream);
+  if (e != cudaSuccess) {
+    cudaFree(b.cells);
+    cudaFree(b.count);
+    cudaFree(b.prefix);
+    cudaFree(b.ticket);
+    return fail(ctx, PC_ERR_NOMEM, std::string("level buffer allocation: ") + cudaGetErrorString(e));
+  }
+  b.busy = true;
+  ctx->pool.push_back(b);
+  *idx = (int)ctx->pool.size() - 1;
+  return PC_OK;
+}
+
+int max_blocks(const pc_context* ctx, int per_sm) {
+  int b = ctx->sms * std::max(1, per_sm);
+  if (ctx->opt_grid_blocks > 0) b = std::min(b, ctx->opt_grid_blocks);
+  return std::max(1, b);
+}
+
+int grid_for(const pc_context* ctx, uint64_t n, int per_sm) {
+  const uint64_t want = (n + (uint64_t)kBlock * 4 - 1) / ((uint64_t)kBlock * 4);
+  return (int)std::max<uint64_t>(1, std::min<uint64_t>(want, (uint64_t)max_blocks(ctx, per_sm)));
+}
+
+uint32_t bits_for(uint64_t n) {  // bits needed for values in [0, n)
+  uint32_t b = 0;
+  while (b < 64 && (n - 1) >> b) ++b;
+  return n <= 1 ? 0 : b;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* pc_version(void) { return "procell-gb300 0.1 (sm_103a)"; }
+
+const char* pc_last_error(const pc_context* ctx) {
+  return ctx ? ctx->err.c_str() : g_create_error.c_str();
+}
+
+int pc_create(pc_context** out, int device) {
+  if (!out) return PC_ERR_INVALID;
+  *out = nullptr;
+  pc_context* ctx = new (std::nothrow) pc_context();
+  if (!ctx) return PC_ERR_NOMEM;
+  auto bail = [&](cudaError_t e, const char* what) {
+    g_create_error = std::string(what) + ": " + cudaGetErrorString(e);
+    delete ctx;
+    return PC_ERR_CUDA;
+  };
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) return bail(e, "cudaSetDevice");
+  ctx->device = device;
+  e = cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, device);
+  if (e != cudaSuccess) return bail(e, "cudaDeviceGetAttribute");
+  e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return bail(e, "cudaStreamCreate");
+  ctx->stream = ctx->own_stream;
+  const int oe = occupancy_blocks_per_sm(&ctx->root_bps, &ctx->div_bps);
+  if (oe != 0) return bail((cudaError_t)oe, "occupancy query (is the sm_103a binary loadable?)");
+  ctx->zig_host = build_zig_tables();
+  if ((e = cudaMalloc(&ctx->zig_dev, sizeof(ZigTables))) != cudaSuccess) return bail(e, "cudaMalloc");
+  if ((e = cudaMemcpy(ctx->zig_dev, &ctx->zig_host, sizeof(ZigTables), cudaMemcpyHostToDevice)) != cudaSuccess)
+    return bail(e, "cudaMemcpy");
+  if ((e = cudaMalloc(&ctx->stats_dev, 4 * sizeof(unsigned long long))) != cudaSuccess) return bail(e, "cudaMalloc");
+  if ((e = cudaMalloc(&ctx->error_dev, sizeof(uint32_t))) != cudaSuccess) return bail(e, "cudaMalloc");
+  if ((e = cudaMallocHost(&ctx->pinned, 64 * sizeof(unsigned long long))) != cudaSuccess)
+    return bail(e, "cudaMallocHost");
+  for (auto& ev : ctx->ev)
+    if ((e = cudaEventCreate(&ev)) != cudaSuccess) return bail(e, "cudaEventCreate");
+  size_t fr = 0, tot = 0;
+  if ((e = cudaMemGetInfo(&fr, &tot)) != cudaSuccess) return bail(e, "cudaMemGetInfo");
+  ctx->free_at_start = fr;
+  *out = ctx;
+  return PC_OK;
+}
+
+void pc_destroy(pc_context* ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  free_pool(ctx);
+  cudaFree(ctx->zig_dev);
+  cudaFree(ctx->stats_dev);
+  cudaFree(ctx->error_dev);
+  cudaFreeHost(ctx->pinned);
+  for (auto& ev : ctx->ev)
+    if (ev) cudaEventDestroy(ev);
+  if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+  delete ctx;
+}
+
+int pc_set_stream(pc_context* ctx, void* stream) {
+  if (!ctx) return PC_ERR_INVALID;
+  ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
+  return PC_OK;
+}
+
+int pc_set_option(pc_context* ctx, const char* name, double value) {
+  if (!ctx || !name) return PC_ERR_INVALID;
+  if (!(value >= 0.0) || !std::isfinite(value)) return fail(ctx, PC_ERR_INVALID, "option value must be >= 0");
+  const std::string n(name);
+  if (n == "memory_budget_bytes") {
+    ctx->opt_budget = value;
+  } else if (n == "max_slice_cells") {
+    ctx->opt_max_slice = (uint64_t)value;
+  } else if (n == "max_root_chunk") {
+    ctx->opt_max_root_chunk = (uint64_t)value;
+  } else if (n == "grid_blocks") {
+    ctx->opt_grid_blocks = (int)value;
+  } else {
+    return fail(ctx, PC_ERR_INVALID, "unknown option " + n);
+  }
+  if (n == "memory_budget_bytes" || n == "grid_blocks") free_pool(ctx);
+  return PC_OK;
+}
+
+int pc_plan_create(pc_context* ctx, const pc_bin* bins, uint64_t n_bins, const pc_cell_type* types,
+                   uint32_t n_types, double t_max, double phi, uint64_t seed, pc_plan** out) {
+  if (!ctx || !out || (n_bins && !bins) || (n_types && !types)) return fail(ctx, PC_ERR_INVALID, "null argument");
+  *out = nullptr;
+  if (!(t_max >= 0.0) || std::isinf(t_max)) return fail(ctx, PC_ERR_INVALID, "t_max must be finite and >= 0");
+  if (!(phi >= 0.0) || std::isinf(phi)) return fail(ctx, PC_ERR_INVALID, "phi must be finite and > 0 (0 = automatic)");
+  if (n_types == 0)
+    return fail(ctx, PC_ERR_INVALID, "ERROR: proportion distribution of cell types does not sum to 1, aborting.");
+  if (n_types > (uint32_t)kMaxTypes)
+    return fail(ctx, PC_ERR_UNSUPPORTED, "at most 64 cell types are supported");
+
+  pc_plan* p = new (std::nothrow) pc_plan();
+  if (!p) return fail(ctx, PC_ERR_NOMEM, "host allocation");
+  std::memset(&p->stats, 0, sizeof(p->stats));
+  auto reject = [&](int code, const std::string& m) {
+    delete p;
+    return fail(ctx, code, m);
+  };
+
+  // Threshold (parser.cu:80-96: with no threshold given, the smallest value with a
+  // nonzero frequency; the `threshold == 0.0 ||` test is the reference's).
+  double threshold = phi;
+  if (threshold == 0.0) {
+    for (uint64_t i = 0; i < n_bins; ++i)
+      if (bins[i].frequency > 0 && (threshold == 0.0 || bins[i].value < threshold)) threshold = bins[i].value;
+  }
+  if (!(threshold > 0.0) || std::isinf(threshold)) return reject(PC_ERR_INVALID, "phi must be finite and > 0");
+  p->phi = threshold;
+  p->t_max = (t_max == 0.0) ? 0.0 : t_max;  // normalise -0
+  p->seed = seed;
+
+  // Bins with a nonzero frequency, in file order; output value set (parser.cu:98-151).
+  std::vector<double> chain;
+  p->bin_start.push_back(0);
+  uint64_t total = 0;
+  for (uint64_t i = 0; i < n_bins; ++i) {
+    if (bins[i].frequency == 0) continue;
+    const double v = bins[i].value;
+    if (!std::isfinite(v)) return reject(PC_ERR_INVALID, "histogram values must be finite");
+    if (bins[i].frequency > 0xFFFFFFFFull - total)
+      return reject(PC_ERR_UNSUPPORTED, "more than 2^32-1 initial cells");
+    total += bins[i].frequency;
+    p->bin_value.push_back(v);
+    p->bin_start.push_back(total);
+    for (double cur = v; cur >= threshold; cur = cur / 2) chain.push_back(cur);
+  }
+  if (p->bin_value.size() >= (1u << 24)) return reject(PC_ERR_UNSUPPORTED, "at most 2^24 nonzero bins");
+  std::sort(chain.begin(), chain.end());
+  chain.erase(std::unique(chain.begin(), chain.end()), chain.end());
+  p->values = chain;
+  p->roots_total = total;
+  p->root_begin = 0;
+  p->root_end = total;
+
+  // Phi cap per bin: a cell of generation g divides only while its fluorescence, the bin
+  // value halved g times, still satisfies `f / 2 > phi` (proliferation.cu:323).
+  std::vector<uint32_t> cap(p->bin_value.size());
+  uint32_t gmax = 0;
+  for (size_t b = 0; b < p->bin_value.size(); ++b) {
+    uint32_t c = 0;
+    for (double f = p->bin_value[b]; f / 2 > threshold && c < 4096; f = f / 2) ++c;
+    cap[b] = c;
+    gmax = std::max(gmax, c);
+  }
+  p->gmax = gmax;
+
+  // Cell types: ratio-sum check, stable sort by ratio descending, cumulative ratios in
+  // that order (parser.cu:46-66,184; cell.cu:81-104).
+  double sum = 0.0;
+  for (uint32_t i = 0; i < n_types; ++i) {
+    if (!std::isfinite(types[i].ratio) || !std::isfinite(types[i].mean) || !std::isfinite(types[i].sd))
+      return reject(PC_ERR_INVALID, "cell type parameters must be finite");
+    sum += types[i].ratio;
+  }
+  if (std::fabs(1.0 - sum) > 1.0 / std::pow(10.0, 8.0))
+    return reject(PC_ERR_INVALID, "ERROR: proportion distribution of cell types does not sum to 1, aborting.");
+  std::vector<uint32_t> order(n_types);
+  for (uint32_t i = 0; i < n_types; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](uint32_t a, uint32_t b) { return types[a].ratio > types[b].ratio; });
+  double acc = 0.0;
+  double max_mu = 0.0, max_sig = 0.0;
+  bool est_ok = in_est_range(p->t_max);
+  for (uint32_t s = 0; s < n_types; ++s) {
+    const pc_cell_type& src = types[order[s]];
+    TypeDev t;
+    std::memset(&t, 0, sizeof(t));
+    acc += src.ratio;
+    t.cum = acc;
+    t.mu = src.mean;
+    t.sigma = src.sd;
+    t.mu_f = (float)src.mean;
+    t.sigma_f = (float)src.sd;
+    t.mode = src.mean < 0.0 ? kModeQuiescent : (src.mean == 0.0 ? kModeZeroMean : kModeNormal);
+    truncation_bounds(src.mean, src.sd, t.zlo, t.zhi);
+    if (t.mode == kModeNormal) {
+      max_mu = std::max(max_mu, std::fabs(src.mean));
+      max_sig = std::max(max_sig, std::fabs(src.sd));
+      est_ok = est_ok && in_est_range(src.mean) && in_est_range(src.sd);
+    }
+    p->types.push_back(t);
+    p->sorted_to_file.push_back(order[s]);
+  }
+  p->fallback = 0;
+  for (uint32_t s = 0; s < n_types; ++s)
+    if (types[order[s]].ratio > 0.0) p->fallback = s;
+  // FP32 estimate band: 8x the worst-case error 2^-21 (t_max + |mu| + 9|sigma|).
+  const double margin = std::ldexp(p->t_max + max_mu + 9.0 * max_sig, -18);
+  p->t_hi = std::nextafter((float)(p->t_max + margin), INFINITY);
+  p->t_lo = std::nextafter((float)(p->t_max - margin), -INFINITY);
+  p->est_ok = est_ok ? 1 : 0;
+
+  // Root chunk and key layout: key = root_local * 2^g + path must fit 64 bits.
+  uint64_t chunk = std::max<uint64_t>(1, total);
+  const uint32_t want_bits = gmax >= 45 ? 20u : 65u - gmax;  // room for gmax - 1 path bits
+  if (want_bits < 64) chunk = std::min<uint64_t>(chunk, 1ull << want_bits);
+  if (ctx->opt_max_root_chunk) chunk = std::min<uint64_t>(chunk, std::max<uint64_t>(1, ctx->opt_max_root_chunk));
+  p->chunk = chunk;
+  const uint32_t rb = bits_for(chunk);
+  p->g_store_max = std::min<uint32_t>(62u, 64u - rb);
+  p->bin_info.resize(p->bin_value.size());
+  for (size_t b = 0; b < p->bin_value.size(); ++b) {
+    uint32_t c = cap[b];
+    uint32_t clamped = 0;
+    if (c > p->g_store_max + 1) {
+      c = p->g_store_max + 1;
+      clamped = 0x200u;
+    }
+    p->bin_info[b] = c | (p->bin_value[b] >= threshold ? 0x100u : 0u) | clamped;
+  }
+  p->hist_gens = std::min(gmax, p->g_store_max + 1) + 1;
+
+  // (bin, generation) -> output value index, following each bin's halving chain.
+  const size_t nb = p->bin_value.size();
+  p->vidx.assign(nb * p->hist_gens, -1);
+  for (size_t b = 0; b < nb; ++b) {
+    double f = p->bin_value[b];
+    for (uint32_t g = 0; g < p->hist_gens; ++g, f = f / 2) {
+      auto it = std::lower_bound(p->values.begin(), p->values.end(), f);
+      if (it != p->values.end() && *it == f) p->vidx[b * p->hist_gens + g] = it - p->values.begin();
+    }
+  }
+
+  // Device copies.
+  PC_CUDA(ctx, cudaSetDevice(ctx->device));
+  const size_t nt = p->types.size();
+  p->hist_elems = (size_t)p->hist_gens * std::max<size_t>(1, nb) * nt;
+  cudaError_t e = cudaMalloc(&p->types_dev, nt * sizeof(TypeDev));
+  if (e == cudaSuccess) e = cudaMalloc(&p->bin_info_dev, std::max<size_t>(1, nb) * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&p->bin_start_dev, (nb + 1) * sizeof(uint64_t));
+  if (e == cudaSuccess) e = cudaMalloc(&p->root_rec_dev, std::max<uint64_t>(1, chunk) * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&p->hist_dev, p->hist_elems * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMemcpyAsync(p->types_dev, p->types.data(), nt * sizeof(TypeDev), cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess && nb)
+    e = cudaMemcpyAsync(p->bin_info_dev, p->bin_info.data(), nb * sizeof(uint32_t), cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(p->bin_start_dev, p->bin_start.data(), (nb + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  p->upload_bytes = nt * sizeof(TypeDev) + nb * sizeof(uint32_t) + (nb + 1) * sizeof(uint64_t);
+  if (e != cudaSuccess) {
+    pc_plan_destroy(p);
+    return fail(ctx, e == cudaErrorMemoryAllocation ? PC_ERR_NOMEM : PC_ERR_CUDA,
+                std::string("plan upload: ") + cudaGetErrorString(e));
+  }
+  *out = p;
+  return PC_OK;
+}
+
+int pc_plan_set_roots(pc_context* ctx, pc_plan* p, uint64_t root_begin, uint64_t root_end) {
+  if (!ctx || !p) return PC_ERR_INVALID;
+  if (root_begin > root_end || root_end > p->roots_total)
+    return fail(ctx, PC_ERR_INVALID, "root range outside [0, number of initial cells]");
+  p->root_begin = root_begin;
+  p->root_end = root_end;
+  return PC_OK;
+}
+
+void pc_plan_destroy(pc_plan* p) {
+  if (!p) return;
+  cudaFree(p->types_dev);
+  cudaFree(p->bin_info_dev);
+  cudaFree(p->bin_start_dev);
+  cudaFree(p->root_rec_dev);
+  cudaFree(p->hist_dev);
+  delete p;
+}
+
+int pc_plan_run(pc_context* ctx, pc_plan* p) {
+  if (!ctx || !p) return PC_ERR_INVALID;
+  PC_CUDA(ctx, cudaSetDevice(ctx->device));
+  cudaStream_t st = ctx->stream;
+  std::memset(&p->stats, 0, sizeof(p->stats));
+  PC_CUDA(ctx, cudaMemsetAsync(p->hist_dev, 0, p->hist_elems * sizeof(unsigned long long), st));
+  PC_CUDA(ctx, cudaMemsetAsync(ctx->stats_dev, 0, 4 * sizeof(unsigned long long), st));
+  PC_CUDA(ctx, cudaMemsetAsync(ctx->error_dev, 0, sizeof(uint32_t), st));
+  const uint64_t nroots = p->root_end - p->root_begin;
+  p->stats.roots = nroots;
+  p->ran = true;
+  if (nroots == 0 || p->bin_value.empty()) {
+    PC_CUDA(ctx, cudaStreamSynchronize(st));
+    return PC_OK;
+  }
+
+  // Level-buffer geometry from the memory budget: the depth-first stack never holds more
+  // than one buffer per generation plus one, so (levels + 2) buffers always fit.
+  const int rmax = max_blocks(ctx, ctx->root_bps), dmax = max_blocks(ctx, ctx->div_bps);
+  const uint32_t segs = (uint32_t)std::max(rmax, dmax) * kWarpsPerBlock;
+  double budget = ctx->opt_budget > 0 ? ctx->opt_budget : 0.5 * (double)ctx->free_at_start;
+  const uint32_t levels = std::min<uint32_t>(p->gmax, 40u) + 2u;
+  // Any size <= budget / levels is safe; a buffer near 64 cells per root usually holds a
+  // whole generation, so most generations run as a single sweep.
+  uint64_t cells = (uint64_t)(budget / levels / sizeof(ulonglong2));
+  cells = std::min<uint64_t>(cells, std::max<uint64_t>(1ull << 24, 64ull * nroots));
+  cells = std::max<uint64_t>(cells, 4ull * segs + 1024);
+  if (ctx->pool_cells != cells || ctx->pool_segs < segs) {
+    PC_CUDA(ctx, cudaStreamSynchronize(st));
+    free_pool(ctx);
+    ctx->pool_cells = cells;
+    ctx->pool_segs = segs;
+  }
+  uint64_t max_slice = (cells - 2ull * segs) / 2;
+  if (ctx->opt_max_slice) max_slice = std::min<uint64_t>(max_slice, std::max<uint64_t>(1, ctx->opt_max_slice));
+  const uint64_t chunk = std::min<uint64_t>(p->chunk, cells - segs);
+
+  RunArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.k0 = (uint32_t)p->seed;
+  a.k1 = (uint32_t)(p->seed >> 32);
+  a.t_max = p->t_max;
+  a.t_hi = p->t_hi;
+  a.t_lo = p->t_lo;
+  a.est_ok = p->est_ok;
+  a.ntypes = (uint32_t)p->types.size();
+  a.nbins = (uint32_t)p->bin_value.size();
+  a.fallback = p->fallback;
+  a.hist_gens = p->hist_gens;
+  a.g_store_max = p->g_store_max;
+  a.types = p->types_dev;
+  a.zig = ctx->zig_dev;
+  a.bin_info = p->bin_info_dev;
+  a.bin_start = p->bin_start_dev;
+  a.root_rec = p->root_rec_dev;
+  a.hist = p->hist_dev;
+  a.stats = ctx->stats_dev;
+  a.error = ctx->error_dev;
+
+  struct Entry {
+    int buf;
+    uint32_t gen, nseg;
+    uint64_t stride, pos, n;
+  };
+  std::vector<Entry> stack;
+  float ms = 0.f;
+  double dev_ms = 0.0, div_ms = 0.0;
+  uint64_t divisions = 0;
+  uint32_t sweeps = 0, max_gen = 0;
+
+  for (uint64_t c0 = p->root_begin; c0 < p->root_end; c0 += chunk) {
+    const uint64_t n = std::min<uint64_t>(chunk, p->root_end - c0);
+    a.root_base = c0;
+    int b0 = -1;
+    int rc = acquire(ctx, &b0);
+    if (rc != PC_OK) return rc;
+    LevelBuf& L = ctx->pool[b0];
+    const int blocks = grid_for(ctx, n, ctx->root_bps);
+    const uint32_t nseg = (uint32_t)blocks * kWarpsPerBlock;
+    LevelOut o{L.cells, L.count, L.prefix, L.ticket, (n + nseg - 1) / nseg};
+    PC_CUDA(ctx, cudaEventRecord(ctx->ev[0], st));
+    PC_CUDA(ctx, (cudaError_t)launch_root_sweep(a, 0, n, o, blocks, st));
+    PC_CUDA(ctx, cudaEventRecord(ctx->ev[1], st));
+    PC_CUDA(ctx, cudaMemcpyAsync(ctx->pinned, L.prefix + nseg, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+    PC_CUDA(ctx, cudaStreamSynchronize(st));
+    PC_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]));
+    dev_ms += ms;
+    const uint64_t n0 = ctx->pinned[0];
+    if (n0 == 0) {
+      L.busy = false;
+      continue;
+    }
+    stack.push_back(Entry{b0, 0u, nseg, o.stride, 0, n0});
+    while (!stack.empty()) {
+      Entry& top = stack.back();
+      const uint64_t len = std::min<uint64_t>(top.n - top.pos, max_slice);
+      int bo = -1;
+      rc = acquire(ctx, &bo);
+      if (rc != PC_OK) return rc;
+      const LevelBuf& In = ctx->pool[top.buf];
+      const LevelBuf& Out = ctx->pool[bo];
+      const int blocks_d = grid_for(ctx, len, ctx->div_bps);
+      const uint32_t oseg = (uint32_t)blocks_d * kWarpsPerBlock;
+      LevelIn li{In.cells, In.prefix, top.nseg, top.stride, top.pos, top.pos + len};
+      LevelOut lo{Out.cells, Out.count, Out.prefix, Out.ticket, 2 * ((len + oseg - 1) / oseg)};
+      const uint32_t gen = top.gen;
+      PC_CUDA(ctx, cudaEventRecord(ctx->ev[2], st));
+      PC_CUDA(ctx, (cudaError_t)launch_divide_sweep(a, li, gen, lo, blocks_d, st));
+      PC_CUDA(ctx, cudaEventRecord(ctx->ev[3], st));
+      PC_CUDA(ctx, cudaMemcpyAsync(ctx->pinned, Out.prefix + oseg, sizeof(unsigned long long),
+                                   cudaMemcpyDeviceToHost, st));
+      divisions += len;
+      ++sweeps;
+      max_gen = std::max(max_gen, gen + 1);
+      top.pos += len;
+      if (top.pos == top.n) {
+        ctx->pool[top.buf].busy = false;  // stream order protects the in-flight read
+        stack.pop_back();
+      }
+      PC_CUDA(ctx, cudaStreamSynchronize(st));
+      PC_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]));
+      dev_ms += ms;
+      div_ms += ms;
+      const uint64_t n_out = ctx->pinned[0];
+      if (n_out > 0 && gen + 1 <= p->g_store_max) {
+        stack.push_back(Entry{bo, gen + 1, oseg, lo.stride, 0, n_out});
+      } else {
+        ctx->pool[bo].busy = false;
+      }
+    }
+  }
+  PC_CUDA(ctx, cudaMemcpyAsync(ctx->pinned, ctx->stats_dev, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+  PC_CUDA(ctx, cudaMemcpyAsync(ctx->pinned + 8, ctx->error_dev, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  PC_CUDA(ctx, cudaStreamSynchronize(st));
+  p->stats.vanished = ctx->pinned[0];
+  p->stats.uncounted = ctx->pinned[1];
+  p->stats.divisions = divisions;
+  p->stats.sweeps = sweeps;
+  p->stats.max_generation = max_gen;
+  p->stats.device_ms = dev_ms;
+  p->stats.divide_ms = div_ms;
+  p->stats.h2d_bytes = p->upload_bytes;
+  p->stats.d2h_bytes = (uint64_t)(sweeps + (p->root_end - p->root_begin + chunk - 1) / chunk) * 8u + 40u;
+  const uint32_t err = (uint32_t)(ctx->pinned[8] & 0xFFFFFFFFu);
+  if (err & 2u) return fail(ctx, PC_ERR_CUDA, "internal: the normal sampler exceeded its rejection budget");
+  if (err & 1u)
+    return fail(ctx, PC_ERR_DEPTH, "a lineage exceeded the deepest generation the key layout holds");
+  return PC_OK;
+}
+
+int pc_plan_stats(pc_context* ctx, const pc_plan* p, pc_stats* out) {
+  if (!ctx || !p || !out) return PC_ERR_INVALID;
+  if (!p->ran) return fail(ctx, PC_ERR_INVALID, "plan has not run");
+  *out = p->stats;
+  return PC_OK;
+}
+
+int pc_plan_raw_counts(pc_context* ctx, pc_plan* p, uint64_t* host_out, uint64_t capacity,
+                       uint64_t* n_elems, uint32_t dims[3]) {
+  if (!ctx || !p) return PC_ERR_INVALID;
+  const uint32_t nb = (uint32_t)p->bin_value.size(), nt = (uint32_t)p->types.size();
+  const uint64_t n = (uint64_t)p->hist_gens * nb * nt;
+  if (n_elems) *n_elems = n;
+  if (dims) {
+    dims[0] = p->hist_gens;
+    dims[1] = nb;
+    dims[2] = nt;
+  }
+  if (!host_out) return PC_OK;
+  if (capacity < n) return fail(ctx, PC_ERR_INVALID, "raw count buffer too small");
+  if (!p->ran) return fail(ctx, PC_ERR_INVALID, "plan has not run");
+  std::vector<unsigned long long> h(n);
+  if (n) {
+    PC_CUDA(ctx, cudaMemcpyAsync(h.data(), p->hist_dev, n * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
+    PC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  }
+  for (uint64_t gb = 0; gb < (uint64_t)p->hist_gens * nb; ++gb)
+    for (uint32_t k = 0; k < nt; ++k) host_out[gb * nt + p->sorted_to_file[k]] = h[gb * nt + k];
+  return PC_OK;
+}
+
+int pc_plan_result(pc_context* ctx, pc_plan* p, pc_histogram* out) {
+  if (!ctx || !p || !out) return PC_ERR_INVALID;
+  std::memset(out, 0, sizeof(*out));
+  if (!p->ran) return fail(ctx, PC_ERR_INVALID, "plan has not run");
+  const uint32_t nb = (uint32_t)p->bin_value.size(), nt = (uint32_t)p->types.size();
+  const uint64_t n = (uint64_t)p->hist_gens * nb * nt;
+  std::vector<unsigned long long> h(n);
+  if (n) {
+    PC_CUDA(ctx, cudaMemcpyAsync(h.data(), p->hist_dev, n * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
+    PC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  }
+  const uint64_t nv = p->values.size();
+  out->n_values = nv;
+  out->n_types = nt;
+  out->values = (double*)std::malloc(std::max<uint64_t>(1, nv) * sizeof(double));
+  out->totals = (uint64_t*)std::calloc(std::max<uint64_t>(1, nv), sizeof(uint64_t));
+  out->per_type = (uint64_t*)std::calloc(std::max<uint64_t>(1, nv * nt), sizeof(uint64_t));
+  if (!out->values || !out->totals || !out->per_type) {
+    pc_histogram_free(out);
+    return fail(ctx, PC_ERR_NOMEM, "host allocation");
+  }
+  if (nv) std::memcpy(out->values, p->values.data(), nv * sizeof(double));
+  uint64_t leaves = 0;
+  for (uint32_t g = 0; g < p->hist_gens; ++g)
+    for (uint32_t b = 0; b < nb; ++b) {
+      const int64_t vi = p->vidx[(uint64_t)b * p->hist_gens + g];
+      for (uint32_t k = 0; k < nt; ++k) {
+        const uint64_t c = h[((uint64_t)g * nb + b) * nt + k];
+        if (!c) continue;
+        if (vi < 0) {
+          pc_histogram_free(out);
+          return fail(ctx, PC_ERR_CUDA, "internal: leaf counted outside the output value set");
+        }
+        out->totals[vi] += c;
+        out->per_type[(uint64_t)vi * nt + p->sorted_to_file[k]] += c;
+        leaves += c;
+      }
+    }
+  out->stats = p->stats;
+  out->stats.leaves = leaves;
+  out->stats.d2h_bytes += n * sizeof(unsigned long long);
+  return PC_OK;
+}
+
+void pc_histogram_free(pc_histogram* h) {
+  if (!h) return;
+  std::free(h->values);
+  std::free(h->totals);
+  std::free(h->per_type);
+  h->values = nullptr;
+  h->totals = nullptr;
+  h->per_type = nullptr;
+  h->n_values = 0;
+}
+
+int pc_simulate(pc_context* ctx, const pc_bin* bins, uint64_t n_bins, const pc_cell_type* types,
+                uint32_t n_types, double t_max, double phi, uint64_t seed, pc_histogram* out) {
+  pc_plan* p = nullptr;
+  int rc = pc_plan_create(ctx, bins, n_bins, types, n_types, t_max, phi, seed, &p);
+  if (rc != PC_OK) return rc;
+  rc = pc_plan_run(ctx, p);
+  if (rc == PC_OK) rc = pc_plan_result(ctx, p, out);
+  pc_plan_destroy(p);
+  return rc;
+}
+
+int pc_debug_philox(pc_context* ctx, const uint32_t* ctr, uint64_t n, const uint32_t key[2], uint32_t* out) {
+  if (!ctx || (n && (!ctr || !out)) || !key) return PC_ERR_INVALID;
+  if (n == 0) return PC_OK;
+  uint32_t *dc = nullptr, *dout = nullptr;
+  PC_CUDA(ctx, cudaMalloc(&dc, n * 16));
+  cudaError_t e = cudaMalloc(&dout, n * 16);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dc, ctr, n * 16, cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess) e = (cudaError_t)launch_debug_philox(dc, n, key[0], key[1], dout, ctx->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out, dout, n * 16, cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  cudaFree(dc);
+  cudaFree(dout);
+  if (e != cudaSuccess) return fail(ctx, PC_ERR_CUDA, std::string("debug philox: ") + cudaGetErrorString(e));
+  return PC_OK;
+}
+
+int pc_debug_normals(pc_context* ctx, uint64_t seed, uint32_t root, uint64_t first_parent, uint64_t count, float* z) {
+  if (!ctx || (count && !z)) return PC_ERR_INVALID;
+  if (count == 0) return PC_OK;
+  float* dz = nullptr;
+  PC_CUDA(ctx, cudaMalloc(&dz, count * sizeof(float)));
+  cudaError_t e = (cudaError_t)launch_debug_normals(ctx->zig_dev, (uint32_t)seed, (uint32_t)(seed >> 32), root,
+                                                    first_parent, count, dz, ctx->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(z, dz, count * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  cudaFree(dz);
+  if (e != cudaSuccess) return fail(ctx, PC_ERR_CUDA, std::string("debug normals: ") + cudaGetErrorString(e));
+  return PC_OK;
+}
+
+int pc_debug_tables(pc_context* ctx, uint32_t* k, uint32_t* w_bits, uint32_t* f_bits) {
+  if (!ctx) return PC_ERR_INVALID;
+  ZigTables t;
+  PC_CUDA(ctx, cudaMemcpy(&t, ctx->zig_dev, sizeof(t), cudaMemcpyDeviceToHost));
+  if (k) std::memcpy(k, t.k, sizeof(t.k));
+  if (w_bits) std::memcpy(w_bits, t.w, sizeof(t.w));
+  if (f_bits) std::memcpy(f_bits, t.f, sizeof(t.f));
+  return PC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,90 @@
+// Internal interface between the host driver (pc_api.cpp) and the sm_103a kernels
+// (pc_kernels.cu). Not part of the public ABI.
+//
+// Data layout in HBM
+// ------------------
+// * A live cell is 16 bytes: {double due; uint64 key}. `due` is the time at which the
+//   cell is due to divide (the reference's t + timer, proliferation.cu:404-410), and
+//   key = root_local * 2^g + path for a cell of generation g, path being its g
+//   left/right choices from the root. Its heap index (the Philox node address) is
+//   2^g + path. Fluorescence is never stored: it is the bin value halved g times.
+// * A level buffer holds the cells of one generation that will divide. It is split into
+//   one segment per warp of the kernel that produced it; segment s holds count[s]
+//   cells at cells + s * stride, and prefix[] (nseg + 1 entries, exclusive) is written
+//   by the producer's last block. Concatenated in segment order the cells are sorted by
+//   key, so every level is sorted by (root, path).
+// * root_rec[r] = bin << 8 | sorted type index for each initial cell of the chunk.
+// * bin_info[b] = phi cap (bits 0-7: a cell of generation g in bin b may divide iff
+//   g < cap) | countable at generation 0 (bit 8: value >= phi) | cap clamped by the key
+//   layout (bit 9).
+// * hist[(g * nbins + b) * ntypes + k] counts the leaves of generation g, bin b, type k.
+#pragma once
+
+#include <stdint.h>
+
+#include "pc_rng.h"
+
+namespace pc {
+
+constexpr int kMaxTypes = 64;
+constexpr int kBlock = 256;
+constexpr int kWarpsPerBlock = kBlock / 32;
+
+enum TypeMode : int32_t { kModeNormal = 0, kModeQuiescent = 1, kModeZeroMean = 2 };
+
+// One cell type, in the descending-ratio order the reference samples in.
+struct TypeDev {
+  double mu, sigma, cum;
+  float mu_f, sigma_f;
+  float zlo, zhi;  // the FP32 z range for which fma(sigma, z, mu) > 0 (the truncation)
+  int32_t mode;
+  int32_t pad;
+};
+
+struct RunArgs {
+  uint32_t k0, k1;           // seed
+  double t_max;
+  float t_hi, t_lo;          // FP32 band around t_max for the estimate
+  int32_t est_ok;            // FP32 estimate allowed (inputs in range)
+  uint32_t ntypes, nbins, fallback;
+  uint32_t hist_gens;
+  uint32_t g_store_max;      // deepest generation a stored key can hold
+  uint64_t root_base;        // global index of chunk-local root 0
+  const TypeDev* types;      // [ntypes]
+  const ZigTables* zig;
+  const uint32_t* bin_info;  // [nbins]
+  const uint64_t* bin_start; // [nbins + 1] global root offsets
+  uint32_t* root_rec;        // [chunk]
+  unsigned long long* hist;  // [hist_gens][nbins][ntypes]
+  unsigned long long* stats; // [0] vanished, [1] uncounted, [2] max generation
+  uint32_t* error;           // bit 0: depth overflow, bit 1: sampler round budget exhausted
+};
+
+struct LevelIn {
+  const ulonglong2* cells;
+  const unsigned long long* prefix;  // nseg + 1
+  uint32_t nseg;
+  uint64_t stride;
+  uint64_t lo, hi;  // virtual range of this launch
+};
+
+struct LevelOut {
+  ulonglong2* cells;
+  unsigned long long* count;   // [nseg]
+  unsigned long long* prefix;  // [nseg + 1]
+  uint32_t* ticket;
+  uint64_t stride;
+};
+
+// Launchers (pc_kernels.cu). All return the cudaError_t of the launch as int.
+int launch_root_sweep(const RunArgs& a, uint64_t root_lo, uint64_t root_hi, const LevelOut& out,
+                      int blocks, void* stream);
+int launch_divide_sweep(const RunArgs& a, const LevelIn& in, uint32_t gen, const LevelOut& out,
+                        int blocks, void* stream);
+int launch_debug_philox(const uint32_t* ctr, uint64_t n, uint32_t k0, uint32_t k1, uint32_t* out,
+                        void* stream);
+int launch_debug_normals(const ZigTables* zig, uint32_t k0, uint32_t k1, uint32_t root,
+                         uint64_t first_parent, uint64_t count, float* z, void* stream);
+int occupancy_blocks_per_sm(int* root_blocks, int* divide_blocks);
+
+}  // namespace pc

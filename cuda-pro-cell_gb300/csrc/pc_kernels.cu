@@ -1,0 +1,434 @@
+// sm_103a kernels of the proliferation path.
+//
+// The reference runs one thread per cell and recurses one tree level per CUDA Dynamic
+// Parallelism child grid (device::proliferate, src/simulation/proliferation.cu:289-402),
+// reading 40-byte cells from full-size level buffers that are mostly empty. Here each
+// generation is one data-parallel sweep over a dense, sorted buffer of the cells that
+// will divide:
+//
+//   root sweep     one lane per initial cell: type, first division time and initial age
+//                  (create_cell with type -1, src/simulation/cell.cu:25-79), then either
+//                  a gen-0 leaf, a vanished root, or a dividing cell written to level 0.
+//   division sweep one lane per dividing cell of generation g: one Philox block gives both
+//                  daughters' first-attempt normals, the daughters' due times are
+//                  computed, leaves (due > t_max, proliferation.cu:404-410) are counted
+//                  straight into the (generation, bin, type) histogram and never stored,
+//                  and daughters that will divide again are written to level g+1.
+//
+// Memory traffic per division is one 16-byte read plus one 16-byte write per daughter
+// that divides again; leaves and vanished cells cost no HBM bytes. Each warp owns a
+// contiguous slice of the input and its own output segment, so compaction needs only
+// warp ballots, and the output stays sorted by (root, path) with no atomics.
+#include <cuda_runtime.h>
+
+#include "pc_engine.h"
+
+namespace pc {
+
+namespace {
+
+constexpr uint32_t kFull = 0xFFFFFFFFu;
+
+struct Smem {
+  ZigTables zig;
+  TypeDev types[kMaxTypes];
+};
+
+__device__ __forceinline__ void stage(Smem& s, const RunArgs& a) {
+  const uint32_t* zs = reinterpret_cast<const uint32_t*>(a.zig);
+  uint32_t* zd = reinterpret_cast<uint32_t*>(&s.zig);
+  for (uint32_t i = threadIdx.x; i < sizeof(ZigTables) / 4; i += blockDim.x) zd[i] = __ldg(zs + i);
+  const uint32_t* ts = reinterpret_cast<const uint32_t*>(a.types);
+  uint32_t* td = reinterpret_cast<uint32_t*>(s.types);
+  const uint32_t nt = a.ntypes * (uint32_t)(sizeof(TypeDev) / 4);
+  for (uint32_t i = threadIdx.x; i < nt; i += blockDim.x) td[i] = __ldg(ts + i);
+}
+
+// Rejection path of one daughter's normal: the generic ziggurat plus the truncation
+// tau > 0 (src/simulation/cell.cu:114-118), drawing from the node's private stream.
+// A round budget far beyond anything a correct table produces (the acceptance rate of a
+// round is above 1/2) turns a would-be endless loop into error bit 1.
+constexpr uint32_t kRoundBudget = 1u << 16;
+
+__device__ __noinline__ float slow_z(uint32_t j, uint32_t layer, uint64_t node, uint32_t root,
+                                     uint32_t k0, uint32_t k1, const TypeDev& T,
+                                     const ZigTables& Z, uint32_t* error) {
+  ChildStream cs = child_stream(node, root, k0, k1);
+  uint32_t budget = kRoundBudget;
+  while (budget > 0u) {
+    const float z = zig_normal(j, layer, cs, Z, budget);
+    if (budget == 0u) break;
+    if (z >= T.zlo && z <= T.zhi) return z;
+    j = cs.next();
+    layer = cs.next() & 127u;
+    --budget;
+  }
+  atomicOr(error, 2u);
+  return 0.0f;
+}
+
+// First-attempt fast path (about 98.8% of draws): one strip test, one FP32 multiply.
+__device__ __forceinline__ float draw_z(uint32_t j, uint32_t layer, uint64_t node, uint32_t root,
+                                        uint32_t k0, uint32_t k1, const TypeDev& T,
+                                        const ZigTables& Z, uint32_t* error) {
+  const uint32_t mag = j & 0x7FFFFFFFu;
+  if (mag < Z.k[layer]) {
+    const float x = __fmul_rn((float)mag, Z.w[layer]);
+    const float z = (j >> 31) ? -x : x;
+    if (z >= T.zlo && z <= T.zhi) return z;
+  }
+  return slow_z(j, layer, node, root, k0, k1, T, Z, error);
+}
+
+enum Fate : int { kNone = 0, kLeaf = 1, kEmit = 2, kVanish = 3 };
+
+// Fate of one daughter born at `birth` with normal z. The FP32 estimate decides leaves
+// and clear non-leaves without FP64 work; the band around t_max (8x the worst-case FP32
+// error) and every daughter that is stored use the exact FP64 due time
+// birth + fma(sigma, z, mu), the reference's t + timer.
+__device__ __forceinline__ int fate(double birth, float birth_f, float z, const TypeDev& T,
+                                    const RunArgs& a, bool can_divide, double& due) {
+  if (a.est_ok) {
+    const float est = __fadd_rn(birth_f, __fadd_rn(T.mu_f, __fmul_rn(T.sigma_f, z)));
+    if (est > a.t_hi) return kLeaf;
+    if (est < a.t_lo && !can_divide) return kVanish;
+    if (est < a.t_lo) {
+      due = birth + fma(T.sigma, (double)z, T.mu);
+      return kEmit;
+    }
+  }
+  due = birth + fma(T.sigma, (double)z, T.mu);
+  if (due > a.t_max) return kLeaf;
+  return can_divide ? kEmit : kVanish;
+}
+
+// Warp-aggregated leaf counting: lanes holding leaves of the same (bin, type) add once.
+__device__ __forceinline__ void count_leaves(unsigned long long* hist_g, uint32_t cls,
+                                             uint32_t nleaf, uint32_t lane) {
+  const uint32_t any = __ballot_sync(kFull, nleaf != 0u);
+  if (any == 0u) return;
+  const uint32_t key = nleaf ? cls : 0xFFFFFFFFu;
+  const uint32_t grp = __match_any_sync(kFull, key);
+  const uint32_t b0 = __ballot_sync(kFull, (nleaf & 1u) != 0u);
+  const uint32_t b1 = __ballot_sync(kFull, (nleaf & 2u) != 0u);
+  if (nleaf != 0u && (uint32_t)(__ffs(grp) - 1) == lane) {
+    const unsigned long long c = (unsigned long long)(__popc(grp & b0) + 2 * __popc(grp & b1));
+    atomicAdd(hist_g + cls, c);
+  }
+}
+
+__device__ __forceinline__ unsigned long long warp_sum(unsigned long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+  return v;
+}
+
+// The last block to finish turns the per-warp output counts into the exclusive prefix
+// the next sweep reads (the threadfence/ticket pattern; no block waits on another).
+__device__ void finish_level(const LevelOut& out, uint32_t nseg) {
+  __shared__ int s_last;
+  __shared__ unsigned long long s_sum[kBlock];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    s_last = (atomicAdd(out.ticket, 1u) == gridDim.x - 1u) ? 1 : 0;
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  const uint32_t per = (nseg + kBlock - 1) / kBlock;
+  const uint32_t b = min(nseg, threadIdx.x * per), e = min(nseg, b + per);
+  unsigned long long acc = 0;
+  for (uint32_t i = b; i < e; ++i) acc += __ldcg(out.count + i);
+  s_sum[threadIdx.x] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long run = 0;
+    for (int i = 0; i < kBlock; ++i) {
+      const unsigned long long t = s_sum[i];
+      s_sum[i] = run;
+      run += t;
+    }
+    out.prefix[nseg] = run;
+    *out.ticket = 0u;
+  }
+  __syncthreads();
+  unsigned long long run = s_sum[threadIdx.x];
+  for (uint32_t i = b; i < e; ++i) {
+    out.prefix[i] = run;
+    run += __ldcg(out.count + i);
+  }
+}
+
+__device__ __forceinline__ uint32_t last_le(const unsigned long long* prefix, uint32_t n,
+                                            unsigned long long v) {
+  // largest s in [0, n-1] with prefix[s] <= v (prefix[0] == 0)
+  uint32_t lo = 0, hi = n - 1u;
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi + 1u) >> 1;
+    if (__ldg(prefix + mid) <= v)
+      lo = mid;
+    else
+      hi = mid - 1u;
+  }
+  return lo;
+}
+
+// ------------------------------------------------------------------ root sweep ------
+__global__ void __launch_bounds__(kBlock) k_roots(const RunArgs a, const uint64_t lo,
+                                                  const uint64_t hi, const LevelOut out) {
+  __shared__ Smem s;
+  stage(s, a);
+  __syncthreads();
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t wg = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
+  const uint32_t nw = gridDim.x * kWarpsPerBlock;
+  const uint64_t len = hi - lo;
+  const uint64_t ra = lo + len * wg / nw, rb = lo + len * (wg + 1u) / nw;
+  ulonglong2* ob = out.cells + (uint64_t)wg * out.stride;
+  uint64_t out_n = 0;
+  unsigned long long uncounted = 0, vanished = 0;
+  // bin of the warp's first root: largest b with bin_start[b] <= global root
+  uint32_t bin = 0;
+  {
+    const uint64_t g0 = a.root_base + ra;
+    uint32_t l = 0, h = a.nbins - 1u;
+    while (l < h) {
+      const uint32_t m = (l + h + 1u) >> 1;
+      if (__ldg(a.bin_start + m) <= g0)
+        l = m;
+      else
+        h = m - 1u;
+    }
+    bin = l;
+  }
+  uint64_t bin_hi = __ldg(a.bin_start + bin + 1u);
+  for (uint64_t v0 = ra; v0 < rb; v0 += 32u) {
+    const uint64_t rl = v0 + lane;
+    const bool act = rl < rb;
+    int f = kNone;
+    double d0 = 0.0;
+    uint32_t nleaf = 0, cls = 0;
+    if (act) {
+      const uint64_t rg = a.root_base + rl;
+      while (rg >= bin_hi) {
+        ++bin;
+        bin_hi = __ldg(a.bin_start + bin + 1u);
+      }
+      const uint32_t root = (uint32_t)rg;
+      const u32x4 R = philox(u32x4{0u, 0u, root, kPurposeRoot}, a.k0, a.k1);
+      const double u_type = unit53_closed_open(R.x, R.y);
+      const double u_age = unit53_open_closed(R.z, R.w);
+      uint32_t ty = a.fallback;
+      for (uint32_t i = 0; i < a.ntypes; ++i) {
+        if (u_type < s.types[i].cum) {
+          ty = i;
+          break;
+        }
+      }
+      a.root_rec[rl] = (bin << 8) | ty;
+      const TypeDev& T = s.types[ty];
+      const uint32_t info = __ldg(a.bin_info + bin);
+      bool leaf;
+      if (T.mode == kModeQuiescent) {
+        leaf = true;  // timer -1: out of time at once (cell.cu:69-75)
+      } else {
+        double tau = 0.0;
+        if (T.mode == kModeNormal) {
+          const u32x4 P = philox(u32x4{0u, 0u, root, kPurposePair}, a.k0, a.k1);
+          const float z = draw_z(P.y, (P.z >> 8) & 127u, 1ull, root, a.k0, a.k1, T, s.zig, a.error);
+          tau = fma(T.sigma, (double)z, T.mu);
+        }
+        d0 = tau * u_age + tau;  // t = tau * U (cell.cu:124-143), due = t + timer
+        leaf = d0 > a.t_max;
+      }
+      if (leaf) {
+        if (info & 0x100u) {
+          nleaf = 1u;
+          cls = bin * a.ntypes + ty;
+        } else {
+          ++uncounted;
+        }
+      } else if ((info & 0xFFu) > 0u) {
+        f = kEmit;
+      } else {
+        ++vanished;
+      }
+    }
+    count_leaves(a.hist, cls, nleaf, lane);
+    const uint32_t em = __ballot_sync(kFull, f == kEmit);
+    if (f == kEmit) {
+      const uint32_t pos = __popc(em & ((1u << lane) - 1u));
+      ob[out_n + pos] = make_ulonglong2((unsigned long long)__double_as_longlong(d0), rl);
+    }
+    out_n += __popc(em);
+  }
+  vanished = warp_sum(vanished);
+  uncounted = warp_sum(uncounted);
+  if (lane == 0) {
+    out.count[wg] = out_n;
+    if (vanished) atomicAdd(a.stats + 0, vanished);
+    if (uncounted) atomicAdd(a.stats + 1, uncounted);
+    __threadfence();
+  }
+  finish_level(out, nw);
+}
+
+// -------------------------------------------------------------- division sweep ------
+__global__ void __launch_bounds__(kBlock) k_divide(const RunArgs a, const LevelIn in,
+                                                   const uint32_t g, const LevelOut out) {
+  __shared__ Smem s;
+  stage(s, a);
+  __syncthreads();
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t wg = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
+  const uint32_t nw = gridDim.x * kWarpsPerBlock;
+  const uint64_t len = in.hi - in.lo;
+  const uint64_t va = in.lo + len * wg / nw, vb = in.lo + len * (wg + 1u) / nw;
+  ulonglong2* ob = out.cells + (uint64_t)wg * out.stride;
+  uint64_t out_n = 0;
+  unsigned long long vanished = 0;
+  uint32_t depth_error = 0;
+  const uint32_t g1 = g + 1u;
+  const uint64_t gmask = (1ull << g) - 1ull;
+  unsigned long long* hist_g1 = a.hist + (uint64_t)g1 * a.nbins * a.ntypes;
+  uint32_t seg = 0;
+  uint64_t seg_lo = 0, seg_hi = 0;
+  if (va < vb) {
+    seg = last_le(in.prefix, in.nseg, va);
+    seg_lo = __ldg(in.prefix + seg);
+    seg_hi = __ldg(in.prefix + seg + 1u);
+  }
+  for (uint64_t v0 = va; v0 < vb; v0 += 32u) {
+    const uint64_t v = v0 + lane;
+    const bool act = v < vb;
+    int f0 = kNone, f1 = kNone;
+    double due0 = 0.0, due1 = 0.0;
+    uint64_t key = 0;
+    uint32_t nleaf = 0, cls = 0;
+    if (act) {
+      while (v >= seg_hi) {
+        ++seg;
+        seg_lo = seg_hi;
+        seg_hi = __ldg(in.prefix + seg + 1u);
+      }
+      const ulonglong2 c = __ldg(in.cells + (uint64_t)seg * in.stride + (v - seg_lo));
+      const double d = __longlong_as_double((long long)c.x);
+      key = c.y;
+      const uint64_t rl = key >> g;
+      const uint64_t node = (1ull << g) | (key & gmask);
+      const uint32_t root = (uint32_t)(a.root_base + rl);
+      const uint32_t rec = __ldg(a.root_rec + rl);
+      const uint32_t bin = rec >> 8, ty = rec & 0xFFu;
+      const uint32_t info = __ldg(a.bin_info + bin);
+      const uint32_t cap = info & 0xFFu;
+      const bool can_divide = g1 < cap;
+      const TypeDev& T = s.types[ty];
+      if (T.mode == kModeZeroMean) {
+        // tau == 0: the daughters are due at the parent's own due time
+        due0 = d;
+        due1 = d;
+        f0 = f1 = (d > a.t_max) ? kLeaf : (can_divide ? kEmit : kVanish);
+      } else {
+        const u32x4 P = philox(u32x4{(uint32_t)node, (uint32_t)(node >> 32), root, kPurposePair},
+                               a.k0, a.k1);
+        const float z0 = draw_z(P.x, P.z & 127u, 2ull * node, root, a.k0, a.k1, T, s.zig, a.error);
+        const float z1 =
+            draw_z(P.y, (P.z >> 8) & 127u, 2ull * node + 1ull, root, a.k0, a.k1, T, s.zig, a.error);
+        const float df = __double2float_rz(d);
+        f0 = fate(d, df, z0, T, a, can_divide, due0);
+        f1 = fate(d, df, z1, T, a, can_divide, due1);
+      }
+      if ((info & 0x200u) && g1 == cap && (f0 == kVanish || f1 == kVanish)) depth_error = 1u;
+      nleaf = (f0 == kLeaf ? 1u : 0u) + (f1 == kLeaf ? 1u : 0u);
+      vanished += (f0 == kVanish ? 1u : 0u) + (f1 == kVanish ? 1u : 0u);
+      cls = bin * a.ntypes + ty;
+    }
+    count_leaves(hist_g1, cls, nleaf, lane);
+    const uint32_t e0 = __ballot_sync(kFull, f0 == kEmit);
+    const uint32_t e1 = __ballot_sync(kFull, f1 == kEmit);
+    const uint32_t lt = (1u << lane) - 1u;
+    ulonglong2* dst = ob + out_n + __popc(e0 & lt) + __popc(e1 & lt);
+    if (f0 == kEmit) dst[0] = make_ulonglong2((unsigned long long)__double_as_longlong(due0), 2ull * key);
+    if (f1 == kEmit)
+      dst[f0 == kEmit ? 1 : 0] =
+          make_ulonglong2((unsigned long long)__double_as_longlong(due1), 2ull * key + 1ull);
+    out_n += __popc(e0) + __popc(e1);
+  }
+  vanished = warp_sum(vanished);
+  depth_error = __reduce_or_sync(kFull, depth_error);
+  if (lane == 0) {
+    out.count[wg] = out_n;
+    if (vanished) atomicAdd(a.stats + 0, vanished);
+    if (depth_error) atomicOr(a.error, 1u);
+    __threadfence();
+  }
+  finish_level(out, nw);
+}
+
+// ------------------------------------------------------------------ diagnostics -----
+__global__ void k_debug_philox(const uint32_t* ctr, uint64_t n, uint32_t k0, uint32_t k1,
+                               uint32_t* out) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const u32x4 r = philox(u32x4{ctr[4 * i], ctr[4 * i + 1], ctr[4 * i + 2], ctr[4 * i + 3]}, k0, k1);
+  out[4 * i] = r.x;
+  out[4 * i + 1] = r.y;
+  out[4 * i + 2] = r.z;
+  out[4 * i + 3] = r.w;
+}
+
+__global__ void k_debug_normals(const ZigTables* zig, uint32_t k0, uint32_t k1, uint32_t root,
+                                uint64_t first_parent, uint64_t count, float* z) {
+  __shared__ ZigTables Z;
+  for (uint32_t i = threadIdx.x; i < sizeof(ZigTables) / 4; i += blockDim.x)
+    reinterpret_cast<uint32_t*>(&Z)[i] = reinterpret_cast<const uint32_t*>(zig)[i];
+  __syncthreads();
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const uint64_t parent = first_parent + i / 2;
+  const uint32_t c = (uint32_t)(i & 1u);
+  const u32x4 P = philox(u32x4{(uint32_t)parent, (uint32_t)(parent >> 32), root, kPurposePair}, k0, k1);
+  ChildStream cs = child_stream(2ull * parent + c, root, k0, k1);
+  uint32_t budget = kRoundBudget;
+  z[i] = zig_normal(c ? P.y : P.x, (P.z >> (8u * c)) & 127u, cs, Z, budget);
+}
+
+}  // namespace
+
+int launch_root_sweep(const RunArgs& a, uint64_t root_lo, uint64_t root_hi, const LevelOut& out,
+                      int blocks, void* stream) {
+  k_roots<<<blocks, kBlock, 0, (cudaStream_t)stream>>>(a, root_lo, root_hi, out);
+  return (int)cudaGetLastError();
+}
+
+int launch_divide_sweep(const RunArgs& a, const LevelIn& in, uint32_t gen, const LevelOut& out,
+                        int blocks, void* stream) {
+  k_divide<<<blocks, kBlock, 0, (cudaStream_t)stream>>>(a, in, gen, out);
+  return (int)cudaGetLastError();
+}
+
+int launch_debug_philox(const uint32_t* ctr, uint64_t n, uint32_t k0, uint32_t k1, uint32_t* out,
+                        void* stream) {
+  if (n == 0) return 0;
+  const unsigned blocks = (unsigned)((n + 255) / 256);
+  k_debug_philox<<<blocks, 256, 0, (cudaStream_t)stream>>>(ctr, n, k0, k1, out);
+  return (int)cudaGetLastError();
+}
+
+int launch_debug_normals(const ZigTables* zig, uint32_t k0, uint32_t k1, uint32_t root,
+                         uint64_t first_parent, uint64_t count, float* z, void* stream) {
+  if (count == 0) return 0;
+  const unsigned blocks = (unsigned)((count + 255) / 256);
+  k_debug_normals<<<blocks, 256, 0, (cudaStream_t)stream>>>(zig, k0, k1, root, first_parent, count, z);
+  return (int)cudaGetLastError();
+}
+
+int occupancy_blocks_per_sm(int* root_blocks, int* divide_blocks) {
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(root_blocks, k_roots, kBlock, 0);
+  if (e != cudaSuccess) return (int)e;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(divide_blocks, k_divide, kBlock, 0);
+  return (int)e;
+}
+
+}  // namespace pc

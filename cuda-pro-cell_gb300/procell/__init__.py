@@ -1,0 +1,168 @@
+"""Python front end of the GB300 proliferation engine (libprocell.so).
+
+    from procell import Engine
+    eng = Engine()                       # a pc_context on cuda:0
+    h = eng.simulate(bins, types, t_max=168, phi=None, seed=7)
+    h.values, h.totals, h.per_type, h.stats
+
+bins are (value, frequency) rows and types (ratio, mean, sd) rows, both in file order, as
+in the reference's histogram and cell-type files.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib
+from ._lib import ProcellError
+
+__all__ = ["Engine", "Result", "ProcellError", "format_histogram"]
+
+
+@dataclass
+class Result:
+    values: np.ndarray      # float64 [V] ascending output value set
+    totals: np.ndarray      # uint64 [V]
+    per_type: np.ndarray    # uint64 [V, ntypes] (file order)
+    stats: dict = field(default_factory=dict)
+
+
+class Plan:
+    """A prepared input resident in HBM (pc_plan). run() may be repeated."""
+
+    def __init__(self, engine: "Engine", bins, types, t_max, phi=None, seed=0):
+        self.engine = engine
+        L = engine.L
+        self._bins = _lib.bins_array(bins)
+        self._types = _lib.types_array(types)
+        h = ctypes.c_void_p()
+        rc = L.pc_plan_create(engine.ctx, self._bins, len(bins), self._types, len(types),
+                              float(t_max), 0.0 if phi is None else float(phi), int(seed),
+                              ctypes.byref(h))
+        engine._check(rc)
+        self.handle = h
+
+    def set_roots(self, begin, end):
+        self.engine._check(self.engine.L.pc_plan_set_roots(self.engine.ctx, self.handle,
+                                                           int(begin), int(end)))
+
+    def run(self):
+        self.engine._check(self.engine.L.pc_plan_run(self.engine.ctx, self.handle))
+
+    def stats(self) -> dict:
+        st = _lib.Stats()
+        self.engine._check(self.engine.L.pc_plan_stats(self.engine.ctx, self.handle, ctypes.byref(st)))
+        return {k: getattr(st, k) for k, _ in _lib.Stats._fields_}
+
+    def result(self) -> Result:
+        h = _lib.Histogram()
+        self.engine._check(self.engine.L.pc_plan_result(self.engine.ctx, self.handle, ctypes.byref(h)))
+        try:
+            return Result(*_lib.histogram_to_numpy(h))
+        finally:
+            self.engine.L.pc_histogram_free(ctypes.byref(h))
+
+    def raw_counts(self) -> np.ndarray:
+        L, n = self.engine.L, ctypes.c_uint64()
+        dims = (ctypes.c_uint32 * 3)()
+        self.engine._check(L.pc_plan_raw_counts(self.engine.ctx, self.handle, None, 0,
+                                                ctypes.byref(n), dims))
+        out = np.zeros(int(n.value), np.uint64)
+        self.engine._check(L.pc_plan_raw_counts(
+            self.engine.ctx, self.handle, out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
+            int(n.value), ctypes.byref(n), dims))
+        return out.reshape(dims[0], dims[1], dims[2])
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.engine.L.pc_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Engine:
+    def __init__(self, device: int = 0):
+        self.L = _lib.load()
+        ctx = ctypes.c_void_p()
+        rc = self.L.pc_create(ctypes.byref(ctx), int(device))
+        if rc != 0:
+            raise ProcellError(rc, self.L.pc_last_error(None).decode())
+        self.ctx = ctx
+
+    def _check(self, rc):
+        if rc != 0:
+            raise ProcellError(rc, self.L.pc_last_error(self.ctx).decode())
+
+    def set_stream(self, stream_handle: int):
+        """Run on an existing cudaStream_t (e.g. torch.cuda.current_stream().cuda_stream)."""
+        self._check(self.L.pc_set_stream(self.ctx, ctypes.c_void_p(int(stream_handle))))
+
+    def set_option(self, name: str, value: float):
+        self._check(self.L.pc_set_option(self.ctx, name.encode(), float(value)))
+
+    def plan(self, bins, types, t_max, phi=None, seed=0) -> Plan:
+        return Plan(self, bins, types, t_max, phi, seed)
+
+    def simulate(self, bins, types, t_max, phi=None, seed=0, root_begin=None, root_end=None) -> Result:
+        p = self.plan(bins, types, t_max, phi, seed)
+        try:
+            if root_begin is not None or root_end is not None:
+                total = sum(int(f) for _, f in bins)
+                p.set_roots(root_begin or 0, total if root_end is None else root_end)
+            p.run()
+            return p.result()
+        finally:
+            p.close()
+
+    def philox(self, ctrs: np.ndarray, key) -> np.ndarray:
+        c = np.ascontiguousarray(ctrs, dtype=np.uint32).reshape(-1, 4)
+        out = np.zeros_like(c)
+        k = (ctypes.c_uint32 * 2)(*key)
+        self._check(self.L.pc_debug_philox(self.ctx, c.ctypes.data_as(_lib.U32P), c.shape[0], k,
+                                           out.ctypes.data_as(_lib.U32P)))
+        return out
+
+    def normals(self, seed, root, first_parent, count) -> np.ndarray:
+        z = np.zeros(int(count), np.float32)
+        self._check(self.L.pc_debug_normals(self.ctx, int(seed), int(root), int(first_parent),
+                                            int(count), z.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+        return z
+
+    def tables(self):
+        k = np.zeros(128, np.uint32)
+        w = np.zeros(128, np.uint32)
+        f = np.zeros(129, np.uint32)
+        self._check(self.L.pc_debug_tables(self.ctx, k.ctypes.data_as(_lib.U32P),
+                                           w.ctypes.data_as(_lib.U32P), f.ctypes.data_as(_lib.U32P)))
+        return k, w.view(np.float32), f.view(np.float32)
+
+    def close(self):
+        if getattr(self, "ctx", None):
+            self.L.pc_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def format_histogram(values, totals, per_type, track_ratio: bool) -> str:
+    """The output text of the reference's io::save_fluorescences (src/io/parser.cu:187-217)."""
+    out = []
+    for i, v in enumerate(values):
+        if int(totals[i]) == 0:
+            continue
+        row = "%.10g\t%d" % (v, int(totals[i]))
+        if track_ratio:
+            row += "".join("\t%d" % int(c) for c in per_type[i])
+        out.append(row + "\n")
+    return "".join(out)

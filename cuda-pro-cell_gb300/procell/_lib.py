@@ -1,0 +1,124 @@
+"""ctypes binding of libprocell.so (include/procell.h).
+
+The library must have been built (cuda-pro-cell_gb300/build.py); loading fails loudly
+otherwise. There is no CPU fallback: every simulation runs on the GPU.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(PKG, "build", "libprocell.so")
+CLI_PATH = os.path.join(PKG, "build", "procell")
+
+PC_OK = 0
+ERRORS = {1: "PC_ERR_INVALID", 2: "PC_ERR_CUDA", 3: "PC_ERR_NOMEM", 4: "PC_ERR_DEPTH",
+          5: "PC_ERR_UNSUPPORTED", 6: "PC_ERR_IO"}
+
+
+class Bin(ctypes.Structure):
+    _fields_ = [("value", ctypes.c_double), ("frequency", ctypes.c_uint64)]
+
+
+class CellType(ctypes.Structure):
+    _fields_ = [("ratio", ctypes.c_double), ("mean", ctypes.c_double), ("sd", ctypes.c_double)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("roots", ctypes.c_uint64), ("divisions", ctypes.c_uint64),
+                ("leaves", ctypes.c_uint64), ("uncounted", ctypes.c_uint64),
+                ("vanished", ctypes.c_uint64), ("max_generation", ctypes.c_uint32),
+                ("sweeps", ctypes.c_uint32), ("device_ms", ctypes.c_double),
+                ("divide_ms", ctypes.c_double), ("h2d_bytes", ctypes.c_uint64),
+                ("d2h_bytes", ctypes.c_uint64)]
+
+
+class Histogram(ctypes.Structure):
+    _fields_ = [("n_values", ctypes.c_uint64), ("n_types", ctypes.c_uint32),
+                ("values", ctypes.POINTER(ctypes.c_double)),
+                ("totals", ctypes.POINTER(ctypes.c_uint64)),
+                ("per_type", ctypes.POINTER(ctypes.c_uint64)), ("stats", Stats)]
+
+
+# (name, restype, argtypes) of every exported symbol of include/procell.h
+VP, U32P, U64P = ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint64)
+SIGNATURES = [
+    ("pc_create", ctypes.c_int, [ctypes.POINTER(VP), ctypes.c_int]),
+    ("pc_destroy", None, [VP]),
+    ("pc_last_error", ctypes.c_char_p, [VP]),
+    ("pc_version", ctypes.c_char_p, []),
+    ("pc_set_stream", ctypes.c_int, [VP, VP]),
+    ("pc_set_option", ctypes.c_int, [VP, ctypes.c_char_p, ctypes.c_double]),
+    ("pc_plan_create", ctypes.c_int, [VP, ctypes.POINTER(Bin), ctypes.c_uint64,
+                                      ctypes.POINTER(CellType), ctypes.c_uint32, ctypes.c_double,
+                                      ctypes.c_double, ctypes.c_uint64, ctypes.POINTER(VP)]),
+    ("pc_plan_set_roots", ctypes.c_int, [VP, VP, ctypes.c_uint64, ctypes.c_uint64]),
+    ("pc_plan_run", ctypes.c_int, [VP, VP]),
+    ("pc_plan_stats", ctypes.c_int, [VP, VP, ctypes.POINTER(Stats)]),
+    ("pc_plan_result", ctypes.c_int, [VP, VP, ctypes.POINTER(Histogram)]),
+    ("pc_plan_raw_counts", ctypes.c_int, [VP, VP, U64P, ctypes.c_uint64, U64P, U32P]),
+    ("pc_plan_destroy", None, [VP]),
+    ("pc_simulate", ctypes.c_int, [VP, ctypes.POINTER(Bin), ctypes.c_uint64,
+                                   ctypes.POINTER(CellType), ctypes.c_uint32, ctypes.c_double,
+                                   ctypes.c_double, ctypes.c_uint64, ctypes.POINTER(Histogram)]),
+    ("pc_histogram_free", None, [ctypes.POINTER(Histogram)]),
+    ("pc_load_histogram", ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(ctypes.POINTER(Bin)), U64P]),
+    ("pc_load_cell_types", ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(ctypes.POINTER(CellType)), U32P]),
+    ("pc_write_histogram", ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(Histogram), ctypes.c_int]),
+    ("pc_free", None, [VP]),
+    ("pc_debug_philox", ctypes.c_int, [VP, U32P, ctypes.c_uint64, U32P, U32P]),
+    ("pc_debug_normals", ctypes.c_int, [VP, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint64,
+                                        ctypes.c_uint64, ctypes.POINTER(ctypes.c_float)]),
+    ("pc_debug_tables", ctypes.c_int, [VP, U32P, U32P, U32P]),
+]
+
+_lib = None
+
+
+def load() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"libprocell.so is not built ({LIB_PATH}); run "
+                               "`python cuda-pro-cell_gb300/build.py` first")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, res, args in SIGNATURES:
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+class ProcellError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+def bins_array(bins):
+    arr = (Bin * max(1, len(bins)))()
+    for i, (v, f) in enumerate(bins):
+        arr[i].value = float(v)
+        arr[i].frequency = int(f)
+    return arr
+
+
+def types_array(types):
+    arr = (CellType * max(1, len(types)))()
+    for i, (r, m, s) in enumerate(types):
+        arr[i].ratio, arr[i].mean, arr[i].sd = float(r), float(m), float(s)
+    return arr
+
+
+def histogram_to_numpy(h: Histogram):
+    nv, nt = int(h.n_values), int(h.n_types)
+    values = np.ctypeslib.as_array(h.values, shape=(max(1, nv),))[:nv].copy()
+    totals = np.ctypeslib.as_array(h.totals, shape=(max(1, nv),))[:nv].copy()
+    per = np.ctypeslib.as_array(h.per_type, shape=(max(1, nv * nt),))[:nv * nt].copy().reshape(nv, nt)
+    st = h.stats
+    stats = {k: getattr(st, k) for k, _ in Stats._fields_}
+    return values, totals.astype(np.uint64), per.astype(np.uint64), stats

@@ -1,0 +1,169 @@
+/* procell: GB300-native (sm_103a) engine for ProCell's stochastic proliferation path.
+ *
+ * C ABI of libprocell.so. Plain pointers and sizes only; no CUDA or C++ types cross it.
+ * Every entry point returns PC_OK (0) or a PC_ERR_* code; pc_last_error() then holds a
+ * one-line message. A context is used by one host thread at a time.
+ *
+ * What the reference exposes for this path, and what replaces it here:
+ *
+ *  reference (ericniso/cuda-pro-cell)                         this library
+ *  ---------------------------------------------------------  --------------------------
+ *  Simulator::create_cell_population                            pc_plan_create + pc_plan_run
+ *    -> simulation::create_cells_population                      (root sweep on the GPU;
+ *       src/simulation/cells_population.cu:18-54                  roots never leave HBM)
+ *  Simulator::start_simulation                                  pc_plan_run
+ *    -> bool simulation::proliferate(cell_types&, uint64_t size,
+ *         uint64_t tree_depth, cell* h_cells, double t_max,
+ *         double threshold, fluorescences_result&, bool track_ratio)
+ *       src/simulation/proliferation.h:12-19,
+ *       src/simulation/proliferation.cu:26-215
+ *  the filled fluorescences_result (value, frequency, ratio[])  pc_plan_result -> pc_histogram
+ *    src/simulation/data_types.h:32-37, parser.cu:126-151
+ *  io::load_fluorescences / load_cell_types / save_fluorescences pc_load_histogram,
+ *    src/io/parser.cu:68-217                                      pc_load_cell_types,
+ *                                                                 pc_write_histogram
+ *  the whole process (main, src/main.cu:18-34)                  the `procell` CLI, or
+ *                                                                 pc_simulate in one call
+ *
+ * Differences at the boundary: the reference takes ownership of a host array of 40-byte
+ * root cells that it created on the GPU and copied back (cells_population.cu:52); here
+ * roots are generated in HBM from the histogram and never cross PCIe/C2C. The reference
+ * reports no errors (proliferate always returns true); here every CUDA failure is
+ * returned as a status. Counts are uint64 (the reference adds into the low 32 bits).
+ */
+#ifndef PROCELL_H
+#define PROCELL_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PC_OK 0
+#define PC_ERR_INVALID 1     /* bad argument or input (message says which) */
+#define PC_ERR_CUDA 2        /* a CUDA runtime call failed */
+#define PC_ERR_NOMEM 3       /* device or host allocation failed / budget too small */
+#define PC_ERR_DEPTH 4       /* a lineage went deeper than the key layout allows */
+#define PC_ERR_UNSUPPORTED 5 /* e.g. more cell types than the kernels hold */
+#define PC_ERR_IO 6          /* a file could not be opened or written */
+
+/* One histogram row, as in the reference's `fluorescence` (data_types.h:26-30). */
+typedef struct pc_bin {
+  double value;
+  uint64_t frequency;
+} pc_bin;
+
+/* One cell type in file order (the reference's `cell_type` without `name`, which is the
+ * 0-based line index, data_types.h:19-24). mean < 0 marks a quiescent type. */
+typedef struct pc_cell_type {
+  double ratio;
+  double mean;
+  double sd;
+} pc_cell_type;
+
+typedef struct pc_stats {
+  uint64_t roots;           /* initial cells simulated */
+  uint64_t divisions;       /* internal tree nodes */
+  uint64_t leaves;          /* leaves counted into the histogram */
+  uint64_t uncounted;       /* out-of-time roots whose value is below phi */
+  uint64_t vanished;        /* due cells whose daughters would fall to phi or below */
+  uint32_t max_generation;  /* deepest generation reached */
+  uint32_t sweeps;          /* kernel launches of the division sweep */
+  double device_ms;         /* summed duration of the simulation kernels (CUDA events) */
+  double divide_ms;         /* ... of the division sweeps alone */
+  uint64_t h2d_bytes;       /* host-to-device bytes of the plan and the run */
+  uint64_t d2h_bytes;       /* device-to-host bytes of the run and the result */
+} pc_stats;
+
+/* The output histogram: every value of the reference's output value set (each nonzero
+ * bin value halved while >= phi, deduplicated, ascending; parser.cu:126-151), the total
+ * count and the per-type counts (row-major [n_values][n_types], types in file order).
+ * Rows with total 0 are kept; the writer skips them as the reference does. */
+typedef struct pc_histogram {
+  uint64_t n_values;
+  uint32_t n_types;
+  double* values;
+  uint64_t* totals;
+  uint64_t* per_type;
+  pc_stats stats;
+} pc_histogram;
+
+typedef struct pc_context pc_context;
+typedef struct pc_plan pc_plan;
+
+/* Context: device, stream, memory pool. device = CUDA ordinal. */
+int pc_create(pc_context** out, int device);
+void pc_destroy(pc_context* ctx);
+const char* pc_last_error(const pc_context* ctx); /* ctx may be NULL (creation errors) */
+const char* pc_version(void);
+
+/* Use `stream` (a cudaStream_t) for all work of this context; NULL = the context's own. */
+int pc_set_stream(pc_context* ctx, void* stream);
+
+/* Tuning knobs (results never depend on them):
+ *   "memory_budget_bytes" device bytes the level buffers may use (default: half of the
+ *                         free memory at first use)
+ *   "max_slice_cells"     cap on cells per division-sweep launch (default: from budget)
+ *   "max_root_chunk"      cap on roots per root-sweep launch (default: from budget)
+ *   "grid_blocks"         blocks per launch (default: resident blocks x SMs)
+ */
+int pc_set_option(pc_context* ctx, const char* name, double value);
+
+/* phi == 0 selects the reference's automatic threshold: the smallest value with a
+ * nonzero frequency (parser.cu:80-96). phi < 0 is invalid. seed keys the random stream;
+ * equal inputs and seed give bit-identical histograms on any run, chunking or device. */
+int pc_plan_create(pc_context* ctx, const pc_bin* bins, uint64_t n_bins,
+                   const pc_cell_type* types, uint32_t n_types, double t_max, double phi,
+                   uint64_t seed, pc_plan** out);
+/* Restrict the plan to initial cells [root_begin, root_end) of the file order (a shard).
+ * Shards of one plan are disjoint and their histograms add up to the full one. */
+int pc_plan_set_roots(pc_context* ctx, pc_plan* plan, uint64_t root_begin, uint64_t root_end);
+/* Run all sweeps on the device. Counts stay in HBM until pc_plan_result. */
+int pc_plan_run(pc_context* ctx, pc_plan* plan);
+/* Statistics of the last pc_plan_run (leaves is filled by pc_plan_result only). */
+int pc_plan_stats(pc_context* ctx, const pc_plan* plan, pc_stats* out);
+/* Copy the counts to the host and merge equal values into `out` (free with
+ * pc_histogram_free). */
+int pc_plan_result(pc_context* ctx, pc_plan* plan, pc_histogram* out);
+/* The raw per-(generation, bin, type) counts as uint64 [gens][bins][types], bins in file
+ * order of the nonzero rows and types in file order. *n_elems gets the element count;
+ * pass host_out = NULL to query the shape (gens, bins, types in dims[3]). */
+int pc_plan_raw_counts(pc_context* ctx, pc_plan* plan, uint64_t* host_out, uint64_t capacity,
+                       uint64_t* n_elems, uint32_t dims[3]);
+void pc_plan_destroy(pc_plan* plan);
+
+/* One call: plan, run, result, destroy. */
+int pc_simulate(pc_context* ctx, const pc_bin* bins, uint64_t n_bins, const pc_cell_type* types,
+                uint32_t n_types, double t_max, double phi, uint64_t seed, pc_histogram* out);
+void pc_histogram_free(pc_histogram* h);
+
+/* File formats of the reference (parser.cu:68-217). Loaders read with the reference's
+ * `in >> a >> b` semantics (stop at the first unparsable token). The loaders allocate
+ * *out with malloc; release it with pc_free. pc_load_cell_types also applies the
+ * reference's ratio-sum check (|1 - sum| <= 1e-8) and returns PC_ERR_INVALID with the
+ * reference's message when it fails. */
+int pc_load_histogram(const char* path, pc_bin** out, uint64_t* n);
+int pc_load_cell_types(const char* path, pc_cell_type** out, uint32_t* n);
+/* Writes rows with a nonzero total as `value\ttotal[\tper-type...]\n` with 10 significant
+ * digits (the reference's std::ostream precision(10)). path NULL or "-" = stdout. */
+int pc_write_histogram(const char* path, const pc_histogram* h, int track_ratio);
+void pc_free(void* p);
+
+/* Diagnostics for the parity tests: evaluate the engine's random stream on the device.
+ * pc_debug_philox: out[4*i..] = Philox4x32-10(ctr[4*i..], key) for i < n.
+ * pc_debug_normals: z[i] = first-attempt normal of child (i & 1) of node first_parent+i/2
+ *                   under `root` (no truncation), as the division sweep computes it.
+ * pc_debug_tables: the device's ziggurat tables (k[128], w bits[128], f bits[129]). */
+int pc_debug_philox(pc_context* ctx, const uint32_t* ctr, uint64_t n, const uint32_t key[2],
+                    uint32_t* out);
+int pc_debug_normals(pc_context* ctx, uint64_t seed, uint32_t root, uint64_t first_parent,
+                     uint64_t count, float* z);
+int pc_debug_tables(pc_context* ctx, uint32_t* k, uint32_t* w_bits, uint32_t* f_bits);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PROCELL_H */
