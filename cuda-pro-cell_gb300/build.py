@@ -45,7 +45,10 @@ def _stale(target, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build(verbose: bool = False) -> str:
+def build(verbose: bool = False, out: str | None = None, defines=()) -> str:
+    """Compile into `out` (default cuda-pro-cell_gb300/build). `defines` are extra
+    -DNAME=VALUE macros for the device code (tuning variants)."""
+    OUT = out or globals()["OUT"]
     os.makedirs(OUT, exist_ok=True)
     cuda = _cuda_home()
     nvcc = os.path.join(cuda, "bin", "nvcc")
@@ -57,9 +60,11 @@ def build(verbose: bool = False) -> str:
     k_src = os.path.join(CSRC, "pc_kernels.cu")
     k_obj = os.path.join(OUT, "pc_kernels.o")
     objs.append(k_obj)
-    if _stale(k_obj, [k_src] + headers):
+    dflags = ["-D" + d for d in defines]
+    if defines or _stale(k_obj, [k_src] + headers):
         jobs.append([nvcc, *ARCH, "-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xptxas", "-v",
-                     "-Xcompiler", "-fPIC,-ffp-contract=off", "-I" + INCLUDE, "-c", k_src, "-o", k_obj])
+                     "-Xcompiler", "-fPIC,-ffp-contract=off", "-I" + INCLUDE, *dflags, "-c", k_src,
+                     "-o", k_obj])
     for name in ("pc_api.cpp", "pc_io.cpp"):
         src = os.path.join(CSRC, name)
         obj = os.path.join(OUT, name.replace(".cpp", ".o"))
@@ -71,7 +76,7 @@ def build(verbose: bool = False) -> str:
         for out in ex.map(_run, jobs):
             logs.append(out)
     lib = os.path.join(OUT, "libprocell.so")
-    if _stale(lib, objs):
+    if defines or _stale(lib, objs):
         logs.append(_run([nvcc, *ARCH, "-shared", "-Xcompiler", "-fPIC", "-o", lib, *objs]))
     cli_src = os.path.join(CSRC, "procell_cli.cpp")
     cli = os.path.join(OUT, "procell")
@@ -84,4 +89,10 @@ def build(verbose: bool = False) -> str:
 
 
 if __name__ == "__main__":
-    print(build(verbose=True))
+    import argparse
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--out", default=None)
+    ap.add_argument("--define", action="append", default=[])
+    ap.add_argument("--quiet", action="store_true")
+    a = ap.parse_args()
+    print(build(verbose=not a.quiet, out=a.out, defines=a.define))

@@ -73,7 +73,7 @@ struct pc_plan {
   TypeDev* types_dev = nullptr;
   uint32_t* bin_info_dev = nullptr;
   uint64_t* bin_start_dev = nullptr;
-  uint32_t* root_rec_dev = nullptr;
+  unsigned long long* root_rec_dev = nullptr;
   unsigned long long* hist_dev = nullptr;
   size_t hist_elems = 0;
   pc_stats stats;
@@ -440,7 +440,7 @@ int pc_plan_create(pc_context* ctx, const pc_bin* bins, uint64_t n_bins, const p
   cudaError_t e = cudaMalloc(&p->types_dev, nt * sizeof(TypeDev));
   if (e == cudaSuccess) e = cudaMalloc(&p->bin_info_dev, std::max<size_t>(1, nb) * sizeof(uint32_t));
   if (e == cudaSuccess) e = cudaMalloc(&p->bin_start_dev, (nb + 1) * sizeof(uint64_t));
-  if (e == cudaSuccess) e = cudaMalloc(&p->root_rec_dev, std::max<uint64_t>(1, chunk) * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&p->root_rec_dev, std::max<uint64_t>(1, chunk) * sizeof(unsigned long long));
   if (e == cudaSuccess) e = cudaMalloc(&p->hist_dev, p->hist_elems * sizeof(unsigned long long));
   if (e == cudaSuccess) e = cudaMemcpyAsync(p->types_dev, p->types.data(), nt * sizeof(TypeDev), cudaMemcpyHostToDevice, ctx->stream);
   if (e == cudaSuccess && nb)

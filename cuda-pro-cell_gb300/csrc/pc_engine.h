@@ -13,10 +13,13 @@
 //   cells at cells + s * stride, and prefix[] (nseg + 1 entries, exclusive) is written
 //   by the producer's last block. Concatenated in segment order the cells are sorted by
 //   key, so every level is sorted by (root, path).
-// * root_rec[r] = bin << 8 | sorted type index for each initial cell of the chunk.
 // * bin_info[b] = phi cap (bits 0-7: a cell of generation g in bin b may divide iff
 //   g < cap) | countable at generation 0 (bit 8: value >= phi) | cap clamped by the key
 //   layout (bit 9).
+// * root_rec[r] (uint64, one per initial cell of the chunk, written by the root sweep):
+//   bits 0-31 histogram class bin * ntypes + type, bits 32-39 sorted type index,
+//   bits 40-47 the bin's phi cap, bits 48-49 bin_info bits 8-9. One load gives the
+//   division sweep everything it needs about a cell's root.
 // * hist[(g * nbins + b) * ntypes + k] counts the leaves of generation g, bin b, type k.
 #pragma once
 
@@ -54,7 +57,7 @@ struct RunArgs {
   const ZigTables* zig;
   const uint32_t* bin_info;  // [nbins]
   const uint64_t* bin_start; // [nbins + 1] global root offsets
-  uint32_t* root_rec;        // [chunk]
+  unsigned long long* root_rec;  // [chunk]
   unsigned long long* hist;  // [hist_gens][nbins][ntypes]
   unsigned long long* stats; // [0] vanished, [1] uncounted, [2] max generation
   uint32_t* error;           // bit 0: depth overflow, bit 1: sampler round budget exhausted

@@ -28,6 +28,11 @@ namespace pc {
 namespace {
 
 constexpr uint32_t kFull = 0xFFFFFFFFu;
+// Resident blocks per SM the division sweep is compiled for (caps registers per thread).
+#ifndef PC_DIVIDE_MIN_BLOCKS
+#define PC_DIVIDE_MIN_BLOCKS 4
+#endif
+constexpr int kDivideMinBlocks = PC_DIVIDE_MIN_BLOCKS;
 
 struct Smem {
   ZigTables zig;
@@ -50,26 +55,28 @@ __device__ __forceinline__ void stage(Smem& s, const RunArgs& a) {
 // round is above 1/2) turns a would-be endless loop into error bit 1.
 constexpr uint32_t kRoundBudget = 1u << 16;
 
-__device__ __noinline__ float slow_z(uint32_t j, uint32_t layer, uint64_t node, uint32_t root,
-                                     uint32_t k0, uint32_t k1, const TypeDev& T,
+__device__ __noinline__ float slow_z(uint32_t j, uint32_t layer, uint32_t wedge, uint64_t node,
+                                     uint32_t root, uint32_t k0, uint32_t k1, const TypeDev& T,
                                      const ZigTables& Z, uint32_t* error) {
   ChildStream cs = child_stream(node, root, k0, k1);
   uint32_t budget = kRoundBudget;
+  bool have_wedge = true;
   while (budget > 0u) {
-    const float z = zig_normal(j, layer, cs, Z, budget);
+    const float z = zig_normal(j, layer, have_wedge, wedge, cs, Z, budget);
     if (budget == 0u) break;
     if (z >= T.zlo && z <= T.zhi) return z;
+    have_wedge = false;
     j = cs.next();
-    layer = cs.next() & 127u;
+    layer = cs.next() & 255u;
     --budget;
   }
   atomicOr(error, 2u);
   return 0.0f;
 }
 
-// First-attempt fast path (about 98.8% of draws): one strip test, one FP32 multiply.
-__device__ __forceinline__ float draw_z(uint32_t j, uint32_t layer, uint64_t node, uint32_t root,
-                                        uint32_t k0, uint32_t k1, const TypeDev& T,
+// First-attempt fast path (about 98.5% of draws): one strip test, one FP32 multiply.
+__device__ __forceinline__ float draw_z(uint32_t j, uint32_t layer, uint32_t wedge, uint64_t node,
+                                        uint32_t root, uint32_t k0, uint32_t k1, const TypeDev& T,
                                         const ZigTables& Z, uint32_t* error) {
   const uint32_t mag = j & 0x7FFFFFFFu;
   if (mag < Z.k[layer]) {
@@ -77,10 +84,35 @@ __device__ __forceinline__ float draw_z(uint32_t j, uint32_t layer, uint64_t nod
     const float z = (j >> 31) ? -x : x;
     if (z >= T.zlo && z <= T.zhi) return z;
   }
-  return slow_z(j, layer, node, root, k0, k1, T, Z, error);
+  return slow_z(j, layer, wedge, node, root, k0, k1, T, Z, error);
 }
 
 enum Fate : int { kNone = 0, kLeaf = 1, kEmit = 2, kVanish = 3 };
+
+// GB300 runs FP64 arithmetic and every FP64<->FP32 conversion on a pipe of 2 lanes per
+// clock per SM, so the conversions and comparisons below are done on the bits instead.
+//
+// Exact float -> double for zero or a normal float (z is never subnormal: |z| >= the
+// smallest ziggurat strip width, about 1e-10): rebias the exponent, widen the mantissa.
+__device__ __forceinline__ double f32_to_f64(float z) {
+  const uint32_t f = __float_as_uint(z);
+  const uint32_t a = f & 0x7FFFFFFFu;
+  const uint32_t hi = (f & 0x80000000u) | (a ? (a >> 3) + (896u << 20) : 0u);
+  return __hiloint2double((int)hi, (int)(f << 29));
+}
+
+// A non-negative double truncated to FP32 (values below 2^-126 become 0; the estimate's
+// error band covers both truncations). Valid while d < 2^128, which est_ok guarantees.
+__device__ __forceinline__ float f64_to_f32_rz(double d) {
+  const uint32_t hi = (uint32_t)__double2hiint(d), lo = (uint32_t)__double2loint(d);
+  if (hi < (897u << 20)) return 0.0f;
+  return __uint_as_float(((hi - (896u << 20)) << 3) | (lo >> 29));
+}
+
+// a > b for non-negative doubles (IEEE order equals integer order of the bit patterns).
+__device__ __forceinline__ bool gt_nonneg(double a, double b) {
+  return __double_as_longlong(a) > __double_as_longlong(b);
+}
 
 // Fate of one daughter born at `birth` with normal z. The FP32 estimate decides leaves
 // and clear non-leaves without FP64 work; the band around t_max (8x the worst-case FP32
@@ -88,17 +120,17 @@ enum Fate : int { kNone = 0, kLeaf = 1, kEmit = 2, kVanish = 3 };
 // birth + fma(sigma, z, mu), the reference's t + timer.
 __device__ __forceinline__ int fate(double birth, float birth_f, float z, const TypeDev& T,
                                     const RunArgs& a, bool can_divide, double& due) {
+  bool exact = true;
   if (a.est_ok) {
     const float est = __fadd_rn(birth_f, __fadd_rn(T.mu_f, __fmul_rn(T.sigma_f, z)));
     if (est > a.t_hi) return kLeaf;
-    if (est < a.t_lo && !can_divide) return kVanish;
     if (est < a.t_lo) {
-      due = birth + fma(T.sigma, (double)z, T.mu);
-      return kEmit;
+      if (!can_divide) return kVanish;
+      exact = false;
     }
   }
-  due = birth + fma(T.sigma, (double)z, T.mu);
-  if (due > a.t_max) return kLeaf;
+  due = birth + fma(T.sigma, f32_to_f64(z), T.mu);
+  if (exact && gt_nonneg(due, a.t_max)) return kLeaf;
   return can_divide ? kEmit : kVanish;
 }
 
@@ -226,9 +258,12 @@ __global__ void __launch_bounds__(kBlock) k_roots(const RunArgs a, const uint64_
           break;
         }
       }
-      a.root_rec[rl] = (bin << 8) | ty;
-      const TypeDev& T = s.types[ty];
       const uint32_t info = __ldg(a.bin_info + bin);
+      cls = bin * a.ntypes + ty;
+      a.root_rec[rl] = (unsigned long long)cls | ((unsigned long long)ty << 32) |
+                       ((unsigned long long)(info & 0xFFu) << 40) |
+                       ((unsigned long long)((info >> 8) & 3u) << 48);
+      const TypeDev& T = s.types[ty];
       bool leaf;
       if (T.mode == kModeQuiescent) {
         leaf = true;  // timer -1: out of time at once (cell.cu:69-75)
@@ -236,19 +271,18 @@ __global__ void __launch_bounds__(kBlock) k_roots(const RunArgs a, const uint64_
         double tau = 0.0;
         if (T.mode == kModeNormal) {
           const u32x4 P = philox(u32x4{0u, 0u, root, kPurposePair}, a.k0, a.k1);
-          const float z = draw_z(P.y, (P.z >> 8) & 127u, 1ull, root, a.k0, a.k1, T, s.zig, a.error);
-          tau = fma(T.sigma, (double)z, T.mu);
+          const float z = draw_z(P.y, (P.z >> 8) & 255u, pair_wedge_bits(P, 1u), 1ull, root, a.k0,
+                                 a.k1, T, s.zig, a.error);
+          tau = fma(T.sigma, f32_to_f64(z), T.mu);
         }
         d0 = tau * u_age + tau;  // t = tau * U (cell.cu:124-143), due = t + timer
-        leaf = d0 > a.t_max;
+        leaf = gt_nonneg(d0, a.t_max);
       }
       if (leaf) {
-        if (info & 0x100u) {
+        if (info & 0x100u)
           nleaf = 1u;
-          cls = bin * a.ntypes + ty;
-        } else {
+        else
           ++uncounted;
-        }
       } else if ((info & 0xFFu) > 0u) {
         f = kEmit;
       } else {
@@ -275,8 +309,25 @@ __global__ void __launch_bounds__(kBlock) k_roots(const RunArgs a, const uint64_
 }
 
 // -------------------------------------------------------------- division sweep ------
-__global__ void __launch_bounds__(kBlock) k_divide(const RunArgs a, const LevelIn in,
-                                                   const uint32_t g, const LevelOut out) {
+// Segment cursor over an input level: maps a virtual index to its cell, moving forward.
+struct Cursor {
+  const ulonglong2* cells;
+  const unsigned long long* prefix;
+  uint64_t stride;
+  uint32_t seg;
+  uint64_t seg_lo, seg_hi;
+  __device__ __forceinline__ ulonglong2 load(uint64_t v) {
+    while (v >= seg_hi) {
+      ++seg;
+      seg_lo = seg_hi;
+      seg_hi = __ldg(prefix + seg + 1u);
+    }
+    return __ldg(cells + (uint64_t)seg * stride + (v - seg_lo));
+  }
+};
+
+__global__ void __launch_bounds__(kBlock, kDivideMinBlocks) k_divide(const RunArgs a, const LevelIn in,
+                                                                     const uint32_t g, const LevelOut out) {
   __shared__ Smem s;
   stage(s, a);
   __syncthreads();
@@ -292,57 +343,53 @@ __global__ void __launch_bounds__(kBlock) k_divide(const RunArgs a, const LevelI
   const uint32_t g1 = g + 1u;
   const uint64_t gmask = (1ull << g) - 1ull;
   unsigned long long* hist_g1 = a.hist + (uint64_t)g1 * a.nbins * a.ntypes;
-  uint32_t seg = 0;
-  uint64_t seg_lo = 0, seg_hi = 0;
+  Cursor cur{in.cells, in.prefix, in.stride, 0u, 0ull, 0ull};
+  ulonglong2 next = make_ulonglong2(0ull, 0ull);
   if (va < vb) {
-    seg = last_le(in.prefix, in.nseg, va);
-    seg_lo = __ldg(in.prefix + seg);
-    seg_hi = __ldg(in.prefix + seg + 1u);
+    cur.seg = last_le(in.prefix, in.nseg, va);
+    cur.seg_lo = __ldg(in.prefix + cur.seg);
+    cur.seg_hi = __ldg(in.prefix + cur.seg + 1u);
+    if (va + lane < vb) next = cur.load(va + lane);
   }
   for (uint64_t v0 = va; v0 < vb; v0 += 32u) {
-    const uint64_t v = v0 + lane;
-    const bool act = v < vb;
+    const bool act = v0 + lane < vb;
+    const ulonglong2 c = next;
+    // prefetch the next step's cell while this one is processed
+    if (v0 + 32u + lane < vb) next = cur.load(v0 + 32u + lane);
     int f0 = kNone, f1 = kNone;
     double due0 = 0.0, due1 = 0.0;
-    uint64_t key = 0;
+    const uint64_t key = c.y;
     uint32_t nleaf = 0, cls = 0;
     if (act) {
-      while (v >= seg_hi) {
-        ++seg;
-        seg_lo = seg_hi;
-        seg_hi = __ldg(in.prefix + seg + 1u);
-      }
-      const ulonglong2 c = __ldg(in.cells + (uint64_t)seg * in.stride + (v - seg_lo));
       const double d = __longlong_as_double((long long)c.x);
-      key = c.y;
       const uint64_t rl = key >> g;
+      const unsigned long long rec = __ldg(a.root_rec + rl);  // consumed after Philox
       const uint64_t node = (1ull << g) | (key & gmask);
       const uint32_t root = (uint32_t)(a.root_base + rl);
-      const uint32_t rec = __ldg(a.root_rec + rl);
-      const uint32_t bin = rec >> 8, ty = rec & 0xFFu;
-      const uint32_t info = __ldg(a.bin_info + bin);
-      const uint32_t cap = info & 0xFFu;
+      const u32x4 P = philox(u32x4{(uint32_t)node, (uint32_t)(node >> 32), root, kPurposePair}, a.k0, a.k1);
+      cls = (uint32_t)rec;
+      const uint32_t ty = (uint32_t)(rec >> 32) & 0xFFu;
+      const uint32_t cap = (uint32_t)(rec >> 40) & 0xFFu;
+      const bool clamped = ((rec >> 49) & 1ull) != 0ull;
       const bool can_divide = g1 < cap;
       const TypeDev& T = s.types[ty];
       if (T.mode == kModeZeroMean) {
         // tau == 0: the daughters are due at the parent's own due time
         due0 = d;
         due1 = d;
-        f0 = f1 = (d > a.t_max) ? kLeaf : (can_divide ? kEmit : kVanish);
+        f0 = f1 = gt_nonneg(d, a.t_max) ? kLeaf : (can_divide ? kEmit : kVanish);
       } else {
-        const u32x4 P = philox(u32x4{(uint32_t)node, (uint32_t)(node >> 32), root, kPurposePair},
-                               a.k0, a.k1);
-        const float z0 = draw_z(P.x, P.z & 127u, 2ull * node, root, a.k0, a.k1, T, s.zig, a.error);
-        const float z1 =
-            draw_z(P.y, (P.z >> 8) & 127u, 2ull * node + 1ull, root, a.k0, a.k1, T, s.zig, a.error);
-        const float df = __double2float_rz(d);
+        const float z0 = draw_z(P.x, P.z & 255u, pair_wedge_bits(P, 0u), 2ull * node, root, a.k0,
+                                a.k1, T, s.zig, a.error);
+        const float z1 = draw_z(P.y, (P.z >> 8) & 255u, pair_wedge_bits(P, 1u), 2ull * node + 1ull,
+                                root, a.k0, a.k1, T, s.zig, a.error);
+        const float df = f64_to_f32_rz(d);
         f0 = fate(d, df, z0, T, a, can_divide, due0);
         f1 = fate(d, df, z1, T, a, can_divide, due1);
       }
-      if ((info & 0x200u) && g1 == cap && (f0 == kVanish || f1 == kVanish)) depth_error = 1u;
+      if (clamped && g1 == cap && (f0 == kVanish || f1 == kVanish)) depth_error = 1u;
       nleaf = (f0 == kLeaf ? 1u : 0u) + (f1 == kLeaf ? 1u : 0u);
       vanished += (f0 == kVanish ? 1u : 0u) + (f1 == kVanish ? 1u : 0u);
-      cls = bin * a.ntypes + ty;
     }
     count_leaves(hist_g1, cls, nleaf, lane);
     const uint32_t e0 = __ballot_sync(kFull, f0 == kEmit);
@@ -391,7 +438,7 @@ __global__ void k_debug_normals(const ZigTables* zig, uint32_t k0, uint32_t k1, 
   const u32x4 P = philox(u32x4{(uint32_t)parent, (uint32_t)(parent >> 32), root, kPurposePair}, k0, k1);
   ChildStream cs = child_stream(2ull * parent + c, root, k0, k1);
   uint32_t budget = kRoundBudget;
-  z[i] = zig_normal(c ? P.y : P.x, (P.z >> (8u * c)) & 127u, cs, Z, budget);
+  z[i] = zig_normal(c ? P.y : P.x, (P.z >> (8u * c)) & 255u, true, pair_wedge_bits(P, c), cs, Z, budget);
 }
 
 }  // namespace

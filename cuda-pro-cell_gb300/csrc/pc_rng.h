@@ -12,17 +12,21 @@
 //
 // * PURPOSE_ROOT  node 0, index 0: the root's type uniform (words x,y) and its
 //                 initial-age uniform U (words z,w); see cell.cu:81-104 and :124-143.
-// * PURPOSE_PAIR  node n: the first-attempt normal draws of both children 2n and 2n+1
-//                 (child c takes word c as the signed 31-bit magnitude and byte c of
-//                 word z as its ziggurat layer). The root is child 1 of node 0.
+// * PURPOSE_PAIR  node n: the first-attempt normal draws of both children 2n and 2n+1.
+//                 Child c takes word c (x or y) as its sign and 31-bit magnitude, byte c
+//                 of word z as its ziggurat layer, and a 24-bit wedge uniform: child 0
+//                 the low 24 bits of w, child 1 the top byte of w above the top 16 bits
+//                 of z. The root is child 1 of node 0.
 // * PURPOSE_CHILD node m, index i: the i-th block of the child's private stream, used
-//                 only when the first attempt is rejected (ziggurat wedge/tail or the
-//                 truncation tau <= 0 of cell.cu:114-118).
+//                 only when the first attempt is rejected (ziggurat tail, wedge
+//                 rejection, or the truncation tau <= 0 of cell.cu:114-118).
 //
-// The normal variate is a 128-layer ziggurat (Marsaglia & Tsang, "The Ziggurat Method
+// The normal variate is a 256-layer ziggurat (Marsaglia & Tsang, "The Ziggurat Method
 // for Generating Random Variables", J. Stat. Softw. 5(8), 2000) evaluated in FP32 with
 // independent layer bits (Doornik, "An Improved Ziggurat Method to Generate Normal
-// Random Samples", 2005). Its rare wedge/tail steps need exp and log; both are written
+// Random Samples", 2005); the first attempt of a daughter needs no Philox block beyond
+// the pair block unless it falls in the tail or its wedge test rejects (about 0.7% of
+// draws; 98.5% pass the strip test alone). Its rare wedge/tail steps need exp and log; both are written
 // below from textbook range reduction plus polynomial/series evaluation with only
 // IEEE-754 add, multiply and divide, so host and device produce identical bits.
 // Device code must be compiled with --fmad=false and host code with
@@ -204,19 +208,26 @@ PC_HD float zig_logf(float u) {
 }
 
 // Ziggurat tables. Layer 0 is the base strip (the rectangle [0,r] x [0,f(r)] plus the
-// tail beyond r); layer i = 1..127 is the rectangle [0, x_i] x [f(x_i), f(x_{i+1})] with
-// x_1 = r > x_2 > ... > x_127 and x_128 = 0. A 31-bit magnitude `mag` in layer i maps to
+// tail beyond r); layer i = 1..255 is the rectangle [0, x_i] x [f(x_i), f(x_{i+1})] with
+// x_1 = r > x_2 > ... > x_255 and x_256 = 0. A 31-bit magnitude `mag` in layer i maps to
 // x = mag * w[i]; it lies under the curve without further tests iff mag < k[i].
-constexpr int kZigLayers = 128;
-constexpr double kZigR = 3.442619855899;            // Marsaglia & Tsang 2000, 128 layers
-constexpr double kZigV = 9.91256303526217e-3;       // area of each layer
+// r solves the construction's closure condition (the top layer has area v) and
+// v = r f(r) + integral_r^inf f; both were computed by bisection to 20 digits.
+constexpr int kZigLayers = 256;
+constexpr double kZigR = 3.6541528853610088;
+constexpr double kZigV = 4.9286732339746553e-3;  // area of each layer
 constexpr float kZigRf = (float)kZigR;
 
 struct ZigTables {
   uint32_t k[kZigLayers];
   float w[kZigLayers];
-  float f[kZigLayers + 1];  // f[i] = exp(-x_i^2/2) for i >= 1, f[128] = 1, f[0] unused
+  float f[kZigLayers + 1];  // f[i] = exp(-x_i^2/2) for i >= 1, f[256] = 1, f[0] unused
 };
+
+// The first-attempt wedge uniform of child c from its pair block (24 bits, see above).
+PC_HD uint32_t pair_wedge_bits(const u32x4& P, uint32_t c) {
+  return c == 0u ? (P.w << 8) : ((P.w & 0xFF000000u) | ((P.z >> 16) << 8));
+}
 
 // A node's private block stream (PURPOSE_CHILD), consumed four words at a time.
 struct ChildStream {
@@ -248,14 +259,17 @@ PC_HD ChildStream child_stream(uint64_t node, uint32_t root, uint32_t k0, uint32
   return s;
 }
 
-// One standard normal variate. (j, layer) is the first attempt; every further word comes
-// from the node's private stream in a fixed order: wedge -> u; tail -> (u1, u2) repeated
-// until accepted; restart -> (j, layer word). `budget` bounds the total number of
-// rejection rounds (each succeeds with probability > 0.9); when it runs out the function
-// returns 0 with budget == 0 so that the caller can report an error instead of spinning.
+// One standard normal variate. (j, layer) is the first attempt; when `have_wedge` is set,
+// `wedge` holds the first attempt's wedge uniform in its top 24 bits. Every further word
+// comes from the node's private stream in a fixed order: tail -> (u1, u2) repeated until
+// accepted; restart -> (j, layer word); wedge of any other attempt -> u. `budget` bounds
+// the total number of rejection rounds (each succeeds with probability > 0.9); when it
+// runs out the function returns 0 with budget == 0 so that the caller can report an
+// error instead of spinning.
 template <class Tables>
-PC_HD float zig_normal(uint32_t j, uint32_t layer, ChildStream& cs, const Tables& T,
-                       uint32_t& budget) {
+PC_HD float zig_normal(uint32_t j, uint32_t layer, bool have_wedge, uint32_t wedge,
+                       ChildStream& cs, const Tables& T, uint32_t& budget) {
+  bool first = have_wedge;
   for (; budget > 0u; --budget) {
     const uint32_t mag = j & 0x7FFFFFFFu;
     const bool neg = (j >> 31) != 0u;
@@ -277,11 +291,12 @@ PC_HD float zig_normal(uint32_t j, uint32_t layer, ChildStream& cs, const Tables
       return neg ? -x : x;
     }
     const float x = fmul((float)mag, T.w[layer]);
-    const float u = unit_closed_open(cs.next());
+    const float u = unit_closed_open(first ? wedge : cs.next());
     const float y = fadd(T.f[layer], fmul(u, fsub(T.f[layer + 1], T.f[layer])));
     if (y < zig_expf(fmul(-0.5f, fmul(x, x)))) return neg ? -x : x;
+    first = false;
     j = cs.next();
-    layer = cs.next() & 127u;
+    layer = cs.next() & 255u;
   }
   return 0.0f;
 }

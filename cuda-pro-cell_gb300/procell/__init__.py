@@ -136,9 +136,9 @@ class Engine:
         return z
 
     def tables(self):
-        k = np.zeros(128, np.uint32)
-        w = np.zeros(128, np.uint32)
-        f = np.zeros(129, np.uint32)
+        k = np.zeros(256, np.uint32)
+        w = np.zeros(256, np.uint32)
+        f = np.zeros(257, np.uint32)
         self._check(self.L.pc_debug_tables(self.ctx, k.ctypes.data_as(_lib.U32P),
                                            w.ctypes.data_as(_lib.U32P), f.ctypes.data_as(_lib.U32P)))
         return k, w.view(np.float32), f.view(np.float32)

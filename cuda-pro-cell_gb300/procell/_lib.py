@@ -11,7 +11,8 @@ import os
 import numpy as np
 
 PKG = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-LIB_PATH = os.path.join(PKG, "build", "libprocell.so")
+# PROCELL_LIB selects another build of the library (e.g. a tuning variant).
+LIB_PATH = os.environ.get("PROCELL_LIB") or os.path.join(PKG, "build", "libprocell.so")
 CLI_PATH = os.path.join(PKG, "build", "procell")
 
 PC_OK = 0

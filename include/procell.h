@@ -155,7 +155,7 @@ void pc_free(void* p);
  * pc_debug_philox: out[4*i..] = Philox4x32-10(ctr[4*i..], key) for i < n.
  * pc_debug_normals: z[i] = first-attempt normal of child (i & 1) of node first_parent+i/2
  *                   under `root` (no truncation), as the division sweep computes it.
- * pc_debug_tables: the device's ziggurat tables (k[128], w bits[128], f bits[129]). */
+ * pc_debug_tables: the device's ziggurat tables (k[256], w bits[256], f bits[257]). */
 int pc_debug_philox(pc_context* ctx, const uint32_t* ctr, uint64_t n, const uint32_t key[2],
                     uint32_t* out);
 int pc_debug_normals(pc_context* ctx, uint64_t seed, uint32_t root, uint64_t first_parent,

@@ -94,31 +94,35 @@ float o_logf(float u) {
 }
 
 // ------------------------------------------------------------ ziggurat tables ------
-// Marsaglia & Tsang (2000) 128-layer construction for the normal density f(x) =
-// exp(-x^2/2): x_1 = r, x_{i+1} = sqrt(-2 ln(v/x_i + f(x_i))), base width v/f(r).
+// Marsaglia & Tsang (2000) construction with 256 layers for the normal density
+// f(x) = exp(-x^2/2): x_1 = r, x_{i+1} = sqrt(-2 ln(v/x_i + f(x_i))), base width v/f(r),
+// with r = 3.6541528853610088 and v = 4.9286732339746553e-3 (the closure of the 256-layer
+// construction, solved numerically).
+const int kLayers = 256;
+
 struct Tables {
-  uint32_t k[128];
-  float w[128];
-  float f[129];
+  uint32_t k[kLayers];
+  float w[kLayers];
+  float f[kLayers + 1];
 };
 
 Tables make_tables() {
-  const double r = 3.442619855899, v = 9.91256303526217e-3, two31 = 2147483648.0;
-  double x[129];
+  const double r = 3.6541528853610088, v = 4.9286732339746553e-3, two31 = 2147483648.0;
+  double x[kLayers + 1];
   x[1] = r;
-  for (int i = 1; i < 127; ++i) x[i + 1] = std::sqrt(-2.0 * std::log(v / x[i] + std::exp(-0.5 * x[i] * x[i])));
-  x[128] = 0.0;
+  for (int i = 1; i < kLayers - 1; ++i) x[i + 1] = std::sqrt(-2.0 * std::log(v / x[i] + std::exp(-0.5 * x[i] * x[i])));
+  x[kLayers] = 0.0;
   const double base = v / std::exp(-0.5 * r * r);
   Tables t;
   t.k[0] = (uint32_t)std::floor(r / base * two31);
   t.w[0] = (float)(base / two31);
   t.f[0] = 0.0f;
-  for (int i = 1; i < 128; ++i) {
+  for (int i = 1; i < kLayers; ++i) {
     t.k[i] = (uint32_t)std::floor(x[i + 1] / x[i] * two31);
     t.w[i] = (float)(x[i] / two31);
     t.f[i] = (float)std::exp(-0.5 * x[i] * x[i]);
   }
-  t.f[128] = 1.0f;
+  t.f[kLayers] = 1.0f;
   return t;
 }
 
@@ -156,10 +160,12 @@ float u24_open_closed(uint32_t w) { return (float)((w >> 8) + 1u) * 5.9604644775
 float u24_closed_open(uint32_t w) { return (float)(w >> 8) * 5.9604644775390625e-8f; }
 
 // One ziggurat normal: fast strip test, else the tail (layer 0) or the wedge test, and a
-// full restart from the node stream when the wedge rejects.
-float ziggurat(uint32_t j, uint32_t layer, NodeStream& ns) {
+// full restart from the node stream when the wedge rejects. The first attempt's wedge
+// uniform comes from the pair block when `have_wedge` is set.
+float ziggurat(uint32_t j, uint32_t layer, bool have_wedge, uint32_t wedge_bits, NodeStream& ns) {
   const Tables& t = tables();
-  const float rf = (float)3.442619855899;
+  const float rf = (float)3.6541528853610088;
+  bool first = have_wedge;
   while (true) {
     const uint32_t mag = j & 0x7FFFFFFFu;
     const float sign = (j & 0x80000000u) ? -1.0f : 1.0f;
@@ -172,30 +178,47 @@ float ziggurat(uint32_t j, uint32_t layer, NodeStream& ns) {
       }
     }
     const float x = (float)mag * t.w[layer];
-    const float u = u24_closed_open(ns.next());
+    const float u = u24_closed_open(first ? wedge_bits : ns.next());
     if (t.f[layer] + u * (t.f[layer + 1] - t.f[layer]) < o_expf(-0.5f * (x * x)))
       return sign * x;
+    first = false;
     j = ns.next();
-    layer = ns.next() & 127u;
+    layer = ns.next() & 255u;
   }
+}
+
+// Pair block of node `parent`: child c's magnitude word, layer byte and wedge bits
+// (child 0: low 24 bits of word 3; child 1: top byte of word 3, top half of word 2).
+struct PairDraw {
+  uint32_t j, layer, wedge;
+};
+
+PairDraw pair_draw(uint64_t parent, uint32_t c, uint32_t root, uint32_t k0, uint32_t k1) {
+  const uint32_t pc[4] = {(uint32_t)parent, (uint32_t)(parent >> 32), root, kPair};
+  uint32_t pw[4];
+  philox_block(pc, k0, k1, pw);
+  PairDraw d;
+  d.j = pw[c];
+  d.layer = (pw[2] >> (8 * c)) & 255u;
+  d.wedge = c == 0 ? (pw[3] << 8) : ((pw[3] & 0xFF000000u) | ((pw[2] >> 16) << 8));
+  return d;
 }
 
 // The division time of child c of node `parent` (restates determine_cell_timer,
 // src/simulation/cell.cu:106-122: tau ~ N(mean, sd) truncated to tau > 0 by rejection).
 double draw_tau(uint64_t parent, uint32_t c, uint32_t root, uint32_t k0, uint32_t k1,
                 double mean, double sd) {
-  const uint32_t pc[4] = {(uint32_t)parent, (uint32_t)(parent >> 32), root, kPair};
-  uint32_t pw[4];
-  philox_block(pc, k0, k1, pw);
-  uint32_t j = pw[c];
-  uint32_t layer = (pw[2] >> (8 * c)) & 127u;
+  const PairDraw p = pair_draw(parent, c, root, k0, k1);
+  uint32_t j = p.j, layer = p.layer;
+  bool have_wedge = true;
   NodeStream ns(2 * parent + c, root, k0, k1);
   while (true) {
-    const float z = ziggurat(j, layer, ns);
+    const float z = ziggurat(j, layer, have_wedge, p.wedge, ns);
     const double tau = std::fma(sd, (double)z, mean);
     if (tau > 0.0) return tau;
+    have_wedge = false;
     j = ns.next();
-    layer = ns.next() & 127u;
+    layer = ns.next() & 255u;
   }
 }
 
@@ -488,11 +511,11 @@ void oracle_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]
 
 void oracle_tables(uint32_t* k, uint32_t* w_bits, uint32_t* f_bits) {
   const Tables& t = tables();
-  for (int i = 0; i < 128; ++i) {
+  for (int i = 0; i < kLayers; ++i) {
     k[i] = t.k[i];
     w_bits[i] = float_to_bits(t.w[i]);
   }
-  for (int i = 0; i < 129; ++i) f_bits[i] = float_to_bits(t.f[i]);
+  for (int i = 0; i <= kLayers; ++i) f_bits[i] = float_to_bits(t.f[i]);
 }
 
 void oracle_normals(uint64_t seed, uint32_t root, uint64_t first_parent, uint64_t count, float* z) {
@@ -500,11 +523,9 @@ void oracle_normals(uint64_t seed, uint32_t root, uint64_t first_parent, uint64_
   for (uint64_t i = 0; i < count; ++i) {
     const uint64_t parent = first_parent + i / 2;
     const uint32_t c = (uint32_t)(i & 1);
-    const uint32_t pc[4] = {(uint32_t)parent, (uint32_t)(parent >> 32), root, kPair};
-    uint32_t pw[4];
-    philox_block(pc, k0, k1, pw);
+    const PairDraw p = pair_draw(parent, c, root, k0, k1);
     NodeStream ns(2 * parent + c, root, k0, k1);
-    z[i] = ziggurat(pw[c], (pw[2] >> (8 * c)) & 127u, ns);
+    z[i] = ziggurat(p.j, p.layer, true, p.wedge, ns);
   }
 }
 

@@ -45,7 +45,7 @@ void oracle_result_free(oracle_result* r);
 
 /* Philox4x32-10 of one counter block. */
 void oracle_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
-/* The FP32 ziggurat tables (k[128], w[128] as bits, f[129] as bits). */
+/* The FP32 ziggurat tables (k[256], w[256] as bits, f[257] as bits). */
 void oracle_tables(uint32_t* k, uint32_t* w_bits, uint32_t* f_bits);
 /* Standard normals drawn for the children of nodes: z[i] is the first-attempt variate of
  * child (i & 1) of parent node (first_parent + i/2) under root `root` (no truncation). */

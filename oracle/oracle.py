@@ -119,9 +119,9 @@ def philox(ctr, key):
 
 def tables():
     L = lib()
-    k = np.zeros(128, np.uint32)
-    w = np.zeros(128, np.uint32)
-    f = np.zeros(129, np.uint32)
+    k = np.zeros(256, np.uint32)
+    w = np.zeros(256, np.uint32)
+    f = np.zeros(257, np.uint32)
     L.oracle_tables(_ptr(k, ctypes.c_uint32), _ptr(w, ctypes.c_uint32), _ptr(f, ctypes.c_uint32))
     return k, w.view(np.float32), f.view(np.float32)
 
