@@ -518,6 +518,8 @@ int pc_plan_run(pc_context* ctx, pc_plan* p) {
   std::memset(&a, 0, sizeof(a));
   a.k0 = (uint32_t)p->seed;
   a.k1 = (uint32_t)(p->seed >> 32);
+  philox_key_schedule(a.k0, a.k1, a.ks);
+  const bool narrow = p->gmax <= 32;
   a.t_max = p->t_max;
   a.t_hi = p->t_hi;
   a.t_lo = p->t_lo;
@@ -558,7 +560,7 @@ int pc_plan_run(pc_context* ctx, pc_plan* p) {
     const uint32_t nseg = (uint32_t)blocks * kWarpsPerBlock;
     LevelOut o{L.cells, L.count, L.prefix, L.ticket, (n + nseg - 1) / nseg};
     PC_CUDA(ctx, cudaEventRecord(ctx->ev[0], st));
-    PC_CUDA(ctx, (cudaError_t)launch_root_sweep(a, 0, n, o, blocks, st));
+    PC_CUDA(ctx, (cudaError_t)launch_root_sweep(a, 0, n, o, blocks, narrow, st));
     PC_CUDA(ctx, cudaEventRecord(ctx->ev[1], st));
     PC_CUDA(ctx, cudaMemcpyAsync(ctx->pinned, L.prefix + nseg, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
     PC_CUDA(ctx, cudaStreamSynchronize(st));
@@ -584,7 +586,7 @@ int pc_plan_run(pc_context* ctx, pc_plan* p) {
       LevelOut lo{Out.cells, Out.count, Out.prefix, Out.ticket, 2 * ((len + oseg - 1) / oseg)};
       const uint32_t gen = top.gen;
       PC_CUDA(ctx, cudaEventRecord(ctx->ev[2], st));
-      PC_CUDA(ctx, (cudaError_t)launch_divide_sweep(a, li, gen, lo, blocks_d, st));
+      PC_CUDA(ctx, (cudaError_t)launch_divide_sweep(a, li, gen, lo, blocks_d, narrow, st));
       PC_CUDA(ctx, cudaEventRecord(ctx->ev[3], st));
       PC_CUDA(ctx, cudaMemcpyAsync(ctx->pinned, Out.prefix + oseg, sizeof(unsigned long long),
                                    cudaMemcpyDeviceToHost, st));

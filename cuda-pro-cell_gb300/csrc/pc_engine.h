@@ -4,10 +4,14 @@
 // Data layout in HBM
 // ------------------
 // * A live cell is 16 bytes: {double due; uint64 key}. `due` is the time at which the
-//   cell is due to divide (the reference's t + timer, proliferation.cu:404-410), and
-//   key = root_local * 2^g + path for a cell of generation g, path being its g
-//   left/right choices from the root. Its heap index (the Philox node address) is
-//   2^g + path. Fluorescence is never stored: it is the bin value halved g times.
+//   cell is due to divide (the reference's t + timer, proliferation.cu:404-410). The key
+//   names the tree node: its root (chunk-local index) and its heap index
+//   node = 2^g + path for a cell of generation g, path being its g left/right choices
+//   from the root (the Philox node address). Two layouts:
+//     narrow (every stored generation <= 31): key = root_local << 32 | node, so the
+//            daughters' keys are key + node + c with 32-bit arithmetic;
+//     wide   (deeper trees):                   key = root_local * 2^g + path.
+//   Fluorescence is never stored: it is the bin value halved g times.
 // * A level buffer holds the cells of one generation that will divide. It is split into
 //   one segment per warp of the kernel that produced it; segment s holds count[s]
 //   cells at cells + s * stride, and prefix[] (nseg + 1 entries, exclusive) is written
@@ -46,6 +50,7 @@ struct TypeDev {
 
 struct RunArgs {
   uint32_t k0, k1;           // seed
+  uint32_t ks[20];           // Philox key schedule of the seed
   double t_max;
   float t_hi, t_lo;          // FP32 band around t_max for the estimate
   int32_t est_ok;            // FP32 estimate allowed (inputs in range)
@@ -81,9 +86,9 @@ struct LevelOut {
 
 // Launchers (pc_kernels.cu). All return the cudaError_t of the launch as int.
 int launch_root_sweep(const RunArgs& a, uint64_t root_lo, uint64_t root_hi, const LevelOut& out,
-                      int blocks, void* stream);
+                      int blocks, bool narrow, void* stream);
 int launch_divide_sweep(const RunArgs& a, const LevelIn& in, uint32_t gen, const LevelOut& out,
-                        int blocks, void* stream);
+                        int blocks, bool narrow, void* stream);
 int launch_debug_philox(const uint32_t* ctr, uint64_t n, uint32_t k0, uint32_t k1, uint32_t* out,
                         void* stream);
 int launch_debug_normals(const ZigTables* zig, uint32_t k0, uint32_t k1, uint32_t root,

@@ -30,7 +30,7 @@ namespace {
 constexpr uint32_t kFull = 0xFFFFFFFFu;
 // Resident blocks per SM the division sweep is compiled for (caps registers per thread).
 #ifndef PC_DIVIDE_MIN_BLOCKS
-#define PC_DIVIDE_MIN_BLOCKS 4
+#define PC_DIVIDE_MIN_BLOCKS 3
 #endif
 constexpr int kDivideMinBlocks = PC_DIVIDE_MIN_BLOCKS;
 
@@ -134,18 +134,23 @@ __device__ __forceinline__ int fate(double birth, float birth_f, float z, const 
   return can_divide ? kEmit : kVanish;
 }
 
-// Warp-aggregated leaf counting: lanes holding leaves of the same (bin, type) add once.
+// Warp-aggregated leaf counting. Lanes hold consecutive cells of a level sorted by root,
+// so equal (bin, type) classes form runs of neighbouring lanes; the first lane of each
+// run adds the run's leaves with one atomic.
 __device__ __forceinline__ void count_leaves(unsigned long long* hist_g, uint32_t cls,
                                              uint32_t nleaf, uint32_t lane) {
-  const uint32_t any = __ballot_sync(kFull, nleaf != 0u);
-  if (any == 0u) return;
-  const uint32_t key = nleaf ? cls : 0xFFFFFFFFu;
-  const uint32_t grp = __match_any_sync(kFull, key);
   const uint32_t b0 = __ballot_sync(kFull, (nleaf & 1u) != 0u);
   const uint32_t b1 = __ballot_sync(kFull, (nleaf & 2u) != 0u);
-  if (nleaf != 0u && (uint32_t)(__ffs(grp) - 1) == lane) {
-    const unsigned long long c = (unsigned long long)(__popc(grp & b0) + 2 * __popc(grp & b1));
-    atomicAdd(hist_g + cls, c);
+  if ((b0 | b1) == 0u) return;
+  const uint32_t key = nleaf ? cls : 0xFFFFFFFFu;
+  const uint32_t prev = __shfl_up_sync(kFull, key, 1);
+  const bool head = lane == 0u || key != prev;
+  const uint32_t heads = __ballot_sync(kFull, head);
+  if (head && nleaf != 0u) {
+    const uint32_t after = heads & ~((2u << lane) - 1u);
+    const uint32_t end_mask = after ? ((1u << (__ffs(after) - 1)) - 1u) : kFull;
+    const uint32_t run = end_mask & ~((1u << lane) - 1u);
+    atomicAdd(hist_g + cls, (unsigned long long)(__popc(run & b0) + 2 * __popc(run & b1)));
   }
 }
 
@@ -207,6 +212,7 @@ __device__ __forceinline__ uint32_t last_le(const unsigned long long* prefix, ui
 }
 
 // ------------------------------------------------------------------ root sweep ------
+template <bool Narrow>
 __global__ void __launch_bounds__(kBlock) k_roots(const RunArgs a, const uint64_t lo,
                                                   const uint64_t hi, const LevelOut out) {
   __shared__ Smem s;
@@ -248,7 +254,7 @@ __global__ void __launch_bounds__(kBlock) k_roots(const RunArgs a, const uint64_
         bin_hi = __ldg(a.bin_start + bin + 1u);
       }
       const uint32_t root = (uint32_t)rg;
-      const u32x4 R = philox(u32x4{0u, 0u, root, kPurposeRoot}, a.k0, a.k1);
+      const u32x4 R = philox_ks(u32x4{0u, 0u, root, kPurposeRoot}, a.ks);
       const double u_type = unit53_closed_open(R.x, R.y);
       const double u_age = unit53_open_closed(R.z, R.w);
       uint32_t ty = a.fallback;
@@ -270,7 +276,7 @@ __global__ void __launch_bounds__(kBlock) k_roots(const RunArgs a, const uint64_
       } else {
         double tau = 0.0;
         if (T.mode == kModeNormal) {
-          const u32x4 P = philox(u32x4{0u, 0u, root, kPurposePair}, a.k0, a.k1);
+          const u32x4 P = philox_ks(u32x4{0u, 0u, root, kPurposePair}, a.ks);
           const float z = draw_z(P.y, (P.z >> 8) & 255u, pair_wedge_bits(P, 1u), 1ull, root, a.k0,
                                  a.k1, T, s.zig, a.error);
           tau = fma(T.sigma, f32_to_f64(z), T.mu);
@@ -293,7 +299,8 @@ __global__ void __launch_bounds__(kBlock) k_roots(const RunArgs a, const uint64_
     const uint32_t em = __ballot_sync(kFull, f == kEmit);
     if (f == kEmit) {
       const uint32_t pos = __popc(em & ((1u << lane) - 1u));
-      ob[out_n + pos] = make_ulonglong2((unsigned long long)__double_as_longlong(d0), rl);
+      const unsigned long long key = Narrow ? ((unsigned long long)rl << 32) | 1ull : rl;
+      ob[out_n + pos] = make_ulonglong2((unsigned long long)__double_as_longlong(d0), key);
     }
     out_n += __popc(em);
   }
@@ -326,23 +333,64 @@ struct Cursor {
   }
 };
 
+// Daughters whose first ziggurat attempt is not accepted by the strip test (about 1.5%)
+// wait in a per-warp queue until 32 are pending; the warp then draws them together with
+// every lane busy instead of stalling 31 lanes behind one. 96 entries hold the 31 left
+// over plus the 64 a step can add.
+constexpr int kQueue = 96;
+struct DeferQueue {
+  double birth[kQueue];
+  unsigned long long key[kQueue];  // the daughter's own key
+  uint32_t j[kQueue];              // first-attempt magnitude word
+  uint32_t lw[kQueue];             // first-attempt wedge bits (top 24) | layer (low 8)
+  uint32_t cls[kQueue];            // histogram class
+  uint32_t meta[kQueue];           // type | can_divide << 8 | clamped << 9
+};
+
+// Leaf counts of one block in shared memory: a window of classes starting at the class of
+// the block's first cell (its input is sorted by root, so its classes are few and
+// contiguous); classes outside the window go straight to global memory.
+constexpr uint32_t kHistWindow = 2048;
+
+struct DivideSmem {
+  DeferQueue q[kWarpsPerBlock];
+  uint32_t hist[kHistWindow];
+  uint32_t base;
+};
+
+__device__ __forceinline__ void add_leaves(DivideSmem& sm, unsigned long long* hist_g, uint32_t cls,
+                                           uint32_t n) {
+  const uint32_t i = cls - sm.base;
+  if (i < kHistWindow)
+    atomicAdd(&sm.hist[i], n);
+  else
+    atomicAdd(hist_g + cls, (unsigned long long)n);
+}
+
+template <bool Narrow>
+__device__ __forceinline__ void decode(uint64_t key, uint32_t g, uint64_t& rl, uint64_t& node) {
+  if (Narrow) {
+    rl = key >> 32;
+    node = (uint32_t)key;
+  } else {
+    rl = key >> g;
+    node = (1ull << g) | (key & ((1ull << g) - 1ull));
+  }
+}
+
+template <bool Narrow>
 __global__ void __launch_bounds__(kBlock, kDivideMinBlocks) k_divide(const RunArgs a, const LevelIn in,
                                                                      const uint32_t g, const LevelOut out) {
   __shared__ Smem s;
+  __shared__ DivideSmem sm;
   stage(s, a);
-  __syncthreads();
-  const uint32_t lane = threadIdx.x & 31u;
-  const uint32_t wg = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
+  for (uint32_t i = threadIdx.x; i < kHistWindow; i += blockDim.x) sm.hist[i] = 0u;
+  const uint32_t lane = threadIdx.x & 31u, wib = threadIdx.x >> 5;
+  const uint32_t wg = blockIdx.x * kWarpsPerBlock + wib;
   const uint32_t nw = gridDim.x * kWarpsPerBlock;
   const uint64_t len = in.hi - in.lo;
   const uint64_t va = in.lo + len * wg / nw, vb = in.lo + len * (wg + 1u) / nw;
-  ulonglong2* ob = out.cells + (uint64_t)wg * out.stride;
-  uint64_t out_n = 0;
-  unsigned long long vanished = 0;
-  uint32_t depth_error = 0;
   const uint32_t g1 = g + 1u;
-  const uint64_t gmask = (1ull << g) - 1ull;
-  unsigned long long* hist_g1 = a.hist + (uint64_t)g1 * a.nbins * a.ntypes;
   Cursor cur{in.cells, in.prefix, in.stride, 0u, 0ull, 0ull};
   ulonglong2 next = make_ulonglong2(0ull, 0ull);
   if (va < vb) {
@@ -351,27 +399,86 @@ __global__ void __launch_bounds__(kBlock, kDivideMinBlocks) k_divide(const RunAr
     cur.seg_hi = __ldg(in.prefix + cur.seg + 1u);
     if (va + lane < vb) next = cur.load(va + lane);
   }
+  if (threadIdx.x == 0) {
+    // histogram window: from the class of the block's first bin
+    const uint64_t b0 = in.lo + len * (blockIdx.x * kWarpsPerBlock) / nw;
+    uint32_t base = 0u;
+    if (b0 < in.hi) {
+      Cursor c0{in.cells, in.prefix, in.stride, last_le(in.prefix, in.nseg, b0), 0ull, 0ull};
+      c0.seg_lo = __ldg(in.prefix + c0.seg);
+      c0.seg_hi = __ldg(in.prefix + c0.seg + 1u);
+      uint64_t rl, node;
+      decode<Narrow>(c0.load(b0).y, g, rl, node);
+      const unsigned long long rec = __ldg(a.root_rec + rl);
+      base = (uint32_t)rec - ((uint32_t)(rec >> 32) & 0xFFu);
+    }
+    sm.base = base;
+  }
+  __syncthreads();
+
+  DeferQueue& q = sm.q[wib];
+  uint32_t qn = 0;
+  ulonglong2* ob = out.cells + (uint64_t)wg * out.stride;
+  uint64_t out_n = 0;
+  unsigned long long vanished = 0;
+  uint32_t depth_error = 0;
+  unsigned long long* hist_g1 = a.hist + (uint64_t)g1 * a.nbins * a.ntypes;
+  const uint32_t lt = (1u << lane) - 1u;
+
+  // Resolve the queued daughters in [qn - cnt, qn): one per lane, lanes >= cnt idle.
+  auto drain = [&](uint32_t cnt) {
+    int f = kNone;
+    double due = 0.0;
+    unsigned long long key = 0ull;
+    if (lane < cnt) {
+      const uint32_t e = qn - cnt + lane;
+      key = q.key[e];
+      const double birth = q.birth[e];
+      const uint32_t meta = q.meta[e], cls = q.cls[e], lw = q.lw[e];
+      uint64_t rl, node;
+      decode<Narrow>(key, g1, rl, node);
+      const uint32_t root = (uint32_t)(a.root_base + rl);
+      const TypeDev& T = s.types[meta & 0xFFu];
+      const bool can_divide = (meta >> 8) & 1u;
+      const float z = slow_z(q.j[e], lw & 0xFFu, lw & 0xFFFFFF00u, node, root, a.k0, a.k1, T, s.zig, a.error);
+      f = fate(birth, f64_to_f32_rz(birth), z, T, a, can_divide, due);
+      if (f == kLeaf) add_leaves(sm, hist_g1, cls, 1u);
+      if (f == kVanish) {
+        ++vanished;
+        if ((meta >> 9) & 1u) depth_error = 1u;
+      }
+    }
+    const uint32_t em = __ballot_sync(kFull, f == kEmit);
+    if (f == kEmit) ob[out_n + __popc(em & lt)] = make_ulonglong2((unsigned long long)__double_as_longlong(due), key);
+    out_n += __popc(em);
+    qn -= cnt;
+    __syncwarp();
+  };
+
   for (uint64_t v0 = va; v0 < vb; v0 += 32u) {
     const bool act = v0 + lane < vb;
     const ulonglong2 c = next;
     // prefetch the next step's cell while this one is processed
     if (v0 + 32u + lane < vb) next = cur.load(v0 + 32u + lane);
     int f0 = kNone, f1 = kNone;
-    double due0 = 0.0, due1 = 0.0;
+    bool q0 = false, q1 = false;
+    double due0 = 0.0, due1 = 0.0, d = 0.0;
     const uint64_t key = c.y;
-    uint32_t nleaf = 0, cls = 0;
+    uint32_t cls = 0, ty = 0, meta = 0;
+    u32x4 P = {0u, 0u, 0u, 0u};
     if (act) {
-      const double d = __longlong_as_double((long long)c.x);
-      const uint64_t rl = key >> g;
+      d = __longlong_as_double((long long)c.x);
+      uint64_t rl, node;
+      decode<Narrow>(key, g, rl, node);
       const unsigned long long rec = __ldg(a.root_rec + rl);  // consumed after Philox
-      const uint64_t node = (1ull << g) | (key & gmask);
       const uint32_t root = (uint32_t)(a.root_base + rl);
-      const u32x4 P = philox(u32x4{(uint32_t)node, (uint32_t)(node >> 32), root, kPurposePair}, a.k0, a.k1);
+      P = philox_ks(u32x4{(uint32_t)node, (uint32_t)(node >> 32), root, kPurposePair}, a.ks);
       cls = (uint32_t)rec;
-      const uint32_t ty = (uint32_t)(rec >> 32) & 0xFFu;
+      ty = (uint32_t)(rec >> 32) & 0xFFu;
       const uint32_t cap = (uint32_t)(rec >> 40) & 0xFFu;
-      const bool clamped = ((rec >> 49) & 1ull) != 0ull;
+      const bool clamped = ((rec >> 49) & 1ull) != 0ull && g1 == cap;
       const bool can_divide = g1 < cap;
+      meta = ty | (can_divide ? 0x100u : 0u) | (clamped ? 0x200u : 0u);
       const TypeDev& T = s.types[ty];
       if (T.mode == kModeZeroMean) {
         // tau == 0: the daughters are due at the parent's own due time
@@ -379,29 +486,62 @@ __global__ void __launch_bounds__(kBlock, kDivideMinBlocks) k_divide(const RunAr
         due1 = d;
         f0 = f1 = gt_nonneg(d, a.t_max) ? kLeaf : (can_divide ? kEmit : kVanish);
       } else {
-        const float z0 = draw_z(P.x, P.z & 255u, pair_wedge_bits(P, 0u), 2ull * node, root, a.k0,
-                                a.k1, T, s.zig, a.error);
-        const float z1 = draw_z(P.y, (P.z >> 8) & 255u, pair_wedge_bits(P, 1u), 2ull * node + 1ull,
-                                root, a.k0, a.k1, T, s.zig, a.error);
         const float df = f64_to_f32_rz(d);
-        f0 = fate(d, df, z0, T, a, can_divide, due0);
-        f1 = fate(d, df, z1, T, a, can_divide, due1);
+        const uint32_t m0 = P.x & 0x7FFFFFFFu, l0 = P.z & 255u;
+        const uint32_t m1 = P.y & 0x7FFFFFFFu, l1 = (P.z >> 8) & 255u;
+        if (m0 < s.zig.k[l0]) {
+          const float x = __fmul_rn((float)m0, s.zig.w[l0]);
+          const float z = (P.x >> 31) ? -x : x;
+          if (z >= T.zlo && z <= T.zhi) f0 = fate(d, df, z, T, a, can_divide, due0);
+        }
+        if (m1 < s.zig.k[l1]) {
+          const float x = __fmul_rn((float)m1, s.zig.w[l1]);
+          const float z = (P.y >> 31) ? -x : x;
+          if (z >= T.zlo && z <= T.zhi) f1 = fate(d, df, z, T, a, can_divide, due1);
+        }
+        q0 = f0 == kNone;
+        q1 = f1 == kNone;
       }
-      if (clamped && g1 == cap && (f0 == kVanish || f1 == kVanish)) depth_error = 1u;
-      nleaf = (f0 == kLeaf ? 1u : 0u) + (f1 == kLeaf ? 1u : 0u);
+      if (clamped && (f0 == kVanish || f1 == kVanish)) depth_error = 1u;
+      const uint32_t nleaf = (f0 == kLeaf ? 1u : 0u) + (f1 == kLeaf ? 1u : 0u);
+      if (nleaf) add_leaves(sm, hist_g1, cls, nleaf);
       vanished += (f0 == kVanish ? 1u : 0u) + (f1 == kVanish ? 1u : 0u);
     }
-    count_leaves(hist_g1, cls, nleaf, lane);
+    // daughters' keys: narrow root << 32 | (2 node + c), wide 2 key + c
+    const unsigned long long kd = Narrow ? key + (uint32_t)key : 2ull * key;
     const uint32_t e0 = __ballot_sync(kFull, f0 == kEmit);
     const uint32_t e1 = __ballot_sync(kFull, f1 == kEmit);
-    const uint32_t lt = (1u << lane) - 1u;
     ulonglong2* dst = ob + out_n + __popc(e0 & lt) + __popc(e1 & lt);
-    if (f0 == kEmit) dst[0] = make_ulonglong2((unsigned long long)__double_as_longlong(due0), 2ull * key);
-    if (f1 == kEmit)
-      dst[f0 == kEmit ? 1 : 0] =
-          make_ulonglong2((unsigned long long)__double_as_longlong(due1), 2ull * key + 1ull);
+    if (f0 == kEmit) dst[0] = make_ulonglong2((unsigned long long)__double_as_longlong(due0), kd);
+    if (f1 == kEmit) dst[f0 == kEmit ? 1 : 0] = make_ulonglong2((unsigned long long)__double_as_longlong(due1), kd + 1ull);
     out_n += __popc(e0) + __popc(e1);
+    // queue the daughters the strip test did not settle
+    const uint32_t d0m = __ballot_sync(kFull, q0), d1m = __ballot_sync(kFull, q1);
+    if (d0m | d1m) {
+      uint32_t e = qn + __popc(d0m & lt) + __popc(d1m & lt);
+      if (q0) {
+        q.birth[e] = d;
+        q.key[e] = kd;
+        q.j[e] = P.x;
+        q.lw[e] = (P.w << 8) | (P.z & 255u);
+        q.cls[e] = cls;
+        q.meta[e] = meta;
+        ++e;
+      }
+      if (q1) {
+        q.birth[e] = d;
+        q.key[e] = kd + 1ull;
+        q.j[e] = P.y;
+        q.lw[e] = ((P.w & 0xFF000000u) | ((P.z >> 16) << 8)) | ((P.z >> 8) & 255u);
+        q.cls[e] = cls;
+        q.meta[e] = meta;
+      }
+      qn += __popc(d0m) + __popc(d1m);
+      __syncwarp();
+      while (qn >= 32u) drain(32u);
+    }
   }
+  if (qn) drain(qn);
   vanished = warp_sum(vanished);
   depth_error = __reduce_or_sync(kFull, depth_error);
   if (lane == 0) {
@@ -409,6 +549,12 @@ __global__ void __launch_bounds__(kBlock, kDivideMinBlocks) k_divide(const RunAr
     if (vanished) atomicAdd(a.stats + 0, vanished);
     if (depth_error) atomicOr(a.error, 1u);
     __threadfence();
+  }
+  __syncthreads();
+  const uint32_t nclass = a.nbins * a.ntypes;
+  for (uint32_t i = threadIdx.x; i < kHistWindow; i += blockDim.x) {
+    const uint32_t c = sm.hist[i];
+    if (c && sm.base + i < nclass) atomicAdd(hist_g1 + sm.base + i, (unsigned long long)c);
   }
   finish_level(out, nw);
 }
@@ -444,14 +590,20 @@ __global__ void k_debug_normals(const ZigTables* zig, uint32_t k0, uint32_t k1, 
 }  // namespace
 
 int launch_root_sweep(const RunArgs& a, uint64_t root_lo, uint64_t root_hi, const LevelOut& out,
-                      int blocks, void* stream) {
-  k_roots<<<blocks, kBlock, 0, (cudaStream_t)stream>>>(a, root_lo, root_hi, out);
+                      int blocks, bool narrow, void* stream) {
+  if (narrow)
+    k_roots<true><<<blocks, kBlock, 0, (cudaStream_t)stream>>>(a, root_lo, root_hi, out);
+  else
+    k_roots<false><<<blocks, kBlock, 0, (cudaStream_t)stream>>>(a, root_lo, root_hi, out);
   return (int)cudaGetLastError();
 }
 
 int launch_divide_sweep(const RunArgs& a, const LevelIn& in, uint32_t gen, const LevelOut& out,
-                        int blocks, void* stream) {
-  k_divide<<<blocks, kBlock, 0, (cudaStream_t)stream>>>(a, in, gen, out);
+                        int blocks, bool narrow, void* stream) {
+  if (narrow)
+    k_divide<true><<<blocks, kBlock, 0, (cudaStream_t)stream>>>(a, in, gen, out);
+  else
+    k_divide<false><<<blocks, kBlock, 0, (cudaStream_t)stream>>>(a, in, gen, out);
   return (int)cudaGetLastError();
 }
 
@@ -472,9 +624,13 @@ int launch_debug_normals(const ZigTables* zig, uint32_t k0, uint32_t k1, uint32_
 }
 
 int occupancy_blocks_per_sm(int* root_blocks, int* divide_blocks) {
-  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(root_blocks, k_roots, kBlock, 0);
-  if (e != cudaSuccess) return (int)e;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(divide_blocks, k_divide, kBlock, 0);
+  int r1 = 0, r2 = 0, d1 = 0, d2 = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r1, k_roots<true>, kBlock, 0);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r2, k_roots<false>, kBlock, 0);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d1, k_divide<true>, kBlock, 0);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d2, k_divide<false>, kBlock, 0);
+  *root_blocks = r1 < r2 ? r1 : r2;
+  *divide_blocks = d1 < d2 ? d1 : d2;
   return (int)e;
 }
 

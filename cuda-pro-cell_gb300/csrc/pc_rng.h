@@ -88,6 +88,32 @@ PC_HD u32x4 philox(u32x4 c, uint32_t k0, uint32_t k1) {
   return c;
 }
 
+// Philox with a precomputed key schedule ks[2i], ks[2i+1] = key + i * (W0, W1): the same
+// function as philox(); in a kernel whose parameters hold `ks`, every key word becomes an
+// immediate constant-bank operand of the XORs.
+PC_HD u32x4 philox_ks(u32x4 c, const uint32_t* ks) {
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
+  for (int i = 0; i < 10; ++i) {
+    uint32_t hi0, lo0, hi1, lo1;
+    mulhilo32(kPhiloxM0, c.x, hi0, lo0);
+    mulhilo32(kPhiloxM1, c.z, hi1, lo1);
+    const u32x4 n = {hi1 ^ c.y ^ ks[2 * i], lo1, hi0 ^ c.w ^ ks[2 * i + 1], lo0};
+    c = n;
+  }
+  return c;
+}
+
+PC_HD void philox_key_schedule(uint32_t k0, uint32_t k1, uint32_t* ks) {
+  for (int i = 0; i < 10; ++i) {
+    ks[2 * i] = k0;
+    ks[2 * i + 1] = k1;
+    k0 += kPhiloxW0;
+    k1 += kPhiloxW1;
+  }
+}
+
 // ---- IEEE round-to-nearest FP32 helpers (no contraction on either side) -------------
 PC_HD float fmul(float a, float b) {
 #if defined(__CUDA_ARCH__)
