@@ -30,7 +30,7 @@ namespace {
 constexpr uint32_t kFull = 0xFFFFFFFFu;
 // Resident blocks per SM the division sweep is compiled for (caps registers per thread).
 #ifndef PC_DIVIDE_MIN_BLOCKS
-#define PC_DIVIDE_MIN_BLOCKS 3
+#define PC_DIVIDE_MIN_BLOCKS 4
 #endif
 constexpr int kDivideMinBlocks = PC_DIVIDE_MIN_BLOCKS;
 
@@ -162,9 +162,8 @@ __device__ __forceinline__ unsigned long long warp_sum(unsigned long long v) {
 
 // The last block to finish turns the per-warp output counts into the exclusive prefix
 // the next sweep reads (the threadfence/ticket pattern; no block waits on another).
-__device__ void finish_level(const LevelOut& out, uint32_t nseg) {
+__device__ void finish_level(const LevelOut& out, uint32_t nseg, unsigned long long* s_sum) {
   __shared__ int s_last;
-  __shared__ unsigned long long s_sum[kBlock];
   __syncthreads();
   if (threadIdx.x == 0) {
     __threadfence();
@@ -216,6 +215,7 @@ template <bool Narrow>
 __global__ void __launch_bounds__(kBlock) k_roots(const RunArgs a, const uint64_t lo,
                                                   const uint64_t hi, const LevelOut out) {
   __shared__ Smem s;
+  __shared__ unsigned long long s_scan[kBlock];
   stage(s, a);
   __syncthreads();
   const uint32_t lane = threadIdx.x & 31u;
@@ -312,48 +312,26 @@ __global__ void __launch_bounds__(kBlock) k_roots(const RunArgs a, const uint64_
     if (uncounted) atomicAdd(a.stats + 1, uncounted);
     __threadfence();
   }
-  finish_level(out, nw);
+  finish_level(out, nw, s_scan);
 }
 
 // -------------------------------------------------------------- division sweep ------
-// Segment cursor over an input level: maps a virtual index to its cell, moving forward.
-struct Cursor {
-  const ulonglong2* cells;
-  const unsigned long long* prefix;
-  uint64_t stride;
-  uint32_t seg;
-  uint64_t seg_lo, seg_hi;
-  __device__ __forceinline__ ulonglong2 load(uint64_t v) {
-    while (v >= seg_hi) {
-      ++seg;
-      seg_lo = seg_hi;
-      seg_hi = __ldg(prefix + seg + 1u);
-    }
-    return __ldg(cells + (uint64_t)seg * stride + (v - seg_lo));
-  }
-};
-
-// Daughters whose first ziggurat attempt is not accepted by the strip test (about 1.5%)
-// wait in a per-warp queue until 32 are pending; the warp then draws them together with
-// every lane busy instead of stalling 31 lanes behind one. 96 entries hold the 31 left
-// over plus the 64 a step can add.
-constexpr int kQueue = 96;
-struct DeferQueue {
-  double birth[kQueue];
-  unsigned long long key[kQueue];  // the daughter's own key
-  uint32_t j[kQueue];              // first-attempt magnitude word
-  uint32_t lw[kQueue];             // first-attempt wedge bits (top 24) | layer (low 8)
-  uint32_t cls[kQueue];            // histogram class
-  uint32_t meta[kQueue];           // type | can_divide << 8 | clamped << 9
-};
+// Each warp owns a contiguous slice of n input cells and an output segment of 2n slots.
+// The main loop settles each daughter from its first-attempt normal: a leaf (counted
+// into the histogram, never stored), a vanished cell, or a dividing cell whose exact FP64
+// due time is written to the front of the segment. Daughters whose first attempt is not
+// accepted by the ziggurat strip test (about 1.5%) are written as (birth, key) to the back
+// of the segment and resolved after the main loop, 32 at a time with every lane busy;
+// their first-attempt bits are re-derived from the parent's Philox block. The rejection
+// path thus costs the main loop neither registers nor idle lanes. Resolved cells are
+// appended to the front; each input cell contributes at most two cells to front + back.
 
 // Leaf counts of one block in shared memory: a window of classes starting at the class of
-// the block's first cell (its input is sorted by root, so its classes are few and
-// contiguous); classes outside the window go straight to global memory.
+// the block's first cell (its input comes from a level sorted by root, so its classes are
+// few and close together); classes outside the window go straight to global memory.
 constexpr uint32_t kHistWindow = 2048;
 
 struct DivideSmem {
-  DeferQueue q[kWarpsPerBlock];
   uint32_t hist[kHistWindow];
   uint32_t base;
 };
@@ -383,32 +361,25 @@ __global__ void __launch_bounds__(kBlock, kDivideMinBlocks) k_divide(const RunAr
                                                                      const uint32_t g, const LevelOut out) {
   __shared__ Smem s;
   __shared__ DivideSmem sm;
+  __shared__ unsigned long long s_scan[kBlock];
   stage(s, a);
   for (uint32_t i = threadIdx.x; i < kHistWindow; i += blockDim.x) sm.hist[i] = 0u;
-  const uint32_t lane = threadIdx.x & 31u, wib = threadIdx.x >> 5;
-  const uint32_t wg = blockIdx.x * kWarpsPerBlock + wib;
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t wg = blockIdx.x * kWarpsPerBlock + (threadIdx.x >> 5);
   const uint32_t nw = gridDim.x * kWarpsPerBlock;
   const uint64_t len = in.hi - in.lo;
-  const uint64_t va = in.lo + len * wg / nw, vb = in.lo + len * (wg + 1u) / nw;
+  const uint64_t va = in.lo + len * wg / nw;
+  const uint32_t n = (uint32_t)(in.lo + len * (wg + 1u) / nw - va);  // cells of this warp
   const uint32_t g1 = g + 1u;
-  Cursor cur{in.cells, in.prefix, in.stride, 0u, 0ull, 0ull};
-  ulonglong2 next = make_ulonglong2(0ull, 0ull);
-  if (va < vb) {
-    cur.seg = last_le(in.prefix, in.nseg, va);
-    cur.seg_lo = __ldg(in.prefix + cur.seg);
-    cur.seg_hi = __ldg(in.prefix + cur.seg + 1u);
-    if (va + lane < vb) next = cur.load(va + lane);
-  }
   if (threadIdx.x == 0) {
     // histogram window: from the class of the block's first bin
     const uint64_t b0 = in.lo + len * (blockIdx.x * kWarpsPerBlock) / nw;
     uint32_t base = 0u;
     if (b0 < in.hi) {
-      Cursor c0{in.cells, in.prefix, in.stride, last_le(in.prefix, in.nseg, b0), 0ull, 0ull};
-      c0.seg_lo = __ldg(in.prefix + c0.seg);
-      c0.seg_hi = __ldg(in.prefix + c0.seg + 1u);
+      const uint32_t sg = last_le(in.prefix, in.nseg, b0);
+      const ulonglong2 c0 = __ldg(in.cells + (uint64_t)sg * in.stride + (b0 - __ldg(in.prefix + sg)));
       uint64_t rl, node;
-      decode<Narrow>(c0.load(b0).y, g, rl, node);
+      decode<Narrow>(c0.y, g, rl, node);
       const unsigned long long rec = __ldg(a.root_rec + rl);
       base = (uint32_t)rec - ((uint32_t)(rec >> 32) & 0xFFu);
     }
@@ -416,147 +387,155 @@ __global__ void __launch_bounds__(kBlock, kDivideMinBlocks) k_divide(const RunAr
   }
   __syncthreads();
 
-  DeferQueue& q = sm.q[wib];
-  uint32_t qn = 0;
-  ulonglong2* ob = out.cells + (uint64_t)wg * out.stride;
-  uint64_t out_n = 0;
-  unsigned long long vanished = 0;
-  uint32_t depth_error = 0;
-  unsigned long long* hist_g1 = a.hist + (uint64_t)g1 * a.nbins * a.ntypes;
-  const uint32_t lt = (1u << lane) - 1u;
+  // Segment cursor in warp-relative indices: input cells [.., hi_rel) of segment `seg`
+  // start at seg_ptr + index.
+  uint32_t seg = 0, hi_rel = 0;
+  const ulonglong2* seg_ptr = in.cells;
+  unsigned long long seg_hi_abs = 0ull;
+  auto locate = [&](uint32_t i) -> const ulonglong2* {
+    while (i >= hi_rel) {
+      const unsigned long long lo_abs = seg_hi_abs;
+      ++seg;
+      seg_hi_abs = __ldg(in.prefix + seg + 1u);
+      seg_ptr = in.cells + (uint64_t)seg * in.stride - (lo_abs - va);
+      hi_rel = (uint32_t)min(seg_hi_abs - va, (unsigned long long)n);
+    }
+    return seg_ptr + i;
+  };
+  ulonglong2 next = make_ulonglong2(0ull, 0ull);
+  if (n) {
+    seg = last_le(in.prefix, in.nseg, va);
+    const unsigned long long lo_abs = __ldg(in.prefix + seg);
+    seg_hi_abs = __ldg(in.prefix + seg + 1u);
+    seg_ptr = in.cells + (uint64_t)seg * in.stride - (lo_abs - va);
+    hi_rel = (uint32_t)min(seg_hi_abs - va, (unsigned long long)n);
+    if (lane < n) next = __ldg(locate(lane));
+  }
 
-  // Resolve the queued daughters in [qn - cnt, qn): one per lane, lanes >= cnt idle.
-  auto drain = [&](uint32_t cnt) {
+  ulonglong2* const ob = out.cells + (uint64_t)wg * out.stride;
+  ulonglong2* const back = ob + 2u * n;  // pending daughters at back[-1], back[-2], ...
+  const uint32_t lt = (1u << lane) - 1u;
+  uint32_t front = 0, pending = 0, vanished = 0, depth_error = 0;
+  unsigned long long* const hist_g1 = a.hist + (uint64_t)g1 * a.nbins * a.ntypes;
+  const bool eok = a.est_ok != 0;
+
+  for (uint32_t i0 = 0; i0 < n; i0 += 32u) {
+    const bool act = i0 + lane < n;
+    const ulonglong2 c = next;
+    // prefetch the next step's cell while this one is processed
+    if (i0 + 32u + lane < n) next = __ldg(locate(i0 + 32u + lane));
+    const double d = __longlong_as_double((long long)c.x);
+    uint64_t rl, node;
+    decode<Narrow>(c.y, g, rl, node);
+    const unsigned long long rec = act ? __ldg(a.root_rec + rl) : 0ull;  // consumed after Philox
+    const u32x4 P = philox_ks(u32x4{(uint32_t)node, (uint32_t)(node >> 32), (uint32_t)(a.root_base + rl),
+                                    kPurposePair}, a.ks);
+    const uint32_t ty = (uint32_t)(rec >> 32) & 0xFFu;
+    const uint32_t cap = (uint32_t)(rec >> 40) & 0xFFu;
+    const bool can_divide = g1 < cap;
+    const TypeDev& T = s.types[ty];
+    const bool zero_mean = T.mode == kModeZeroMean;  // tau == 0: no draw, due = birth
+    // first attempts of both daughters: strip test, truncation bounds
+    const uint32_t l0 = P.z & 255u, l1 = (P.z >> 8) & 255u;
+    float z0 = __fmul_rn((float)(P.x & 0x7FFFFFFFu), s.zig.w[l0]);
+    float z1 = __fmul_rn((float)(P.y & 0x7FFFFFFFu), s.zig.w[l1]);
+    z0 = zero_mean ? 0.0f : ((P.x >> 31) ? -z0 : z0);
+    z1 = zero_mean ? 0.0f : ((P.y >> 31) ? -z1 : z1);
+    const bool ok0 = act && (zero_mean || ((P.x & 0x7FFFFFFFu) < s.zig.k[l0] && z0 >= T.zlo && z0 <= T.zhi));
+    const bool ok1 = act && (zero_mean || ((P.y & 0x7FFFFFFFu) < s.zig.k[l1] && z1 >= T.zlo && z1 <= T.zhi));
+    // FP32 estimates settle clear leaves and clear non-leaves
+    const float df = f64_to_f32_rz(d);
+    const float est0 = __fadd_rn(df, __fadd_rn(T.mu_f, __fmul_rn(T.sigma_f, z0)));
+    const float est1 = __fadd_rn(df, __fadd_rn(T.mu_f, __fmul_rn(T.sigma_f, z1)));
+    const bool sure0 = eok && est0 < a.t_lo, sure1 = eok && est1 < a.t_lo;
+    bool leaf0 = ok0 && eok && est0 > a.t_hi, leaf1 = ok1 && eok && est1 > a.t_hi;
+    // exact FP64 due times where a daughter will be stored or is inside the band
+    double due0 = 0.0, due1 = 0.0;
+    const bool x0 = ok0 && !leaf0 && (can_divide || !sure0), x1 = ok1 && !leaf1 && (can_divide || !sure1);
+    if (x0) due0 = d + fma(T.sigma, f32_to_f64(z0), T.mu);
+    if (x1) due1 = d + fma(T.sigma, f32_to_f64(z1), T.mu);
+    leaf0 = leaf0 || (x0 && !sure0 && gt_nonneg(due0, a.t_max));
+    leaf1 = leaf1 || (x1 && !sure1 && gt_nonneg(due1, a.t_max));
+    const bool em0 = ok0 && !leaf0 && can_divide, em1 = ok1 && !leaf1 && can_divide;
+    const bool van0 = ok0 && !leaf0 && !can_divide, van1 = ok1 && !leaf1 && !can_divide;
+    const uint32_t nleaf = (leaf0 ? 1u : 0u) + (leaf1 ? 1u : 0u);
+    if (nleaf) add_leaves(sm, hist_g1, (uint32_t)rec, nleaf);
+    vanished += (van0 ? 1u : 0u) + (van1 ? 1u : 0u);
+    if (((rec >> 49) & 1ull) && g1 == cap && (van0 || van1)) depth_error = 1u;
+    // daughters' keys: narrow root << 32 | (2 node + c), wide 2 key + c
+    const unsigned long long kd = Narrow ? c.y + (uint32_t)c.y : 2ull * c.y;
+    const uint32_t e0 = __ballot_sync(kFull, em0), e1 = __ballot_sync(kFull, em1);
+    ulonglong2* dst = ob + front + __popc(e0 & lt) + __popc(e1 & lt);
+    if (em0) dst[0] = make_ulonglong2((unsigned long long)__double_as_longlong(due0), kd);
+    if (em1) dst[em0 ? 1 : 0] = make_ulonglong2((unsigned long long)__double_as_longlong(due1), kd + 1ull);
+    front += __popc(e0) + __popc(e1);
+    // daughters the strip test did not settle: park (birth, key) at the back
+    const bool sl0 = act && !ok0, sl1 = act && !ok1;
+    const uint32_t p0 = __ballot_sync(kFull, sl0), p1 = __ballot_sync(kFull, sl1);
+    if (p0 | p1) {
+      ulonglong2* pd = back - 1u - pending - __popc(p0 & lt) - __popc(p1 & lt);
+      if (sl0) pd[0] = make_ulonglong2((unsigned long long)__double_as_longlong(d), kd);
+      if (sl1) *(pd - (sl0 ? 1 : 0)) = make_ulonglong2((unsigned long long)__double_as_longlong(d), kd + 1ull);
+      pending += __popc(p0) + __popc(p1);
+    }
+  }
+
+  // Resolve the parked daughters, 32 at a time: re-derive the first attempt from the
+  // parent's pair block, draw with the rejection path, settle exactly, append to the front.
+  // Rounds take the records nearest the front first (the last parked): front + pending
+  // <= 2n, so a round's writes, at most one per record resolved so far, stay below every
+  // record not yet read.
+  __syncwarp();
+  for (uint32_t hi = pending; hi > 0u;) {
+    const uint32_t lo = hi > 32u ? hi - 32u : 0u;
+    const bool act = lo + lane < hi;
     int f = kNone;
     double due = 0.0;
     unsigned long long key = 0ull;
-    if (lane < cnt) {
-      const uint32_t e = qn - cnt + lane;
-      key = q.key[e];
-      const double birth = q.birth[e];
-      const uint32_t meta = q.meta[e], cls = q.cls[e], lw = q.lw[e];
+    if (act) {
+      const ulonglong2 pc = back[-1 - (int64_t)(lo + lane)];
+      key = pc.y;
+      const double birth = __longlong_as_double((long long)pc.x);
       uint64_t rl, node;
       decode<Narrow>(key, g1, rl, node);
+      const unsigned long long rec = __ldg(a.root_rec + rl);
       const uint32_t root = (uint32_t)(a.root_base + rl);
-      const TypeDev& T = s.types[meta & 0xFFu];
-      const bool can_divide = (meta >> 8) & 1u;
-      const float z = slow_z(q.j[e], lw & 0xFFu, lw & 0xFFFFFF00u, node, root, a.k0, a.k1, T, s.zig, a.error);
-      f = fate(birth, f64_to_f32_rz(birth), z, T, a, can_divide, due);
-      if (f == kLeaf) add_leaves(sm, hist_g1, cls, 1u);
+      const uint32_t cap = (uint32_t)(rec >> 40) & 0xFFu;
+      const TypeDev& T = s.types[(uint32_t)(rec >> 32) & 0xFFu];
+      const uint64_t parent = node >> 1;
+      const uint32_t ch = (uint32_t)(node & 1ull);
+      const u32x4 P = philox_ks(u32x4{(uint32_t)parent, (uint32_t)(parent >> 32), root, kPurposePair}, a.ks);
+      const float z = slow_z(ch ? P.y : P.x, (P.z >> (8u * ch)) & 255u, pair_wedge_bits(P, ch), node, root,
+                             a.k0, a.k1, T, s.zig, a.error);
+      f = fate(birth, f64_to_f32_rz(birth), z, T, a, g1 < cap, due);
+      if (f == kLeaf) add_leaves(sm, hist_g1, (uint32_t)rec, 1u);
       if (f == kVanish) {
         ++vanished;
-        if ((meta >> 9) & 1u) depth_error = 1u;
+        if (((rec >> 49) & 1ull) && g1 == cap) depth_error = 1u;
       }
     }
+    __syncwarp();  // every parked record of this round is read before the front grows
     const uint32_t em = __ballot_sync(kFull, f == kEmit);
-    if (f == kEmit) ob[out_n + __popc(em & lt)] = make_ulonglong2((unsigned long long)__double_as_longlong(due), key);
-    out_n += __popc(em);
-    qn -= cnt;
-    __syncwarp();
-  };
-
-  for (uint64_t v0 = va; v0 < vb; v0 += 32u) {
-    const bool act = v0 + lane < vb;
-    const ulonglong2 c = next;
-    // prefetch the next step's cell while this one is processed
-    if (v0 + 32u + lane < vb) next = cur.load(v0 + 32u + lane);
-    int f0 = kNone, f1 = kNone;
-    bool q0 = false, q1 = false;
-    double due0 = 0.0, due1 = 0.0, d = 0.0;
-    const uint64_t key = c.y;
-    uint32_t cls = 0, ty = 0, meta = 0;
-    u32x4 P = {0u, 0u, 0u, 0u};
-    if (act) {
-      d = __longlong_as_double((long long)c.x);
-      uint64_t rl, node;
-      decode<Narrow>(key, g, rl, node);
-      const unsigned long long rec = __ldg(a.root_rec + rl);  // consumed after Philox
-      const uint32_t root = (uint32_t)(a.root_base + rl);
-      P = philox_ks(u32x4{(uint32_t)node, (uint32_t)(node >> 32), root, kPurposePair}, a.ks);
-      cls = (uint32_t)rec;
-      ty = (uint32_t)(rec >> 32) & 0xFFu;
-      const uint32_t cap = (uint32_t)(rec >> 40) & 0xFFu;
-      const bool clamped = ((rec >> 49) & 1ull) != 0ull && g1 == cap;
-      const bool can_divide = g1 < cap;
-      meta = ty | (can_divide ? 0x100u : 0u) | (clamped ? 0x200u : 0u);
-      const TypeDev& T = s.types[ty];
-      if (T.mode == kModeZeroMean) {
-        // tau == 0: the daughters are due at the parent's own due time
-        due0 = d;
-        due1 = d;
-        f0 = f1 = gt_nonneg(d, a.t_max) ? kLeaf : (can_divide ? kEmit : kVanish);
-      } else {
-        const float df = f64_to_f32_rz(d);
-        const uint32_t m0 = P.x & 0x7FFFFFFFu, l0 = P.z & 255u;
-        const uint32_t m1 = P.y & 0x7FFFFFFFu, l1 = (P.z >> 8) & 255u;
-        if (m0 < s.zig.k[l0]) {
-          const float x = __fmul_rn((float)m0, s.zig.w[l0]);
-          const float z = (P.x >> 31) ? -x : x;
-          if (z >= T.zlo && z <= T.zhi) f0 = fate(d, df, z, T, a, can_divide, due0);
-        }
-        if (m1 < s.zig.k[l1]) {
-          const float x = __fmul_rn((float)m1, s.zig.w[l1]);
-          const float z = (P.y >> 31) ? -x : x;
-          if (z >= T.zlo && z <= T.zhi) f1 = fate(d, df, z, T, a, can_divide, due1);
-        }
-        q0 = f0 == kNone;
-        q1 = f1 == kNone;
-      }
-      if (clamped && (f0 == kVanish || f1 == kVanish)) depth_error = 1u;
-      const uint32_t nleaf = (f0 == kLeaf ? 1u : 0u) + (f1 == kLeaf ? 1u : 0u);
-      if (nleaf) add_leaves(sm, hist_g1, cls, nleaf);
-      vanished += (f0 == kVanish ? 1u : 0u) + (f1 == kVanish ? 1u : 0u);
-    }
-    // daughters' keys: narrow root << 32 | (2 node + c), wide 2 key + c
-    const unsigned long long kd = Narrow ? key + (uint32_t)key : 2ull * key;
-    const uint32_t e0 = __ballot_sync(kFull, f0 == kEmit);
-    const uint32_t e1 = __ballot_sync(kFull, f1 == kEmit);
-    ulonglong2* dst = ob + out_n + __popc(e0 & lt) + __popc(e1 & lt);
-    if (f0 == kEmit) dst[0] = make_ulonglong2((unsigned long long)__double_as_longlong(due0), kd);
-    if (f1 == kEmit) dst[f0 == kEmit ? 1 : 0] = make_ulonglong2((unsigned long long)__double_as_longlong(due1), kd + 1ull);
-    out_n += __popc(e0) + __popc(e1);
-    // queue the daughters the strip test did not settle
-    const uint32_t d0m = __ballot_sync(kFull, q0), d1m = __ballot_sync(kFull, q1);
-    if (d0m | d1m) {
-      uint32_t e = qn + __popc(d0m & lt) + __popc(d1m & lt);
-      if (q0) {
-        q.birth[e] = d;
-        q.key[e] = kd;
-        q.j[e] = P.x;
-        q.lw[e] = (P.w << 8) | (P.z & 255u);
-        q.cls[e] = cls;
-        q.meta[e] = meta;
-        ++e;
-      }
-      if (q1) {
-        q.birth[e] = d;
-        q.key[e] = kd + 1ull;
-        q.j[e] = P.y;
-        q.lw[e] = ((P.w & 0xFF000000u) | ((P.z >> 16) << 8)) | ((P.z >> 8) & 255u);
-        q.cls[e] = cls;
-        q.meta[e] = meta;
-      }
-      qn += __popc(d0m) + __popc(d1m);
-      __syncwarp();
-      while (qn >= 32u) drain(32u);
-    }
+    if (f == kEmit) ob[front + __popc(em & lt)] = make_ulonglong2((unsigned long long)__double_as_longlong(due), key);
+    front += __popc(em);
+    hi = lo;
   }
-  if (qn) drain(qn);
-  vanished = warp_sum(vanished);
+
+  const unsigned long long v = warp_sum((unsigned long long)vanished);
   depth_error = __reduce_or_sync(kFull, depth_error);
   if (lane == 0) {
-    out.count[wg] = out_n;
-    if (vanished) atomicAdd(a.stats + 0, vanished);
+    out.count[wg] = front;
+    if (v) atomicAdd(a.stats + 0, v);
     if (depth_error) atomicOr(a.error, 1u);
     __threadfence();
   }
   __syncthreads();
   const uint32_t nclass = a.nbins * a.ntypes;
   for (uint32_t i = threadIdx.x; i < kHistWindow; i += blockDim.x) {
-    const uint32_t c = sm.hist[i];
-    if (c && sm.base + i < nclass) atomicAdd(hist_g1 + sm.base + i, (unsigned long long)c);
+    const uint32_t cnt = sm.hist[i];
+    if (cnt && sm.base + i < nclass) atomicAdd(hist_g1 + sm.base + i, (unsigned long long)cnt);
   }
-  finish_level(out, nw);
+  finish_level(out, nw, s_scan);
 }
 
 // ------------------------------------------------------------------ diagnostics -----
