@@ -385,6 +385,14 @@ int pc_plan_create(pc_context* ctx, const pc_bin* bins, uint64_t n_bins, const p
     t.sigma_f = (float)src.sd;
     t.mode = src.mean < 0.0 ? kModeQuiescent : (src.mean == 0.0 ? kModeZeroMean : kModeNormal);
     truncation_bounds(src.mean, src.sd, t.zlo, t.zhi);
+    if (t.mode == kModeZeroMean) {
+      // tau = 0 for every cell of the type: with sigma = mu = 0, fma(0, z, 0) = +0 for any
+      // z, so the kernels need no special case (and accept every z)
+      t.sigma = 0.0;
+      t.sigma_f = 0.0f;
+      t.zlo = -INFINITY;
+      t.zhi = INFINITY;
+    }
     if (t.mode == kModeNormal) {
       max_mu = std::max(max_mu, std::fabs(src.mean));
       max_sig = std::max(max_sig, std::fabs(src.sd));

@@ -33,6 +33,11 @@ constexpr uint32_t kFull = 0xFFFFFFFFu;
 #define PC_DIVIDE_MIN_BLOCKS 4
 #endif
 constexpr int kDivideMinBlocks = PC_DIVIDE_MIN_BLOCKS;
+// Input cells each lane carries per step of the division sweep.
+#ifndef PC_CELLS_PER_LANE
+#define PC_CELLS_PER_LANE 1
+#endif
+constexpr int kCellsPerLane = PC_CELLS_PER_LANE;
 
 struct Smem {
   ZigTables zig;
@@ -356,7 +361,68 @@ __device__ __forceinline__ void decode(uint64_t key, uint32_t g, uint64_t& rl, u
   }
 }
 
+// The first-attempt classification of both daughters of one input cell.
+struct CellDraw {
+  double due0, due1;           // exact due times (valid where stored)
+  unsigned long long kd;       // key of daughter 0 (daughter 1: kd + 1)
+  double birth;
+  uint32_t cls;
+  bool em0, em1;               // stored (will divide)
+  bool sl0, sl1;               // parked for the rejection path
+  uint32_t nleaf, nvanish;
+  bool overflow;               // a daughter vanished only because the key layout is full
+};
+
 template <bool Narrow>
+__device__ __forceinline__ CellDraw classify(const ulonglong2 c, bool act, uint32_t g, const RunArgs& a,
+                                             const Smem& s) {
+  CellDraw r;
+  const uint32_t g1 = g + 1u;
+  const double d = __longlong_as_double((long long)c.x);
+  uint64_t rl, node;
+  decode<Narrow>(c.y, g, rl, node);
+  const unsigned long long rec = act ? __ldg(a.root_rec + rl) : 0ull;  // consumed after Philox
+  const u32x4 P = philox_ks(u32x4{(uint32_t)node, (uint32_t)(node >> 32), (uint32_t)(a.root_base + rl),
+                                  kPurposePair}, a.ks);
+  const uint32_t cap = (uint32_t)(rec >> 40) & 0xFFu;
+  const bool can_divide = g1 < cap;
+  const TypeDev& T = s.types[(uint32_t)(rec >> 32) & 0xFFu];
+  // first attempts of both daughters: strip test and truncation bounds (zero-mean types
+  // carry sigma = mu = 0 and unbounded z, so any accepted z gives tau = 0)
+  const uint32_t l0 = P.z & 255u, l1 = (P.z >> 8) & 255u;
+  float z0 = __fmul_rn((float)(P.x & 0x7FFFFFFFu), s.zig.w[l0]);
+  float z1 = __fmul_rn((float)(P.y & 0x7FFFFFFFu), s.zig.w[l1]);
+  z0 = (P.x >> 31) ? -z0 : z0;
+  z1 = (P.y >> 31) ? -z1 : z1;
+  const bool ok0 = act && (P.x & 0x7FFFFFFFu) < s.zig.k[l0] && z0 >= T.zlo && z0 <= T.zhi;
+  const bool ok1 = act && (P.y & 0x7FFFFFFFu) < s.zig.k[l1] && z1 >= T.zlo && z1 <= T.zhi;
+  // FP32 estimates settle clear leaves and clear non-leaves; the exact FP64 due times
+  // decide the band and are what gets stored
+  const float df = f64_to_f32_rz(d);
+  const float est0 = __fadd_rn(df, __fadd_rn(T.mu_f, __fmul_rn(T.sigma_f, z0)));
+  const float est1 = __fadd_rn(df, __fadd_rn(T.mu_f, __fmul_rn(T.sigma_f, z1)));
+  const bool eok = a.est_ok != 0;
+  const bool sure0 = eok && est0 < a.t_lo, sure1 = eok && est1 < a.t_lo;
+  r.due0 = d + fma(T.sigma, f32_to_f64(z0), T.mu);
+  r.due1 = d + fma(T.sigma, f32_to_f64(z1), T.mu);
+  const bool leaf0 = ok0 && ((eok && est0 > a.t_hi) || (!sure0 && gt_nonneg(r.due0, a.t_max)));
+  const bool leaf1 = ok1 && ((eok && est1 > a.t_hi) || (!sure1 && gt_nonneg(r.due1, a.t_max)));
+  r.em0 = ok0 && !leaf0 && can_divide;
+  r.em1 = ok1 && !leaf1 && can_divide;
+  const bool van0 = ok0 && !leaf0 && !can_divide, van1 = ok1 && !leaf1 && !can_divide;
+  r.sl0 = act && !ok0;
+  r.sl1 = act && !ok1;
+  r.nleaf = (leaf0 ? 1u : 0u) + (leaf1 ? 1u : 0u);
+  r.nvanish = (van0 ? 1u : 0u) + (van1 ? 1u : 0u);
+  r.overflow = !Narrow && ((rec >> 49) & 1ull) && g1 == cap && (van0 || van1);
+  r.cls = (uint32_t)rec;
+  r.birth = d;
+  // daughters' keys: narrow root << 32 | (2 node + c), wide 2 key + c
+  r.kd = Narrow ? c.y + (uint32_t)c.y : 2ull * c.y;
+  return r;
+}
+
+template <bool Narrow, int kCells>
 __global__ void __launch_bounds__(kBlock, kDivideMinBlocks) k_divide(const RunArgs a, const LevelIn in,
                                                                      const uint32_t g, const LevelOut out) {
   __shared__ Smem s;
@@ -402,14 +468,19 @@ __global__ void __launch_bounds__(kBlock, kDivideMinBlocks) k_divide(const RunAr
     }
     return seg_ptr + i;
   };
-  ulonglong2 next = make_ulonglong2(0ull, 0ull);
+  constexpr uint32_t kStep = 32u * kCells;
+  ulonglong2 next[kCells];
+#pragma unroll
+  for (int k = 0; k < kCells; ++k) next[k] = make_ulonglong2(0ull, 0ull);
   if (n) {
     seg = last_le(in.prefix, in.nseg, va);
     const unsigned long long lo_abs = __ldg(in.prefix + seg);
     seg_hi_abs = __ldg(in.prefix + seg + 1u);
     seg_ptr = in.cells + (uint64_t)seg * in.stride - (lo_abs - va);
     hi_rel = (uint32_t)min(seg_hi_abs - va, (unsigned long long)n);
-    if (lane < n) next = __ldg(locate(lane));
+#pragma unroll
+    for (int k = 0; k < kCells; ++k)
+      if (32u * k + lane < n) next[k] = __ldg(locate(32u * k + lane));
   }
 
   ulonglong2* const ob = out.cells + (uint64_t)wg * out.stride;
@@ -417,66 +488,37 @@ __global__ void __launch_bounds__(kBlock, kDivideMinBlocks) k_divide(const RunAr
   const uint32_t lt = (1u << lane) - 1u;
   uint32_t front = 0, pending = 0, vanished = 0, depth_error = 0;
   unsigned long long* const hist_g1 = a.hist + (uint64_t)g1 * a.nbins * a.ntypes;
-  const bool eok = a.est_ok != 0;
 
-  for (uint32_t i0 = 0; i0 < n; i0 += 32u) {
-    const bool act = i0 + lane < n;
-    const ulonglong2 c = next;
-    // prefetch the next step's cell while this one is processed
-    if (i0 + 32u + lane < n) next = __ldg(locate(i0 + 32u + lane));
-    const double d = __longlong_as_double((long long)c.x);
-    uint64_t rl, node;
-    decode<Narrow>(c.y, g, rl, node);
-    const unsigned long long rec = act ? __ldg(a.root_rec + rl) : 0ull;  // consumed after Philox
-    const u32x4 P = philox_ks(u32x4{(uint32_t)node, (uint32_t)(node >> 32), (uint32_t)(a.root_base + rl),
-                                    kPurposePair}, a.ks);
-    const uint32_t ty = (uint32_t)(rec >> 32) & 0xFFu;
-    const uint32_t cap = (uint32_t)(rec >> 40) & 0xFFu;
-    const bool can_divide = g1 < cap;
-    const TypeDev& T = s.types[ty];
-    const bool zero_mean = T.mode == kModeZeroMean;  // tau == 0: no draw, due = birth
-    // first attempts of both daughters: strip test, truncation bounds
-    const uint32_t l0 = P.z & 255u, l1 = (P.z >> 8) & 255u;
-    float z0 = __fmul_rn((float)(P.x & 0x7FFFFFFFu), s.zig.w[l0]);
-    float z1 = __fmul_rn((float)(P.y & 0x7FFFFFFFu), s.zig.w[l1]);
-    z0 = zero_mean ? 0.0f : ((P.x >> 31) ? -z0 : z0);
-    z1 = zero_mean ? 0.0f : ((P.y >> 31) ? -z1 : z1);
-    const bool ok0 = act && (zero_mean || ((P.x & 0x7FFFFFFFu) < s.zig.k[l0] && z0 >= T.zlo && z0 <= T.zhi));
-    const bool ok1 = act && (zero_mean || ((P.y & 0x7FFFFFFFu) < s.zig.k[l1] && z1 >= T.zlo && z1 <= T.zhi));
-    // FP32 estimates settle clear leaves and clear non-leaves
-    const float df = f64_to_f32_rz(d);
-    const float est0 = __fadd_rn(df, __fadd_rn(T.mu_f, __fmul_rn(T.sigma_f, z0)));
-    const float est1 = __fadd_rn(df, __fadd_rn(T.mu_f, __fmul_rn(T.sigma_f, z1)));
-    const bool sure0 = eok && est0 < a.t_lo, sure1 = eok && est1 < a.t_lo;
-    bool leaf0 = ok0 && eok && est0 > a.t_hi, leaf1 = ok1 && eok && est1 > a.t_hi;
-    // exact FP64 due times where a daughter will be stored or is inside the band
-    double due0 = 0.0, due1 = 0.0;
-    const bool x0 = ok0 && !leaf0 && (can_divide || !sure0), x1 = ok1 && !leaf1 && (can_divide || !sure1);
-    if (x0) due0 = d + fma(T.sigma, f32_to_f64(z0), T.mu);
-    if (x1) due1 = d + fma(T.sigma, f32_to_f64(z1), T.mu);
-    leaf0 = leaf0 || (x0 && !sure0 && gt_nonneg(due0, a.t_max));
-    leaf1 = leaf1 || (x1 && !sure1 && gt_nonneg(due1, a.t_max));
-    const bool em0 = ok0 && !leaf0 && can_divide, em1 = ok1 && !leaf1 && can_divide;
-    const bool van0 = ok0 && !leaf0 && !can_divide, van1 = ok1 && !leaf1 && !can_divide;
-    const uint32_t nleaf = (leaf0 ? 1u : 0u) + (leaf1 ? 1u : 0u);
-    if (nleaf) add_leaves(sm, hist_g1, (uint32_t)rec, nleaf);
-    vanished += (van0 ? 1u : 0u) + (van1 ? 1u : 0u);
-    if (((rec >> 49) & 1ull) && g1 == cap && (van0 || van1)) depth_error = 1u;
-    // daughters' keys: narrow root << 32 | (2 node + c), wide 2 key + c
-    const unsigned long long kd = Narrow ? c.y + (uint32_t)c.y : 2ull * c.y;
-    const uint32_t e0 = __ballot_sync(kFull, em0), e1 = __ballot_sync(kFull, em1);
-    ulonglong2* dst = ob + front + __popc(e0 & lt) + __popc(e1 & lt);
-    if (em0) dst[0] = make_ulonglong2((unsigned long long)__double_as_longlong(due0), kd);
-    if (em1) dst[em0 ? 1 : 0] = make_ulonglong2((unsigned long long)__double_as_longlong(due1), kd + 1ull);
-    front += __popc(e0) + __popc(e1);
-    // daughters the strip test did not settle: park (birth, key) at the back
-    const bool sl0 = act && !ok0, sl1 = act && !ok1;
-    const uint32_t p0 = __ballot_sync(kFull, sl0), p1 = __ballot_sync(kFull, sl1);
-    if (p0 | p1) {
-      ulonglong2* pd = back - 1u - pending - __popc(p0 & lt) - __popc(p1 & lt);
-      if (sl0) pd[0] = make_ulonglong2((unsigned long long)__double_as_longlong(d), kd);
-      if (sl1) *(pd - (sl0 ? 1 : 0)) = make_ulonglong2((unsigned long long)__double_as_longlong(d), kd + 1ull);
-      pending += __popc(p0) + __popc(p1);
+  for (uint32_t i0 = 0; i0 < n; i0 += kStep) {
+    CellDraw r[kCells];
+#pragma unroll
+    for (int k = 0; k < kCells; ++k) {
+      const ulonglong2 c = next[k];
+      const uint32_t i = i0 + 32u * k + lane;
+      // prefetch the next step's cells while these are processed
+      if (i + kStep < n) next[k] = __ldg(locate(i + kStep));
+      r[k] = classify<Narrow>(c, i < n, g, a, s);
+    }
+#pragma unroll
+    for (int k = 0; k < kCells; ++k) {
+      if (r[k].nleaf) add_leaves(sm, hist_g1, r[k].cls, r[k].nleaf);
+      vanished += r[k].nvanish;
+      if (r[k].overflow) depth_error = 1u;
+      const uint32_t e0 = __ballot_sync(kFull, r[k].em0), e1 = __ballot_sync(kFull, r[k].em1);
+      ulonglong2* dst = ob + front + __popc(e0 & lt) + __popc(e1 & lt);
+      if (r[k].em0) dst[0] = make_ulonglong2((unsigned long long)__double_as_longlong(r[k].due0), r[k].kd);
+      if (r[k].em1)
+        dst[r[k].em0 ? 1 : 0] = make_ulonglong2((unsigned long long)__double_as_longlong(r[k].due1), r[k].kd + 1ull);
+      front += __popc(e0) + __popc(e1);
+      // daughters the strip test did not settle: park (birth, key) at the back
+      const uint32_t p0 = __ballot_sync(kFull, r[k].sl0), p1 = __ballot_sync(kFull, r[k].sl1);
+      if (p0 | p1) {
+        ulonglong2* pd = back - 1u - pending - __popc(p0 & lt) - __popc(p1 & lt);
+        const unsigned long long bb = (unsigned long long)__double_as_longlong(r[k].birth);
+        if (r[k].sl0) pd[0] = make_ulonglong2(bb, r[k].kd);
+        if (r[k].sl1) *(pd - (r[k].sl0 ? 1 : 0)) = make_ulonglong2(bb, r[k].kd + 1ull);
+        pending += __popc(p0) + __popc(p1);
+      }
     }
   }
 
@@ -511,7 +553,7 @@ __global__ void __launch_bounds__(kBlock, kDivideMinBlocks) k_divide(const RunAr
       if (f == kLeaf) add_leaves(sm, hist_g1, (uint32_t)rec, 1u);
       if (f == kVanish) {
         ++vanished;
-        if (((rec >> 49) & 1ull) && g1 == cap) depth_error = 1u;
+        if (!Narrow && ((rec >> 49) & 1ull) && g1 == cap) depth_error = 1u;
       }
     }
     __syncwarp();  // every parked record of this round is read before the front grows
@@ -580,9 +622,9 @@ int launch_root_sweep(const RunArgs& a, uint64_t root_lo, uint64_t root_hi, cons
 int launch_divide_sweep(const RunArgs& a, const LevelIn& in, uint32_t gen, const LevelOut& out,
                         int blocks, bool narrow, void* stream) {
   if (narrow)
-    k_divide<true><<<blocks, kBlock, 0, (cudaStream_t)stream>>>(a, in, gen, out);
+    k_divide<true, kCellsPerLane><<<blocks, kBlock, 0, (cudaStream_t)stream>>>(a, in, gen, out);
   else
-    k_divide<false><<<blocks, kBlock, 0, (cudaStream_t)stream>>>(a, in, gen, out);
+    k_divide<false, kCellsPerLane><<<blocks, kBlock, 0, (cudaStream_t)stream>>>(a, in, gen, out);
   return (int)cudaGetLastError();
 }
 
@@ -606,8 +648,10 @@ int occupancy_blocks_per_sm(int* root_blocks, int* divide_blocks) {
   int r1 = 0, r2 = 0, d1 = 0, d2 = 0;
   cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r1, k_roots<true>, kBlock, 0);
   if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r2, k_roots<false>, kBlock, 0);
-  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d1, k_divide<true>, kBlock, 0);
-  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d2, k_divide<false>, kBlock, 0);
+  if (e == cudaSuccess)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d1, k_divide<true, kCellsPerLane>, kBlock, 0);
+  if (e == cudaSuccess)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d2, k_divide<false, kCellsPerLane>, kBlock, 0);
   *root_blocks = r1 < r2 ? r1 : r2;
   *divide_blocks = d1 < d2 ? d1 : d2;
   return (int)e;
