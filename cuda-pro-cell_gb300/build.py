@@ -57,14 +57,15 @@ def build(verbose: bool = False, out: str | None = None, defines=()) -> str:
                   "-I" + os.path.join(cuda, "include"), "-I" + INCLUDE]
     jobs = []
     objs = []
-    k_src = os.path.join(CSRC, "pc_kernels.cu")
-    k_obj = os.path.join(OUT, "pc_kernels.o")
-    objs.append(k_obj)
     dflags = ["-D" + d for d in defines]
-    if defines or _stale(k_obj, [k_src] + headers):
-        jobs.append([nvcc, *ARCH, "-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xptxas", "-v",
-                     "-Xcompiler", "-fPIC,-ffp-contract=off", "-I" + INCLUDE, *dflags, "-c", k_src,
-                     "-o", k_obj])
+    for name in ("pc_kernels.cu", "pc_noalloc.cu"):
+        k_src = os.path.join(CSRC, name)
+        k_obj = os.path.join(OUT, name.replace(".cu", ".o"))
+        objs.append(k_obj)
+        if defines or _stale(k_obj, [k_src] + headers):
+            jobs.append([nvcc, *ARCH, "-O3", "-lineinfo", "--fmad=false", "-std=c++17", "-Xptxas", "-v",
+                         "-Xcompiler", "-fPIC,-ffp-contract=off", "-I" + INCLUDE, *dflags, "-c", k_src,
+                         "-o", k_obj])
     for name in ("pc_api.cpp", "pc_io.cpp"):
         src = os.path.join(CSRC, name)
         obj = os.path.join(OUT, name.replace(".cpp", ".o"))

@@ -205,6 +205,15 @@ uint32_t bits_for(uint64_t n) {  // bits needed for values in [0, n)
 
 }  // namespace
 
+namespace pc {
+// Host helpers shared with the allocation-free entry point (pc_noalloc.cu).
+ZigTables host_zig_tables() { return build_zig_tables(); }
+void host_truncation_bounds(double mu, double sigma, float& zlo, float& zhi) {
+  truncation_bounds(mu, sigma, zlo, zhi);
+}
+bool host_in_est_range(double x) { return in_est_range(x); }
+}  // namespace pc
+
 extern "C" {
 
 const char* pc_version(void) { return "procell-gb300 0.1 (sm_103a)"; }

@@ -95,4 +95,9 @@ int launch_debug_normals(const ZigTables* zig, uint32_t k0, uint32_t k1, uint32_
                          uint64_t first_parent, uint64_t count, float* z, void* stream);
 int occupancy_blocks_per_sm(int* root_blocks, int* divide_blocks);
 
+// Host helpers (pc_api.cpp).
+ZigTables host_zig_tables();
+void host_truncation_bounds(double mu, double sigma, float& zlo, float& zhi);
+bool host_in_est_range(double x);
+
 }  // namespace pc

@@ -151,6 +151,34 @@ int pc_load_cell_types(const char* path, pc_cell_type** out, uint32_t* n);
 int pc_write_histogram(const char* path, const pc_histogram* h, int track_ratio);
 void pc_free(void* p);
 
+/* Allocation-free simulation. No counterpart in the reference: it exists for callers that
+ * may not allocate device memory themselves, e.g. a host application whose own pool owns
+ * all GPU memory, code that must avoid the device-wide synchronisation cudaMalloc and
+ * cudaFree imply, or a deployment with a memory budget certified in advance.
+ *
+ * It runs the same simulation as pc_simulate (bit-identical counts for the same inputs and
+ * seed) with every intermediate in one static device array of PC_NOALLOC_SCRATCH_BYTES
+ * (64 MiB) that each GPU loading this library reserves until the process exits; it calls
+ * no cudaMalloc, cudaFree or other allocating routine, on the device or the host. Inputs
+ * are host arrays in file order; the result is the raw per-(generation, bin, type) counts
+ * written to the caller's `raw_counts` (capacity in elements), laid out as
+ * pc_plan_raw_counts; dims receives (generations, nonzero bins, types) even when the
+ * buffer is too small. Work is issued on `stream` (a cudaStream_t; NULL = the default
+ * stream) of the current device and the call returns when it has finished.
+ *
+ * Limits: inputs whose rows, per-bin tables, counts and level buffers do not fit in the
+ * array are rejected with PC_ERR_NOMEM and a message; at most 64 cell types. The first call
+ * on a device looks up the array's device address (cudaGetSymbolAddress) with that device
+ * current; make that first call before any stream capture. All calls share the array and
+ * it keeps the last call's contents (each call clears what must start at zero): calls that
+ * overlap on the GPU race, so serialise them. On error, a message is written to `err`
+ * (err_len bytes, may be NULL). */
+#define PC_NOALLOC_SCRATCH_BYTES (64u << 20)
+int pc_simulate_noalloc(const pc_bin* bins, uint64_t n_bins, const pc_cell_type* types,
+                        uint32_t n_types, double t_max, double phi, uint64_t seed, void* stream,
+                        uint64_t* raw_counts, uint64_t capacity, uint32_t dims[3], pc_stats* stats,
+                        char* err, size_t err_len);
+
 /* Diagnostics for the parity tests: evaluate the engine's random stream on the device.
  * pc_debug_philox: out[4*i..] = Philox4x32-10(ctr[4*i..], key) for i < n.
  * pc_debug_normals: z[i] = first-attempt normal of child (i & 1) of node first_parent+i/2
