@@ -9,7 +9,7 @@ from inputs already resident in HBM (`value`), and the same through the C ABI wi
 buffers, the upload and the histogram download inside the timed region (`e2e`). The
 default workload is the 1e7-cell configuration: 4096 bins, fluorescence log-uniform on
 [1, 1e6], Poisson(2500) cells per bin, five types (means U[30, 60], sd 0.3 x mean,
-Dirichlet ratios), t_max 336, phi 1; about 3.9e9 divisions per step.
+Dirichlet ratios), t_max 336, phi 1; 3.55e9 divisions per step.
 
 Under torchrun each rank runs its own instance (seed + rank) of the workload on its own
 GPU: weak scaling, no collective on the data path; value = all ranks' divisions / the
@@ -122,17 +122,18 @@ def describe(w):
 
 
 def cpu_sample(w, target_s, nthreads, oracle):
-    """Oracle divisions/s on a prefix of the workload's initial cells sized to ~target_s."""
+    """Oracle divisions/s on a prefix of the workload's initial cells sized to ~target_s:
+    a probe run sizes the sample, which grows (at most three times) while it runs under half
+    the target."""
     n = w.roots
-    probe = max(1, n // 2048)
-    t = time.perf_counter()
-    r = oracle.simulate(w.bins, w.types, w.t_max, w.phi, seed=w.seed, root_end=probe, nthreads=nthreads)
-    dt = max(time.perf_counter() - t, 1e-3)
-    rate_roots = probe / dt
-    m = int(min(n, max(probe, rate_roots * target_s)))
-    t = time.perf_counter()
-    r = oracle.simulate(w.bins, w.types, w.t_max, w.phi, seed=w.seed, root_end=m, nthreads=nthreads)
-    dt = time.perf_counter() - t
+    m = max(1, n // 2048)
+    for _ in range(4):
+        t = time.perf_counter()
+        r = oracle.simulate(w.bins, w.types, w.t_max, w.phi, seed=w.seed, root_end=m, nthreads=nthreads)
+        dt = max(time.perf_counter() - t, 1e-3)
+        if dt >= 0.5 * target_s or m >= n:
+            break
+        m = int(min(n, max(m + 1, m * target_s / dt)))
     return r.stats["divisions"], dt, m
 
 

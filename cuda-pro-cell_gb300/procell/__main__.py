@@ -1,0 +1,41 @@
+"""Run a named synthetic workload on the GPU and print its statistics.
+
+    PYTHONPATH=cuda-pro-cell_gb300 python -m procell medium --runs 2 --budget 2e9
+
+Workloads are those of procell.configs (small, medium, large). --budget limits the device
+memory of the level buffers (memory_budget_bytes), e.g. to keep a profiler capture small.
+"""
+import argparse
+import json
+import time
+
+from . import Engine
+from . import configs
+
+
+def main():
+    ap = argparse.ArgumentParser(prog="python -m procell")
+    ap.add_argument("workload", choices=["small", "medium", "large"])
+    ap.add_argument("--runs", type=int, default=1)
+    ap.add_argument("--budget", type=float, default=0.0)
+    ap.add_argument("--seed", type=int, default=None)
+    a = ap.parse_args()
+    w = configs.by_name(a.workload)
+    eng = Engine(0)
+    if a.budget > 0:
+        eng.set_option("memory_budget_bytes", a.budget)
+    plan = eng.plan(w.bins, w.types, w.t_max, w.phi, w.seed if a.seed is None else a.seed)
+    for i in range(a.runs):
+        t = time.perf_counter()
+        plan.run()
+        dt = time.perf_counter() - t
+        s = plan.stats()
+        print(json.dumps({"workload": a.workload, "run": i, "wall_ms": round(1e3 * dt, 3),
+                          "divisions": s["divisions"], "sweeps": s["sweeps"],
+                          "device_ms": round(s["device_ms"], 3)}), flush=True)
+    plan.close()
+    eng.close()
+
+
+if __name__ == "__main__":
+    main()
