@@ -309,13 +309,184 @@ def run_ours(args):
     return 0
 
 
+def batched_instances():
+    """The batched workload as (bins, types, t_max, phi, seed) rows with numpy bins."""
+    import numpy as np
+    import procell.configs as cfg
+    out = []
+    for w in cfg.batched():
+        v = np.array([b[0] for b in w.bins], np.float64)
+        f = np.array([b[1] for b in w.bins], np.uint64)
+        out.append(((v, f), w.types, w.t_max, w.phi, w.seed))
+    return out
+
+
+def simulate_batch_e2e(eng, instances):
+    """pc_simulate_batch with host inputs: upload, run, every instance's merged histogram
+    back on the host. Returns (seconds, h2d bytes, d2h bytes, divisions)."""
+    import ctypes
+    from procell import _lib
+    keep = []
+    arr = (_lib.Instance * len(instances))()
+    for i, (bins, types, t_max, phi, seed) in enumerate(instances):
+        b, t = _lib.bins_numpy(bins), _lib.types_numpy(types)
+        keep += [b, t]
+        arr[i].bins = b.ctypes.data_as(ctypes.POINTER(_lib.Bin))
+        arr[i].n_bins = len(b)
+        arr[i].types = t.ctypes.data_as(ctypes.POINTER(_lib.CellType))
+        arr[i].n_types = len(t)
+        arr[i].t_max, arr[i].phi, arr[i].seed = t_max, phi, seed
+    hs = (_lib.Histogram * len(instances))()
+    t0 = time.perf_counter()
+    rc = eng.L.pc_simulate_batch(eng.ctx, arr, len(instances), hs)
+    dt = time.perf_counter() - t0
+    eng._check(rc)
+    h2d = sum(len(k) * k.itemsize for k in keep)
+    d2h = sum(int(h.n_values) * 8 * (2 + int(h.n_types)) for h in hs)
+    for h in hs:
+        eng.L.pc_histogram_free(ctypes.byref(h))
+    return dt, h2d, d2h
+
+
+def run_batched(args):
+    """Batched form: instances/s of one batch run against looping the plain form."""
+    import numpy as np
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if rank != 0 and world > 1:
+        return 0  # one GPU: the batched workload is a single-GPU job
+    import build as pkg_build
+    pkg_build.build()
+    from procell import Engine
+
+    instances = batched_instances()
+    n = len(instances)
+    eng = Engine(local)
+    stream = torch.cuda.current_stream()
+    eng.set_stream(stream.cuda_stream)
+    batch = eng.batch(instances)
+    for _ in range(args.warmup):
+        batch.run()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    divisions = roots = sweeps = 0
+    divide_ms = device_ms = 0.0
+    e0.record(stream)
+    for _ in range(args.steps):
+        batch.run()
+        st = batch.stats()
+        divisions += st["divisions"]
+        roots += st["roots"]
+        sweeps += st["sweeps"]
+        divide_ms += st["divide_ms"]
+        device_ms += st["device_ms"]
+    e1.record(stream)
+    torch.cuda.synchronize()
+    elapsed_ms = e0.elapsed_time(e1)
+    e2e_t = h2d = d2h = 0
+    for _ in range(args.steps):
+        dt, hb, db = simulate_batch_e2e(eng, instances)
+        e2e_t += dt
+        h2d += hb
+        d2h += db
+    clk = clocks.stop()
+    batch_counts = [batch.raw_counts(i) for i in range(n)]
+    batch.close()
+
+    # looping the plain form over the same instances: one pc_simulate per instance (host
+    # inputs in, merged histogram out), and plan + run + raw counts for the parity check
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for bins, types, t_max, phi, seed in instances:
+        eng.simulate(bins, types, t_max, phi, seed)
+    torch.cuda.synchronize()
+    loop_s = time.perf_counter() - t0
+    same = 0
+    for i, (bins, types, t_max, phi, seed) in enumerate(instances):
+        p = eng.plan(bins, types, t_max, phi, seed)
+        p.run()
+        same += int(np.array_equal(p.raw_counts(), batch_counts[i]))
+        p.close()
+
+    hbm, peak_kind = peaks()
+    alg_bytes = 2 * ALG_BYTES_PER_NODE * divisions
+    launches = max(1, sweeps)
+    achieved = alg_bytes / (divide_ms * 1e-3) / 1e9 if divide_ms > 0 else None
+    value = n * args.steps / (elapsed_ms * 1e-3)
+    e2e_value = n * args.steps / e2e_t
+    cpu = None
+    if not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+        oracle.build()
+        cores = os.cpu_count() or 1
+        order = np.random.default_rng(0).permutation(n)
+        t0 = time.perf_counter()
+        done = 0
+        for i in order:
+            bins, types, t_max, phi, seed = instances[i]
+            rows = list(zip(bins[0].tolist(), bins[1].tolist()))
+            oracle.simulate(rows, types, t_max, phi, seed=seed, nthreads=cores)
+            done += 1
+            if time.perf_counter() - t0 > args.cpu_seconds:
+                break
+        cs = time.perf_counter() - t0
+        cpu = {"value": done / cs, "unit": "instances/s", "cores": cores, "kind": "port",
+               "sample": "oracle on %d instances drawn at random from the %d (%.1f s)" % (done, n, cs)}
+    line = {
+        "metric": "instances/s (batched form)",
+        "value": value,
+        "unit": "instances/s",
+        "n_gpus": 1,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": elapsed_ms / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded generator, procell/configs.py batched())",
+        "config": {"workload": "batched: %d instances, %d initial cells, bins U[32,1024], cells "
+                               "log-U[1e3,1e6], 1-4 types (+quiescent 20%%), t_max U[48,336], "
+                               "fluorescence log-U[1,1e4], phi = min nonzero bin" % (n, roots // args.steps),
+                   "divisions_per_step": divisions // args.steps,
+                   "nodes_per_step": (roots + 2 * divisions) // args.steps,
+                   "l2": "no flush: each step streams %.0f GB of level buffers, >> 129 MB L2"
+                         % (2 * 16 * divisions / args.steps / 1e9)},
+        "divisions_per_s": divisions / (elapsed_ms * 1e-3),
+        "loop_plain": {"instances_per_s": n / loop_s, "seconds": loop_s,
+                       "how": "one pc_simulate per instance (host inputs, merged histogram out)"},
+        "speedup_vs_loop_plain": (n / loop_s and value / (n / loop_s)),
+        "e2e_speedup_vs_loop_plain": e2e_value / (n / loop_s),
+        "bit_exact_instances": "%d/%d" % (same, n),
+        "e2e": {"value": e2e_value, "unit": "instances/s", "h2d_bytes_per_step": h2d // args.steps,
+                "d2h_bytes_per_step": d2h // args.steps},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": (achieved / hbm) if achieved else None, "traffic": None,
+                     "peak_source": peak_kind, "kernel": "k_divide",
+                     "launches_per_step": sweeps / args.steps,
+                     "alg_bytes_per_launch": alg_bytes / launches},
+        "gpu_launches": sweeps + args.steps,
+        "clocks": clk,
+        "device_ms_per_step": device_ms / args.steps,
+    }
+    if cpu:
+        line["cpu_baseline"] = cpu
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["small", "medium", "large"], default="large")
+    ap.add_argument("--workload", choices=["small", "medium", "large", "batched"], default="large")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
@@ -323,6 +494,8 @@ def main():
         print("warning: --warmup < 3 violates the timing rules", file=sys.stderr)
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "batched":
+        return run_batched(args)
     return run_ours(args)
 
 

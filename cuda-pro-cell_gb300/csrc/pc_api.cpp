@@ -55,31 +55,51 @@ struct pc_context {
   uint64_t free_at_start = 0;
 };
 
-struct pc_plan {
-  std::vector<double> bin_value;
-  std::vector<uint64_t> bin_start;
-  std::vector<uint32_t> bin_info;
-  std::vector<TypeDev> types;
+// One simulation input: a histogram, a type set, t_max, phi and a seed, prepared once.
+struct InstanceHost {
+  std::vector<double> bin_value;  // nonzero bins, file order
+  std::vector<uint64_t> bin_freq;
+  std::vector<uint32_t> cap;      // phi cap per bin: generations a lineage may divide
+  std::vector<double> values;     // output value set, ascending
+  std::vector<TypeDev> types;     // sorted by ratio, descending
   std::vector<uint32_t> sorted_to_file;
-  uint32_t fallback = 0;
+  uint32_t fallback = 0, gmax = 0;
   double t_max = 0.0, phi = 0.0;
-  uint64_t seed = 0;
-  std::vector<double> values;
-  std::vector<int64_t> vidx;  // [nbins][hist_gens]
-  uint32_t gmax = 0, hist_gens = 1, g_store_max = 0;
-  uint64_t roots_total = 0, root_begin = 0, root_end = 0, chunk = 1;
+  uint64_t seed = 0, roots = 0;
   float t_hi = 0.f, t_lo = 0.f;
   int est_ok = 0;
-  TypeDev* types_dev = nullptr;
+  // placement in the plan
+  uint64_t root_begin = 0, class_begin = 0;
+  uint32_t bin_begin = 0, type_begin = 0, hist_gens = 1;
+  std::vector<int64_t> vidx;  // [nbins][hist_gens] -> output value index or -1
+};
+
+struct pc_plan {
+  std::vector<InstanceHost> inst;  // one for pc_plan_create, many for pc_batch_create
+  bool batched = false;
+  std::vector<uint64_t> bin_start;  // [nbins + 1] over all instances' bins
+  std::vector<uint32_t> bin_info;
+  uint32_t nbins = 0, gmax = 0, hist_gens = 1, g_store_max = 0;
+  uint64_t nclass = 0;
+  uint64_t roots_total = 0, root_begin = 0, root_end = 0, chunk = 1;
+  TypeDev* types_dev = nullptr;         // plain form
+  BatchType* btypes_dev = nullptr;      // batched form
+  InstanceDev* inst_dev = nullptr;
+  uint32_t* bin_inst_dev = nullptr;
+  uint32_t* bin_class_dev = nullptr;
   uint32_t* bin_info_dev = nullptr;
   uint64_t* bin_start_dev = nullptr;
   unsigned long long* root_rec_dev = nullptr;
   unsigned long long* hist_dev = nullptr;
   size_t hist_elems = 0;
+  std::vector<unsigned long long> hist_host;  // batched form: whole table after a run
+  bool hist_host_valid = false;
   pc_stats stats;
   uint64_t upload_bytes = 0;
   bool ran = false;
 };
+
+struct pc_batch : pc_plan {};
 
 namespace {
 
@@ -299,24 +319,22 @@ int pc_set_option(pc_context* ctx, const char* name, double value) {
   return PC_OK;
 }
 
-int pc_plan_create(pc_context* ctx, const pc_bin* bins, uint64_t n_bins, const pc_cell_type* types,
-                   uint32_t n_types, double t_max, double phi, uint64_t seed, pc_plan** out) {
-  if (!ctx || !out || (n_bins && !bins) || (n_types && !types)) return fail(ctx, PC_ERR_INVALID, "null argument");
-  *out = nullptr;
-  if (!(t_max >= 0.0) || std::isinf(t_max)) return fail(ctx, PC_ERR_INVALID, "t_max must be finite and >= 0");
-  if (!(phi >= 0.0) || std::isinf(phi)) return fail(ctx, PC_ERR_INVALID, "phi must be finite and > 0 (0 = automatic)");
-  if (n_types == 0)
-    return fail(ctx, PC_ERR_INVALID, "ERROR: proportion distribution of cell types does not sum to 1, aborting.");
-  if (n_types > (uint32_t)kMaxTypes)
-    return fail(ctx, PC_ERR_UNSUPPORTED, "at most 64 cell types are supported");
+}  // extern "C"
 
-  pc_plan* p = new (std::nothrow) pc_plan();
-  if (!p) return fail(ctx, PC_ERR_NOMEM, "host allocation");
-  std::memset(&p->stats, 0, sizeof(p->stats));
-  auto reject = [&](int code, const std::string& m) {
-    delete p;
-    return fail(ctx, code, m);
-  };
+namespace {
+
+// Host part of the reference's pipeline for one input: the output value set and bin
+// layout of io::load_fluorescences (src/io/parser.cu:68-154), the type table of
+// io::load_cell_types (parser.cu:156-185), and the per-bin phi cap implied by the
+// division test `fluorescence / 2 > threshold` (proliferation.cu:323).
+int prepare_instance(const pc_bin* bins, uint64_t n_bins, const pc_cell_type* types, uint32_t n_types,
+                     double t_max, double phi, uint64_t seed, InstanceHost& I, std::string& msg) {
+  if ((n_bins && !bins) || (n_types && !types)) return msg = "null argument", PC_ERR_INVALID;
+  if (!(t_max >= 0.0) || std::isinf(t_max)) return msg = "t_max must be finite and >= 0", PC_ERR_INVALID;
+  if (!(phi >= 0.0) || std::isinf(phi)) return msg = "phi must be finite and > 0 (0 = automatic)", PC_ERR_INVALID;
+  if (n_types == 0)
+    return msg = "ERROR: proportion distribution of cell types does not sum to 1, aborting.", PC_ERR_INVALID;
+  if (n_types > (uint32_t)kMaxTypes) return msg = "at most 64 cell types are supported", PC_ERR_UNSUPPORTED;
 
   // Threshold (parser.cu:80-96: with no threshold given, the smallest value with a
   // nonzero frequency; the `threshold == 0.0 ||` test is the reference's).
@@ -325,63 +343,58 @@ int pc_plan_create(pc_context* ctx, const pc_bin* bins, uint64_t n_bins, const p
     for (uint64_t i = 0; i < n_bins; ++i)
       if (bins[i].frequency > 0 && (threshold == 0.0 || bins[i].value < threshold)) threshold = bins[i].value;
   }
-  if (!(threshold > 0.0) || std::isinf(threshold)) return reject(PC_ERR_INVALID, "phi must be finite and > 0");
-  p->phi = threshold;
-  p->t_max = (t_max == 0.0) ? 0.0 : t_max;  // normalise -0
-  p->seed = seed;
+  if (!(threshold > 0.0) || std::isinf(threshold)) return msg = "phi must be finite and > 0", PC_ERR_INVALID;
+  I.phi = threshold;
+  I.t_max = (t_max == 0.0) ? 0.0 : t_max;  // normalise -0
+  I.seed = seed;
 
   // Bins with a nonzero frequency, in file order; output value set (parser.cu:98-151).
   std::vector<double> chain;
-  p->bin_start.push_back(0);
   uint64_t total = 0;
   for (uint64_t i = 0; i < n_bins; ++i) {
     if (bins[i].frequency == 0) continue;
     const double v = bins[i].value;
-    if (!std::isfinite(v)) return reject(PC_ERR_INVALID, "histogram values must be finite");
-    if (bins[i].frequency > 0xFFFFFFFFull - total)
-      return reject(PC_ERR_UNSUPPORTED, "more than 2^32-1 initial cells");
+    if (!std::isfinite(v)) return msg = "histogram values must be finite", PC_ERR_INVALID;
+    if (bins[i].frequency > 0xFFFFFFFFull - total) return msg = "more than 2^32-1 initial cells", PC_ERR_UNSUPPORTED;
     total += bins[i].frequency;
-    p->bin_value.push_back(v);
-    p->bin_start.push_back(total);
+    I.bin_value.push_back(v);
+    I.bin_freq.push_back(bins[i].frequency);
     for (double cur = v; cur >= threshold; cur = cur / 2) chain.push_back(cur);
   }
-  if (p->bin_value.size() >= (1u << 24)) return reject(PC_ERR_UNSUPPORTED, "at most 2^24 nonzero bins");
+  if (I.bin_value.size() >= (1u << 24)) return msg = "at most 2^24 nonzero bins", PC_ERR_UNSUPPORTED;
   std::sort(chain.begin(), chain.end());
   chain.erase(std::unique(chain.begin(), chain.end()), chain.end());
-  p->values = chain;
-  p->roots_total = total;
-  p->root_begin = 0;
-  p->root_end = total;
+  I.values = chain;
+  I.roots = total;
 
   // Phi cap per bin: a cell of generation g divides only while its fluorescence, the bin
   // value halved g times, still satisfies `f / 2 > phi` (proliferation.cu:323).
-  std::vector<uint32_t> cap(p->bin_value.size());
-  uint32_t gmax = 0;
-  for (size_t b = 0; b < p->bin_value.size(); ++b) {
+  I.cap.resize(I.bin_value.size());
+  I.gmax = 0;
+  for (size_t b = 0; b < I.bin_value.size(); ++b) {
     uint32_t c = 0;
-    for (double f = p->bin_value[b]; f / 2 > threshold && c < 4096; f = f / 2) ++c;
-    cap[b] = c;
-    gmax = std::max(gmax, c);
+    for (double f = I.bin_value[b]; f / 2 > threshold && c < 4096; f = f / 2) ++c;
+    I.cap[b] = c;
+    I.gmax = std::max(I.gmax, c);
   }
-  p->gmax = gmax;
 
   // Cell types: ratio-sum check, stable sort by ratio descending, cumulative ratios in
   // that order (parser.cu:46-66,184; cell.cu:81-104).
   double sum = 0.0;
   for (uint32_t i = 0; i < n_types; ++i) {
     if (!std::isfinite(types[i].ratio) || !std::isfinite(types[i].mean) || !std::isfinite(types[i].sd))
-      return reject(PC_ERR_INVALID, "cell type parameters must be finite");
+      return msg = "cell type parameters must be finite", PC_ERR_INVALID;
     sum += types[i].ratio;
   }
   if (std::fabs(1.0 - sum) > 1.0 / std::pow(10.0, 8.0))
-    return reject(PC_ERR_INVALID, "ERROR: proportion distribution of cell types does not sum to 1, aborting.");
+    return msg = "ERROR: proportion distribution of cell types does not sum to 1, aborting.", PC_ERR_INVALID;
   std::vector<uint32_t> order(n_types);
   for (uint32_t i = 0; i < n_types; ++i) order[i] = i;
   std::stable_sort(order.begin(), order.end(),
                    [&](uint32_t a, uint32_t b) { return types[a].ratio > types[b].ratio; });
   double acc = 0.0;
   double max_mu = 0.0, max_sig = 0.0;
-  bool est_ok = in_est_range(p->t_max);
+  bool est_ok = in_est_range(I.t_max);
   for (uint32_t s = 0; s < n_types; ++s) {
     const pc_cell_type& src = types[order[s]];
     TypeDev t;
@@ -407,69 +420,236 @@ int pc_plan_create(pc_context* ctx, const pc_bin* bins, uint64_t n_bins, const p
       max_sig = std::max(max_sig, std::fabs(src.sd));
       est_ok = est_ok && in_est_range(src.mean) && in_est_range(src.sd);
     }
-    p->types.push_back(t);
-    p->sorted_to_file.push_back(order[s]);
+    I.types.push_back(t);
+    I.sorted_to_file.push_back(order[s]);
   }
-  p->fallback = 0;
+  I.fallback = 0;
   for (uint32_t s = 0; s < n_types; ++s)
-    if (types[order[s]].ratio > 0.0) p->fallback = s;
+    if (types[order[s]].ratio > 0.0) I.fallback = s;
   // FP32 estimate band: 8x the worst-case error 2^-21 (t_max + |mu| + 9|sigma|).
-  const double margin = std::ldexp(p->t_max + max_mu + 9.0 * max_sig, -18);
-  p->t_hi = std::nextafter((float)(p->t_max + margin), INFINITY);
-  p->t_lo = std::nextafter((float)(p->t_max - margin), -INFINITY);
-  p->est_ok = est_ok ? 1 : 0;
+  const double margin = std::ldexp(I.t_max + max_mu + 9.0 * max_sig, -18);
+  I.t_hi = std::nextafter((float)(I.t_max + margin), INFINITY);
+  I.t_lo = std::nextafter((float)(I.t_max - margin), -INFINITY);
+  I.est_ok = est_ok ? 1 : 0;
+  return PC_OK;
+}
 
-  // Root chunk and key layout: key = root_local * 2^g + path must fit 64 bits.
-  uint64_t chunk = std::max<uint64_t>(1, total);
+// Lays the plan's instances out one after another (initial cells, bins, types, histogram
+// classes), fixes the root chunk and key layout, and uploads the tables.
+int finalize_plan(pc_context* ctx, pc_plan* p) {
+  uint64_t roots = 0, classes = 0;
+  uint32_t bins = 0, ntypes_all = 0, gmax = 0;
+  for (auto& I : p->inst) {
+    I.root_begin = roots;
+    I.bin_begin = bins;
+    I.type_begin = ntypes_all;
+    I.class_begin = classes;
+    roots += I.roots;
+    bins += (uint32_t)I.bin_value.size();
+    ntypes_all += (uint32_t)I.types.size();
+    classes += (uint64_t)I.bin_value.size() * I.types.size();
+    gmax = std::max(gmax, I.gmax);
+    if (bins >= (1u << 24)) return fail(ctx, PC_ERR_UNSUPPORTED, "at most 2^24 nonzero bins in one run");
+  }
+  if (p->batched && ntypes_all > 0xFFFFu) return fail(ctx, PC_ERR_UNSUPPORTED, "at most 65535 cell types in one batch");
+  if (classes > 0xFFFFFFFFull) return fail(ctx, PC_ERR_UNSUPPORTED, "more than 2^32-1 (bin, type) classes in one run");
+  p->nbins = bins;
+  p->gmax = gmax;
+  p->nclass = classes;
+  p->roots_total = roots;
+  p->root_begin = 0;
+  p->root_end = roots;
+  p->bin_start.assign(1, 0);
+  for (const auto& I : p->inst)
+    for (uint64_t f : I.bin_freq) p->bin_start.push_back(p->bin_start.back() + f);
+
+  // Root chunk and key layout: key = root_local * 2^g + path must fit 64 bits; the narrow
+  // layout (root_local << 32 | heap node) needs root_local < 2^32.
+  uint64_t chunk = std::max<uint64_t>(1, roots);
   const uint32_t want_bits = gmax >= 45 ? 20u : 65u - gmax;  // room for gmax - 1 path bits
   if (want_bits < 64) chunk = std::min<uint64_t>(chunk, 1ull << want_bits);
+  if (gmax <= 32) chunk = std::min<uint64_t>(chunk, 1ull << 32);
+  if (p->batched) chunk = std::min<uint64_t>(chunk, 1ull << 28);  // 2 GiB of root records
   if (ctx->opt_max_root_chunk) chunk = std::min<uint64_t>(chunk, std::max<uint64_t>(1, ctx->opt_max_root_chunk));
   p->chunk = chunk;
   const uint32_t rb = bits_for(chunk);
   p->g_store_max = std::min<uint32_t>(62u, 64u - rb);
-  p->bin_info.resize(p->bin_value.size());
-  for (size_t b = 0; b < p->bin_value.size(); ++b) {
-    uint32_t c = cap[b];
-    uint32_t clamped = 0;
-    if (c > p->g_store_max + 1) {
-      c = p->g_store_max + 1;
-      clamped = 0x200u;
-    }
-    p->bin_info[b] = c | (p->bin_value[b] >= threshold ? 0x100u : 0u) | clamped;
-  }
   p->hist_gens = std::min(gmax, p->g_store_max + 1) + 1;
 
-  // (bin, generation) -> output value index, following each bin's halving chain.
-  const size_t nb = p->bin_value.size();
-  p->vidx.assign(nb * p->hist_gens, -1);
-  for (size_t b = 0; b < nb; ++b) {
-    double f = p->bin_value[b];
-    for (uint32_t g = 0; g < p->hist_gens; ++g, f = f / 2) {
-      auto it = std::lower_bound(p->values.begin(), p->values.end(), f);
-      if (it != p->values.end() && *it == f) p->vidx[b * p->hist_gens + g] = it - p->values.begin();
+  std::vector<uint32_t> bin_inst, bin_class;
+  std::vector<BatchType> btypes;
+  std::vector<InstanceDev> idev;
+  p->bin_info.clear();
+  for (uint32_t i = 0; i < (uint32_t)p->inst.size(); ++i) {
+    InstanceHost& I = p->inst[i];
+    const uint32_t nt = (uint32_t)I.types.size();
+    for (size_t b = 0; b < I.bin_value.size(); ++b) {
+      uint32_t c = I.cap[b];
+      uint32_t clamped = 0;
+      if (c > p->g_store_max + 1) {
+        c = p->g_store_max + 1;
+        clamped = 0x200u;
+      }
+      p->bin_info.push_back(c | (I.bin_value[b] >= I.phi ? 0x100u : 0u) | clamped);
+      bin_inst.push_back(i);
+      bin_class.push_back((uint32_t)(I.class_begin + b * nt));
+    }
+    // (bin, generation) -> output value index, following each bin's halving chain.
+    I.hist_gens = std::min(I.gmax, p->g_store_max + 1) + 1;
+    const size_t nb = I.bin_value.size();
+    I.vidx.assign(nb * I.hist_gens, -1);
+    for (size_t b = 0; b < nb; ++b) {
+      double f = I.bin_value[b];
+      for (uint32_t g = 0; g < I.hist_gens; ++g, f = f / 2) {
+        auto it = std::lower_bound(I.values.begin(), I.values.end(), f);
+        if (it != I.values.end() && *it == f) I.vidx[b * I.hist_gens + g] = it - I.values.begin();
+      }
+    }
+    if (p->batched) {
+      for (uint32_t k = 0; k < nt; ++k) {
+        BatchType bt;
+        std::memset(&bt, 0, sizeof(bt));
+        bt.t = I.types[k];
+        bt.t_max = I.t_max;
+        bt.t_hi = I.t_hi;
+        bt.t_lo = I.t_lo;
+        bt.k0 = (uint32_t)I.seed;
+        bt.k1 = (uint32_t)(I.seed >> 32);
+        bt.root_begin = I.root_begin;
+        bt.est_ok = I.est_ok;
+        bt.instance = i;
+        btypes.push_back(bt);
+      }
+      InstanceDev d;
+      std::memset(&d, 0, sizeof(d));
+      d.type_begin = I.type_begin;
+      d.ntypes = nt;
+      d.fallback = I.fallback;
+      d.k0 = (uint32_t)I.seed;
+      d.k1 = (uint32_t)(I.seed >> 32);
+      d.root_begin = I.root_begin;
+      d.t_max = I.t_max;
+      idev.push_back(d);
     }
   }
 
   // Device copies.
   PC_CUDA(ctx, cudaSetDevice(ctx->device));
-  const size_t nt = p->types.size();
-  p->hist_elems = (size_t)p->hist_gens * std::max<size_t>(1, nb) * nt;
-  cudaError_t e = cudaMalloc(&p->types_dev, nt * sizeof(TypeDev));
-  if (e == cudaSuccess) e = cudaMalloc(&p->bin_info_dev, std::max<size_t>(1, nb) * sizeof(uint32_t));
+  cudaStream_t st = ctx->stream;
+  const size_t nb = bins;
+  p->hist_elems = (size_t)p->hist_gens * std::max<uint64_t>(1, classes);
+  p->upload_bytes = nb * sizeof(uint32_t) + (nb + 1) * sizeof(uint64_t);
+  cudaError_t e = cudaMalloc(&p->bin_info_dev, std::max<size_t>(1, nb) * sizeof(uint32_t));
   if (e == cudaSuccess) e = cudaMalloc(&p->bin_start_dev, (nb + 1) * sizeof(uint64_t));
   if (e == cudaSuccess) e = cudaMalloc(&p->root_rec_dev, std::max<uint64_t>(1, chunk) * sizeof(unsigned long long));
   if (e == cudaSuccess) e = cudaMalloc(&p->hist_dev, p->hist_elems * sizeof(unsigned long long));
-  if (e == cudaSuccess) e = cudaMemcpyAsync(p->types_dev, p->types.data(), nt * sizeof(TypeDev), cudaMemcpyHostToDevice, ctx->stream);
   if (e == cudaSuccess && nb)
-    e = cudaMemcpyAsync(p->bin_info_dev, p->bin_info.data(), nb * sizeof(uint32_t), cudaMemcpyHostToDevice, ctx->stream);
+    e = cudaMemcpyAsync(p->bin_info_dev, p->bin_info.data(), nb * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess)
-    e = cudaMemcpyAsync(p->bin_start_dev, p->bin_start.data(), (nb + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, ctx->stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
-  p->upload_bytes = nt * sizeof(TypeDev) + nb * sizeof(uint32_t) + (nb + 1) * sizeof(uint64_t);
-  if (e != cudaSuccess) {
-    pc_plan_destroy(p);
+    e = cudaMemcpyAsync(p->bin_start_dev, p->bin_start.data(), (nb + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, st);
+  if (!p->batched) {
+    const size_t nt = p->inst[0].types.size();
+    if (e == cudaSuccess) e = cudaMalloc(&p->types_dev, nt * sizeof(TypeDev));
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(p->types_dev, p->inst[0].types.data(), nt * sizeof(TypeDev), cudaMemcpyHostToDevice, st);
+    p->upload_bytes += nt * sizeof(TypeDev);
+  } else {
+    if (e == cudaSuccess) e = cudaMalloc(&p->btypes_dev, btypes.size() * sizeof(BatchType));
+    if (e == cudaSuccess) e = cudaMalloc(&p->inst_dev, idev.size() * sizeof(InstanceDev));
+    if (e == cudaSuccess) e = cudaMalloc(&p->bin_inst_dev, std::max<size_t>(1, nb) * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&p->bin_class_dev, std::max<size_t>(1, nb) * sizeof(uint32_t));
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(p->btypes_dev, btypes.data(), btypes.size() * sizeof(BatchType), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(p->inst_dev, idev.data(), idev.size() * sizeof(InstanceDev), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && nb)
+      e = cudaMemcpyAsync(p->bin_inst_dev, bin_inst.data(), nb * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && nb)
+      e = cudaMemcpyAsync(p->bin_class_dev, bin_class.data(), nb * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
+    p->upload_bytes += btypes.size() * sizeof(BatchType) + idev.size() * sizeof(InstanceDev) + 2 * nb * sizeof(uint32_t);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess)
     return fail(ctx, e == cudaErrorMemoryAllocation ? PC_ERR_NOMEM : PC_ERR_CUDA,
                 std::string("plan upload: ") + cudaGetErrorString(e));
+  return PC_OK;
+}
+
+// Raw counts of one instance in its own [hist_gens][bins][types] layout, types in file
+// order, from the plan's [generation][class] table.
+void instance_counts(const pc_plan* p, const InstanceHost& I, const unsigned long long* h, uint64_t* out) {
+  const uint32_t nb = (uint32_t)I.bin_value.size(), nt = (uint32_t)I.types.size();
+  for (uint32_t g = 0; g < I.hist_gens; ++g)
+    for (uint32_t b = 0; b < nb; ++b)
+      for (uint32_t k = 0; k < nt; ++k)
+        out[((uint64_t)g * nb + b) * nt + I.sorted_to_file[k]] = h[g * p->nclass + I.class_begin + (uint64_t)b * nt + k];
+}
+
+// The merged histogram of one instance (value set ascending, totals, per-type columns).
+int instance_result(pc_context* ctx, const pc_plan* p, const InstanceHost& I, const unsigned long long* h,
+                    pc_histogram* out) {
+  const uint32_t nb = (uint32_t)I.bin_value.size(), nt = (uint32_t)I.types.size();
+  const uint64_t nv = I.values.size();
+  out->n_values = nv;
+  out->n_types = nt;
+  out->values = (double*)std::malloc(std::max<uint64_t>(1, nv) * sizeof(double));
+  out->totals = (uint64_t*)std::calloc(std::max<uint64_t>(1, nv), sizeof(uint64_t));
+  out->per_type = (uint64_t*)std::calloc(std::max<uint64_t>(1, nv * nt), sizeof(uint64_t));
+  if (!out->values || !out->totals || !out->per_type) {
+    pc_histogram_free(out);
+    return fail(ctx, PC_ERR_NOMEM, "host allocation");
+  }
+  if (nv) std::memcpy(out->values, I.values.data(), nv * sizeof(double));
+  uint64_t leaves = 0;
+  for (uint32_t g = 0; g < I.hist_gens; ++g)
+    for (uint32_t b = 0; b < nb; ++b) {
+      const int64_t vi = I.vidx[(uint64_t)b * I.hist_gens + g];
+      for (uint32_t k = 0; k < nt; ++k) {
+        const uint64_t c = h[g * p->nclass + I.class_begin + (uint64_t)b * nt + k];
+        if (!c) continue;
+        if (vi < 0) {
+          pc_histogram_free(out);
+          return fail(ctx, PC_ERR_CUDA, "internal: leaf counted outside the output value set");
+        }
+        out->totals[vi] += c;
+        out->per_type[(uint64_t)vi * nt + I.sorted_to_file[k]] += c;
+        leaves += c;
+      }
+    }
+  out->stats.leaves = leaves;
+  return PC_OK;
+}
+
+int fetch_hist(pc_context* ctx, pc_plan* p, std::vector<unsigned long long>& h) {
+  h.resize(p->hist_elems);
+  PC_CUDA(ctx, cudaMemcpyAsync(h.data(), p->hist_dev, p->hist_elems * sizeof(unsigned long long),
+                               cudaMemcpyDeviceToHost, ctx->stream));
+  PC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return PC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pc_plan_create(pc_context* ctx, const pc_bin* bins, uint64_t n_bins, const pc_cell_type* types,
+                   uint32_t n_types, double t_max, double phi, uint64_t seed, pc_plan** out) {
+  if (!ctx || !out) return fail(ctx, PC_ERR_INVALID, "null argument");
+  *out = nullptr;
+  pc_plan* p = new (std::nothrow) pc_plan();
+  if (!p) return fail(ctx, PC_ERR_NOMEM, "host allocation");
+  std::memset(&p->stats, 0, sizeof(p->stats));
+  p->inst.resize(1);
+  std::string msg;
+  int rc = prepare_instance(bins, n_bins, types, n_types, t_max, phi, seed, p->inst[0], msg);
+  if (rc != PC_OK) {
+    delete p;
+    return fail(ctx, rc, msg);
+  }
+  rc = finalize_plan(ctx, p);
+  if (rc != PC_OK) {
+    pc_plan_destroy(p);
+    return rc;
   }
   *out = p;
   return PC_OK;
@@ -487,6 +667,10 @@ int pc_plan_set_roots(pc_context* ctx, pc_plan* p, uint64_t root_begin, uint64_t
 void pc_plan_destroy(pc_plan* p) {
   if (!p) return;
   cudaFree(p->types_dev);
+  cudaFree(p->btypes_dev);
+  cudaFree(p->inst_dev);
+  cudaFree(p->bin_inst_dev);
+  cudaFree(p->bin_class_dev);
   cudaFree(p->bin_info_dev);
   cudaFree(p->bin_start_dev);
   cudaFree(p->root_rec_dev);
@@ -505,7 +689,8 @@ int pc_plan_run(pc_context* ctx, pc_plan* p) {
   const uint64_t nroots = p->root_end - p->root_begin;
   p->stats.roots = nroots;
   p->ran = true;
-  if (nroots == 0 || p->bin_value.empty()) {
+  p->hist_host_valid = false;
+  if (nroots == 0 || p->nbins == 0) {
     PC_CUDA(ctx, cudaStreamSynchronize(st));
     return PC_OK;
   }
@@ -533,20 +718,29 @@ int pc_plan_run(pc_context* ctx, pc_plan* p) {
 
   RunArgs a;
   std::memset(&a, 0, sizeof(a));
-  a.k0 = (uint32_t)p->seed;
-  a.k1 = (uint32_t)(p->seed >> 32);
-  philox_key_schedule(a.k0, a.k1, a.ks);
+  const InstanceHost& I0 = p->inst[0];
   const bool narrow = p->gmax <= 32;
-  a.t_max = p->t_max;
-  a.t_hi = p->t_hi;
-  a.t_lo = p->t_lo;
-  a.est_ok = p->est_ok;
-  a.ntypes = (uint32_t)p->types.size();
-  a.nbins = (uint32_t)p->bin_value.size();
-  a.fallback = p->fallback;
+  if (!p->batched) {
+    a.k0 = (uint32_t)I0.seed;
+    a.k1 = (uint32_t)(I0.seed >> 32);
+    philox_key_schedule(a.k0, a.k1, a.ks);
+    a.t_max = I0.t_max;
+    a.t_hi = I0.t_hi;
+    a.t_lo = I0.t_lo;
+    a.est_ok = I0.est_ok;
+    a.ntypes = (uint32_t)I0.types.size();
+    a.fallback = I0.fallback;
+    a.types = p->types_dev;
+  } else {
+    a.btypes = p->btypes_dev;
+    a.inst = p->inst_dev;
+    a.bin_inst = p->bin_inst_dev;
+    a.bin_class = p->bin_class_dev;
+  }
+  a.nbins = p->nbins;
+  a.nclass = (uint32_t)p->nclass;
   a.hist_gens = p->hist_gens;
   a.g_store_max = p->g_store_max;
-  a.types = p->types_dev;
   a.zig = ctx->zig_dev;
   a.bin_info = p->bin_info_dev;
   a.bin_start = p->bin_start_dev;
@@ -655,69 +849,39 @@ int pc_plan_stats(pc_context* ctx, const pc_plan* p, pc_stats* out) {
 
 int pc_plan_raw_counts(pc_context* ctx, pc_plan* p, uint64_t* host_out, uint64_t capacity,
                        uint64_t* n_elems, uint32_t dims[3]) {
-  if (!ctx || !p) return PC_ERR_INVALID;
-  const uint32_t nb = (uint32_t)p->bin_value.size(), nt = (uint32_t)p->types.size();
-  const uint64_t n = (uint64_t)p->hist_gens * nb * nt;
+  if (!ctx || !p || p->inst.empty()) return PC_ERR_INVALID;
+  const InstanceHost& I = p->inst[0];
+  const uint32_t nb = (uint32_t)I.bin_value.size(), nt = (uint32_t)I.types.size();
+  const uint64_t n = (uint64_t)I.hist_gens * nb * nt;
   if (n_elems) *n_elems = n;
   if (dims) {
-    dims[0] = p->hist_gens;
+    dims[0] = I.hist_gens;
     dims[1] = nb;
     dims[2] = nt;
   }
   if (!host_out) return PC_OK;
   if (capacity < n) return fail(ctx, PC_ERR_INVALID, "raw count buffer too small");
   if (!p->ran) return fail(ctx, PC_ERR_INVALID, "plan has not run");
-  std::vector<unsigned long long> h(n);
-  if (n) {
-    PC_CUDA(ctx, cudaMemcpyAsync(h.data(), p->hist_dev, n * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
-    PC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-  }
-  for (uint64_t gb = 0; gb < (uint64_t)p->hist_gens * nb; ++gb)
-    for (uint32_t k = 0; k < nt; ++k) host_out[gb * nt + p->sorted_to_file[k]] = h[gb * nt + k];
+  std::vector<unsigned long long> h;
+  const int rc = fetch_hist(ctx, p, h);
+  if (rc != PC_OK) return rc;
+  instance_counts(p, I, h.data(), host_out);
   return PC_OK;
 }
 
 int pc_plan_result(pc_context* ctx, pc_plan* p, pc_histogram* out) {
-  if (!ctx || !p || !out) return PC_ERR_INVALID;
+  if (!ctx || !p || !out || p->inst.empty()) return PC_ERR_INVALID;
   std::memset(out, 0, sizeof(*out));
   if (!p->ran) return fail(ctx, PC_ERR_INVALID, "plan has not run");
-  const uint32_t nb = (uint32_t)p->bin_value.size(), nt = (uint32_t)p->types.size();
-  const uint64_t n = (uint64_t)p->hist_gens * nb * nt;
-  std::vector<unsigned long long> h(n);
-  if (n) {
-    PC_CUDA(ctx, cudaMemcpyAsync(h.data(), p->hist_dev, n * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
-    PC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-  }
-  const uint64_t nv = p->values.size();
-  out->n_values = nv;
-  out->n_types = nt;
-  out->values = (double*)std::malloc(std::max<uint64_t>(1, nv) * sizeof(double));
-  out->totals = (uint64_t*)std::calloc(std::max<uint64_t>(1, nv), sizeof(uint64_t));
-  out->per_type = (uint64_t*)std::calloc(std::max<uint64_t>(1, nv * nt), sizeof(uint64_t));
-  if (!out->values || !out->totals || !out->per_type) {
-    pc_histogram_free(out);
-    return fail(ctx, PC_ERR_NOMEM, "host allocation");
-  }
-  if (nv) std::memcpy(out->values, p->values.data(), nv * sizeof(double));
-  uint64_t leaves = 0;
-  for (uint32_t g = 0; g < p->hist_gens; ++g)
-    for (uint32_t b = 0; b < nb; ++b) {
-      const int64_t vi = p->vidx[(uint64_t)b * p->hist_gens + g];
-      for (uint32_t k = 0; k < nt; ++k) {
-        const uint64_t c = h[((uint64_t)g * nb + b) * nt + k];
-        if (!c) continue;
-        if (vi < 0) {
-          pc_histogram_free(out);
-          return fail(ctx, PC_ERR_CUDA, "internal: leaf counted outside the output value set");
-        }
-        out->totals[vi] += c;
-        out->per_type[(uint64_t)vi * nt + p->sorted_to_file[k]] += c;
-        leaves += c;
-      }
-    }
+  std::vector<unsigned long long> h;
+  int rc = fetch_hist(ctx, p, h);
+  if (rc != PC_OK) return rc;
+  rc = instance_result(ctx, p, p->inst[0], h.data(), out);
+  if (rc != PC_OK) return rc;
+  const uint64_t leaves = out->stats.leaves;
   out->stats = p->stats;
   out->stats.leaves = leaves;
-  out->stats.d2h_bytes += n * sizeof(unsigned long long);
+  out->stats.d2h_bytes += p->hist_elems * sizeof(unsigned long long);
   return PC_OK;
 }
 
@@ -740,6 +904,99 @@ int pc_simulate(pc_context* ctx, const pc_bin* bins, uint64_t n_bins, const pc_c
   rc = pc_plan_run(ctx, p);
   if (rc == PC_OK) rc = pc_plan_result(ctx, p, out);
   pc_plan_destroy(p);
+  return rc;
+}
+
+int pc_batch_create(pc_context* ctx, const pc_instance* instances, uint32_t n_instances, pc_batch** out) {
+  if (!ctx || !out || (n_instances && !instances)) return fail(ctx, PC_ERR_INVALID, "null argument");
+  *out = nullptr;
+  if (n_instances == 0) return fail(ctx, PC_ERR_INVALID, "a batch needs at least one instance");
+  pc_batch* b = new (std::nothrow) pc_batch();
+  if (!b) return fail(ctx, PC_ERR_NOMEM, "host allocation");
+  std::memset(&b->stats, 0, sizeof(b->stats));
+  b->batched = true;
+  b->inst.resize(n_instances);
+  for (uint32_t i = 0; i < n_instances; ++i) {
+    const pc_instance& x = instances[i];
+    std::string msg;
+    const int rc = prepare_instance(x.bins, x.n_bins, x.types, x.n_types, x.t_max, x.phi, x.seed, b->inst[i], msg);
+    if (rc != PC_OK) {
+      delete b;
+      return fail(ctx, rc, "instance " + std::to_string(i) + ": " + msg);
+    }
+  }
+  const int rc = finalize_plan(ctx, b);
+  if (rc != PC_OK) {
+    pc_batch_destroy(b);
+    return rc;
+  }
+  *out = b;
+  return PC_OK;
+}
+
+int pc_batch_run(pc_context* ctx, pc_batch* b) { return pc_plan_run(ctx, b); }
+
+int pc_batch_stats(pc_context* ctx, const pc_batch* b, pc_stats* out) { return pc_plan_stats(ctx, b, out); }
+
+uint32_t pc_batch_size(const pc_batch* b) { return b ? (uint32_t)b->inst.size() : 0u; }
+
+static int batch_table(pc_context* ctx, pc_batch* b, uint32_t instance) {
+  if (instance >= b->inst.size()) return fail(ctx, PC_ERR_INVALID, "instance index out of range");
+  if (!b->ran) return fail(ctx, PC_ERR_INVALID, "batch has not run");
+  if (!b->hist_host_valid) {
+    const int rc = fetch_hist(ctx, b, b->hist_host);
+    if (rc != PC_OK) return rc;
+    b->hist_host_valid = true;
+  }
+  return PC_OK;
+}
+
+int pc_batch_raw_counts(pc_context* ctx, pc_batch* b, uint32_t instance, uint64_t* host_out, uint64_t capacity,
+                        uint64_t* n_elems, uint32_t dims[3]) {
+  if (!ctx || !b) return PC_ERR_INVALID;
+  if (instance >= b->inst.size()) return fail(ctx, PC_ERR_INVALID, "instance index out of range");
+  const InstanceHost& I = b->inst[instance];
+  const uint32_t nb = (uint32_t)I.bin_value.size(), nt = (uint32_t)I.types.size();
+  const uint64_t n = (uint64_t)I.hist_gens * nb * nt;
+  if (n_elems) *n_elems = n;
+  if (dims) {
+    dims[0] = I.hist_gens;
+    dims[1] = nb;
+    dims[2] = nt;
+  }
+  if (!host_out) return PC_OK;
+  if (capacity < n) return fail(ctx, PC_ERR_INVALID, "raw count buffer too small");
+  const int rc = batch_table(ctx, b, instance);
+  if (rc != PC_OK) return rc;
+  instance_counts(b, I, b->hist_host.data(), host_out);
+  return PC_OK;
+}
+
+int pc_batch_result(pc_context* ctx, pc_batch* b, uint32_t instance, pc_histogram* out) {
+  if (!ctx || !b || !out) return PC_ERR_INVALID;
+  std::memset(out, 0, sizeof(*out));
+  int rc = batch_table(ctx, b, instance);
+  if (rc != PC_OK) return rc;
+  const InstanceHost& I = b->inst[instance];
+  rc = instance_result(ctx, b, I, b->hist_host.data(), out);
+  if (rc != PC_OK) return rc;
+  out->stats.roots = I.roots;
+  return PC_OK;
+}
+
+void pc_batch_destroy(pc_batch* b) { pc_plan_destroy(b); }
+
+int pc_simulate_batch(pc_context* ctx, const pc_instance* instances, uint32_t n_instances, pc_histogram* out) {
+  if (!ctx || !out) return fail(ctx, PC_ERR_INVALID, "null argument");
+  for (uint32_t i = 0; i < n_instances; ++i) std::memset(out + i, 0, sizeof(pc_histogram));
+  pc_batch* b = nullptr;
+  int rc = pc_batch_create(ctx, instances, n_instances, &b);
+  if (rc != PC_OK) return rc;
+  rc = pc_batch_run(ctx, b);
+  for (uint32_t i = 0; rc == PC_OK && i < n_instances; ++i) rc = pc_batch_result(ctx, b, i, out + i);
+  if (rc != PC_OK)
+    for (uint32_t i = 0; i < n_instances; ++i) pc_histogram_free(out + i);
+  pc_batch_destroy(b);
   return rc;
 }
 

@@ -21,10 +21,13 @@
 //   g < cap) | countable at generation 0 (bit 8: value >= phi) | cap clamped by the key
 //   layout (bit 9).
 // * root_rec[r] (uint64, one per initial cell of the chunk, written by the root sweep):
-//   bits 0-31 histogram class bin * ntypes + type, bits 32-39 sorted type index,
-//   bits 40-47 the bin's phi cap, bits 48-49 bin_info bits 8-9. One load gives the
-//   division sweep everything it needs about a cell's root.
-// * hist[(g * nbins + b) * ntypes + k] counts the leaves of generation g, bin b, type k.
+//   bits 0-31 histogram class, bits 32-47 type index (sorted order; in the batched form the
+//   index into the concatenated type table), bits 48-55 the bin's phi cap, bit 56
+//   countable at generation 0, bit 57 cap clamped. One load gives the division sweep
+//   everything it needs about a cell's root.
+// * hist[g * nclass + class] counts the leaves of generation g per class. Plain form:
+//   class = bin * ntypes + type. Batched form: class = bin_class[bin] + the type's index
+//   within its instance, bins being the concatenated nonzero bins of all instances.
 #pragma once
 
 #include <stdint.h>
@@ -48,6 +51,25 @@ struct TypeDev {
   int32_t pad;
 };
 
+// Batched form: the parameters of one type together with its instance's (one table
+// entry per type of every instance, in instance order).
+struct BatchType {
+  TypeDev t;
+  double t_max;
+  float t_hi, t_lo;
+  uint32_t k0, k1;      // the instance's seed
+  uint64_t root_begin;  // the instance's first initial cell in the batch
+  int32_t est_ok;
+  uint32_t instance;
+};
+
+struct InstanceDev {
+  uint32_t type_begin, ntypes, fallback, pad;
+  uint32_t k0, k1;
+  uint64_t root_begin;
+  double t_max;
+};
+
 struct RunArgs {
   uint32_t k0, k1;           // seed
   uint32_t ks[20];           // Philox key schedule of the seed
@@ -66,6 +88,12 @@ struct RunArgs {
   unsigned long long* hist;  // [hist_gens][nbins][ntypes]
   unsigned long long* stats; // [0] vanished, [1] uncounted, [2] max generation
   uint32_t* error;           // bit 0: depth overflow, bit 1: sampler round budget exhausted
+  uint32_t nclass;           // histogram classes per generation
+  // batched form only (null otherwise)
+  const BatchType* btypes;   // [all types]
+  const InstanceDev* inst;   // [instances]
+  const uint32_t* bin_inst;  // [nbins] instance of each bin
+  const uint32_t* bin_class; // [nbins] first histogram class of each bin
 };
 
 struct LevelIn {
@@ -89,6 +117,7 @@ int launch_root_sweep(const RunArgs& a, uint64_t root_lo, uint64_t root_hi, cons
                       int blocks, bool narrow, void* stream);
 int launch_divide_sweep(const RunArgs& a, const LevelIn& in, uint32_t gen, const LevelOut& out,
                         int blocks, bool narrow, void* stream);
+// a.btypes != nullptr selects the batched instantiations of both sweeps.
 int launch_debug_philox(const uint32_t* ctr, uint64_t n, uint32_t k0, uint32_t k1, uint32_t* out,
                         void* stream);
 int launch_debug_normals(const ZigTables* zig, uint32_t k0, uint32_t k1, uint32_t root,

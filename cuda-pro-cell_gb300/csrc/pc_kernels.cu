@@ -21,6 +21,8 @@
 // warp ballots, and the output stays sorted by (root, path) with no atomics.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "pc_engine.h"
 
 namespace pc {
@@ -41,13 +43,15 @@ constexpr int kCellsPerLane = PC_CELLS_PER_LANE;
 
 struct Smem {
   ZigTables zig;
-  TypeDev types[kMaxTypes];
+  TypeDev types[kMaxTypes];  // plain form only
+  __device__ __forceinline__ const ZigTables& zig_or(const RunArgs&) const { return zig; }
 };
 
 __device__ __forceinline__ void stage(Smem& s, const RunArgs& a) {
   const uint32_t* zs = reinterpret_cast<const uint32_t*>(a.zig);
   uint32_t* zd = reinterpret_cast<uint32_t*>(&s.zig);
   for (uint32_t i = threadIdx.x; i < sizeof(ZigTables) / 4; i += blockDim.x) zd[i] = __ldg(zs + i);
+  if (a.btypes) return;  // batched form: types come from the batch table
   const uint32_t* ts = reinterpret_cast<const uint32_t*>(a.types);
   uint32_t* td = reinterpret_cast<uint32_t*>(s.types);
   const uint32_t nt = a.ntypes * (uint32_t)(sizeof(TypeDev) / 4);
@@ -119,23 +123,65 @@ __device__ __forceinline__ bool gt_nonneg(double a, double b) {
   return __double_as_longlong(a) > __double_as_longlong(b);
 }
 
+// What a cell's type, and in the batched form its instance, supplies to the sweeps.
+struct TypeCtx {
+  const TypeDev* t;  // mu, sigma, truncation bounds (shared memory or the batch table)
+  double t_max;
+  float t_hi, t_lo;
+  bool eok;
+  uint64_t root_begin;  // batch index of the instance's first initial cell
+  uint32_t k0, k1;      // the instance's seed
+};
+
+template <bool Batched>
+__device__ __forceinline__ TypeCtx type_ctx(const RunArgs& a, const TypeDev* smem_types, uint32_t ty) {
+  TypeCtx c;
+  if (Batched) {
+    const BatchType* b = a.btypes + ty;
+    c.t = &b->t;
+    c.t_max = __ldg(&b->t_max);
+    c.t_hi = __ldg(&b->t_hi);
+    c.t_lo = __ldg(&b->t_lo);
+    c.eok = __ldg(&b->est_ok) != 0;
+    c.root_begin = __ldg(&b->root_begin);
+    c.k0 = __ldg(&b->k0);
+    c.k1 = __ldg(&b->k1);
+  } else {
+    c.t = smem_types + ty;
+    c.t_max = a.t_max;
+    c.t_hi = a.t_hi;
+    c.t_lo = a.t_lo;
+    c.eok = a.est_ok != 0;
+    c.root_begin = 0;
+    c.k0 = a.k0;
+    c.k1 = a.k1;
+  }
+  return c;
+}
+
+// Root record fields (layout in pc_engine.h).
+__device__ __forceinline__ uint32_t rec_type(unsigned long long r) { return (uint32_t)(r >> 32) & 0xFFFFu; }
+__device__ __forceinline__ uint32_t rec_cap(unsigned long long r) { return (uint32_t)(r >> 48) & 0xFFu; }
+__device__ __forceinline__ bool rec_clamped(unsigned long long r) { return ((r >> 57) & 1ull) != 0ull; }
+
 // Fate of one daughter born at `birth` with normal z. The FP32 estimate decides leaves
 // and clear non-leaves without FP64 work; the band around t_max (8x the worst-case FP32
 // error) and every daughter that is stored use the exact FP64 due time
 // birth + fma(sigma, z, mu), the reference's t + timer.
-__device__ __forceinline__ int fate(double birth, float birth_f, float z, const TypeDev& T,
-                                    const RunArgs& a, bool can_divide, double& due) {
+__device__ __forceinline__ int fate(double birth, float birth_f, float z, const TypeCtx& c,
+                                    bool can_divide, double& due) {
+  const TypeDev& T = *c.t;
   bool exact = true;
-  if (a.est_ok) {
+  if (c.eok) {
     const float est = __fadd_rn(birth_f, __fadd_rn(T.mu_f, __fmul_rn(T.sigma_f, z)));
-    if (est > a.t_hi) return kLeaf;
-    if (est < a.t_lo) {
+    if (est > c.t_hi) return kLeaf;
+    if (est < c.t_lo) {
       if (!can_divide) return kVanish;
       exact = false;
     }
   }
   due = birth + fma(T.sigma, f32_to_f64(z), T.mu);
-  if (exact && gt_nonneg(due, a.t_max)) return kLeaf;
+  if (exact && gt_nonneg(due, c.t_max)) return kLeaf;
   return can_divide ? kEmit : kVanish;
 }
 
@@ -216,7 +262,7 @@ __device__ __forceinline__ uint32_t last_le(const unsigned long long* prefix, ui
 }
 
 // ------------------------------------------------------------------ root sweep ------
-template <bool Narrow>
+template <bool Narrow, bool Batched>
 __global__ void __launch_bounds__(kBlock) k_roots(const RunArgs a, const uint64_t lo,
                                                   const uint64_t hi, const LevelOut out) {
   __shared__ Smem s;
@@ -231,7 +277,7 @@ __global__ void __launch_bounds__(kBlock) k_roots(const RunArgs a, const uint64_
   ulonglong2* ob = out.cells + (uint64_t)wg * out.stride;
   uint64_t out_n = 0;
   unsigned long long uncounted = 0, vanished = 0;
-  // bin of the warp's first root: largest b with bin_start[b] <= global root
+  // bin of the warp's first root: largest b with bin_start[b] <= batch root index
   uint32_t bin = 0;
   {
     const uint64_t g0 = a.root_base + ra;
@@ -258,36 +304,54 @@ __global__ void __launch_bounds__(kBlock) k_roots(const RunArgs a, const uint64_
         ++bin;
         bin_hi = __ldg(a.bin_start + bin + 1u);
       }
-      const uint32_t root = (uint32_t)rg;
-      const u32x4 R = philox_ks(u32x4{0u, 0u, root, kPurposeRoot}, a.ks);
+      // the instance: its types, seed, first root and t_max
+      uint32_t type_begin = 0, ntypes = a.ntypes, fallback = a.fallback, k0 = a.k0, k1 = a.k1;
+      uint64_t root_begin = 0;
+      double t_max = a.t_max;
+      if (Batched) {
+        const InstanceDev& I = a.inst[__ldg(a.bin_inst + bin)];
+        type_begin = I.type_begin;
+        ntypes = I.ntypes;
+        fallback = I.fallback;
+        k0 = I.k0;
+        k1 = I.k1;
+        root_begin = I.root_begin;
+        t_max = I.t_max;
+      }
+      const uint32_t root = (uint32_t)(rg - root_begin);
+      const u32x4 R = Batched ? philox(u32x4{0u, 0u, root, kPurposeRoot}, k0, k1)
+                              : philox_ks(u32x4{0u, 0u, root, kPurposeRoot}, a.ks);
       const double u_type = unit53_closed_open(R.x, R.y);
       const double u_age = unit53_open_closed(R.z, R.w);
-      uint32_t ty = a.fallback;
-      for (uint32_t i = 0; i < a.ntypes; ++i) {
-        if (u_type < s.types[i].cum) {
+      const TypeDev* types = Batched ? &a.btypes[type_begin].t : s.types;
+      const size_t tstride = Batched ? sizeof(BatchType) : sizeof(TypeDev);
+      auto type_at = [&](uint32_t i) -> const TypeDev& {
+        return *reinterpret_cast<const TypeDev*>(reinterpret_cast<const char*>(types) + i * tstride);
+      };
+      uint32_t ty = fallback;
+      for (uint32_t i = 0; i < ntypes; ++i) {
+        if (u_type < type_at(i).cum) {
           ty = i;
           break;
         }
       }
       const uint32_t info = __ldg(a.bin_info + bin);
-      cls = bin * a.ntypes + ty;
-      a.root_rec[rl] = (unsigned long long)cls | ((unsigned long long)ty << 32) |
-                       ((unsigned long long)(info & 0xFFu) << 40) |
-                       ((unsigned long long)((info >> 8) & 3u) << 48);
-      const TypeDev& T = s.types[ty];
+      cls = Batched ? __ldg(a.bin_class + bin) + ty : bin * a.ntypes + ty;
+      a.root_rec[rl] = (unsigned long long)cls | ((unsigned long long)(type_begin + ty) << 32) |
+                       ((unsigned long long)(info & 0xFFu) << 48) |
+                       ((unsigned long long)((info >> 8) & 3u) << 56);
+      const TypeDev& T = type_at(ty);
       bool leaf;
       if (T.mode == kModeQuiescent) {
         leaf = true;  // timer -1: out of time at once (cell.cu:69-75)
       } else {
-        double tau = 0.0;
-        if (T.mode == kModeNormal) {
-          const u32x4 P = philox_ks(u32x4{0u, 0u, root, kPurposePair}, a.ks);
-          const float z = draw_z(P.y, (P.z >> 8) & 255u, pair_wedge_bits(P, 1u), 1ull, root, a.k0,
-                                 a.k1, T, s.zig, a.error);
-          tau = fma(T.sigma, f32_to_f64(z), T.mu);
-        }
+        const u32x4 P = Batched ? philox(u32x4{0u, 0u, root, kPurposePair}, k0, k1)
+                                : philox_ks(u32x4{0u, 0u, root, kPurposePair}, a.ks);
+        const float z = draw_z(P.y, (P.z >> 8) & 255u, pair_wedge_bits(P, 1u), 1ull, root, k0, k1, T,
+                               s.zig_or(a), a.error);
+        const double tau = fma(T.sigma, f32_to_f64(z), T.mu);  // 0 for zero-mean types
         d0 = tau * u_age + tau;  // t = tau * U (cell.cu:124-143), due = t + timer
-        leaf = gt_nonneg(d0, a.t_max);
+        leaf = gt_nonneg(d0, t_max);
       }
       if (leaf) {
         if (info & 0x100u)
@@ -331,9 +395,10 @@ __global__ void __launch_bounds__(kBlock) k_roots(const RunArgs a, const uint64_
 // path thus costs the main loop neither registers nor idle lanes. Resolved cells are
 // appended to the front; each input cell contributes at most two cells to front + back.
 
-// Leaf counts of one block in shared memory: a window of classes starting at the class of
-// the block's first cell (its input comes from a level sorted by root, so its classes are
-// few and close together); classes outside the window go straight to global memory.
+// Leaf counts of one block in shared memory: a window of classes starting just below the
+// class of the block's first cell (its input comes from a level sorted by root, so its
+// classes are few and close together); classes outside the window go straight to global
+// memory.
 constexpr uint32_t kHistWindow = 2048;
 
 struct DivideSmem {
@@ -373,7 +438,7 @@ struct CellDraw {
   bool overflow;               // a daughter vanished only because the key layout is full
 };
 
-template <bool Narrow>
+template <bool Narrow, bool Batched>
 __device__ __forceinline__ CellDraw classify(const ulonglong2 c, bool act, uint32_t g, const RunArgs& a,
                                              const Smem& s) {
   CellDraw r;
@@ -382,31 +447,37 @@ __device__ __forceinline__ CellDraw classify(const ulonglong2 c, bool act, uint3
   uint64_t rl, node;
   decode<Narrow>(c.y, g, rl, node);
   const unsigned long long rec = act ? __ldg(a.root_rec + rl) : 0ull;  // consumed after Philox
-  const u32x4 P = philox_ks(u32x4{(uint32_t)node, (uint32_t)(node >> 32), (uint32_t)(a.root_base + rl),
-                                  kPurposePair}, a.ks);
-  const uint32_t cap = (uint32_t)(rec >> 40) & 0xFFu;
+  const uint32_t cap = rec_cap(rec);
   const bool can_divide = g1 < cap;
-  const TypeDev& T = s.types[(uint32_t)(rec >> 32) & 0xFFu];
+  const TypeCtx tc = type_ctx<Batched>(a, s.types, rec_type(rec));
+  const TypeDev& T = *tc.t;
+  const uint32_t root = (uint32_t)(a.root_base + rl - tc.root_begin);
+  const u32x4 P = Batched ? philox(u32x4{(uint32_t)node, (uint32_t)(node >> 32), root, kPurposePair}, tc.k0, tc.k1)
+                          : philox_ks(u32x4{(uint32_t)node, (uint32_t)(node >> 32), root, kPurposePair}, a.ks);
   // first attempts of both daughters: strip test and truncation bounds (zero-mean types
   // carry sigma = mu = 0 and unbounded z, so any accepted z gives tau = 0)
+  const ZigTables& Z = s.zig_or(a);
   const uint32_t l0 = P.z & 255u, l1 = (P.z >> 8) & 255u;
-  float z0 = __fmul_rn((float)(P.x & 0x7FFFFFFFu), s.zig.w[l0]);
-  float z1 = __fmul_rn((float)(P.y & 0x7FFFFFFFu), s.zig.w[l1]);
+  float z0 = __fmul_rn((float)(P.x & 0x7FFFFFFFu), Z.w[l0]);
+  float z1 = __fmul_rn((float)(P.y & 0x7FFFFFFFu), Z.w[l1]);
   z0 = (P.x >> 31) ? -z0 : z0;
   z1 = (P.y >> 31) ? -z1 : z1;
-  const bool ok0 = act && (P.x & 0x7FFFFFFFu) < s.zig.k[l0] && z0 >= T.zlo && z0 <= T.zhi;
-  const bool ok1 = act && (P.y & 0x7FFFFFFFu) < s.zig.k[l1] && z1 >= T.zlo && z1 <= T.zhi;
+  const float zlo = T.zlo, zhi = T.zhi;
+  const bool ok0 = act && (P.x & 0x7FFFFFFFu) < Z.k[l0] && z0 >= zlo && z0 <= zhi;
+  const bool ok1 = act && (P.y & 0x7FFFFFFFu) < Z.k[l1] && z1 >= zlo && z1 <= zhi;
   // FP32 estimates settle clear leaves and clear non-leaves; the exact FP64 due times
   // decide the band and are what gets stored
   const float df = f64_to_f32_rz(d);
-  const float est0 = __fadd_rn(df, __fadd_rn(T.mu_f, __fmul_rn(T.sigma_f, z0)));
-  const float est1 = __fadd_rn(df, __fadd_rn(T.mu_f, __fmul_rn(T.sigma_f, z1)));
-  const bool eok = a.est_ok != 0;
-  const bool sure0 = eok && est0 < a.t_lo, sure1 = eok && est1 < a.t_lo;
-  r.due0 = d + fma(T.sigma, f32_to_f64(z0), T.mu);
-  r.due1 = d + fma(T.sigma, f32_to_f64(z1), T.mu);
-  const bool leaf0 = ok0 && ((eok && est0 > a.t_hi) || (!sure0 && gt_nonneg(r.due0, a.t_max)));
-  const bool leaf1 = ok1 && ((eok && est1 > a.t_hi) || (!sure1 && gt_nonneg(r.due1, a.t_max)));
+  const float mu_f = T.mu_f, sigma_f = T.sigma_f;
+  const float est0 = __fadd_rn(df, __fadd_rn(mu_f, __fmul_rn(sigma_f, z0)));
+  const float est1 = __fadd_rn(df, __fadd_rn(mu_f, __fmul_rn(sigma_f, z1)));
+  const bool eok = tc.eok;
+  const bool sure0 = eok && est0 < tc.t_lo, sure1 = eok && est1 < tc.t_lo;
+  const double mu = T.mu, sigma = T.sigma;
+  r.due0 = d + fma(sigma, f32_to_f64(z0), mu);
+  r.due1 = d + fma(sigma, f32_to_f64(z1), mu);
+  const bool leaf0 = ok0 && ((eok && est0 > tc.t_hi) || (!sure0 && gt_nonneg(r.due0, tc.t_max)));
+  const bool leaf1 = ok1 && ((eok && est1 > tc.t_hi) || (!sure1 && gt_nonneg(r.due1, tc.t_max)));
   r.em0 = ok0 && !leaf0 && can_divide;
   r.em1 = ok1 && !leaf1 && can_divide;
   const bool van0 = ok0 && !leaf0 && !can_divide, van1 = ok1 && !leaf1 && !can_divide;
@@ -414,7 +485,7 @@ __device__ __forceinline__ CellDraw classify(const ulonglong2 c, bool act, uint3
   r.sl1 = act && !ok1;
   r.nleaf = (leaf0 ? 1u : 0u) + (leaf1 ? 1u : 0u);
   r.nvanish = (van0 ? 1u : 0u) + (van1 ? 1u : 0u);
-  r.overflow = !Narrow && ((rec >> 49) & 1ull) && g1 == cap && (van0 || van1);
+  r.overflow = !Narrow && rec_clamped(rec) && g1 == cap && (van0 || van1);
   r.cls = (uint32_t)rec;
   r.birth = d;
   // daughters' keys: narrow root << 32 | (2 node + c), wide 2 key + c
@@ -422,7 +493,7 @@ __device__ __forceinline__ CellDraw classify(const ulonglong2 c, bool act, uint3
   return r;
 }
 
-template <bool Narrow, int kCells>
+template <bool Narrow, bool Batched, int kCells>
 __global__ void __launch_bounds__(kBlock, kDivideMinBlocks) k_divide(const RunArgs a, const LevelIn in,
                                                                      const uint32_t g, const LevelOut out) {
   __shared__ Smem s;
@@ -438,7 +509,7 @@ __global__ void __launch_bounds__(kBlock, kDivideMinBlocks) k_divide(const RunAr
   const uint32_t n = (uint32_t)(in.lo + len * (wg + 1u) / nw - va);  // cells of this warp
   const uint32_t g1 = g + 1u;
   if (threadIdx.x == 0) {
-    // histogram window: from the class of the block's first bin
+    // histogram window: from just below the class of the block's first cell
     const uint64_t b0 = in.lo + len * (blockIdx.x * kWarpsPerBlock) / nw;
     uint32_t base = 0u;
     if (b0 < in.hi) {
@@ -446,8 +517,8 @@ __global__ void __launch_bounds__(kBlock, kDivideMinBlocks) k_divide(const RunAr
       const ulonglong2 c0 = __ldg(in.cells + (uint64_t)sg * in.stride + (b0 - __ldg(in.prefix + sg)));
       uint64_t rl, node;
       decode<Narrow>(c0.y, g, rl, node);
-      const unsigned long long rec = __ldg(a.root_rec + rl);
-      base = (uint32_t)rec - ((uint32_t)(rec >> 32) & 0xFFu);
+      const uint32_t cls0 = (uint32_t)__ldg(a.root_rec + rl);
+      base = cls0 - min(cls0, (uint32_t)kMaxTypes - 1u);
     }
     sm.base = base;
   }
@@ -487,7 +558,7 @@ __global__ void __launch_bounds__(kBlock, kDivideMinBlocks) k_divide(const RunAr
   ulonglong2* const back = ob + 2u * n;  // pending daughters at back[-1], back[-2], ...
   const uint32_t lt = (1u << lane) - 1u;
   uint32_t front = 0, pending = 0, vanished = 0, depth_error = 0;
-  unsigned long long* const hist_g1 = a.hist + (uint64_t)g1 * a.nbins * a.ntypes;
+  unsigned long long* const hist_g1 = a.hist + (uint64_t)g1 * a.nclass;
 
   for (uint32_t i0 = 0; i0 < n; i0 += kStep) {
     CellDraw r[kCells];
@@ -497,7 +568,7 @@ __global__ void __launch_bounds__(kBlock, kDivideMinBlocks) k_divide(const RunAr
       const uint32_t i = i0 + 32u * k + lane;
       // prefetch the next step's cells while these are processed
       if (i + kStep < n) next[k] = __ldg(locate(i + kStep));
-      r[k] = classify<Narrow>(c, i < n, g, a, s);
+      r[k] = classify<Narrow, Batched>(c, i < n, g, a, s);
     }
 #pragma unroll
     for (int k = 0; k < kCells; ++k) {
@@ -541,19 +612,19 @@ __global__ void __launch_bounds__(kBlock, kDivideMinBlocks) k_divide(const RunAr
       uint64_t rl, node;
       decode<Narrow>(key, g1, rl, node);
       const unsigned long long rec = __ldg(a.root_rec + rl);
-      const uint32_t root = (uint32_t)(a.root_base + rl);
-      const uint32_t cap = (uint32_t)(rec >> 40) & 0xFFu;
-      const TypeDev& T = s.types[(uint32_t)(rec >> 32) & 0xFFu];
+      const uint32_t cap = rec_cap(rec);
+      const TypeCtx tc = type_ctx<Batched>(a, s.types, rec_type(rec));
+      const uint32_t root = (uint32_t)(a.root_base + rl - tc.root_begin);
       const uint64_t parent = node >> 1;
       const uint32_t ch = (uint32_t)(node & 1ull);
-      const u32x4 P = philox_ks(u32x4{(uint32_t)parent, (uint32_t)(parent >> 32), root, kPurposePair}, a.ks);
+      const u32x4 P = philox(u32x4{(uint32_t)parent, (uint32_t)(parent >> 32), root, kPurposePair}, tc.k0, tc.k1);
       const float z = slow_z(ch ? P.y : P.x, (P.z >> (8u * ch)) & 255u, pair_wedge_bits(P, ch), node, root,
-                             a.k0, a.k1, T, s.zig, a.error);
-      f = fate(birth, f64_to_f32_rz(birth), z, T, a, g1 < cap, due);
+                             tc.k0, tc.k1, *tc.t, s.zig_or(a), a.error);
+      f = fate(birth, f64_to_f32_rz(birth), z, tc, g1 < cap, due);
       if (f == kLeaf) add_leaves(sm, hist_g1, (uint32_t)rec, 1u);
       if (f == kVanish) {
         ++vanished;
-        if (!Narrow && ((rec >> 49) & 1ull) && g1 == cap) depth_error = 1u;
+        if (!Narrow && rec_clamped(rec) && g1 == cap) depth_error = 1u;
       }
     }
     __syncwarp();  // every parked record of this round is read before the front grows
@@ -572,10 +643,9 @@ __global__ void __launch_bounds__(kBlock, kDivideMinBlocks) k_divide(const RunAr
     __threadfence();
   }
   __syncthreads();
-  const uint32_t nclass = a.nbins * a.ntypes;
   for (uint32_t i = threadIdx.x; i < kHistWindow; i += blockDim.x) {
     const uint32_t cnt = sm.hist[i];
-    if (cnt && sm.base + i < nclass) atomicAdd(hist_g1 + sm.base + i, (unsigned long long)cnt);
+    if (cnt && sm.base + i < a.nclass) atomicAdd(hist_g1 + sm.base + i, (unsigned long long)cnt);
   }
   finish_level(out, nw, s_scan);
 }
@@ -612,19 +682,35 @@ __global__ void k_debug_normals(const ZigTables* zig, uint32_t k0, uint32_t k1, 
 
 int launch_root_sweep(const RunArgs& a, uint64_t root_lo, uint64_t root_hi, const LevelOut& out,
                       int blocks, bool narrow, void* stream) {
-  if (narrow)
-    k_roots<true><<<blocks, kBlock, 0, (cudaStream_t)stream>>>(a, root_lo, root_hi, out);
-  else
-    k_roots<false><<<blocks, kBlock, 0, (cudaStream_t)stream>>>(a, root_lo, root_hi, out);
+  cudaStream_t st = (cudaStream_t)stream;
+  if (a.btypes) {
+    if (narrow)
+      k_roots<true, true><<<blocks, kBlock, 0, st>>>(a, root_lo, root_hi, out);
+    else
+      k_roots<false, true><<<blocks, kBlock, 0, st>>>(a, root_lo, root_hi, out);
+  } else {
+    if (narrow)
+      k_roots<true, false><<<blocks, kBlock, 0, st>>>(a, root_lo, root_hi, out);
+    else
+      k_roots<false, false><<<blocks, kBlock, 0, st>>>(a, root_lo, root_hi, out);
+  }
   return (int)cudaGetLastError();
 }
 
 int launch_divide_sweep(const RunArgs& a, const LevelIn& in, uint32_t gen, const LevelOut& out,
                         int blocks, bool narrow, void* stream) {
-  if (narrow)
-    k_divide<true, kCellsPerLane><<<blocks, kBlock, 0, (cudaStream_t)stream>>>(a, in, gen, out);
-  else
-    k_divide<false, kCellsPerLane><<<blocks, kBlock, 0, (cudaStream_t)stream>>>(a, in, gen, out);
+  cudaStream_t st = (cudaStream_t)stream;
+  if (a.btypes) {
+    if (narrow)
+      k_divide<true, true, kCellsPerLane><<<blocks, kBlock, 0, st>>>(a, in, gen, out);
+    else
+      k_divide<false, true, kCellsPerLane><<<blocks, kBlock, 0, st>>>(a, in, gen, out);
+  } else {
+    if (narrow)
+      k_divide<true, false, kCellsPerLane><<<blocks, kBlock, 0, st>>>(a, in, gen, out);
+    else
+      k_divide<false, false, kCellsPerLane><<<blocks, kBlock, 0, st>>>(a, in, gen, out);
+  }
   return (int)cudaGetLastError();
 }
 
@@ -645,15 +731,21 @@ int launch_debug_normals(const ZigTables* zig, uint32_t k0, uint32_t k1, uint32_
 }
 
 int occupancy_blocks_per_sm(int* root_blocks, int* divide_blocks) {
-  int r1 = 0, r2 = 0, d1 = 0, d2 = 0;
-  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r1, k_roots<true>, kBlock, 0);
-  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r2, k_roots<false>, kBlock, 0);
+  int r[4] = {0, 0, 0, 0}, d[4] = {0, 0, 0, 0};
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r[0], k_roots<true, false>, kBlock, 0);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r[1], k_roots<false, false>, kBlock, 0);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r[2], k_roots<true, true>, kBlock, 0);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r[3], k_roots<false, true>, kBlock, 0);
   if (e == cudaSuccess)
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d1, k_divide<true, kCellsPerLane>, kBlock, 0);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d[0], k_divide<true, false, kCellsPerLane>, kBlock, 0);
   if (e == cudaSuccess)
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d2, k_divide<false, kCellsPerLane>, kBlock, 0);
-  *root_blocks = r1 < r2 ? r1 : r2;
-  *divide_blocks = d1 < d2 ? d1 : d2;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d[1], k_divide<false, false, kCellsPerLane>, kBlock, 0);
+  if (e == cudaSuccess)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d[2], k_divide<true, true, kCellsPerLane>, kBlock, 0);
+  if (e == cudaSuccess)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d[3], k_divide<false, true, kCellsPerLane>, kBlock, 0);
+  *root_blocks = *std::min_element(r, r + 4);
+  *divide_blocks = *std::min_element(d, d + 4);
   return (int)e;
 }
 

@@ -335,6 +335,7 @@ extern "C" int pc_simulate_noalloc(const pc_bin* bins, uint64_t n_bins, const pc
   a.est_ok = est_ok ? 1 : 0;
   a.ntypes = n_types;
   a.nbins = (uint32_t)nb;
+  a.nclass = (uint32_t)(nb * n_types);
   a.fallback = fallback;
   a.hist_gens = hist_gens;
   a.g_store_max = g_store_max;

@@ -18,7 +18,7 @@ import numpy as np
 from . import _lib
 from ._lib import ProcellError
 
-__all__ = ["Engine", "Result", "ProcellError", "format_histogram"]
+__all__ = ["Engine", "Batch", "Result", "ProcellError", "format_histogram"]
 
 
 @dataclass
@@ -87,6 +87,75 @@ class Plan:
             pass
 
 
+class Batch:
+    """Many independent instances in one run (pc_batch). Each instance is a dict or tuple
+    (bins, types, t_max, phi, seed); bins may be (values, frequencies) numpy arrays."""
+
+    def __init__(self, engine: "Engine", instances):
+        self.engine = engine
+        self._keep = []
+        arr = (_lib.Instance * max(1, len(instances)))()
+        for i, inst in enumerate(instances):
+            if isinstance(inst, dict):
+                bins, types, t_max = inst["bins"], inst["types"], inst["t_max"]
+                phi, seed = inst.get("phi"), inst.get("seed", 0)
+            else:
+                bins, types, t_max, phi, seed = inst
+            b, t = _lib.bins_numpy(bins), _lib.types_numpy(types)
+            self._keep += [b, t]
+            arr[i].bins = b.ctypes.data_as(ctypes.POINTER(_lib.Bin))
+            arr[i].n_bins = len(b)
+            arr[i].types = t.ctypes.data_as(ctypes.POINTER(_lib.CellType))
+            arr[i].n_types = len(t)
+            arr[i].reserved = 0
+            arr[i].t_max = float(t_max)
+            arr[i].phi = 0.0 if phi is None else float(phi)
+            arr[i].seed = int(seed)
+        h = ctypes.c_void_p()
+        engine._check(engine.L.pc_batch_create(engine.ctx, arr, len(instances), ctypes.byref(h)))
+        self.handle = h
+        self._keep = []  # the library copied the inputs
+        self.size = len(instances)
+
+    def run(self):
+        self.engine._check(self.engine.L.pc_batch_run(self.engine.ctx, self.handle))
+
+    def stats(self) -> dict:
+        st = _lib.Stats()
+        self.engine._check(self.engine.L.pc_batch_stats(self.engine.ctx, self.handle, ctypes.byref(st)))
+        return {k: getattr(st, k) for k, _ in _lib.Stats._fields_}
+
+    def result(self, i: int) -> Result:
+        h = _lib.Histogram()
+        self.engine._check(self.engine.L.pc_batch_result(self.engine.ctx, self.handle, int(i), ctypes.byref(h)))
+        try:
+            return Result(*_lib.histogram_to_numpy(h))
+        finally:
+            self.engine.L.pc_histogram_free(ctypes.byref(h))
+
+    def raw_counts(self, i: int) -> np.ndarray:
+        L, n = self.engine.L, ctypes.c_uint64()
+        dims = (ctypes.c_uint32 * 3)()
+        self.engine._check(L.pc_batch_raw_counts(self.engine.ctx, self.handle, int(i), None, 0,
+                                                 ctypes.byref(n), dims))
+        out = np.zeros(int(n.value), np.uint64)
+        self.engine._check(L.pc_batch_raw_counts(
+            self.engine.ctx, self.handle, int(i), out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
+            int(n.value), ctypes.byref(n), dims))
+        return out.reshape(dims[0], dims[1], dims[2])
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.engine.L.pc_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class Engine:
     def __init__(self, device: int = 0):
         self.L = _lib.load()
@@ -109,6 +178,9 @@ class Engine:
 
     def plan(self, bins, types, t_max, phi=None, seed=0) -> Plan:
         return Plan(self, bins, types, t_max, phi, seed)
+
+    def batch(self, instances) -> Batch:
+        return Batch(self, instances)
 
     def simulate(self, bins, types, t_max, phi=None, seed=0, root_begin=None, root_end=None) -> Result:
         p = self.plan(bins, types, t_max, phi, seed)

@@ -44,6 +44,13 @@ class Histogram(ctypes.Structure):
                 ("per_type", ctypes.POINTER(ctypes.c_uint64)), ("stats", Stats)]
 
 
+class Instance(ctypes.Structure):
+    _fields_ = [("bins", ctypes.POINTER(Bin)), ("n_bins", ctypes.c_uint64),
+                ("types", ctypes.POINTER(CellType)), ("n_types", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32), ("t_max", ctypes.c_double), ("phi", ctypes.c_double),
+                ("seed", ctypes.c_uint64)]
+
+
 # (name, restype, argtypes) of every exported symbol of include/procell.h
 VP, U32P, U64P = ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint64)
 SIGNATURES = [
@@ -66,6 +73,15 @@ SIGNATURES = [
                                    ctypes.POINTER(CellType), ctypes.c_uint32, ctypes.c_double,
                                    ctypes.c_double, ctypes.c_uint64, ctypes.POINTER(Histogram)]),
     ("pc_histogram_free", None, [ctypes.POINTER(Histogram)]),
+    ("pc_batch_create", ctypes.c_int, [VP, ctypes.POINTER(Instance), ctypes.c_uint32, ctypes.POINTER(VP)]),
+    ("pc_batch_run", ctypes.c_int, [VP, VP]),
+    ("pc_batch_stats", ctypes.c_int, [VP, VP, ctypes.POINTER(Stats)]),
+    ("pc_batch_size", ctypes.c_uint32, [VP]),
+    ("pc_batch_result", ctypes.c_int, [VP, VP, ctypes.c_uint32, ctypes.POINTER(Histogram)]),
+    ("pc_batch_raw_counts", ctypes.c_int, [VP, VP, ctypes.c_uint32, U64P, ctypes.c_uint64, U64P, U32P]),
+    ("pc_batch_destroy", None, [VP]),
+    ("pc_simulate_batch", ctypes.c_int, [VP, ctypes.POINTER(Instance), ctypes.c_uint32,
+                                         ctypes.POINTER(Histogram)]),
     ("pc_load_histogram", ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(ctypes.POINTER(Bin)), U64P]),
     ("pc_load_cell_types", ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(ctypes.POINTER(CellType)), U32P]),
     ("pc_write_histogram", ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(Histogram), ctypes.c_int]),
@@ -127,3 +143,28 @@ def histogram_to_numpy(h: Histogram):
     st = h.stats
     stats = {k: getattr(st, k) for k, _ in Stats._fields_}
     return values, totals.astype(np.uint64), per.astype(np.uint64), stats
+
+
+BIN_DTYPE = np.dtype([("value", "<f8"), ("frequency", "<u8")])
+TYPE_DTYPE = np.dtype([("ratio", "<f8"), ("mean", "<f8"), ("sd", "<f8")])
+
+
+def bins_numpy(bins) -> np.ndarray:
+    """(value, frequency) rows as a pc_bin array; accepts a list of pairs or a (values,
+    frequencies) pair of numpy arrays."""
+    if isinstance(bins, tuple) and len(bins) == 2 and isinstance(bins[0], np.ndarray):
+        out = np.empty(len(bins[0]), BIN_DTYPE)
+        out["value"], out["frequency"] = bins[0], bins[1]
+        return out
+    out = np.empty(len(bins), BIN_DTYPE)
+    for i, (v, f) in enumerate(bins):
+        out[i] = (float(v), int(f))
+    return out
+
+
+def types_numpy(types) -> np.ndarray:
+    out = np.empty(len(types), TYPE_DTYPE)
+    for i, (r, m, sd) in enumerate(types):
+        out[i] = (float(r), float(m), float(sd))
+    return out
+

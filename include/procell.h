@@ -139,6 +139,46 @@ int pc_simulate(pc_context* ctx, const pc_bin* bins, uint64_t n_bins, const pc_c
                 uint32_t n_types, double t_max, double phi, uint64_t seed, pc_histogram* out);
 void pc_histogram_free(pc_histogram* h);
 
+/* ---- Batched form (no counterpart in the reference, which runs one input per process) --
+ * Many independent inputs ("instances": each its own histogram, cell types, t_max, phi
+ * and seed) run together: their initial cells are laid end to end and every sweep
+ * processes cells of all instances at once, so the per-run fixed costs (planning,
+ * launches, synchronisation, table transfers) are paid once per batch instead of once per
+ * instance. Each instance's counts are bit-identical to pc_plan_run on that instance
+ * alone with the same seed. Limits: at most 65535 cell types and 2^32-1 (bin, type)
+ * classes over the batch. */
+typedef struct pc_instance {
+  const pc_bin* bins;
+  uint64_t n_bins;
+  const pc_cell_type* types;
+  uint32_t n_types;
+  uint32_t reserved; /* 0 */
+  double t_max;
+  double phi;        /* 0 = automatic, as pc_plan_create */
+  uint64_t seed;
+} pc_instance;
+
+typedef struct pc_batch pc_batch;
+
+/* Validates and uploads every instance (the inputs are copied; the caller's arrays may be
+ * released afterwards). An invalid instance fails the call with its index in the message. */
+int pc_batch_create(pc_context* ctx, const pc_instance* instances, uint32_t n_instances,
+                    pc_batch** out);
+int pc_batch_run(pc_context* ctx, pc_batch* batch);
+/* Whole-batch statistics of the last run. */
+int pc_batch_stats(pc_context* ctx, const pc_batch* batch, pc_stats* out);
+uint32_t pc_batch_size(const pc_batch* batch);
+/* One instance's merged histogram (stats: roots and leaves of that instance only). The
+ * first call after a run copies the whole count table to the host once. */
+int pc_batch_result(pc_context* ctx, pc_batch* batch, uint32_t instance, pc_histogram* out);
+/* One instance's raw counts, in the layout of pc_plan_raw_counts. */
+int pc_batch_raw_counts(pc_context* ctx, pc_batch* batch, uint32_t instance, uint64_t* host_out,
+                        uint64_t capacity, uint64_t* n_elems, uint32_t dims[3]);
+void pc_batch_destroy(pc_batch* batch);
+/* One call: create, run, results (out[n_instances], each freed with pc_histogram_free). */
+int pc_simulate_batch(pc_context* ctx, const pc_instance* instances, uint32_t n_instances,
+                      pc_histogram* out);
+
 /* File formats of the reference (parser.cu:68-217). Loaders read with the reference's
  * `in >> a >> b` semantics (stop at the first unparsable token). The loaders allocate
  * *out with malloc; release it with pc_free. pc_load_cell_types also applies the

@@ -1,0 +1,149 @@
+"""The batched form (pc_batch_*): many independent instances in one run.
+
+Every instance of a batch must give the same uint64 counts, bit for bit, as the plain form
+(pc_plan_run) on that instance alone with the same seed, and through that the oracle's.
+Batches mix uneven instances (different histograms, type sets, t_max, phi, seeds), the
+reference's edge cases per instance, and launch geometries whose root chunks and sweep
+slices straddle instance boundaries.
+"""
+import numpy as np
+import pytest
+
+import procell.configs as cfg
+from procell import ProcellError
+
+pytestmark = pytest.mark.gpu
+
+
+def inst(w):
+    return (w.bins, w.types, w.t_max, w.phi, w.seed)
+
+
+def plain_counts(engine, bins, types, t_max, phi, seed):
+    p = engine.plan(bins, types, t_max, phi, seed)
+    try:
+        p.run()
+        return p.raw_counts(), p.result()
+    finally:
+        p.close()
+
+
+def check_batch(engine, instances):
+    b = engine.batch(instances)
+    try:
+        b.run()
+        st = b.stats()
+        total_roots = 0
+        for i, x in enumerate(instances):
+            want, want_res = plain_counts(engine, *x)
+            got = b.raw_counts(i)
+            assert got.shape == want.shape, (i, got.shape, want.shape)
+            assert np.array_equal(got, want), (i, np.argwhere(got != want)[:5])
+            r = b.result(i)
+            assert np.array_equal(r.values, want_res.values)
+            assert np.array_equal(r.totals, want_res.totals)
+            assert np.array_equal(r.per_type, want_res.per_type)
+            assert r.stats["leaves"] == want_res.stats["leaves"]
+            assert r.stats["roots"] == want_res.stats["roots"]
+            total_roots += want_res.stats["roots"]
+        assert st["roots"] == total_roots
+        return b, st
+    finally:
+        b.close()
+
+
+def small_uneven(n, seed):
+    """Instances with the batched generator's shape, sized down so the plain loop is quick."""
+    rng = np.random.default_rng(seed)
+    ws = cfg.batched(n_instances=n, seed=seed)
+    out = []
+    for w in ws:
+        # keep the histogram, types, t_max and phi; thin the frequencies to <= ~20k cells
+        total = sum(f for _, f in w.bins)
+        keep = min(1.0, 20_000 / max(1, total)) * rng.uniform(0.2, 1.0)
+        bins = [(v, int(f * keep)) for v, f in w.bins]
+        nz = [v for v, f in bins if f > 0]
+        out.append((bins, w.types, w.t_max, min(nz) if nz else 1.0, w.seed))
+    return out
+
+
+EDGE = [
+    # quiescent-only and zero-mean types
+    ([(100.0, 50), (3.0, 20)], [(1.0, -1.0, -1.0)], 50.0, 1.0, 5),
+    ([(64.0, 300), (7.0, 9)], [(0.6, 0.0, 2.0), (0.4, 5.0, 1.0)], 30.0, 1.0, 6),
+    # t_max = 0, phi above every value, zero-frequency rows, an empty histogram
+    ([(500.0, 100)], [(1.0, 10.0, 3.0)], 0.0, 1.0, 7),
+    ([(5.0, 40), (9.0, 0), (3.0, 12)], [(0.5, 8.0, 2.0), (0.5, 12.0, 6.0)], 100.0, 50.0, 8),
+    ([(9.0, 0)], [(1.0, 10.0, 3.0)], 100.0, 1.0, 9),
+    # negative-sd and sd > mean (truncation), many types, automatic phi
+    ([(2000.0, 500), (37.5, 80)], [(0.5, 10.0, -4.0), (0.5, 3.0, 9.0)], 120.0, None, 10),
+    ([(1e4, 200)], [(1.0 / 64, 20.0 + i, 5.0 + 0.1 * i) for i in range(64)], 200.0, 2.0, 11),
+]
+
+
+def test_batch_uneven_matches_plain(engine):
+    check_batch(engine, small_uneven(48, seed=21))
+
+
+def test_batch_edge_instances_match_plain(engine):
+    check_batch(engine, EDGE + small_uneven(6, seed=22))
+
+
+def test_batch_small_config_matches_oracle(engine, oracle_lib):
+    w = cfg.small()
+    other = cfg.small(seed=3)
+    b = engine.batch([inst(other), inst(w), inst(other)])
+    try:
+        b.run()
+        r = b.result(1)
+        o = oracle_lib.simulate(w.bins, w.types, w.t_max, w.phi, seed=w.seed, nthreads=0)
+        assert np.array_equal(r.values, o.values)
+        assert np.array_equal(r.totals, o.totals)
+        assert np.array_equal(r.per_type, o.per_type)
+        assert np.array_equal(b.raw_counts(0), b.raw_counts(2))
+    finally:
+        b.close()
+
+
+def test_batch_wide_key_layout(engine):
+    # an instance whose phi cap exceeds 32 generations puts the whole batch on the wide key layout
+    deep = ([(2.0 ** 40, 3)], [(1.0, 1.0, 0.05)], 6.0, 1.0, 31)
+    check_batch(engine, [deep] + small_uneven(4, seed=23))
+
+
+@pytest.mark.parametrize("opts", [{"max_root_chunk": 777}, {"max_slice_cells": 5000},
+                                  {"grid_blocks": 3}])
+def test_batch_geometry_independent(engine, opts):
+    instances = small_uneven(12, seed=24)
+    ref = engine.batch(instances)
+    ref.run()
+    want = [ref.raw_counts(i) for i in range(len(instances))]
+    ref.close()
+    for k, v in opts.items():
+        engine.set_option(k, v)
+    try:
+        b = engine.batch(instances)
+        b.run()
+        for i in range(len(instances)):
+            assert np.array_equal(b.raw_counts(i), want[i]), i
+        b.close()
+    finally:
+        for k in opts:
+            engine.set_option(k, 0)
+
+
+def test_batch_rerun_and_invalid_instance(engine):
+    instances = small_uneven(5, seed=25)
+    b = engine.batch(instances)
+    b.run()
+    first = [b.raw_counts(i) for i in range(5)]
+    b.run()
+    for i in range(5):
+        assert np.array_equal(b.raw_counts(i), first[i])
+    with pytest.raises(ProcellError, match="instance index out of range"):
+        b.result(5)
+    b.close()
+    bad = list(instances)
+    bad[3] = (bad[3][0], [(0.5, 10.0, 1.0)], 10.0, None, 1)
+    with pytest.raises(ProcellError, match="instance 3: ERROR: proportion"):
+        engine.batch(bad)
