@@ -52,13 +52,14 @@ def build(verbose: bool = False, out: str | None = None, defines=()) -> str:
     os.makedirs(OUT, exist_ok=True)
     cuda = _cuda_home()
     nvcc = os.path.join(cuda, "bin", "nvcc")
-    headers = [os.path.join(CSRC, h) for h in ("pc_rng.h", "pc_engine.h")] + [os.path.join(INCLUDE, "procell.h")]
-    host_flags = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-Wall",
+    headers = [os.path.join(CSRC, h) for h in ("pc_rng.h", "pc_engine.h", "pc_sweeps.cuh")] + \
+        [os.path.join(INCLUDE, "procell.h")]
+    host_flags = ["-O2", "-std=c++17", "-fPIC", "-pthread", "-ffp-contract=off", "-fno-fast-math", "-Wall",
                   "-I" + os.path.join(cuda, "include"), "-I" + INCLUDE]
     jobs = []
     objs = []
     dflags = ["-D" + d for d in defines]
-    for name in ("pc_kernels.cu", "pc_noalloc.cu"):
+    for name in ("pc_kernels.cu", "pc_tuned_plain.cu", "pc_tuned_batched.cu", "pc_noalloc.cu"):
         k_src = os.path.join(CSRC, name)
         k_obj = os.path.join(OUT, name.replace(".cu", ".o"))
         objs.append(k_obj)
@@ -78,7 +79,7 @@ def build(verbose: bool = False, out: str | None = None, defines=()) -> str:
             logs.append(out)
     lib = os.path.join(OUT, "libprocell.so")
     if defines or _stale(lib, objs):
-        logs.append(_run([nvcc, *ARCH, "-shared", "-Xcompiler", "-fPIC", "-o", lib, *objs]))
+        logs.append(_run([nvcc, *ARCH, "-shared", "-Xcompiler", "-fPIC", "-o", lib, *objs, "-lpthread"]))
     cli_src = os.path.join(CSRC, "procell_cli.cpp")
     cli = os.path.join(OUT, "procell")
     if _stale(cli, [cli_src, lib, os.path.join(INCLUDE, "procell.h")]):

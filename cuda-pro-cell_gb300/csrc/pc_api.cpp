@@ -16,9 +16,11 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <atomic>
 #include <map>
 #include <new>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/procell.h"
@@ -43,6 +45,16 @@ struct pc_context {
   double opt_budget = 0.0;
   uint64_t opt_max_slice = 0, opt_max_root_chunk = 0;
   int opt_grid_blocks = 0;
+  int opt_config = kDefaultSweepConfig;  // sweep configuration (narrow key layout)
+  int opt_driver = 0;                    // 0: one launch per sweep, 1: persistent launch
+  int opt_graph = 0;                     // persistent driver: replay a captured CUDA graph
+  // resident blocks per SM of each configuration's kernels: [narrow][batched][config]
+  int occ[2][2][kNumSweepConfigs][3] = {};
+  uint32_t* persist_ctl = nullptr;       // [2] barrier + [8] run totals (u64 [4])
+  // pinned host copy of the last count table read back (plan id and run number it holds)
+  unsigned long long* stage = nullptr;
+  size_t stage_elems = 0;
+  uint64_t stage_plan = 0, stage_run = 0;
   ZigTables zig_host;
   ZigTables* zig_dev = nullptr;
   std::vector<LevelBuf> pool;
@@ -71,7 +83,8 @@ struct InstanceHost {
   // placement in the plan
   uint64_t root_begin = 0, class_begin = 0;
   uint32_t bin_begin = 0, type_begin = 0, hist_gens = 1;
-  std::vector<int64_t> vidx;  // [nbins][hist_gens] -> output value index or -1
+  uint32_t vidx_stride = 1;   // gmax + 1
+  std::vector<int32_t> vidx;  // [nbins][vidx_stride] -> output value index or -1
 };
 
 struct pc_plan {
@@ -92,8 +105,10 @@ struct pc_plan {
   unsigned long long* root_rec_dev = nullptr;
   unsigned long long* hist_dev = nullptr;
   size_t hist_elems = 0;
-  std::vector<unsigned long long> hist_host;  // batched form: whole table after a run
-  bool hist_host_valid = false;
+  uint64_t id = 0, run_id = 0;                // identity of the counts in the pinned stage
+  cudaGraphExec_t graph = nullptr;           // persistent driver: the captured run
+  PersistArgs graph_args;                    // ... and the arguments it was captured with
+  int graph_config = -1, graph_grid = 0;
   pc_stats stats;
   uint64_t upload_bytes = 0;
   bool ran = false;
@@ -212,9 +227,27 @@ int max_blocks(const pc_context* ctx, int per_sm) {
   return std::max(1, b);
 }
 
-int grid_for(const pc_context* ctx, uint64_t n, int per_sm) {
-  const uint64_t want = (n + (uint64_t)kBlock * 4 - 1) / ((uint64_t)kBlock * 4);
+int grid_for(const pc_context* ctx, uint64_t n, int per_sm, int threads) {
+  const uint64_t want = (n + (uint64_t)threads * 4 - 1) / ((uint64_t)threads * 4);
   return (int)std::max<uint64_t>(1, std::min<uint64_t>(want, (uint64_t)max_blocks(ctx, per_sm)));
+}
+
+// f(i) for i in [0, n) on up to `threads` host threads (0 = all cores).
+template <class F>
+void parallel_for(uint32_t n, F&& f, unsigned threads = 0) {
+  unsigned nt = threads ? threads : std::max(1u, std::thread::hardware_concurrency());
+  nt = std::min<unsigned>(std::min<unsigned>(nt, 64u), n);
+  if (nt <= 1) {
+    for (uint32_t i = 0; i < n; ++i) f(i);
+    return;
+  }
+  std::atomic<uint32_t> next{0};
+  std::vector<std::thread> pool;
+  for (unsigned t = 0; t < nt; ++t)
+    pool.emplace_back([&]() {
+      for (uint32_t i; (i = next.fetch_add(1)) < n;) f(i);
+    });
+  for (auto& th : pool) th.join();
 }
 
 uint32_t bits_for(uint64_t n) {  // bits needed for values in [0, n)
@@ -268,6 +301,7 @@ int pc_create(pc_context** out, int device) {
     return bail(e, "cudaMemcpy");
   if ((e = cudaMalloc(&ctx->stats_dev, 4 * sizeof(unsigned long long))) != cudaSuccess) return bail(e, "cudaMalloc");
   if ((e = cudaMalloc(&ctx->error_dev, sizeof(uint32_t))) != cudaSuccess) return bail(e, "cudaMalloc");
+  if ((e = cudaMalloc(&ctx->persist_ctl, 48)) != cudaSuccess) return bail(e, "cudaMalloc");
   if ((e = cudaMallocHost(&ctx->pinned, 64 * sizeof(unsigned long long))) != cudaSuccess)
     return bail(e, "cudaMallocHost");
   for (auto& ev : ctx->ev)
@@ -287,7 +321,9 @@ void pc_destroy(pc_context* ctx) {
   cudaFree(ctx->zig_dev);
   cudaFree(ctx->stats_dev);
   cudaFree(ctx->error_dev);
+  cudaFree(ctx->persist_ctl);
   cudaFreeHost(ctx->pinned);
+  cudaFreeHost(ctx->stage);
   for (auto& ev : ctx->ev)
     if (ev) cudaEventDestroy(ev);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
@@ -312,6 +348,14 @@ int pc_set_option(pc_context* ctx, const char* name, double value) {
     ctx->opt_max_root_chunk = (uint64_t)value;
   } else if (n == "grid_blocks") {
     ctx->opt_grid_blocks = (int)value;
+  } else if (n == "sweep_config") {
+    if (value >= kNumSweepConfigs) return fail(ctx, PC_ERR_INVALID, "sweep_config must be 0..7");
+    ctx->opt_config = (int)value;
+  } else if (n == "driver") {
+    if (value > 1) return fail(ctx, PC_ERR_INVALID, "driver must be 0 (per sweep) or 1 (persistent)");
+    ctx->opt_driver = (int)value;
+  } else if (n == "graph") {
+    ctx->opt_graph = value != 0.0 ? 1 : 0;
   } else {
     return fail(ctx, PC_ERR_INVALID, "unknown option " + n);
   }
@@ -348,23 +392,32 @@ int prepare_instance(const pc_bin* bins, uint64_t n_bins, const pc_cell_type* ty
   I.t_max = (t_max == 0.0) ? 0.0 : t_max;  // normalise -0
   I.seed = seed;
 
-  // Bins with a nonzero frequency, in file order; output value set (parser.cu:98-151).
-  std::vector<double> chain;
+  // Bins with a nonzero frequency, in file order; output value set (parser.cu:98-151):
+  // every bin's halving chain v, v/2, ... while >= phi, sorted and deduplicated. Each chain
+  // entry remembers its (bin, generation), which gives the (bin, generation) -> value index
+  // map of the result merge in the same pass.
+  struct Link {
+    double v;
+    uint32_t bin, gen;
+  };
+  std::vector<Link> chain;
   uint64_t total = 0;
+  uint32_t longest = 0;
   for (uint64_t i = 0; i < n_bins; ++i) {
     if (bins[i].frequency == 0) continue;
     const double v = bins[i].value;
     if (!std::isfinite(v)) return msg = "histogram values must be finite", PC_ERR_INVALID;
     if (bins[i].frequency > 0xFFFFFFFFull - total) return msg = "more than 2^32-1 initial cells", PC_ERR_UNSUPPORTED;
+    if (I.bin_value.size() + 1 >= (1u << 24)) return msg = "at most 2^24 nonzero bins", PC_ERR_UNSUPPORTED;
     total += bins[i].frequency;
+    const uint32_t b = (uint32_t)I.bin_value.size();
     I.bin_value.push_back(v);
     I.bin_freq.push_back(bins[i].frequency);
-    for (double cur = v; cur >= threshold; cur = cur / 2) chain.push_back(cur);
+    uint32_t g = 0;
+    for (double cur = v; cur >= threshold; cur = cur / 2) chain.push_back(Link{cur, b, g++});
+    longest = std::max(longest, g);
   }
-  if (I.bin_value.size() >= (1u << 24)) return msg = "at most 2^24 nonzero bins", PC_ERR_UNSUPPORTED;
-  std::sort(chain.begin(), chain.end());
-  chain.erase(std::unique(chain.begin(), chain.end()), chain.end());
-  I.values = chain;
+  std::sort(chain.begin(), chain.end(), [](const Link& x, const Link& y) { return x.v < y.v; });
   I.roots = total;
 
   // Phi cap per bin: a cell of generation g divides only while its fluorescence, the bin
@@ -376,6 +429,14 @@ int prepare_instance(const pc_bin* bins, uint64_t n_bins, const pc_cell_type* ty
     for (double f = I.bin_value[b]; f / 2 > threshold && c < 4096; f = f / 2) ++c;
     I.cap[b] = c;
     I.gmax = std::max(I.gmax, c);
+  }
+  // Every generation a leaf can have (<= gmax) has a row; chains are never longer.
+  I.vidx_stride = std::max(I.gmax, longest) + 1;
+  I.vidx.assign(I.bin_value.size() * (size_t)I.vidx_stride, -1);
+  I.values.clear();
+  for (size_t i = 0; i < chain.size(); ++i) {
+    if (i == 0 || chain[i].v != chain[i - 1].v) I.values.push_back(chain[i].v);
+    I.vidx[(size_t)chain[i].bin * I.vidx_stride + chain[i].gen] = (int32_t)(I.values.size() - 1);
   }
 
   // Cell types: ratio-sum check, stable sort by ratio descending, cumulative ratios in
@@ -494,17 +555,7 @@ int finalize_plan(pc_context* ctx, pc_plan* p) {
       bin_inst.push_back(i);
       bin_class.push_back((uint32_t)(I.class_begin + b * nt));
     }
-    // (bin, generation) -> output value index, following each bin's halving chain.
     I.hist_gens = std::min(I.gmax, p->g_store_max + 1) + 1;
-    const size_t nb = I.bin_value.size();
-    I.vidx.assign(nb * I.hist_gens, -1);
-    for (size_t b = 0; b < nb; ++b) {
-      double f = I.bin_value[b];
-      for (uint32_t g = 0; g < I.hist_gens; ++g, f = f / 2) {
-        auto it = std::lower_bound(I.values.begin(), I.values.end(), f);
-        if (it != I.values.end() && *it == f) I.vidx[b * I.hist_gens + g] = it - I.values.begin();
-      }
-    }
     if (p->batched) {
       for (uint32_t k = 0; k < nt; ++k) {
         BatchType bt;
@@ -586,8 +637,9 @@ void instance_counts(const pc_plan* p, const InstanceHost& I, const unsigned lon
 }
 
 // The merged histogram of one instance (value set ascending, totals, per-type columns).
-int instance_result(pc_context* ctx, const pc_plan* p, const InstanceHost& I, const unsigned long long* h,
-                    pc_histogram* out) {
+// Touches nothing shared, so instances can be merged on several threads.
+int instance_result(const pc_plan* p, const InstanceHost& I, const unsigned long long* h, pc_histogram* out,
+                    const char** msg) {
   const uint32_t nb = (uint32_t)I.bin_value.size(), nt = (uint32_t)I.types.size();
   const uint64_t nv = I.values.size();
   out->n_values = nv;
@@ -597,19 +649,21 @@ int instance_result(pc_context* ctx, const pc_plan* p, const InstanceHost& I, co
   out->per_type = (uint64_t*)std::calloc(std::max<uint64_t>(1, nv * nt), sizeof(uint64_t));
   if (!out->values || !out->totals || !out->per_type) {
     pc_histogram_free(out);
-    return fail(ctx, PC_ERR_NOMEM, "host allocation");
+    *msg = "host allocation";
+    return PC_ERR_NOMEM;
   }
   if (nv) std::memcpy(out->values, I.values.data(), nv * sizeof(double));
   uint64_t leaves = 0;
   for (uint32_t g = 0; g < I.hist_gens; ++g)
     for (uint32_t b = 0; b < nb; ++b) {
-      const int64_t vi = I.vidx[(uint64_t)b * I.hist_gens + g];
+      const int64_t vi = I.vidx[(uint64_t)b * I.vidx_stride + g];
       for (uint32_t k = 0; k < nt; ++k) {
         const uint64_t c = h[g * p->nclass + I.class_begin + (uint64_t)b * nt + k];
         if (!c) continue;
         if (vi < 0) {
           pc_histogram_free(out);
-          return fail(ctx, PC_ERR_CUDA, "internal: leaf counted outside the output value set");
+          *msg = "internal: leaf counted outside the output value set";
+          return PC_ERR_CUDA;
         }
         out->totals[vi] += c;
         out->per_type[(uint64_t)vi * nt + I.sorted_to_file[k]] += c;
@@ -620,11 +674,27 @@ int instance_result(pc_context* ctx, const pc_plan* p, const InstanceHost& I, co
   return PC_OK;
 }
 
-int fetch_hist(pc_context* ctx, pc_plan* p, std::vector<unsigned long long>& h) {
-  h.resize(p->hist_elems);
-  PC_CUDA(ctx, cudaMemcpyAsync(h.data(), p->hist_dev, p->hist_elems * sizeof(unsigned long long),
-                               cudaMemcpyDeviceToHost, ctx->stream));
-  PC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+std::atomic<uint64_t> g_plan_ids{1};
+
+// The plan's count table after its last run, in the context's pinned stage (read back
+// once per run; the stage grows to the largest table and is reused).
+int stage_table(pc_context* ctx, pc_plan* p, const unsigned long long** out) {
+  if (ctx->stage_plan != p->id || ctx->stage_run != p->run_id || !ctx->stage) {
+    if (ctx->stage_elems < p->hist_elems) {
+      cudaFreeHost(ctx->stage);
+      ctx->stage = nullptr;
+      ctx->stage_elems = 0;
+      PC_CUDA(ctx, cudaMallocHost(&ctx->stage, p->hist_elems * sizeof(unsigned long long)));
+      ctx->stage_elems = p->hist_elems;
+    }
+    ctx->stage_plan = 0;
+    PC_CUDA(ctx, cudaMemcpyAsync(ctx->stage, p->hist_dev, p->hist_elems * sizeof(unsigned long long),
+                                 cudaMemcpyDeviceToHost, ctx->stream));
+    PC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    ctx->stage_plan = p->id;
+    ctx->stage_run = p->run_id;
+  }
+  *out = ctx->stage;
   return PC_OK;
 }
 
@@ -639,6 +709,7 @@ int pc_plan_create(pc_context* ctx, const pc_bin* bins, uint64_t n_bins, const p
   pc_plan* p = new (std::nothrow) pc_plan();
   if (!p) return fail(ctx, PC_ERR_NOMEM, "host allocation");
   std::memset(&p->stats, 0, sizeof(p->stats));
+  p->id = g_plan_ids.fetch_add(1);
   p->inst.resize(1);
   std::string msg;
   int rc = prepare_instance(bins, n_bins, types, n_types, t_max, phi, seed, p->inst[0], msg);
@@ -666,6 +737,7 @@ int pc_plan_set_roots(pc_context* ctx, pc_plan* p, uint64_t root_begin, uint64_t
 
 void pc_plan_destroy(pc_plan* p) {
   if (!p) return;
+  if (p->graph) cudaGraphExecDestroy(p->graph);
   cudaFree(p->types_dev);
   cudaFree(p->btypes_dev);
   cudaFree(p->inst_dev);
@@ -678,48 +750,14 @@ void pc_plan_destroy(pc_plan* p) {
   delete p;
 }
 
-int pc_plan_run(pc_context* ctx, pc_plan* p) {
-  if (!ctx || !p) return PC_ERR_INVALID;
-  PC_CUDA(ctx, cudaSetDevice(ctx->device));
-  cudaStream_t st = ctx->stream;
-  std::memset(&p->stats, 0, sizeof(p->stats));
-  PC_CUDA(ctx, cudaMemsetAsync(p->hist_dev, 0, p->hist_elems * sizeof(unsigned long long), st));
-  PC_CUDA(ctx, cudaMemsetAsync(ctx->stats_dev, 0, 4 * sizeof(unsigned long long), st));
-  PC_CUDA(ctx, cudaMemsetAsync(ctx->error_dev, 0, sizeof(uint32_t), st));
-  const uint64_t nroots = p->root_end - p->root_begin;
-  p->stats.roots = nroots;
-  p->ran = true;
-  p->hist_host_valid = false;
-  if (nroots == 0 || p->nbins == 0) {
-    PC_CUDA(ctx, cudaStreamSynchronize(st));
-    return PC_OK;
-  }
+}  // extern "C"
 
-  // Level-buffer geometry from the memory budget: the depth-first stack never holds more
-  // than one buffer per generation plus one, so (levels + 2) buffers always fit.
-  const int rmax = max_blocks(ctx, ctx->root_bps), dmax = max_blocks(ctx, ctx->div_bps);
-  const uint32_t segs = (uint32_t)std::max(rmax, dmax) * kWarpsPerBlock;
-  double budget = ctx->opt_budget > 0 ? ctx->opt_budget : 0.5 * (double)ctx->free_at_start;
-  const uint32_t levels = std::min<uint32_t>(p->gmax, 40u) + 2u;
-  // Any size <= budget / levels is safe; a buffer near 64 cells per root usually holds a
-  // whole generation, so most generations run as a single sweep.
-  uint64_t cells = (uint64_t)(budget / levels / sizeof(ulonglong2));
-  cells = std::min<uint64_t>(cells, std::max<uint64_t>(1ull << 24, 64ull * nroots));
-  cells = std::max<uint64_t>(cells, 4ull * segs + 1024);
-  if (ctx->pool_cells != cells || ctx->pool_segs < segs) {
-    PC_CUDA(ctx, cudaStreamSynchronize(st));
-    free_pool(ctx);
-    ctx->pool_cells = cells;
-    ctx->pool_segs = segs;
-  }
-  uint64_t max_slice = (cells - 2ull * segs) / 2;
-  if (ctx->opt_max_slice) max_slice = std::min<uint64_t>(max_slice, std::max<uint64_t>(1, ctx->opt_max_slice));
-  const uint64_t chunk = std::min<uint64_t>(p->chunk, cells - segs);
+namespace {
 
+RunArgs make_args(const pc_context* ctx, const pc_plan* p) {
   RunArgs a;
   std::memset(&a, 0, sizeof(a));
   const InstanceHost& I0 = p->inst[0];
-  const bool narrow = p->gmax <= 32;
   if (!p->batched) {
     a.k0 = (uint32_t)I0.seed;
     a.k1 = (uint32_t)(I0.seed >> 32);
@@ -748,6 +786,62 @@ int pc_plan_run(pc_context* ctx, pc_plan* p) {
   a.hist = p->hist_dev;
   a.stats = ctx->stats_dev;
   a.error = ctx->error_dev;
+  return a;
+}
+
+// Resident blocks per SM of a configuration's root, division and persistent kernels.
+int kernel_occupancy(pc_context* ctx, bool narrow, bool batched, int config, const SweepKernels& K, int occ[3]) {
+  int* c = ctx->occ[narrow ? 1 : 0][batched ? 1 : 0][config];
+  if (c[0] == 0) {
+    const int e = K.occupancy(&c[0], &c[1], &c[2]);
+    if (e != 0) {
+      c[0] = 0;
+      return fail(ctx, PC_ERR_CUDA, std::string("occupancy query: ") + cudaGetErrorString((cudaError_t)e));
+    }
+    for (int i = 0; i < 3; ++i) c[i] = std::max(1, c[i]);
+  }
+  for (int i = 0; i < 3; ++i) occ[i] = c[i];
+  return PC_OK;
+}
+
+// Level buffers of `cells` cells each (at least `want`, reused when large enough and not
+// above `cap`), with count/prefix arrays for `segs` segments.
+int ensure_pool_geometry(pc_context* ctx, uint64_t want, uint64_t cap, uint32_t segs) {
+  if (ctx->pool_cells < want || ctx->pool_cells > std::max(cap, want) || ctx->pool_segs < segs) {
+    PC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    free_pool(ctx);
+    ctx->pool_cells = want;
+    ctx->pool_segs = segs;
+  }
+  return PC_OK;
+}
+
+double budget_bytes(const pc_context* ctx) {
+  return ctx->opt_budget > 0 ? ctx->opt_budget : 0.5 * (double)ctx->free_at_start;
+}
+
+// The host driver: one root sweep per chunk, then division sweeps depth-first over a stack
+// of level buffers, the host reading each output level's size.
+int run_per_sweep(pc_context* ctx, pc_plan* p, const SweepKernels& K, const int occ[3], RunArgs& a) {
+  cudaStream_t st = ctx->stream;
+  const uint64_t nroots = p->root_end - p->root_begin;
+  const uint32_t warps = (uint32_t)K.threads / 32u;
+  // Level-buffer geometry from the memory budget: the depth-first stack never holds more
+  // than one buffer per generation plus one, so (levels + 2) buffers always fit.
+  const int rmax = max_blocks(ctx, occ[0]), dmax = max_blocks(ctx, occ[1]);
+  const uint32_t segs = (uint32_t)std::max(rmax, dmax) * warps;
+  const uint32_t levels = std::min<uint32_t>(p->gmax, 40u) + 2u;
+  // Any size <= budget / levels is safe; a buffer near 64 cells per root usually holds a
+  // whole generation, so most generations run as a single sweep.
+  const uint64_t cap = (uint64_t)(budget_bytes(ctx) / levels / sizeof(ulonglong2));
+  uint64_t want = std::min<uint64_t>(cap, std::max<uint64_t>(1ull << 24, 64ull * nroots));
+  want = std::max<uint64_t>(want, 4ull * segs + 1024);
+  int rc = ensure_pool_geometry(ctx, want, cap, segs);
+  if (rc != PC_OK) return rc;
+  const uint64_t cells = ctx->pool_cells;
+  uint64_t max_slice = (cells - 2ull * segs) / 2;
+  if (ctx->opt_max_slice) max_slice = std::min<uint64_t>(max_slice, std::max<uint64_t>(1, ctx->opt_max_slice));
+  const uint64_t chunk = std::min<uint64_t>(p->chunk, cells - segs);
 
   struct Entry {
     int buf;
@@ -758,20 +852,21 @@ int pc_plan_run(pc_context* ctx, pc_plan* p) {
   float ms = 0.f;
   double dev_ms = 0.0, div_ms = 0.0;
   uint64_t divisions = 0;
-  uint32_t sweeps = 0, max_gen = 0;
+  uint32_t sweeps = 0, max_gen = 0, chunks = 0;
 
   for (uint64_t c0 = p->root_begin; c0 < p->root_end; c0 += chunk) {
     const uint64_t n = std::min<uint64_t>(chunk, p->root_end - c0);
     a.root_base = c0;
+    ++chunks;
     int b0 = -1;
-    int rc = acquire(ctx, &b0);
+    rc = acquire(ctx, &b0);
     if (rc != PC_OK) return rc;
     LevelBuf& L = ctx->pool[b0];
-    const int blocks = grid_for(ctx, n, ctx->root_bps);
-    const uint32_t nseg = (uint32_t)blocks * kWarpsPerBlock;
+    const int blocks = grid_for(ctx, n, occ[0], K.threads);
+    const uint32_t nseg = (uint32_t)blocks * warps;
     LevelOut o{L.cells, L.count, L.prefix, L.ticket, (n + nseg - 1) / nseg};
     PC_CUDA(ctx, cudaEventRecord(ctx->ev[0], st));
-    PC_CUDA(ctx, (cudaError_t)launch_root_sweep(a, 0, n, o, blocks, narrow, st));
+    PC_CUDA(ctx, (cudaError_t)K.roots(a, 0, n, o, blocks, st));
     PC_CUDA(ctx, cudaEventRecord(ctx->ev[1], st));
     PC_CUDA(ctx, cudaMemcpyAsync(ctx->pinned, L.prefix + nseg, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
     PC_CUDA(ctx, cudaStreamSynchronize(st));
@@ -791,13 +886,13 @@ int pc_plan_run(pc_context* ctx, pc_plan* p) {
       if (rc != PC_OK) return rc;
       const LevelBuf& In = ctx->pool[top.buf];
       const LevelBuf& Out = ctx->pool[bo];
-      const int blocks_d = grid_for(ctx, len, ctx->div_bps);
-      const uint32_t oseg = (uint32_t)blocks_d * kWarpsPerBlock;
+      const int blocks_d = grid_for(ctx, len, occ[1], K.threads);
+      const uint32_t oseg = (uint32_t)blocks_d * warps;
       LevelIn li{In.cells, In.prefix, top.nseg, top.stride, top.pos, top.pos + len};
       LevelOut lo{Out.cells, Out.count, Out.prefix, Out.ticket, 2 * ((len + oseg - 1) / oseg)};
       const uint32_t gen = top.gen;
       PC_CUDA(ctx, cudaEventRecord(ctx->ev[2], st));
-      PC_CUDA(ctx, (cudaError_t)launch_divide_sweep(a, li, gen, lo, blocks_d, narrow, st));
+      PC_CUDA(ctx, (cudaError_t)K.divide(a, li, gen, lo, blocks_d, st));
       PC_CUDA(ctx, cudaEventRecord(ctx->ev[3], st));
       PC_CUDA(ctx, cudaMemcpyAsync(ctx->pinned, Out.prefix + oseg, sizeof(unsigned long long),
                                    cudaMemcpyDeviceToHost, st));
@@ -824,16 +919,163 @@ int pc_plan_run(pc_context* ctx, pc_plan* p) {
   PC_CUDA(ctx, cudaMemcpyAsync(ctx->pinned, ctx->stats_dev, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
   PC_CUDA(ctx, cudaMemcpyAsync(ctx->pinned + 8, ctx->error_dev, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
   PC_CUDA(ctx, cudaStreamSynchronize(st));
-  p->stats.vanished = ctx->pinned[0];
-  p->stats.uncounted = ctx->pinned[1];
   p->stats.divisions = divisions;
   p->stats.sweeps = sweeps;
   p->stats.max_generation = max_gen;
   p->stats.device_ms = dev_ms;
   p->stats.divide_ms = div_ms;
+  p->stats.d2h_bytes = (uint64_t)(sweeps + chunks) * 8u + 40u;
+  return PC_OK;
+}
+
+// The operations of one persistent run, in stream order (also what a graph captures):
+// clear the counts and control words, the cooperative launch, the totals back to pinned.
+int enqueue_persistent(pc_context* ctx, pc_plan* p, const SweepKernels& K, const PersistArgs& pa, int grid,
+                       cudaStream_t s) {
+  PC_CUDA(ctx, cudaMemsetAsync(p->hist_dev, 0, p->hist_elems * sizeof(unsigned long long), s));
+  PC_CUDA(ctx, cudaMemsetAsync(ctx->stats_dev, 0, 4 * sizeof(unsigned long long), s));
+  PC_CUDA(ctx, cudaMemsetAsync(ctx->error_dev, 0, sizeof(uint32_t), s));
+  PC_CUDA(ctx, cudaMemsetAsync(ctx->persist_ctl, 0, 48, s));
+  PC_CUDA(ctx, (cudaError_t)K.persist(pa, grid, s));
+  PC_CUDA(ctx, cudaMemcpyAsync(ctx->pinned, ctx->stats_dev, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+  PC_CUDA(ctx, cudaMemcpyAsync(ctx->pinned + 8, ctx->error_dev, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+  PC_CUDA(ctx, cudaMemcpyAsync(ctx->pinned + 16, ctx->persist_ctl + 4, 4 * sizeof(unsigned long long),
+                               cudaMemcpyDeviceToHost, s));
+  return PC_OK;
+}
+
+// The persistent driver: the whole run as one cooperative launch (optionally replayed from
+// a captured CUDA graph). Returns PC_ERR_UNSUPPORTED when the plan needs more level
+// buffers than the kernel's schedule holds (the caller then uses the host driver).
+int run_persistent(pc_context* ctx, pc_plan* p, const SweepKernels& K, const int occ[3], const RunArgs& a) {
+  cudaStream_t st = ctx->stream;
+  const uint32_t nbuf = std::min<uint32_t>(p->gmax, p->g_store_max + 1u) + 2u;
+  if (nbuf > (uint32_t)kMaxPool) return PC_ERR_UNSUPPORTED;
+  const uint64_t nroots = p->root_end - p->root_begin;
+  const uint32_t warps = (uint32_t)K.threads / 32u;
+  int grid = ctx->sms * occ[2];
+  if (ctx->opt_grid_blocks > 0) grid = std::min(grid, ctx->opt_grid_blocks);
+  const uint32_t segs = (uint32_t)grid * warps;
+  const uint64_t cap = (uint64_t)(budget_bytes(ctx) / nbuf / sizeof(ulonglong2));
+  uint64_t want = std::min<uint64_t>(cap, std::max<uint64_t>(1ull << 24, 64ull * nroots));
+  want = std::max<uint64_t>(want, 4ull * segs + 1024);
+  int rc = ensure_pool_geometry(ctx, want, cap, segs);
+  if (rc != PC_OK) return rc;
+  const uint64_t cells = ctx->pool_cells;
+  std::vector<int> held;
+  for (uint32_t i = 0; i < nbuf; ++i) {
+    int b = -1;
+    rc = acquire(ctx, &b);
+    if (rc != PC_OK) {
+      for (int h : held) ctx->pool[h].busy = false;
+      return rc;
+    }
+    held.push_back(b);
+  }
+  PersistArgs pa;
+  std::memset(&pa, 0, sizeof(pa));
+  pa.a = a;
+  for (uint32_t i = 0; i < nbuf; ++i) {
+    const LevelBuf& L = ctx->pool[held[i]];
+    pa.cells[i] = L.cells;
+    pa.count[i] = L.count;
+    pa.prefix[i] = L.prefix;
+    pa.ticket[i] = L.ticket;
+  }
+  for (int h : held) ctx->pool[h].busy = false;  // stream order protects the run
+  pa.nbuf = nbuf;
+  pa.g_limit = p->g_store_max;
+  pa.root_lo = p->root_begin;
+  pa.root_hi = p->root_end;
+  pa.chunk = std::min<uint64_t>(p->chunk, cells - segs);
+  pa.max_slice = (cells - 2ull * segs) / 2;
+  if (ctx->opt_max_slice) pa.max_slice = std::min<uint64_t>(pa.max_slice, std::max<uint64_t>(1, ctx->opt_max_slice));
+  pa.barrier = ctx->persist_ctl;
+  pa.out = reinterpret_cast<unsigned long long*>(ctx->persist_ctl + 4);
+  pa.timeout_ns = 20000000000ull;
+
+  float ms = 0.f;
+  PC_CUDA(ctx, cudaEventRecord(ctx->ev[0], st));
+  if (ctx->opt_graph) {
+    const bool same = p->graph && p->graph_config == ctx->opt_config && p->graph_grid == grid &&
+                      std::memcmp(&p->graph_args, &pa, sizeof(pa)) == 0;
+    if (!same) {
+      if (p->graph) cudaGraphExecDestroy(p->graph);
+      p->graph = nullptr;
+      cudaStream_t cap_st = ctx->own_stream;
+      PC_CUDA(ctx, cudaStreamSynchronize(st));
+      PC_CUDA(ctx, cudaStreamBeginCapture(cap_st, cudaStreamCaptureModeThreadLocal));
+      rc = enqueue_persistent(ctx, p, K, pa, grid, cap_st);
+      cudaGraph_t g = nullptr;
+      const cudaError_t ee = cudaStreamEndCapture(cap_st, &g);
+      if (rc != PC_OK) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+      }
+      PC_CUDA(ctx, ee);
+      const cudaError_t ei = cudaGraphInstantiate(&p->graph, g, 0);
+      cudaGraphDestroy(g);
+      PC_CUDA(ctx, ei);
+      p->graph_args = pa;
+      p->graph_config = ctx->opt_config;
+      p->graph_grid = grid;
+    }
+    PC_CUDA(ctx, cudaGraphLaunch(p->graph, st));
+  } else {
+    rc = enqueue_persistent(ctx, p, K, pa, grid, st);
+    if (rc != PC_OK) return rc;
+  }
+  PC_CUDA(ctx, cudaEventRecord(ctx->ev[1], st));
+  PC_CUDA(ctx, cudaStreamSynchronize(st));
+  PC_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]));
+  p->stats.divisions = ctx->pinned[16];
+  p->stats.sweeps = (uint32_t)ctx->pinned[17];
+  p->stats.max_generation = (uint32_t)ctx->pinned[18];
+  p->stats.device_ms = ms;
+  p->stats.divide_ms = ms;  // root and division sweeps share the launch
+  p->stats.d2h_bytes = 72u;
+  return PC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pc_plan_run(pc_context* ctx, pc_plan* p) {
+  if (!ctx || !p) return PC_ERR_INVALID;
+  PC_CUDA(ctx, cudaSetDevice(ctx->device));
+  cudaStream_t st = ctx->stream;
+  std::memset(&p->stats, 0, sizeof(p->stats));
+  const uint64_t nroots = p->root_end - p->root_begin;
+  p->stats.roots = nroots;
+  p->ran = true;
+  ++p->run_id;
+  const bool narrow = p->gmax <= 32;
+  const int config = narrow ? ctx->opt_config : kDefaultSweepConfig;
+  const SweepKernels& K = sweep_kernels(narrow, p->batched, config);
+  int occ[3];
+  int rc = kernel_occupancy(ctx, narrow, p->batched, config, K, occ);
+  if (rc != PC_OK) return rc;
+  RunArgs a = make_args(ctx, p);
+  rc = PC_ERR_UNSUPPORTED;
+  if (ctx->opt_driver == 1 && nroots > 0 && p->nbins > 0) rc = run_persistent(ctx, p, K, occ, a);
+  if (rc == PC_ERR_UNSUPPORTED) {
+    PC_CUDA(ctx, cudaMemsetAsync(p->hist_dev, 0, p->hist_elems * sizeof(unsigned long long), st));
+    PC_CUDA(ctx, cudaMemsetAsync(ctx->stats_dev, 0, 4 * sizeof(unsigned long long), st));
+    PC_CUDA(ctx, cudaMemsetAsync(ctx->error_dev, 0, sizeof(uint32_t), st));
+    if (nroots == 0 || p->nbins == 0) {
+      PC_CUDA(ctx, cudaStreamSynchronize(st));
+      return PC_OK;
+    }
+    rc = run_per_sweep(ctx, p, K, occ, a);
+  }
+  if (rc != PC_OK) return rc;
+  p->stats.vanished = ctx->pinned[0];
+  p->stats.uncounted = ctx->pinned[1];
   p->stats.h2d_bytes = p->upload_bytes;
-  p->stats.d2h_bytes = (uint64_t)(sweeps + (p->root_end - p->root_begin + chunk - 1) / chunk) * 8u + 40u;
   const uint32_t err = (uint32_t)(ctx->pinned[8] & 0xFFFFFFFFu);
+  if (err & 4u) return fail(ctx, PC_ERR_CUDA, "persistent driver: a grid barrier timed out");
+  if (err & 8u) return fail(ctx, PC_ERR_CUDA, "internal: the persistent schedule ran out of level buffers");
   if (err & 2u) return fail(ctx, PC_ERR_CUDA, "internal: the normal sampler exceeded its rejection budget");
   if (err & 1u)
     return fail(ctx, PC_ERR_DEPTH, "a lineage exceeded the deepest generation the key layout holds");
@@ -862,10 +1104,10 @@ int pc_plan_raw_counts(pc_context* ctx, pc_plan* p, uint64_t* host_out, uint64_t
   if (!host_out) return PC_OK;
   if (capacity < n) return fail(ctx, PC_ERR_INVALID, "raw count buffer too small");
   if (!p->ran) return fail(ctx, PC_ERR_INVALID, "plan has not run");
-  std::vector<unsigned long long> h;
-  const int rc = fetch_hist(ctx, p, h);
+  const unsigned long long* h = nullptr;
+  const int rc = stage_table(ctx, p, &h);
   if (rc != PC_OK) return rc;
-  instance_counts(p, I, h.data(), host_out);
+  instance_counts(p, I, h, host_out);
   return PC_OK;
 }
 
@@ -873,11 +1115,12 @@ int pc_plan_result(pc_context* ctx, pc_plan* p, pc_histogram* out) {
   if (!ctx || !p || !out || p->inst.empty()) return PC_ERR_INVALID;
   std::memset(out, 0, sizeof(*out));
   if (!p->ran) return fail(ctx, PC_ERR_INVALID, "plan has not run");
-  std::vector<unsigned long long> h;
-  int rc = fetch_hist(ctx, p, h);
+  const unsigned long long* h = nullptr;
+  int rc = stage_table(ctx, p, &h);
   if (rc != PC_OK) return rc;
-  rc = instance_result(ctx, p, p->inst[0], h.data(), out);
-  if (rc != PC_OK) return rc;
+  const char* msg = "";
+  rc = instance_result(p, p->inst[0], h, out, &msg);
+  if (rc != PC_OK) return fail(ctx, rc, msg);
   const uint64_t leaves = out->stats.leaves;
   out->stats = p->stats;
   out->stats.leaves = leaves;
@@ -914,17 +1157,20 @@ int pc_batch_create(pc_context* ctx, const pc_instance* instances, uint32_t n_in
   pc_batch* b = new (std::nothrow) pc_batch();
   if (!b) return fail(ctx, PC_ERR_NOMEM, "host allocation");
   std::memset(&b->stats, 0, sizeof(b->stats));
+  b->id = g_plan_ids.fetch_add(1);
   b->batched = true;
   b->inst.resize(n_instances);
-  for (uint32_t i = 0; i < n_instances; ++i) {
+  std::vector<int> codes(n_instances, PC_OK);
+  std::vector<std::string> msgs(n_instances);
+  parallel_for(n_instances, [&](uint32_t i) {
     const pc_instance& x = instances[i];
-    std::string msg;
-    const int rc = prepare_instance(x.bins, x.n_bins, x.types, x.n_types, x.t_max, x.phi, x.seed, b->inst[i], msg);
-    if (rc != PC_OK) {
+    codes[i] = prepare_instance(x.bins, x.n_bins, x.types, x.n_types, x.t_max, x.phi, x.seed, b->inst[i], msgs[i]);
+  });
+  for (uint32_t i = 0; i < n_instances; ++i)
+    if (codes[i] != PC_OK) {
       delete b;
-      return fail(ctx, rc, "instance " + std::to_string(i) + ": " + msg);
+      return fail(ctx, codes[i], "instance " + std::to_string(i) + ": " + msgs[i]);
     }
-  }
   const int rc = finalize_plan(ctx, b);
   if (rc != PC_OK) {
     pc_batch_destroy(b);
@@ -940,15 +1186,10 @@ int pc_batch_stats(pc_context* ctx, const pc_batch* b, pc_stats* out) { return p
 
 uint32_t pc_batch_size(const pc_batch* b) { return b ? (uint32_t)b->inst.size() : 0u; }
 
-static int batch_table(pc_context* ctx, pc_batch* b, uint32_t instance) {
+static int batch_table(pc_context* ctx, pc_batch* b, uint32_t instance, const unsigned long long** h) {
   if (instance >= b->inst.size()) return fail(ctx, PC_ERR_INVALID, "instance index out of range");
   if (!b->ran) return fail(ctx, PC_ERR_INVALID, "batch has not run");
-  if (!b->hist_host_valid) {
-    const int rc = fetch_hist(ctx, b, b->hist_host);
-    if (rc != PC_OK) return rc;
-    b->hist_host_valid = true;
-  }
-  return PC_OK;
+  return stage_table(ctx, b, h);
 }
 
 int pc_batch_raw_counts(pc_context* ctx, pc_batch* b, uint32_t instance, uint64_t* host_out, uint64_t capacity,
@@ -966,20 +1207,23 @@ int pc_batch_raw_counts(pc_context* ctx, pc_batch* b, uint32_t instance, uint64_
   }
   if (!host_out) return PC_OK;
   if (capacity < n) return fail(ctx, PC_ERR_INVALID, "raw count buffer too small");
-  const int rc = batch_table(ctx, b, instance);
+  const unsigned long long* h = nullptr;
+  const int rc = batch_table(ctx, b, instance, &h);
   if (rc != PC_OK) return rc;
-  instance_counts(b, I, b->hist_host.data(), host_out);
+  instance_counts(b, I, h, host_out);
   return PC_OK;
 }
 
 int pc_batch_result(pc_context* ctx, pc_batch* b, uint32_t instance, pc_histogram* out) {
   if (!ctx || !b || !out) return PC_ERR_INVALID;
   std::memset(out, 0, sizeof(*out));
-  int rc = batch_table(ctx, b, instance);
+  const unsigned long long* h = nullptr;
+  int rc = batch_table(ctx, b, instance, &h);
   if (rc != PC_OK) return rc;
   const InstanceHost& I = b->inst[instance];
-  rc = instance_result(ctx, b, I, b->hist_host.data(), out);
-  if (rc != PC_OK) return rc;
+  const char* msg = "";
+  rc = instance_result(b, I, h, out, &msg);
+  if (rc != PC_OK) return fail(ctx, rc, msg);
   out->stats.roots = I.roots;
   return PC_OK;
 }
@@ -993,7 +1237,18 @@ int pc_simulate_batch(pc_context* ctx, const pc_instance* instances, uint32_t n_
   int rc = pc_batch_create(ctx, instances, n_instances, &b);
   if (rc != PC_OK) return rc;
   rc = pc_batch_run(ctx, b);
-  for (uint32_t i = 0; rc == PC_OK && i < n_instances; ++i) rc = pc_batch_result(ctx, b, i, out + i);
+  const unsigned long long* h = nullptr;
+  if (rc == PC_OK) rc = batch_table(ctx, b, 0, &h);
+  if (rc == PC_OK) {
+    std::vector<int> codes(n_instances, PC_OK);
+    std::vector<const char*> msgs(n_instances, "");
+    parallel_for(n_instances, [&](uint32_t i) {
+      codes[i] = instance_result(b, b->inst[i], h, out + i, &msgs[i]);
+      out[i].stats.roots = b->inst[i].roots;
+    });
+    for (uint32_t i = 0; rc == PC_OK && i < n_instances; ++i)
+      if (codes[i] != PC_OK) rc = fail(ctx, codes[i], msgs[i]);
+  }
   if (rc != PC_OK)
     for (uint32_t i = 0; i < n_instances; ++i) pc_histogram_free(out + i);
   pc_batch_destroy(b);

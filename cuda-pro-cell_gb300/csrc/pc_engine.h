@@ -1,5 +1,6 @@
 // Internal interface between the host driver (pc_api.cpp) and the sm_103a kernels
-// (pc_kernels.cu). Not part of the public ABI.
+// (pc_sweeps.cuh, instantiated in pc_kernels.cu and pc_tuned_*.cu). Not part of the
+// public ABI.
 //
 // Data layout in HBM
 // ------------------
@@ -112,12 +113,51 @@ struct LevelOut {
   uint64_t stride;
 };
 
-// Launchers (pc_kernels.cu). All return the cudaError_t of the launch as int.
+// Persistent driver: one launch runs every sweep of a plan. Its blocks (all resident: a
+// cooperative launch) walk the same depth-first schedule of root chunks and generation
+// slices as the host driver, each block keeping an identical copy of the schedule in
+// shared memory and deciding from the level totals it reads after a grid barrier.
+constexpr int kMaxPool = 48;
+
+struct PersistArgs {
+  RunArgs a;
+  ulonglong2* cells[kMaxPool];
+  unsigned long long* count[kMaxPool];
+  unsigned long long* prefix[kMaxPool];
+  uint32_t* ticket[kMaxPool];
+  uint32_t nbuf;
+  uint32_t g_limit;                 // deepest generation whose cells are stored
+  uint64_t root_lo, root_hi;        // initial cells of the run
+  uint64_t chunk;                   // initial cells per root sweep
+  uint64_t max_slice;               // input cells per division sweep
+  uint32_t* barrier;                // [2] arrivals, generation (zero before the launch)
+  unsigned long long* out;          // [4] divisions, sweeps, max generation, chunks
+  unsigned long long timeout_ns;    // a grid barrier waiting longer sets error bit 2
+};
+
+// One compiled configuration of the sweeps (the autotuner's search space): threads per
+// block, input cells per lane per step, and where leaf counts are privatised (a window of
+// classes in shared memory, or warp-aggregated atomics straight to the global table).
+struct SweepKernels {
+  int threads, cells, global_hist;
+  int (*roots)(const RunArgs& a, uint64_t lo, uint64_t hi, const LevelOut& out, int blocks, void* stream);
+  int (*divide)(const RunArgs& a, const LevelIn& in, uint32_t gen, const LevelOut& out, int blocks,
+                void* stream);
+  int (*persist)(const PersistArgs& p, int blocks, void* stream);  // cooperative launch
+  int (*occupancy)(int* roots_per_sm, int* divide_per_sm, int* persist_per_sm);
+};
+
+constexpr int kNumSweepConfigs = 8;  // {128, 256} threads x {1, 2} cells x {smem, global}
+constexpr int kDefaultSweepConfig = 4;  // 256 threads, 1 cell per lane, shared-memory window
+// narrow key layout: any configuration; wide layout: the default configuration only.
+const SweepKernels& sweep_kernels(bool narrow, bool batched, int config);
+
+// Launchers of the default configuration (pc_kernels.cu). All return the cudaError_t of
+// the launch as int; a.btypes != nullptr selects the batched instantiations.
 int launch_root_sweep(const RunArgs& a, uint64_t root_lo, uint64_t root_hi, const LevelOut& out,
                       int blocks, bool narrow, void* stream);
 int launch_divide_sweep(const RunArgs& a, const LevelIn& in, uint32_t gen, const LevelOut& out,
                         int blocks, bool narrow, void* stream);
-// a.btypes != nullptr selects the batched instantiations of both sweeps.
 int launch_debug_philox(const uint32_t* ctr, uint64_t n, uint32_t k0, uint32_t k1, uint32_t* out,
                         void* stream);
 int launch_debug_normals(const ZigTables* zig, uint32_t k0, uint32_t k1, uint32_t root,

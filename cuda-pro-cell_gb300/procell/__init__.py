@@ -35,10 +35,10 @@ class Plan:
     def __init__(self, engine: "Engine", bins, types, t_max, phi=None, seed=0):
         self.engine = engine
         L = engine.L
-        self._bins = _lib.bins_array(bins)
-        self._types = _lib.types_array(types)
+        b, t = _lib.bins_numpy(bins), _lib.types_numpy(types)
         h = ctypes.c_void_p()
-        rc = L.pc_plan_create(engine.ctx, self._bins, len(bins), self._types, len(types),
+        rc = L.pc_plan_create(engine.ctx, b.ctypes.data_as(ctypes.POINTER(_lib.Bin)), len(b),
+                              t.ctypes.data_as(ctypes.POINTER(_lib.CellType)), len(t),
                               float(t_max), 0.0 if phi is None else float(phi), int(seed),
                               ctypes.byref(h))
         engine._check(rc)
@@ -186,7 +186,7 @@ class Engine:
         p = self.plan(bins, types, t_max, phi, seed)
         try:
             if root_begin is not None or root_end is not None:
-                total = sum(int(f) for _, f in bins)
+                total = int(_lib.bins_numpy(bins)["frequency"].sum())
                 p.set_roots(root_begin or 0, total if root_end is None else root_end)
             p.run()
             return p.result()
