@@ -144,6 +144,8 @@ def run_reference(args):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     oracle.build()
+    if args.workload == "batched":
+        return run_reference_batched(args)
     w = workload(args.workload)
     cores = os.cpu_count() or 1
     per_step = max(2.0, args.cpu_seconds / 2)
@@ -172,6 +174,33 @@ def run_reference(args):
     return 0
 
 
+def run_reference_batched(args):
+    instances = batched_instances()
+    per_step = max(2.0, args.cpu_seconds / 2)
+    for _ in range(args.warmup):
+        cpu_batched_sample(instances, per_step / 4)
+    vals, secs = [], 0.0
+    for _ in range(args.steps):
+        c = cpu_batched_sample(instances, per_step)
+        vals.append(c)
+    done = sum(float(c["sample"].split()[2]) for c in vals)
+    secs = sum(float(c["sample"].split("(")[1].split()[0]) for c in vals)
+    value = done / secs
+    line = {
+        "impl": "reference", "metric": "instances/s (batched form)", "value": value, "unit": "instances/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded generator, procell/configs.py batched())",
+        "config": {"workload": "batched: %d instances" % len(instances),
+                   "sample": "instances drawn at random, about %.0f s per step" % per_step},
+        "cpu_baseline": {"value": value, "unit": "instances/s", "cores": vals[0]["cores"], "kind": "port",
+                         "sample": "; ".join(c["sample"] for c in vals)},
+        "e2e": {"value": value, "unit": "instances/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_ours(args):
     import torch
     rank, world, local = dist_env()
@@ -192,6 +221,7 @@ def run_ours(args):
     stream = torch.cuda.current_stream()
     eng.set_stream(stream.cuda_stream)
     plan = eng.plan(w.bins, w.types, w.t_max, w.phi, seed)
+    tuning = eng.autotune(plan, repeats=1) if not args.no_tune else None
 
     def barrier():
         torch.cuda.synchronize()
@@ -205,7 +235,7 @@ def run_ours(args):
     clocks.start()
     time.sleep(0.3)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    divisions = roots = sweeps = 0
+    divisions = roots = sweeps = kernels = 0
     divide_ms = device_ms = 0.0
     e0.record(stream)
     for _ in range(args.steps):
@@ -214,6 +244,7 @@ def run_ours(args):
         divisions += st["divisions"]
         roots += st["roots"]
         sweeps += st["sweeps"]
+        kernels += st["kernel_launches"]
         divide_ms += st["divide_ms"]
         device_ms += st["device_ms"]
     e1.record(stream)
@@ -252,7 +283,8 @@ def run_ours(args):
     # dominant kernel: the division sweep. Algorithmic bytes: each division creates two
     # tree nodes, each node's 16-byte state written once and read once (32 B per node).
     alg_bytes = 2 * ALG_BYTES_PER_NODE * divisions
-    launches = max(1, sweeps)
+    persistent = bool(tuning and tuning["driver"])
+    launches = max(1, args.steps if persistent else sweeps)  # launches of the dominant kernel
     achieved = alg_bytes / (divide_ms * 1e-3) / 1e9 if divide_ms > 0 else None
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "traffic_per_division.txt")
@@ -289,17 +321,20 @@ def run_ours(args):
                    "nodes_per_step": (roots + 2 * divisions) // args.steps,
                    "l2": "no flush: each step streams %.0f GB of level buffers, >> 129 MB L2"
                          % (2 * 16 * divisions / args.steps / 1e9),
-                   "parallelism": f"one independent instance per GPU x{world}"},
+                   "parallelism": f"one independent instance per GPU x{world}",
+                   "tuning": tuning},
         "e2e": {"value": tot_e2e_div / e2e_t, "unit": UNIT,
                 "h2d_bytes_per_step": h2d // args.steps, "d2h_bytes_per_step": d2h // args.steps},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": (achieved / hbm) if achieved else None, "traffic": traffic,
                      "peak_source": peak_kind,
-                     "kernel": "k_divide", "launches_per_step": sweeps / args.steps,
+                     "kernel": "k_persist" if (tuning and tuning["driver"]) else "k_divide",
+                     "launches_per_step": launches / args.steps,
                      "alg_bytes_per_launch": alg_bytes / launches,
                      "note": "alg bytes = 64 B per division (two 16-B nodes written+read); the "
-                             "kernel stores only daughters that divide again"},
-        "gpu_launches": (sweeps + args.steps * 1),
+                             "kernel stores only daughters that divide again"
+                             + ("; the persistent launch also runs the root sweep" if persistent else "")},
+        "gpu_launches": kernels,
         "clocks": clk,
         "device_ms_per_step": device_ms / args.steps,
     }
@@ -366,6 +401,7 @@ def run_batched(args):
     stream = torch.cuda.current_stream()
     eng.set_stream(stream.cuda_stream)
     batch = eng.batch(instances)
+    tuning = eng.autotune(batch, repeats=1) if not args.no_tune else None
     for _ in range(args.warmup):
         batch.run()
     torch.cuda.synchronize()
@@ -373,7 +409,7 @@ def run_batched(args):
     clocks.start()
     time.sleep(0.3)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    divisions = roots = sweeps = 0
+    divisions = roots = sweeps = kernels = 0
     divide_ms = device_ms = 0.0
     e0.record(stream)
     for _ in range(args.steps):
@@ -382,6 +418,7 @@ def run_batched(args):
         divisions += st["divisions"]
         roots += st["roots"]
         sweeps += st["sweeps"]
+        kernels += st["kernel_launches"]
         divide_ms += st["divide_ms"]
         device_ms += st["device_ms"]
     e1.record(stream)
@@ -397,46 +434,39 @@ def run_batched(args):
     batch_counts = [batch.raw_counts(i) for i in range(n)]
     batch.close()
 
-    # looping the plain form over the same instances: one pc_simulate per instance (host
-    # inputs in, merged histogram out), and plan + run + raw counts for the parity check
+    # Looping the plain form over the same instances, with the same tuned configuration:
+    # (a) one pc_simulate per instance (host inputs in, merged histogram out), against e2e;
+    # (b) plans created beforehand, one pc_plan_run per instance, against value; the same
+    #     plans give the per-instance parity check.
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for bins, types, t_max, phi, seed in instances:
         eng.simulate(bins, types, t_max, phi, seed)
     torch.cuda.synchronize()
-    loop_s = time.perf_counter() - t0
-    same = 0
-    for i, (bins, types, t_max, phi, seed) in enumerate(instances):
-        p = eng.plan(bins, types, t_max, phi, seed)
+    loop_e2e_s = time.perf_counter() - t0
+    plans = [eng.plan(*x) for x in instances]
+    for p in plans[:64]:
         p.run()
-        same += int(np.array_equal(p.raw_counts(), batch_counts[i]))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for p in plans:
+        p.run()
+    torch.cuda.synchronize()
+    loop_run_s = time.perf_counter() - t0
+    same = sum(int(np.array_equal(p.raw_counts(), batch_counts[i])) for i, p in enumerate(plans))
+    for p in plans:
         p.close()
 
     hbm, peak_kind = peaks()
     alg_bytes = 2 * ALG_BYTES_PER_NODE * divisions
-    launches = max(1, sweeps)
+    persistent = bool(tuning and tuning["driver"])
+    launches = max(1, args.steps if persistent else sweeps)
     achieved = alg_bytes / (divide_ms * 1e-3) / 1e9 if divide_ms > 0 else None
     value = n * args.steps / (elapsed_ms * 1e-3)
     e2e_value = n * args.steps / e2e_t
     cpu = None
     if not args.no_cpu_baseline:
-        sys.path.insert(0, os.path.join(ROOT, "oracle"))
-        import oracle
-        oracle.build()
-        cores = os.cpu_count() or 1
-        order = np.random.default_rng(0).permutation(n)
-        t0 = time.perf_counter()
-        done = 0
-        for i in order:
-            bins, types, t_max, phi, seed = instances[i]
-            rows = list(zip(bins[0].tolist(), bins[1].tolist()))
-            oracle.simulate(rows, types, t_max, phi, seed=seed, nthreads=cores)
-            done += 1
-            if time.perf_counter() - t0 > args.cpu_seconds:
-                break
-        cs = time.perf_counter() - t0
-        cpu = {"value": done / cs, "unit": "instances/s", "cores": cores, "kind": "port",
-               "sample": "oracle on %d instances drawn at random from the %d (%.1f s)" % (done, n, cs)}
+        cpu = cpu_batched_sample(instances, args.cpu_seconds)
     line = {
         "metric": "instances/s (batched form)",
         "value": value,
@@ -455,22 +485,25 @@ def run_batched(args):
                                "fluorescence log-U[1,1e4], phi = min nonzero bin" % (n, roots // args.steps),
                    "divisions_per_step": divisions // args.steps,
                    "nodes_per_step": (roots + 2 * divisions) // args.steps,
+                   "tuning": tuning,
                    "l2": "no flush: each step streams %.0f GB of level buffers, >> 129 MB L2"
                          % (2 * 16 * divisions / args.steps / 1e9)},
         "divisions_per_s": divisions / (elapsed_ms * 1e-3),
-        "loop_plain": {"instances_per_s": n / loop_s, "seconds": loop_s,
-                       "how": "one pc_simulate per instance (host inputs, merged histogram out)"},
-        "speedup_vs_loop_plain": (n / loop_s and value / (n / loop_s)),
-        "e2e_speedup_vs_loop_plain": e2e_value / (n / loop_s),
+        "loop_plain": {"run_instances_per_s": n / loop_run_s,
+                       "e2e_instances_per_s": n / loop_e2e_s,
+                       "run": "plans created beforehand, one pc_plan_run per instance",
+                       "e2e": "one pc_simulate per instance (host inputs, merged histogram out)"},
+        "speedup_vs_loop_plain": value / (n / loop_run_s),
+        "e2e_speedup_vs_loop_plain": e2e_value / (n / loop_e2e_s),
         "bit_exact_instances": "%d/%d" % (same, n),
         "e2e": {"value": e2e_value, "unit": "instances/s", "h2d_bytes_per_step": h2d // args.steps,
                 "d2h_bytes_per_step": d2h // args.steps},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": (achieved / hbm) if achieved else None, "traffic": None,
-                     "peak_source": peak_kind, "kernel": "k_divide",
-                     "launches_per_step": sweeps / args.steps,
+                     "peak_source": peak_kind, "kernel": "k_persist" if persistent else "k_divide",
+                     "launches_per_step": launches / args.steps,
                      "alg_bytes_per_launch": alg_bytes / launches},
-        "gpu_launches": sweeps + args.steps,
+        "gpu_launches": kernels,
         "clocks": clk,
         "device_ms_per_step": device_ms / args.steps,
     }
@@ -478,6 +511,29 @@ def run_batched(args):
         line["cpu_baseline"] = cpu
     print(json.dumps(line), flush=True)
     return 0
+
+
+def cpu_batched_sample(instances, seconds):
+    """Oracle instances/s on instances drawn at random (seeded) until `seconds` pass."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build()
+    cores = os.cpu_count() or 1
+    order = np.random.default_rng(0).permutation(len(instances))
+    t0 = time.perf_counter()
+    done = 0
+    for i in order:
+        bins, types, t_max, phi, seed = instances[i]
+        rows = list(zip(bins[0].tolist(), bins[1].tolist()))
+        oracle.simulate(rows, types, t_max, phi, seed=seed, nthreads=cores)
+        done += 1
+        if time.perf_counter() - t0 > seconds:
+            break
+    cs = time.perf_counter() - t0
+    return {"value": done / cs, "unit": "instances/s", "cores": cores, "kind": "port",
+            "sample": "oracle on %d instances drawn at random from the %d (%.1f s), %d threads"
+                      % (done, len(instances), cs, cores)}
 
 
 def main():
@@ -489,6 +545,7 @@ def main():
     ap.add_argument("--workload", choices=["small", "medium", "large", "batched"], default="large")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (default configuration)")
     args = ap.parse_args()
     if args.warmup < 3:
         print("warning: --warmup < 3 violates the timing rules", file=sys.stderr)

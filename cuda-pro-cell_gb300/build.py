@@ -59,7 +59,7 @@ def build(verbose: bool = False, out: str | None = None, defines=()) -> str:
     jobs = []
     objs = []
     dflags = ["-D" + d for d in defines]
-    for name in ("pc_kernels.cu", "pc_tuned_plain.cu", "pc_tuned_batched.cu", "pc_noalloc.cu"):
+    for name in ("pc_kernels.cu", "pc_tuned_plain.cu", "pc_tuned_batched.cu", "pc_noalloc.cu", "pc_smooth.cu"):
         k_src = os.path.join(CSRC, name)
         k_obj = os.path.join(OUT, name.replace(".cu", ".o"))
         objs.append(k_obj)

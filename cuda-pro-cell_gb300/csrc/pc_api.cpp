@@ -17,6 +17,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <atomic>
+#include <chrono>
 #include <map>
 #include <new>
 #include <string>
@@ -921,6 +922,8 @@ int run_per_sweep(pc_context* ctx, pc_plan* p, const SweepKernels& K, const int 
   PC_CUDA(ctx, cudaStreamSynchronize(st));
   p->stats.divisions = divisions;
   p->stats.sweeps = sweeps;
+  p->stats.root_sweeps = chunks;
+  p->stats.kernel_launches = sweeps + chunks;
   p->stats.max_generation = max_gen;
   p->stats.device_ms = dev_ms;
   p->stats.divide_ms = div_ms;
@@ -1031,6 +1034,8 @@ int run_persistent(pc_context* ctx, pc_plan* p, const SweepKernels& K, const int
   p->stats.divisions = ctx->pinned[16];
   p->stats.sweeps = (uint32_t)ctx->pinned[17];
   p->stats.max_generation = (uint32_t)ctx->pinned[18];
+  p->stats.root_sweeps = (uint32_t)ctx->pinned[19];
+  p->stats.kernel_launches = 1;
   p->stats.device_ms = ms;
   p->stats.divide_ms = ms;  // root and division sweeps share the launch
   p->stats.d2h_bytes = 72u;
@@ -1255,6 +1260,61 @@ int pc_simulate_batch(pc_context* ctx, const pc_instance* instances, uint32_t n_
   return rc;
 }
 
+int pc_autotune(pc_context* ctx, pc_plan* p, uint32_t repeats, pc_tuning* out) {
+  if (!ctx || !p || !out) return PC_ERR_INVALID;
+  std::memset(out, 0, sizeof(*out));
+  repeats = std::max<uint32_t>(1, repeats);
+  const bool narrow = p->gmax <= 32;
+  const int saved[3] = {ctx->opt_config, ctx->opt_driver, ctx->opt_graph};
+  double best = 1e300, dflt = 0.0;
+  int best_cfg = kDefaultSweepConfig, best_drv = 0, n = 0;
+  for (int drv = 0; drv < 2; ++drv)
+    for (int cfg = 0; cfg < kNumSweepConfigs; ++cfg) {
+      if (!narrow && cfg != kDefaultSweepConfig) continue;
+      ctx->opt_config = cfg;
+      ctx->opt_driver = drv;
+      ctx->opt_graph = drv;
+      int rc = pc_plan_run(ctx, p);  // warm-up (and graph capture)
+      double t_best = 1e300;
+      for (uint32_t r = 0; rc == PC_OK && r < repeats; ++r) {
+        const auto t0 = std::chrono::steady_clock::now();
+        rc = pc_plan_run(ctx, p);
+        const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        t_best = std::min(t_best, ms);
+      }
+      if (rc != PC_OK) {
+        ctx->opt_config = saved[0];
+        ctx->opt_driver = saved[1];
+        ctx->opt_graph = saved[2];
+        return rc;
+      }
+      ++n;
+      if (drv == 0 && cfg == kDefaultSweepConfig) dflt = t_best;
+      if (t_best < best) {
+        best = t_best;
+        best_cfg = cfg;
+        best_drv = drv;
+      }
+    }
+  ctx->opt_config = best_cfg;
+  ctx->opt_driver = best_drv;
+  ctx->opt_graph = best_drv;
+  const SweepKernels& K = sweep_kernels(narrow, p->batched, best_cfg);
+  out->config = best_cfg;
+  out->driver = best_drv;
+  out->threads = K.threads;
+  out->cells_per_lane = K.cells;
+  out->global_hist = K.global_hist;
+  out->candidates = n;
+  out->ms = best;
+  out->ms_default = dflt;
+  return PC_OK;
+}
+
+int pc_batch_autotune(pc_context* ctx, pc_batch* b, uint32_t repeats, pc_tuning* out) {
+  return pc_autotune(ctx, b, repeats, out);
+}
+
 int pc_debug_philox(pc_context* ctx, const uint32_t* ctr, uint64_t n, const uint32_t key[2], uint32_t* out) {
   if (!ctx || (n && (!ctr || !out)) || !key) return PC_ERR_INVALID;
   if (n == 0) return PC_OK;
@@ -1296,3 +1356,195 @@ int pc_debug_tables(pc_context* ctx, uint32_t* k, uint32_t* w_bits, uint32_t* f_
 }
 
 }  // extern "C"
+
+// ---- Smoothed (differentiable) form ------------------------------------------------------
+struct pc_smooth {
+  InstanceHost I;  // bins, phi caps, output value set and (bin, generation) -> value map
+  uint32_t ntypes = 0, paths = 1, rows = 1;
+  double h = 0.5;
+  uint64_t* bin_start_dev = nullptr;
+  uint32_t* bin_cap_dev = nullptr;
+  int32_t* vidx_dev = nullptr;
+  uint32_t* inv_off_dev = nullptr;
+  uint32_t* inv_idx_dev = nullptr;
+  double* e_raw_dev = nullptr;   // [cand_cap][nbins][rows]
+  double* part_dev = nullptr;    // [cand_cap][nbins][ntypes * 3]
+  uint32_t cand_cap = 0;
+};
+
+namespace {
+
+SmoothArgs smooth_args(const pc_context* ctx, const pc_smooth* s) {
+  SmoothArgs A;
+  std::memset(&A, 0, sizeof(A));
+  A.k0 = (uint32_t)s->I.seed;
+  A.k1 = (uint32_t)(s->I.seed >> 32);
+  A.nbins = (uint32_t)s->I.bin_value.size();
+  A.rows = s->rows;
+  A.ntypes = s->ntypes;
+  A.paths = s->paths;
+  A.t_max = s->I.t_max;
+  A.inv_h = 1.0 / s->h;
+  A.bin_start = s->bin_start_dev;
+  A.bin_cap = s->bin_cap_dev;
+  A.zig = ctx->zig_dev;
+  A.error = ctx->error_dev;
+  return A;
+}
+
+int smooth_scratch(pc_context* ctx, pc_smooth* s, uint32_t ncand) {
+  if (ncand <= s->cand_cap) return PC_OK;
+  cudaFree(s->e_raw_dev);
+  cudaFree(s->part_dev);
+  s->e_raw_dev = nullptr;
+  s->part_dev = nullptr;
+  s->cand_cap = 0;
+  const size_t nb = std::max<size_t>(1, s->I.bin_value.size());
+  PC_CUDA(ctx, cudaMalloc(&s->e_raw_dev, (size_t)ncand * nb * s->rows * sizeof(double)));
+  PC_CUDA(ctx, cudaMalloc(&s->part_dev, (size_t)ncand * nb * s->ntypes * 3 * sizeof(double)));
+  s->cand_cap = ncand;
+  return PC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pc_smooth_create(pc_context* ctx, const pc_bin* bins, uint64_t n_bins, uint32_t n_types, double t_max,
+                     double phi, double h, uint32_t paths_per_cell, uint64_t seed, pc_smooth** out) {
+  if (!ctx || !out) return fail(ctx, PC_ERR_INVALID, "null argument");
+  *out = nullptr;
+  if (n_types == 0 || n_types > (uint32_t)kSmoothMaxTypes)
+    return fail(ctx, PC_ERR_UNSUPPORTED, "the smoothed form supports 1 to 8 cell types");
+  if (!(h > 0.0) || std::isinf(h)) return fail(ctx, PC_ERR_INVALID, "h must be finite and > 0");
+  if (paths_per_cell == 0) return fail(ctx, PC_ERR_INVALID, "paths_per_cell must be >= 1");
+  pc_smooth* s = new (std::nothrow) pc_smooth();
+  if (!s) return fail(ctx, PC_ERR_NOMEM, "host allocation");
+  std::string msg;
+  const pc_cell_type one{1.0, 1.0, 0.0};  // the value set and caps do not depend on the types
+  int rc = prepare_instance(bins, n_bins, &one, 1, t_max, phi, seed, s->I, msg);
+  if (rc == PC_OK && s->I.gmax + 1 > (uint32_t)kSmoothMaxRows) {
+    rc = PC_ERR_UNSUPPORTED;
+    msg = "the smoothed form supports at most 63 generations per bin";
+  }
+  if (rc != PC_OK) {
+    delete s;
+    return fail(ctx, rc, msg);
+  }
+  s->ntypes = n_types;
+  s->paths = paths_per_cell;
+  s->h = h;
+  s->rows = s->I.gmax + 1;
+  InstanceHost& I = s->I;
+  const size_t nb = I.bin_value.size();
+  std::vector<uint64_t> start(nb + 1, 0);
+  for (size_t b = 0; b < nb; ++b) start[b + 1] = start[b] + I.bin_freq[b];
+  std::vector<int32_t> vidx(nb * s->rows, -1);
+  std::vector<uint32_t> cnt(I.values.size() + 1, 0);
+  for (size_t b = 0; b < nb; ++b)
+    for (uint32_t g = 0; g <= I.cap[b] && g < I.vidx_stride; ++g) {
+      const int32_t v = I.vidx[b * I.vidx_stride + g];
+      vidx[b * s->rows + g] = v;
+      if (v >= 0) ++cnt[v + 1];
+    }
+  for (size_t v = 0; v < I.values.size(); ++v) cnt[v + 1] += cnt[v];
+  std::vector<uint32_t> inv(cnt.back()), fill(cnt.begin(), cnt.end() - 1);
+  for (size_t b = 0; b < nb; ++b)
+    for (uint32_t g = 0; g < s->rows; ++g) {
+      const int32_t v = vidx[b * s->rows + g];
+      if (v >= 0) inv[fill[v]++] = (uint32_t)(b * s->rows + g);
+    }
+  cudaStream_t st = ctx->stream;
+  cudaError_t e = cudaSetDevice(ctx->device);
+  if (e == cudaSuccess) e = cudaMalloc(&s->bin_start_dev, (nb + 1) * sizeof(uint64_t));
+  if (e == cudaSuccess) e = cudaMalloc(&s->bin_cap_dev, std::max<size_t>(1, nb) * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&s->vidx_dev, std::max<size_t>(1, vidx.size()) * sizeof(int32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&s->inv_off_dev, cnt.size() * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&s->inv_idx_dev, std::max<size_t>(1, inv.size()) * sizeof(uint32_t));
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(s->bin_start_dev, start.data(), (nb + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess && nb)
+    e = cudaMemcpyAsync(s->bin_cap_dev, I.cap.data(), nb * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess && !vidx.empty())
+    e = cudaMemcpyAsync(s->vidx_dev, vidx.data(), vidx.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(s->inv_off_dev, cnt.data(), cnt.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess && !inv.empty())
+    e = cudaMemcpyAsync(s->inv_idx_dev, inv.data(), inv.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) {
+    pc_smooth_destroy(s);
+    return fail(ctx, e == cudaErrorMemoryAllocation ? PC_ERR_NOMEM : PC_ERR_CUDA,
+                std::string("smoothed plan upload: ") + cudaGetErrorString(e));
+  }
+  *out = s;
+  return PC_OK;
+}
+
+int pc_smooth_info(const pc_smooth* s, uint64_t* n_values, uint32_t* n_types, uint64_t* n_cells) {
+  if (!s) return PC_ERR_INVALID;
+  if (n_values) *n_values = s->I.values.size();
+  if (n_types) *n_types = s->ntypes;
+  if (n_cells) *n_cells = s->I.roots;
+  return PC_OK;
+}
+
+int pc_smooth_values(const pc_smooth* s, double* values) {
+  if (!s || (!values && !s->I.values.empty())) return PC_ERR_INVALID;
+  if (!s->I.values.empty()) std::memcpy(values, s->I.values.data(), s->I.values.size() * sizeof(double));
+  return PC_OK;
+}
+
+int pc_smooth_forward(pc_context* ctx, pc_smooth* s, const double* params, uint32_t n_candidates,
+                      double* expected) {
+  if (!ctx || !s || (n_candidates && (!params || !expected))) return fail(ctx, PC_ERR_INVALID, "null argument");
+  if (n_candidates == 0) return PC_OK;
+  PC_CUDA(ctx, cudaSetDevice(ctx->device));
+  int rc = smooth_scratch(ctx, s, n_candidates);
+  if (rc != PC_OK) return rc;
+  const SmoothArgs A = smooth_args(ctx, s);
+  const uint32_t nv = (uint32_t)s->I.values.size();
+  PC_CUDA(ctx, (cudaError_t)launch_smooth_forward(A, params, n_candidates, s->e_raw_dev, ctx->stream));
+  PC_CUDA(ctx, (cudaError_t)launch_smooth_merge(s->e_raw_dev, n_candidates, A.nbins * A.rows, s->inv_off_dev,
+                                                s->inv_idx_dev, nv, expected, ctx->stream));
+  return PC_OK;
+}
+
+int pc_smooth_backward(pc_context* ctx, pc_smooth* s, const double* params, uint32_t n_candidates,
+                       const double* grad_expected, double* grad_params) {
+  if (!ctx || !s || (n_candidates && (!params || !grad_expected || !grad_params)))
+    return fail(ctx, PC_ERR_INVALID, "null argument");
+  if (n_candidates == 0) return PC_OK;
+  PC_CUDA(ctx, cudaSetDevice(ctx->device));
+  int rc = smooth_scratch(ctx, s, n_candidates);
+  if (rc != PC_OK) return rc;
+  const SmoothArgs A = smooth_args(ctx, s);
+  PC_CUDA(ctx, (cudaError_t)launch_smooth_backward(A, params, n_candidates, grad_expected,
+                                                   (uint32_t)s->I.values.size(), s->vidx_dev, s->part_dev,
+                                                   grad_params, ctx->stream));
+  return PC_OK;
+}
+
+int pc_smooth_sync(pc_context* ctx) {
+  if (!ctx) return PC_ERR_INVALID;
+  PC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  uint32_t err = 0;
+  PC_CUDA(ctx, cudaMemcpy(&err, ctx->error_dev, sizeof(err), cudaMemcpyDeviceToHost));
+  if (err & 2u) return fail(ctx, PC_ERR_CUDA, "internal: the normal sampler exceeded its rejection budget");
+  return PC_OK;
+}
+
+void pc_smooth_destroy(pc_smooth* s) {
+  if (!s) return;
+  cudaFree(s->bin_start_dev);
+  cudaFree(s->bin_cap_dev);
+  cudaFree(s->vidx_dev);
+  cudaFree(s->inv_off_dev);
+  cudaFree(s->inv_idx_dev);
+  cudaFree(s->e_raw_dev);
+  cudaFree(s->part_dev);
+  delete s;
+}
+
+}  // extern "C"
+

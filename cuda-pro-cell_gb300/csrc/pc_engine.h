@@ -164,6 +164,37 @@ int launch_debug_normals(const ZigTables* zig, uint32_t k0, uint32_t k1, uint32_
                          uint64_t first_parent, uint64_t count, float* z, void* stream);
 int occupancy_blocks_per_sm(int* root_blocks, int* divide_blocks);
 
+// Smoothed (differentiable) form (pc_smooth.cu). For every candidate parameter set c
+// (per type k: ratio, mean, sd) and every bin b, the expected leaf count at generation g
+// of the bin's initial cells, estimated along sampled lineage paths with every hard test
+// "due time <= t_max" replaced by sigmoid((t_max - S)/h).
+constexpr int kSmoothMaxTypes = 8;
+constexpr int kSmoothMaxRows = 64;  // generations per bin (cap + 1)
+
+struct SmoothArgs {
+  uint32_t k0, k1;            // seed
+  uint32_t nbins, rows;       // rows = max cap + 1 (generation rows per bin)
+  uint32_t ntypes, paths;     // paths sampled per initial cell
+  double t_max, inv_h;
+  const uint64_t* bin_start;  // [nbins + 1]
+  const uint32_t* bin_cap;    // [nbins]
+  const ZigTables* zig;
+  uint32_t* error;            // bit 1: sampler round budget exhausted
+};
+
+// e_raw[c][b][g] (FP64) for params[c][k][3] = (ratio, mean, sd).
+int launch_smooth_forward(const SmoothArgs& A, const double* params, uint32_t ncand, double* e_raw,
+                          void* stream);
+// expected[c][v] = sum of e_raw[c][b][g] over the (b, g) of value v (CSR lists inv_off/inv_idx,
+// inv_idx = b * rows + g).
+int launch_smooth_merge(const double* e_raw, uint32_t ncand, uint32_t per_cand, const uint32_t* inv_off,
+                        const uint32_t* inv_idx, uint32_t nvalues, double* expected, void* stream);
+// grad_params[c][k][3] = d(sum_v grad_expected[c][v] * expected[c][v]) / d params[c][k][.],
+// regenerating every normal from its Philox counter; vidx[b][g] maps rows to values (-1: none).
+int launch_smooth_backward(const SmoothArgs& A, const double* params, uint32_t ncand, const double* grad_expected,
+                           uint32_t nvalues, const int32_t* vidx, double* grad_part, double* grad_params,
+                           void* stream);
+
 // Host helpers (pc_api.cpp).
 ZigTables host_zig_tables();
 void host_truncation_bounds(double mu, double sigma, float& zlo, float& zhi);

@@ -446,6 +446,8 @@ extern "C" int pc_simulate_noalloc(const pc_bin* bins, uint64_t n_bins, const pc
     stats->vanished = st_h[0];
     stats->max_generation = max_gen;
     stats->sweeps = sweeps;
+    stats->root_sweeps = (uint32_t)((total + chunk - 1) / chunk);
+    stats->kernel_launches = sweeps + stats->root_sweeps + 1u;  // + the bin setup kernel
     stats->h2d_bytes = 16ull * n_bins + sizeof(TypeDev) * n_types + sizeof(ZigTables);
     stats->d2h_bytes = 8ull * hist_elems + 40 + 8ull * (sweeps + (total + chunk - 1) / chunk);
   }

@@ -59,6 +59,7 @@ constexpr uint32_t kPhiloxW1 = 0xBB67AE85u;
 constexpr uint32_t kPurposeRoot = 0x30000000u;
 constexpr uint32_t kPurposePair = 0x10000000u;
 constexpr uint32_t kPurposeChild = 0x20000000u;
+constexpr uint32_t kPurposePath = 0x40000000u;  // smoothed form: lineage path choices
 
 PC_HD void mulhilo32(uint32_t a, uint32_t b, uint32_t& hi, uint32_t& lo) {
 #if defined(__CUDA_ARCH__)

@@ -1,0 +1,282 @@
+// Smoothed, differentiable form of the proliferation path: expected histogram counts as a
+// smooth function of the cell-type parameters (ratio, mean, sd), and their adjoint.
+//
+// Model. Along one lineage of an initial cell (type k), the due times are S_1 = tau_1 * U +
+// tau_1 (the initial age, src/simulation/cells_population.cu:124-143) and S_j = S_{j-1} +
+// tau_j, tau_j = mean_k + sd_k * z_j, z_j the node's standard normal from the plain form's
+// Philox counters (without the truncation tau > 0). The hard rule "a cell divides iff it is
+// due by t_max" (proliferation.cu:404-410) becomes s_j = sigmoid((T - S_j) / h): the weight
+// of the lineage reaching generation g and stopping there (a leaf) is
+//     w_g = s_1 s_2 ... s_g (1 - s_{g+1}),
+// and a cell of generation g has 2^g lineages of equal law, so the expected number of
+// generation-g leaves of one initial cell is E_g = sum_k ratio_k 2^g E[w_g], 0 <= g <= cap_b,
+// estimated by `paths` lineages sampled per initial cell (uniform random left/right
+// choices; at g = cap_b only "not due" survives, due cells vanish as in the plain form).
+// Types enter analytically through ratio_k, so d/d ratio is exact. Weights are products of
+// sigmoids evaluated in log space (FP32; due times accumulate in FP64), never negative, and a
+// lineage stops once its survival product is below e^-100.
+//
+// Adjoint. dw_g/dtheta = w_g (D_g + s_{g+1} / h dS_{g+1}/dtheta) with the running tangent
+// D_g = -sum_{i <= g} (1 - s_i) / h dS_i/dtheta, dS_j/dmean = U + j and dS_j/dsd = z_1 (1 + U)
+// + z_2 + ... + z_j. The backward kernel walks the same lineages again with the upstream
+// gradients A_g = dL/dE_g, regenerating every z from its counter (nothing of the forward pass
+// is stored).
+//
+// Work layout: one block per (bin, candidate); its threads stride over the bin's initial
+// cells; per-thread partial sums live in shared memory and are reduced in a fixed order,
+// so results are deterministic.
+#include <cuda_runtime.h>
+
+#include "pc_engine.h"
+
+namespace pc {
+
+namespace {
+
+constexpr int kThreads = 128;
+constexpr uint32_t kFull = 0xFFFFFFFFu;
+constexpr uint32_t kBudget = 1u << 16;
+
+__device__ __forceinline__ double f32_to_f64_bits(float z) {
+  const uint32_t f = __float_as_uint(z);
+  const uint32_t a = f & 0x7FFFFFFFu;
+  const uint32_t hi = (f & 0x80000000u) | (a ? (a >> 3) + (896u << 20) : 0u);
+  return __hiloint2double((int)hi, (int)(f << 29));
+}
+
+__device__ __noinline__ float node_z_slow(uint32_t j, uint32_t layer, uint32_t wedge, uint64_t node, uint32_t root,
+                                          uint32_t k0, uint32_t k1, const ZigTables& Z, uint32_t* error) {
+  ChildStream cs = child_stream(node, root, k0, k1);
+  uint32_t budget = kBudget;
+  const float z = zig_normal(j, layer, true, wedge, cs, Z, budget);
+  if (budget == 0u) atomicOr(error, 2u);
+  return z;
+}
+
+// The standard normal of tree node `node` (heap index; the initial cell is node 1): the
+// plain form's draw for that node (first attempt from the parent's pair block, the node's
+// private stream after a rejection), without the truncation.
+__device__ __forceinline__ float node_z(uint64_t node, uint32_t root, uint32_t k0, uint32_t k1, const ZigTables& Z,
+                                        uint32_t* error) {
+  const uint64_t parent = node >> 1;
+  const uint32_t c = (uint32_t)(node & 1ull);
+  const u32x4 P = philox(u32x4{(uint32_t)parent, (uint32_t)(parent >> 32), root, kPurposePair}, k0, k1);
+  const uint32_t j = c ? P.y : P.x;
+  const uint32_t layer = (P.z >> (8u * c)) & 255u;
+  const uint32_t mag = j & 0x7FFFFFFFu;
+  if (mag < Z.k[layer]) {
+    const float x = __fmul_rn((float)mag, Z.w[layer]);
+    return (j >> 31) ? -x : x;
+  }
+  return node_z_slow(j, layer, pair_wedge_bits(P, c), node, root, k0, k1, Z, error);
+}
+
+struct Lineage {
+  uint32_t root;
+  uint32_t steps;   // cap + 1 due times
+  uint64_t bits;    // left/right choices
+  double u_age;     // U in (0, 1]
+};
+
+// log sigmoid(x) and log(1 - sigmoid(x)) = log sigmoid(-x).
+__device__ __forceinline__ void log_sig(float x, float& ls, float& l1m) {
+  const float L = log1pf(expf(-fabsf(x)));
+  ls = -(fmaxf(-x, 0.0f) + L);
+  l1m = -(fmaxf(x, 0.0f) + L);
+}
+
+constexpr float kLogNegligible = -100.0f;  // e^-100 * 2^63 < 1e-24
+
+// One lineage of one type. Forward: adds weight * 2^g * w_g into acc[g * kThreads].
+// Backward: accumulates sum_g A_g 2^g w_g (for the ratio) and its derivatives in mean, sd.
+template <bool Backward>
+__device__ __forceinline__ void walk(const SmoothArgs& A, const ZigTables& Z, const Lineage& L, double mu,
+                                     double sigma, bool fixed_tau, double weight, double* acc, const double* Ag,
+                                     double& g_r, double& g_mu, double& g_sig) {
+  double S = 0.0;
+  float log_p = 0.0f;             // log s_1 ... s_{j-1}
+  float dmu = 0.0f, dsig = 0.0f;  // dS_j / d(mean, sd)
+  float D_mu = 0.0f, D_sig = 0.0f;
+  const float inv_h = (float)A.inv_h;
+  uint64_t node = 1;
+  double scale = 1.0;  // 2^(j-1)
+  for (uint32_t j = 1; j <= L.steps; ++j) {
+    const float z = fixed_tau ? 0.0f : node_z(node, L.root, A.k0, A.k1, Z, A.error);
+    const double tau = fixed_tau ? 0.0 : fma(sigma, f32_to_f64_bits(z), mu);
+    if (j == 1) {
+      S = tau * L.u_age + tau;
+      dmu = (float)(1.0 + L.u_age);
+      dsig = z * dmu;
+    } else {
+      S = S + tau;
+      dmu += 1.0f;
+      dsig += z;
+    }
+    const float x = __double2float_rn((A.t_max - S) * A.inv_h);
+    float ls, l1m;
+    log_sig(x, ls, l1m);
+    const float w = expf(log_p + l1m);  // leaf weight of generation j - 1
+    if constexpr (!Backward) {
+      acc[(j - 1) * kThreads] += weight * scale * (double)w;
+    } else {
+      const double a = Ag[j - 1] * scale * (double)w;
+      g_r += a;
+      if (!fixed_tau) {
+        const float s = expf(ls), one_m_s = expf(l1m);
+        g_mu += a * (double)(D_mu + s * inv_h * dmu);
+        g_sig += a * (double)(D_sig + s * inv_h * dsig);
+        D_mu -= one_m_s * inv_h * dmu;
+        D_sig -= one_m_s * inv_h * dsig;
+      }
+    }
+    log_p += ls;
+    if (log_p < kLogNegligible) break;
+    scale *= 2.0;
+    node = 2ull * node + ((L.bits >> (j - 1u)) & 1ull);
+  }
+}
+
+// Fixed-order sum of rows[q][0..kThreads) for q in [0, nrows), one warp per row.
+__device__ __forceinline__ void reduce_rows(const double* rows, uint32_t nrows, double* out) {
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  for (uint32_t q = warp; q < nrows; q += kThreads / 32) {
+    double v = 0.0;
+#pragma unroll
+    for (int i = 0; i < kThreads / 32; ++i) v += rows[q * kThreads + lane + 32 * i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+    if (lane == 0) out[q] = v;
+  }
+}
+
+template <bool Backward>
+__global__ void __launch_bounds__(kThreads) k_smooth(const SmoothArgs A, const double* __restrict__ params,
+                                                     const double* __restrict__ grad_expected, uint32_t nvalues,
+                                                     const int32_t* __restrict__ vidx, double* __restrict__ out) {
+  extern __shared__ double acc[];  // forward: [rows][kThreads]; backward: [ntypes * 3][kThreads]
+  __shared__ ZigTables Z;
+  __shared__ double prm[kSmoothMaxTypes * 3];
+  __shared__ double Ag[kSmoothMaxRows];
+  const uint32_t b = blockIdx.x, c = blockIdx.y;
+  const uint32_t K = A.ntypes;
+  for (uint32_t i = threadIdx.x; i < sizeof(ZigTables) / 4; i += blockDim.x)
+    reinterpret_cast<uint32_t*>(&Z)[i] = __ldg(reinterpret_cast<const uint32_t*>(A.zig) + i);
+  for (uint32_t i = threadIdx.x; i < K * 3; i += blockDim.x) prm[i] = params[(uint64_t)c * K * 3 + i];
+  const uint32_t nrows = Backward ? K * 3 : A.rows;
+  for (uint32_t i = 0; i < nrows; ++i) acc[i * kThreads + threadIdx.x] = 0.0;
+  const uint32_t cap = __ldg(A.bin_cap + b);
+  if constexpr (Backward) {
+    for (uint32_t g = threadIdx.x; g < kSmoothMaxRows; g += blockDim.x) {
+      double a = 0.0;
+      if (g < A.rows && g <= cap) {
+        const int32_t v = vidx[(uint64_t)b * A.rows + g];
+        if (v >= 0) a = grad_expected[(uint64_t)c * nvalues + v];
+      }
+      Ag[g] = a;
+    }
+  }
+  __syncthreads();
+  const uint64_t r0 = __ldg(A.bin_start + b), r1 = __ldg(A.bin_start + b + 1);
+  const double inv_paths = 1.0 / (double)A.paths;
+  double* my = acc + threadIdx.x;
+  for (uint64_t r = r0 + threadIdx.x; r < r1; r += kThreads) {
+    Lineage L;
+    L.root = (uint32_t)r;
+    L.steps = cap + 1u;
+    const u32x4 R = philox(u32x4{0u, 0u, L.root, kPurposeRoot}, A.k0, A.k1);
+    L.u_age = unit53_open_closed(R.z, R.w);
+    for (uint32_t m = 0; m < A.paths; ++m) {
+      const u32x4 B = philox(u32x4{m, 0u, L.root, kPurposePath}, A.k0, A.k1);
+      L.bits = (uint64_t)B.x | ((uint64_t)B.y << 32);
+      for (uint32_t k = 0; k < K; ++k) {
+        const double ratio = prm[3 * k], mu = prm[3 * k + 1], sd = prm[3 * k + 2];
+        double g_r = 0.0, g_mu = 0.0, g_sig = 0.0;
+        if (mu < 0.0) {
+          // quiescent type: a leaf at generation 0 (cell.cu:69-75)
+          if constexpr (Backward)
+            g_r = Ag[0];
+          else
+            my[0] += ratio * inv_paths;
+        } else {
+          walk<Backward>(A, Z, L, mu, sd, mu == 0.0, ratio * inv_paths, my, Ag, g_r, g_mu, g_sig);
+        }
+        if constexpr (Backward) {
+          my[(3 * k) * kThreads] += g_r * inv_paths;
+          my[(3 * k + 1) * kThreads] += g_mu * ratio * inv_paths;
+          my[(3 * k + 2) * kThreads] += g_sig * ratio * inv_paths;
+        }
+      }
+    }
+  }
+  __syncthreads();
+  reduce_rows(acc, nrows, out + ((uint64_t)c * A.nbins + b) * nrows);
+}
+
+__global__ void k_smooth_merge(const double* __restrict__ e_raw, uint32_t ncand, uint32_t per_cand,
+                               const uint32_t* __restrict__ inv_off, const uint32_t* __restrict__ inv_idx,
+                               uint32_t nvalues, double* __restrict__ expected) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (uint64_t)ncand * nvalues) return;
+  const uint32_t c = (uint32_t)(i / nvalues), v = (uint32_t)(i % nvalues);
+  double s = 0.0;
+  for (uint32_t q = inv_off[v]; q < inv_off[v + 1]; ++q) s += e_raw[(uint64_t)c * per_cand + inv_idx[q]];
+  expected[i] = s;
+}
+
+__global__ void k_smooth_grad_sum(const double* __restrict__ part, uint32_t ncand, uint32_t nbins, uint32_t per_bin,
+                                  double* __restrict__ grad) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (uint64_t)ncand * per_bin) return;
+  const uint32_t c = (uint32_t)(i / per_bin), q = (uint32_t)(i % per_bin);
+  double s = 0.0;
+  for (uint32_t b = 0; b < nbins; ++b) s += part[((uint64_t)c * nbins + b) * per_bin + q];
+  grad[i] = s;
+}
+
+int smem_bytes(uint32_t rows) { return (int)(rows * kThreads * sizeof(double)); }
+
+template <bool Backward>
+int launch_smooth_t(const SmoothArgs& A, const double* params, uint32_t ncand, const double* grad_expected,
+                    uint32_t nvalues, const int32_t* vidx, double* out, cudaStream_t st) {
+  const uint32_t rows = Backward ? A.ntypes * 3u : A.rows;
+  const int smem = smem_bytes(rows);
+  if (smem > 48 * 1024) {
+    const cudaError_t e = cudaFuncSetAttribute(k_smooth<Backward>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return (int)e;
+  }
+  const dim3 grid(A.nbins, ncand);
+  k_smooth<Backward><<<grid, kThreads, smem, st>>>(A, params, grad_expected, nvalues, vidx, out);
+  return (int)cudaGetLastError();
+}
+
+}  // namespace
+
+int launch_smooth_forward(const SmoothArgs& A, const double* params, uint32_t ncand, double* e_raw, void* stream) {
+  if (ncand == 0 || A.nbins == 0) return 0;
+  return launch_smooth_t<false>(A, params, ncand, nullptr, 0, nullptr, e_raw, (cudaStream_t)stream);
+}
+
+int launch_smooth_merge(const double* e_raw, uint32_t ncand, uint32_t per_cand, const uint32_t* inv_off,
+                        const uint32_t* inv_idx, uint32_t nvalues, double* expected, void* stream) {
+  const uint64_t n = (uint64_t)ncand * nvalues;
+  if (n == 0) return 0;
+  k_smooth_merge<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(e_raw, ncand, per_cand, inv_off,
+                                                                              inv_idx, nvalues, expected);
+  return (int)cudaGetLastError();
+}
+
+int launch_smooth_backward(const SmoothArgs& A, const double* params, uint32_t ncand, const double* grad_expected,
+                           uint32_t nvalues, const int32_t* vidx, double* grad_part, double* grad_params,
+                           void* stream) {
+  cudaStream_t st = (cudaStream_t)stream;
+  const uint32_t per_bin = A.ntypes * 3u;
+  const uint64_t n = (uint64_t)ncand * per_bin;
+  if (n == 0) return 0;
+  if (A.nbins == 0) return (int)cudaMemsetAsync(grad_params, 0, n * sizeof(double), st);
+  int e = launch_smooth_t<true>(A, params, ncand, grad_expected, nvalues, vidx, grad_part, st);
+  if (e != 0) return e;
+  k_smooth_grad_sum<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(grad_part, ncand, A.nbins, per_bin, grad_params);
+  return (int)cudaGetLastError();
+}
+
+}  // namespace pc

@@ -170,14 +170,24 @@ class Engine:
             raise ProcellError(rc, self.L.pc_last_error(self.ctx).decode())
 
     def set_stream(self, stream_handle: int):
-        """Run on an existing cudaStream_t (e.g. torch.cuda.current_stream().cuda_stream)."""
-        self._check(self.L.pc_set_stream(self.ctx, ctypes.c_void_p(int(stream_handle))))
+        """Run on an existing cudaStream_t (e.g. torch.cuda.current_stream().cuda_stream).
+        Handle 0, torch's default stream, is the legacy default stream (cudaStreamLegacy)."""
+        h = int(stream_handle) or 1
+        self._check(self.L.pc_set_stream(self.ctx, ctypes.c_void_p(h)))
 
     def set_option(self, name: str, value: float):
         self._check(self.L.pc_set_option(self.ctx, name.encode(), float(value)))
 
     def plan(self, bins, types, t_max, phi=None, seed=0) -> Plan:
         return Plan(self, bins, types, t_max, phi, seed)
+
+    def autotune(self, target, repeats: int = 2) -> dict:
+        """Time every sweep configuration and driver on a Plan or Batch; the context keeps
+        the fastest (results are identical under all of them)."""
+        t = _lib.Tuning()
+        fn = self.L.pc_batch_autotune if isinstance(target, Batch) else self.L.pc_autotune
+        self._check(fn(self.ctx, target.handle, int(repeats), ctypes.byref(t)))
+        return {k: getattr(t, k) for k, _ in _lib.Tuning._fields_}
 
     def batch(self, instances) -> Batch:
         return Batch(self, instances)

@@ -32,7 +32,8 @@ class Stats(ctypes.Structure):
     _fields_ = [("roots", ctypes.c_uint64), ("divisions", ctypes.c_uint64),
                 ("leaves", ctypes.c_uint64), ("uncounted", ctypes.c_uint64),
                 ("vanished", ctypes.c_uint64), ("max_generation", ctypes.c_uint32),
-                ("sweeps", ctypes.c_uint32), ("device_ms", ctypes.c_double),
+                ("sweeps", ctypes.c_uint32), ("root_sweeps", ctypes.c_uint32),
+                ("kernel_launches", ctypes.c_uint32), ("device_ms", ctypes.c_double),
                 ("divide_ms", ctypes.c_double), ("h2d_bytes", ctypes.c_uint64),
                 ("d2h_bytes", ctypes.c_uint64)]
 
@@ -49,6 +50,12 @@ class Instance(ctypes.Structure):
                 ("types", ctypes.POINTER(CellType)), ("n_types", ctypes.c_uint32),
                 ("reserved", ctypes.c_uint32), ("t_max", ctypes.c_double), ("phi", ctypes.c_double),
                 ("seed", ctypes.c_uint64)]
+
+
+class Tuning(ctypes.Structure):
+    _fields_ = [("config", ctypes.c_int32), ("driver", ctypes.c_int32), ("threads", ctypes.c_int32),
+                ("cells_per_lane", ctypes.c_int32), ("global_hist", ctypes.c_int32),
+                ("candidates", ctypes.c_int32), ("ms", ctypes.c_double), ("ms_default", ctypes.c_double)]
 
 
 # (name, restype, argtypes) of every exported symbol of include/procell.h
@@ -82,6 +89,17 @@ SIGNATURES = [
     ("pc_batch_destroy", None, [VP]),
     ("pc_simulate_batch", ctypes.c_int, [VP, ctypes.POINTER(Instance), ctypes.c_uint32,
                                          ctypes.POINTER(Histogram)]),
+    ("pc_autotune", ctypes.c_int, [VP, VP, ctypes.c_uint32, ctypes.POINTER(Tuning)]),
+    ("pc_batch_autotune", ctypes.c_int, [VP, VP, ctypes.c_uint32, ctypes.POINTER(Tuning)]),
+    ("pc_smooth_create", ctypes.c_int, [VP, ctypes.POINTER(Bin), ctypes.c_uint64, ctypes.c_uint32,
+                                        ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_uint32,
+                                        ctypes.c_uint64, ctypes.POINTER(VP)]),
+    ("pc_smooth_info", ctypes.c_int, [VP, U64P, U32P, U64P]),
+    ("pc_smooth_values", ctypes.c_int, [VP, ctypes.POINTER(ctypes.c_double)]),
+    ("pc_smooth_forward", ctypes.c_int, [VP, VP, VP, ctypes.c_uint32, VP]),
+    ("pc_smooth_backward", ctypes.c_int, [VP, VP, VP, ctypes.c_uint32, VP, VP]),
+    ("pc_smooth_sync", ctypes.c_int, [VP]),
+    ("pc_smooth_destroy", None, [VP]),
     ("pc_load_histogram", ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(ctypes.POINTER(Bin)), U64P]),
     ("pc_load_cell_types", ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(ctypes.POINTER(CellType)), U32P]),
     ("pc_write_histogram", ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(Histogram), ctypes.c_int]),

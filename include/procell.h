@@ -70,7 +70,10 @@ typedef struct pc_stats {
   uint64_t uncounted;       /* out-of-time roots whose value is below phi */
   uint64_t vanished;        /* due cells whose daughters would fall to phi or below */
   uint32_t max_generation;  /* deepest generation reached */
-  uint32_t sweeps;          /* kernel launches of the division sweep */
+  uint32_t sweeps;          /* division sweeps (one kernel launch each, or phases of the
+                               persistent launch) */
+  uint32_t root_sweeps;     /* root sweeps (chunks of initial cells) */
+  uint32_t kernel_launches; /* kernels launched by the run */
   double device_ms;         /* summed duration of the simulation kernels (CUDA events) */
   double divide_ms;         /* ... of the division sweeps alone */
   uint64_t h2d_bytes;       /* host-to-device bytes of the plan and the run */
@@ -99,7 +102,9 @@ void pc_destroy(pc_context* ctx);
 const char* pc_last_error(const pc_context* ctx); /* ctx may be NULL (creation errors) */
 const char* pc_version(void);
 
-/* Use `stream` (a cudaStream_t) for all work of this context; NULL = the context's own. */
+/* Use `stream` (a cudaStream_t) for all work of this context; NULL = the context's own
+ * (non-blocking) stream. The legacy default stream is selected by its handle value
+ * cudaStreamLegacy ((void*)1). */
 int pc_set_stream(pc_context* ctx, void* stream);
 
 /* Tuning knobs (results never depend on them):
@@ -108,6 +113,11 @@ int pc_set_stream(pc_context* ctx, void* stream);
  *   "max_slice_cells"     cap on cells per division-sweep launch (default: from budget)
  *   "max_root_chunk"      cap on roots per root-sweep launch (default: from budget)
  *   "grid_blocks"         blocks per launch (default: resident blocks x SMs)
+ *   "sweep_config"        compiled sweep configuration 0-7 (default 4; see pc_autotune)
+ *   "driver"              0: one kernel launch per sweep (default); 1: one persistent
+ *                         cooperative launch per run
+ *   "graph"               1: the persistent driver captures its run in a CUDA graph once
+ *                         per plan and replays it
  */
 int pc_set_option(pc_context* ctx, const char* name, double value);
 
@@ -178,6 +188,58 @@ void pc_batch_destroy(pc_batch* batch);
 /* One call: create, run, results (out[n_instances], each freed with pc_histogram_free). */
 int pc_simulate_batch(pc_context* ctx, const pc_instance* instances, uint32_t n_instances,
                       pc_histogram* out);
+
+/* ---- Autotuning (no counterpart in the reference) -------------------------------------
+ * The sweeps are compiled in several configurations (threads per block, input cells per
+ * lane, and where leaf counts are privatised: a window of classes in shared memory per
+ * block, or warp-aggregated atomics straight to the global table) and can be driven one
+ * launch per sweep or by one persistent cooperative launch replayed from a CUDA graph.
+ * None of this changes a single count. The context options "sweep_config" (0-7),
+ * "driver" (0 per sweep, 1 persistent) and "graph" (0/1) select them; pc_autotune times
+ * every combination on a prepared input and leaves the context set to the fastest. */
+typedef struct pc_tuning {
+  int32_t config;         /* chosen "sweep_config" */
+  int32_t driver;         /* chosen "driver" (graph replay is on with the persistent one) */
+  int32_t threads;        /* threads per block of the chosen configuration */
+  int32_t cells_per_lane;
+  int32_t global_hist;    /* 1: leaf counts go straight to the global table */
+  int32_t candidates;     /* combinations timed */
+  double ms;              /* best wall time of one run with the choice */
+  double ms_default;      /* the same for config 4, one launch per sweep */
+} pc_tuning;
+
+/* Each candidate runs once to warm up, then `repeats` times (best time kept). */
+int pc_autotune(pc_context* ctx, pc_plan* plan, uint32_t repeats, pc_tuning* out);
+int pc_batch_autotune(pc_context* ctx, pc_batch* batch, uint32_t repeats, pc_tuning* out);
+
+/* ---- Smoothed, differentiable form (no counterpart in the reference) -------------------
+ * Expected output-histogram counts as a smooth function of the cell-type parameters, for
+ * calibrating (ratio, mean, sd) per type by gradient descent. Every hard test "due time <=
+ * t_max" of the plain form becomes sigmoid((t_max - S) / h), with due times
+ * S = sum(mean + sd * z) accumulated in FP64 along lineages sampled per initial cell
+ * (`paths_per_cell` each), z taken from the plain form's Philox counters (untruncated).
+ * The bins, t_max, phi and seed are fixed at creation; the parameters of any number of
+ * candidates are passed per call. Quiescent types (mean < 0) count at generation 0.
+ *
+ * params:        device array [n_candidates][n_types][3] (ratio, mean, sd), FP64, types in
+ *                file order (ratios are used as given: normalise them yourself)
+ * expected:      device array [n_candidates][n_values] (FP64), values as pc_smooth_values
+ * grad_expected: device array [n_candidates][n_values], dL/d expected
+ * grad_params:   device array [n_candidates][n_types][3], dL/d params (the adjoint: the
+ *                lineages are walked again, every normal regenerated from its counter)
+ * Both calls are asynchronous on the context's stream; pc_smooth_sync waits and reports. */
+typedef struct pc_smooth pc_smooth;
+int pc_smooth_create(pc_context* ctx, const pc_bin* bins, uint64_t n_bins, uint32_t n_types,
+                     double t_max, double phi, double h, uint32_t paths_per_cell, uint64_t seed,
+                     pc_smooth** out);
+int pc_smooth_info(const pc_smooth* s, uint64_t* n_values, uint32_t* n_types, uint64_t* n_cells);
+int pc_smooth_values(const pc_smooth* s, double* values); /* host array [n_values] */
+int pc_smooth_forward(pc_context* ctx, pc_smooth* s, const double* params, uint32_t n_candidates,
+                      double* expected);
+int pc_smooth_backward(pc_context* ctx, pc_smooth* s, const double* params, uint32_t n_candidates,
+                       const double* grad_expected, double* grad_params);
+int pc_smooth_sync(pc_context* ctx);
+void pc_smooth_destroy(pc_smooth* s);
 
 /* File formats of the reference (parser.cu:68-217). Loaders read with the reference's
  * `in >> a >> b` semantics (stop at the first unparsable token). The loaders allocate

@@ -116,3 +116,16 @@ def test_batched_persistent_every_config(eng, config):
         for i in range(len(instances)):
             assert np.array_equal(b.raw_counts(i), want[i]), i
     b.close()
+
+
+def test_autotune_picks_a_compiled_combination(eng, small_oracle):
+    w, o = small_oracle
+    p = eng.plan(w.bins, w.types, w.t_max, w.phi, w.seed)
+    t = eng.autotune(p, repeats=1)
+    assert t["candidates"] == 16 and 0 <= t["config"] < 8 and t["driver"] in (0, 1)
+    assert t["threads"] in (128, 256) and t["cells_per_lane"] in (1, 2)
+    assert 0 < t["ms"] <= t["ms_default"]
+    p.run()
+    r = p.result()
+    assert np.array_equal(r.per_type, o.per_type)
+    p.close()

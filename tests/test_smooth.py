@@ -1,0 +1,190 @@
+"""The smoothed, differentiable form: forward, hand-written adjoint, torch.autograd.Function.
+
+Checks: (1) the adjoint against central finite differences of the forward (relative step
+1e-4, common random numbers: the same seed, so the same lineages and normals), within 1e-3
+relative; (2) expected counts and their gradients against the analytic Gaussian-sum model
+at sd/mean = 0.1: conditional on the initial age U, S_g ~ N(mean (g + U), sd^2 ((1 + U)^2 +
+g - 1)), and E[sigmoid((T - S) / h)] = P(S + Logistic(0, h) <= T), integrated by quadrature.
+The kernel's leaf weight s_1 ... s_g (1 - s_{g+1}) equals s_g - s_{g+1} up to terms of order
+exp(-mean / h) (= e^-48 here), so E_g = 2^g (P_g - P_{g+1}) is the analytic reference;
+(3) the autograd wrapper and determinism.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+def calib_bins(n_bins=256, cells=100_000, seed=5):
+    rng = np.random.default_rng(seed)
+    v = np.exp(rng.uniform(np.log(1.0), np.log(1e4), n_bins))
+    f = rng.multinomial(cells, np.full(n_bins, 1.0 / n_bins))
+    return [(float(a), int(b)) for a, b in zip(v, f)]
+
+
+def loss_fn(E, target):
+    return ((torch.log1p(E) - torch.log1p(target)) ** 2).sum(dim=1)
+
+
+@pytest.fixture(scope="module")
+def smooth_setup(engine):
+    from procell.smooth import Smooth
+    bins = calib_bins()
+    sm = Smooth(engine, bins, n_types=3, t_max=168.0, phi=None, h=0.5, paths=2, seed=11)
+    yield sm, bins
+    sm.close()
+
+
+def params_tensor(rows):
+    return torch.tensor(rows, dtype=torch.float64, device="cuda")
+
+
+BASE = [[[0.5, 40.0, 8.0], [0.3, 60.0, 15.0], [0.2, 90.0, 20.0]],
+        [[0.2, 35.0, 3.5], [0.45, 55.0, 5.5], [0.35, 80.0, 8.0]]]
+
+
+def test_adjoint_matches_central_differences(smooth_setup):
+    sm, _ = smooth_setup
+    P = params_tensor(BASE)
+    # a target histogram that is not the model itself, so the loss gradient is nonzero
+    target = sm.forward(params_tensor([[[0.4, 45.0, 9.0], [0.4, 58.0, 12.0], [0.2, 85.0, 17.0]]])).repeat(2, 1)
+    E = sm.forward(P)
+    L = loss_fn(E, target)
+    gE = 2.0 * (torch.log1p(E) - torch.log1p(target)) / (1.0 + E)
+    grad = sm.backward(P, gE).cpu().numpy()
+    # central differences: every (candidate, type, parameter) perturbed by +-1e-4 relative,
+    # all in one batch of candidates
+    C, K = P.shape[0], P.shape[1]
+    rows, steps = [], []
+    for c in range(C):
+        for k in range(K):
+            for q in range(3):
+                d = 1e-4 * abs(float(P[c, k, q]))
+                for sgn in (1.0, -1.0):
+                    Q = P[c].clone()
+                    Q[k, q] += sgn * d
+                    rows.append(Q)
+                steps.append(d)
+    Pf = torch.stack(rows)
+    tf = target[:1].expand(Pf.shape[0], -1)
+    Lf = loss_fn(sm.forward(Pf), tf).cpu().numpy()
+    fd = ((Lf[0::2] - Lf[1::2]) / (2.0 * np.array(steps))).reshape(C, K, 3)
+    sm.sync()
+    assert np.all(np.isfinite(grad)) and np.all(np.isfinite(fd))
+    scale = np.abs(fd).max()
+    err = np.abs(grad - fd)
+    assert np.all(err <= 1e-3 * np.abs(fd) + 1e-6 * scale), (grad, fd, err / np.abs(fd))
+
+
+def _gauss_logistic_cdf(T, m, s, h, nodes=160):
+    """E[sigmoid((T - m - s X) / h)], X ~ N(0, 1), by Gauss-Hermite quadrature, and its
+    derivatives with respect to m and s."""
+    x, w = np.polynomial.hermite_e.hermegauss(nodes)
+    w = w / np.sqrt(2.0 * np.pi)
+    a = (T - m[..., None] - s[..., None] * x) / h
+    sig = 1.0 / (1.0 + np.exp(-a))
+    dsig = sig * (1.0 - sig) / h
+    return (sig * w).sum(-1), (-dsig * w).sum(-1), (-dsig * x * w).sum(-1)
+
+
+def analytic_counts(mu, sd, T, h, gens):
+    """Expected leaves per initial cell at generations 0..gens-1 (no phi cap in reach) and
+    d/d mean, d/d sd, for the smoothed model with untruncated normal division times."""
+    u, wu = np.polynomial.legendre.leggauss(64)
+    u = 0.5 * (u + 1.0)
+    wu = 0.5 * wu
+    P = np.zeros(gens + 1)
+    dPm = np.zeros(gens + 1)
+    dPs = np.zeros(gens + 1)
+    P[0] = 1.0
+    for g in range(1, gens + 1):
+        m = mu * (g + u)
+        var_c = (1.0 + u) ** 2 + g - 1.0
+        s = sd * np.sqrt(var_c)
+        p, dm, ds = _gauss_logistic_cdf(T, m, s, h)
+        P[g] = (p * wu).sum()
+        dPm[g] = (dm * (g + u) * wu).sum()
+        dPs[g] = (ds * np.sqrt(var_c) * wu).sum()
+    pw = 2.0 ** np.arange(gens)
+    E = pw * (P[:-1] - P[1:])
+    dEm = pw * (dPm[:-1] - dPm[1:])
+    dEs = pw * (dPs[:-1] - dPs[1:])
+    return E, dEm, dEs
+
+
+def test_gaussian_sum_model(engine):
+    from procell.smooth import Smooth
+    mu, sd, T, h = 24.0, 2.4, 100.0, 0.5
+    value, cells, paths = 2.0 ** 30, 400_000, 4  # one bin; the phi cap (30) is never reached
+    sm = Smooth(engine, [(value, cells)], n_types=1, t_max=T, phi=1.0, h=h, paths=paths, seed=3)
+    gens = 7
+    E_a, dEm_a, dEs_a = analytic_counts(mu, sd, T, h, gens)
+    P = params_tensor([[[1.0, mu, sd]]])
+    E = sm.forward(P)[0].cpu().numpy() / cells
+    vals = sm.values
+    idx = [int(np.searchsorted(vals, value / 2 ** g)) for g in range(gens)]
+    E_mc = E[idx]
+    main = E_a > 0.02 * E_a.max()
+    assert np.all(np.abs(E_mc[main] - E_a[main]) <= 0.02 * E_a[main] + 0.005 * E_a.max()), (E_mc, E_a)
+    # gradients of each generation's expected count: upstream gradient = one-hot on its value
+    for g in np.flatnonzero(main):
+        gE = torch.zeros(1, sm.n_values, dtype=torch.float64, device="cuda")
+        gE[0, idx[g]] = 1.0 / cells
+        grad = sm.backward(P, gE)[0, 0].cpu().numpy()
+        assert abs(grad[1] - dEm_a[g]) <= 0.03 * abs(dEm_a).max(), (g, grad, dEm_a[g])
+        assert abs(grad[2] - dEs_a[g]) <= 0.03 * abs(dEs_a).max() + 1e-4, (g, grad, dEs_a[g])
+        assert abs(grad[0] - E_a[g]) <= 0.02 * E_a[g]  # d/d ratio = the count itself
+    sm.sync()
+    sm.close()
+
+
+def test_autograd_function_and_determinism(smooth_setup):
+    from procell.smooth import expected_counts
+    sm, _ = smooth_setup
+    P = params_tensor(BASE).requires_grad_(True)
+    target = torch.full((2, sm.n_values), 3.0, dtype=torch.float64, device="cuda")
+    E = expected_counts(sm, P)
+    loss = loss_fn(E, target).sum()
+    loss.backward()
+    gE = 2.0 * (torch.log1p(E.detach()) - torch.log1p(target)) / (1.0 + E.detach())
+    direct = sm.backward(P.detach(), gE)
+    assert torch.equal(P.grad, direct)
+    E2 = sm.forward(P.detach())
+    assert torch.equal(E.detach(), E2)
+    sm.sync()
+
+
+def test_quiescent_type_counts_at_generation_zero(engine):
+    from procell.smooth import Smooth
+    sm = Smooth(engine, [(100.0, 1000), (0.5, 200)], n_types=2, t_max=50.0, phi=1.0, h=0.5, paths=1, seed=1)
+    P = params_tensor([[[0.25, -1.0, -1.0], [0.75, 1e6, 1.0]]])  # the second type never divides by t_max
+    E = sm.forward(P)[0].cpu().numpy()
+    # value 100 (countable): every cell is a generation-0 leaf; value 0.5 < phi: not counted
+    i100 = int(np.searchsorted(sm.values, 100.0))
+    assert abs(E[i100] - 1000.0) < 1e-6 and abs(E.sum() - 1000.0) < 1e-6
+    sm.sync()
+    sm.close()
+
+
+def test_matches_cpu_restatement(engine):
+    """Expected counts and gradients against oracle/smooth_ref.py (FP64, independent)."""
+    import smooth_ref
+    from procell.smooth import Smooth
+    bins = [(640.0, 60), (37.0, 45), (3.0, 20), (1500.0, 0), (9.5, 30), (0.7, 10)]
+    t_max, phi, h, paths, seed = 150.0, 1.0, 0.5, 2, 123456789012
+    params = [[[0.5, 30.0, 6.0], [0.3, 45.0, 18.0], [0.2, -1.0, -1.0]],
+              [[0.6, 25.0, 12.0], [0.4, 0.0, 1.0], [0.0, 40.0, 4.0]]]
+    rng = np.random.default_rng(0)
+    sm = Smooth(engine, bins, n_types=3, t_max=t_max, phi=phi, h=h, paths=paths, seed=seed)
+    gE = rng.normal(size=(2, sm.n_values))
+    E_ref, G_ref, vals = smooth_ref.forward_backward(bins, t_max, phi, h, paths, seed, params, gE)
+    assert np.array_equal(vals, sm.values)
+    P = params_tensor(params)
+    E = sm.forward(P).cpu().numpy()
+    G = sm.backward(P, torch.tensor(gE, device="cuda")).cpu().numpy()
+    sm.sync()
+    sm.close()
+    assert np.allclose(E, E_ref, rtol=2e-5, atol=1e-9 * np.abs(E_ref).max()), np.abs(E - E_ref).max()
+    assert np.allclose(G, G_ref, rtol=2e-5, atol=1e-7 * np.abs(G_ref).max()), (G, G_ref)
