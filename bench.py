@@ -146,6 +146,8 @@ def run_reference(args):
     oracle.build()
     if args.workload == "batched":
         return run_reference_batched(args)
+    if args.workload == "calibration":
+        return run_reference_calibration(args)
     w = workload(args.workload)
     cores = os.cpu_count() or 1
     per_step = max(2.0, args.cpu_seconds / 2)
@@ -513,6 +515,157 @@ def run_batched(args):
     return 0
 
 
+def cpu_smooth_sample(bins, phi, t_max, h, paths, seed, params, seconds):
+    """Candidate-gradients/s of the CPU restatement of the smoothed form (oracle/smooth_ref.py,
+    FP64 numpy loops) on one candidate, over a prefix of the bins sized to ~`seconds`, scaled
+    to the whole input by its share of initial cells."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    oracle.build()
+    import smooth_ref
+    P = np.asarray(params, dtype=np.float64).reshape(1, -1, 3)
+    total = sum(f for _, f in bins)
+    nb, spent, cells = 1, 0.0, 0
+    while True:
+        sub = bins[:nb]
+        cells = sum(f for _, f in sub)
+        t = time.perf_counter()
+        E, _, _ = smooth_ref.forward_backward(sub, t_max, phi, h, paths, seed, P)
+        smooth_ref.forward_backward(sub, t_max, phi, h, paths, seed, P, np.ones_like(E))
+        spent = time.perf_counter() - t
+        if spent >= 0.4 * seconds or nb >= len(bins):
+            break
+        nb = min(len(bins), max(nb + 1, int(nb * 0.5 * seconds / max(spent, 1e-3))))
+    per_grad = spent * total / max(1, cells)
+    return {"value": 1.0 / per_grad, "unit": "grads/s", "cores": 1, "kind": "port",
+            "sample": "oracle/smooth_ref.py (FP64, one thread) forward + backward of one candidate on the first "
+                      "%d of %d bins (%d of %d initial cells, %.1f s), scaled by initial cells"
+                      % (nb, len(bins), cells, total, spent)}
+
+
+def run_reference_calibration(args):
+    from procell import calibrate as cb
+    bins, phi, hidden = cb.problem_inputs(7)
+    per_step = max(2.0, args.cpu_seconds / 2)
+    for _ in range(args.warmup):
+        cpu_smooth_sample(bins, phi, 168.0, 0.5, 2, 7 + 2000, hidden, per_step / 4)
+    vals = [cpu_smooth_sample(bins, phi, 168.0, 0.5, 2, 7 + 2000, hidden, per_step) for _ in range(args.steps)]
+    value = sum(v["value"] for v in vals) / len(vals)
+    line = {
+        "impl": "reference", "metric": "fwd+bwd grads/s (smoothed form)", "value": value, "unit": "grads/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / value,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded generator, procell/calibrate.py problem_inputs)",
+        "config": {"workload": "calibration: 256 bins, 1e5 cells, 3 types, t_max 168, h 0.5, 2 lineages per cell",
+                   "note": "the reference has no smoothed form; this is the CPU restatement"},
+        "cpu_baseline": {"value": value, "unit": "grads/s", "cores": 1, "kind": "port",
+                         "sample": vals[-1]["sample"]},
+        "e2e": {"value": value, "unit": "grads/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_calibration(args):
+    """Smoothed form: fwd+bwd candidate-gradients per second at 256 candidates, and
+    gradient descent against particle swarm to equal loss."""
+    import numpy as np
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if rank != 0 and world > 1:
+        return 0
+    import build as pkg_build
+    pkg_build.build()
+    from procell import Engine
+    from procell import calibrate as cb
+    eng = Engine(local)
+    prob = cb.Problem(eng, seed=7)
+    C = 256
+    theta = prob.start(C, 7)
+    stream = torch.cuda.current_stream()
+
+    def step(th):
+        P = prob.params(th)
+        E = prob.smooth.forward(P)
+        gE = 2.0 * (torch.log1p(E) - torch.log1p(prob.target)) / (1.0 + E)
+        return prob.smooth.backward(P, gE), ((torch.log1p(E) - torch.log1p(prob.target)) ** 2).sum(dim=1)
+
+    for _ in range(args.warmup):
+        step(theta)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        g, L = step(theta)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    elapsed_ms = e0.elapsed_time(e1)
+    # end to end: parameters from pinned host memory, gradients and losses back to the host
+    host_theta = theta.cpu().pin_memory()
+    out_g = torch.empty((C, prob.n_types, 3), dtype=torch.float64).pin_memory()
+    out_l = torch.empty(C, dtype=torch.float64).pin_memory()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        th = host_theta.to("cuda", non_blocking=True)
+        g, L = step(th)
+        out_g.copy_(g, non_blocking=True)
+        out_l.copy_(L, non_blocking=True)
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    clk = clocks.stop()
+    h2d = host_theta.numel() * 8
+    d2h = (out_g.numel() + out_l.numel()) * 8
+    comp = cb.compare(eng, candidates=C, seed=7)
+    cpu = None
+    if not args.no_cpu_baseline:
+        cpu = cpu_smooth_sample(prob.bins, prob.phi, prob.t_max, prob.smooth_h, prob.smooth_paths,
+                                prob.smooth_seed, prob.params(theta[:1]).detach().cpu().numpy(),
+                                args.cpu_seconds)
+    value = C * args.steps / (elapsed_ms * 1e-3)
+    hbm, peak_kind = peaks()
+    # algorithmic bytes of one forward + backward: parameters in, expected counts out and in
+    # again as gradients, parameter gradients out
+    alg = (C * prob.n_types * 3 * 8) * 2 + C * prob.smooth.n_values * 8 * 2
+    line = {
+        "metric": "fwd+bwd grads/s (smoothed form)",
+        "value": value,
+        "unit": "grads/s",
+        "n_gpus": 1,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": elapsed_ms / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded generator, procell/calibrate.py Problem)",
+        "config": {"workload": "calibration: 256 bins, 1e5 cells, 3 types, %d candidates, t_max 168, h 0.5, "
+                               "%d lineages per cell; a step = smoothed forward + loss gradient + adjoint"
+                               % (C, prob.smooth_paths),
+                   "l2": "inputs (bins, parameters) are a few MB; the kernels are compute bound"},
+        "calibration": comp,
+        "e2e": {"value": C * args.steps / e2e_s, "unit": "grads/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "roofline": {"bound": "hbm", "achieved": alg / (elapsed_ms * 1e-3 / args.steps) / 1e9, "peak": hbm,
+                     "unit": "GB/s", "frac": alg / (elapsed_ms * 1e-3 / args.steps) / 1e9 / hbm,
+                     "traffic": None, "peak_source": peak_kind, "kernel": "k_smooth",
+                     "note": "not memory bound: per lineage step one Philox block, a ziggurat draw, an "
+                             "FP64 due time and FP32 log-sigmoids; bytes are inputs and outputs only"},
+        "gpu_launches": 4 * args.steps,
+        "clocks": clk,
+    }
+    if cpu:
+        line["cpu_baseline"] = cpu
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def cpu_batched_sample(instances, seconds):
     """Oracle instances/s on instances drawn at random (seeded) until `seconds` pass."""
     import numpy as np
@@ -542,7 +695,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=["small", "medium", "large", "batched"], default="large")
+    ap.add_argument("--workload", choices=["small", "medium", "large", "batched", "calibration"], default="large")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (default configuration)")
@@ -553,6 +706,8 @@ def main():
         return run_reference(args)
     if args.workload == "batched":
         return run_batched(args)
+    if args.workload == "calibration":
+        return run_calibration(args)
     return run_ours(args)
 
 

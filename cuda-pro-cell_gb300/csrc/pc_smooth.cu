@@ -22,9 +22,14 @@
 // gradients A_g = dL/dE_g, regenerating every z from its counter (nothing of the forward pass
 // is stored).
 //
-// Work layout: one block per (bin, candidate); its threads stride over the bin's initial
-// cells; per-thread partial sums live in shared memory and are reduced in a fixed order,
-// so results are deterministic.
+// Work layout: one block per (bin, group of 32 candidates); lane l of every warp is
+// candidate 32 * group + l, and the block's 4 warps take the bin's lineages 32 at a time:
+// first each lane draws one lineage's normals (one Philox block and ziggurat draw per
+// generation) into shared memory, then every lane walks all 32 lineages for its own
+// candidate, reading the shared draws. Each normal is thus drawn once per 32 candidates.
+// Remaining time R = T - S is carried in FP64 (three FP64 operations per step: the division
+// time, R, and the FP64 accumulation). Per-thread partial sums live in shared memory and are
+// reduced over the warps in a fixed order, so results are deterministic.
 #include <cuda_runtime.h>
 
 #include "pc_engine.h"
@@ -34,7 +39,6 @@ namespace pc {
 namespace {
 
 constexpr int kThreads = 128;
-constexpr uint32_t kFull = 0xFFFFFFFFu;
 constexpr uint32_t kBudget = 1u << 16;
 
 __device__ __forceinline__ double f32_to_f64_bits(float z) {
@@ -71,13 +75,6 @@ __device__ __forceinline__ float node_z(uint64_t node, uint32_t root, uint32_t k
   return node_z_slow(j, layer, pair_wedge_bits(P, c), node, root, k0, k1, Z, error);
 }
 
-struct Lineage {
-  uint32_t root;
-  uint32_t steps;   // cap + 1 due times
-  uint64_t bits;    // left/right choices
-  double u_age;     // U in (0, 1]
-};
-
 // log sigmoid(x) and log(1 - sigmoid(x)) = log sigmoid(-x).
 __device__ __forceinline__ void log_sig(float x, float& ls, float& l1m) {
   const float L = log1pf(expf(-fabsf(x)));
@@ -85,131 +82,187 @@ __device__ __forceinline__ void log_sig(float x, float& ls, float& l1m) {
   l1m = -(fmaxf(x, 0.0f) + L);
 }
 
+// A double rounded toward zero to float on the integer pipes (GB300 runs FP64<->FP32
+// conversions on its slow FP64 pipe). |d| < 2^-126 gives 0, |d| >= 2^128 gives inf.
+__device__ __forceinline__ float f64_to_f32_rz_any(double d) {
+  const uint32_t hi = (uint32_t)__double2hiint(d), lo = (uint32_t)__double2loint(d);
+  const uint32_t sign = hi & 0x80000000u, mag = hi & 0x7FFFFFFFu;
+  if (mag < (897u << 20)) return __uint_as_float(sign);
+  if (mag >= (1151u << 20)) return __uint_as_float(sign | 0x7F800000u);
+  return __uint_as_float(sign | ((mag - (896u << 20)) << 3) | (lo >> 29));
+}
+
+// x * 2 for a positive normal double, on the integer pipe.
+__device__ __forceinline__ double twice(double x) {
+  return __longlong_as_double(__double_as_longlong(x) + (1ll << 52));
+}
+
 constexpr float kLogNegligible = -100.0f;  // e^-100 * 2^63 < 1e-24
 
-// One lineage of one type. Forward: adds weight * 2^g * w_g into acc[g * kThreads].
-// Backward: accumulates sum_g A_g 2^g w_g (for the ratio) and its derivatives in mean, sd.
+// One lineage (its normals z[j * 32], j = 0.., and initial age U) for one type of one
+// candidate. Forward: acc[g * kThreads] += weight * 2^g * w_g. Backward (Ag2[g] = 2^g dL/dE_g):
+// accumulates sum_g Ag2[g] w_g and its derivatives in mean and sd.
 template <bool Backward>
-__device__ __forceinline__ void walk(const SmoothArgs& A, const ZigTables& Z, const Lineage& L, double mu,
-                                     double sigma, bool fixed_tau, double weight, double* acc, const double* Ag,
+__device__ __forceinline__ void walk(const SmoothArgs& A, const float* z, double u_age, uint32_t steps, double mu,
+                                     double sigma, bool fixed_tau, double weight, double* acc, const float* Ag2,
                                      double& g_r, double& g_mu, double& g_sig) {
-  double S = 0.0;
+  double R = 0.0;                 // T - S_j
   float log_p = 0.0f;             // log s_1 ... s_{j-1}
   float dmu = 0.0f, dsig = 0.0f;  // dS_j / d(mean, sd)
   float D_mu = 0.0f, D_sig = 0.0f;
   const float inv_h = (float)A.inv_h;
-  uint64_t node = 1;
-  double scale = 1.0;  // 2^(j-1)
-  for (uint32_t j = 1; j <= L.steps; ++j) {
-    const float z = fixed_tau ? 0.0f : node_z(node, L.root, A.k0, A.k1, Z, A.error);
-    const double tau = fixed_tau ? 0.0 : fma(sigma, f32_to_f64_bits(z), mu);
+  double ws = weight;  // weight * 2^(j-1)
+  float f_r = 0.0f, f_mu = 0.0f, f_sig = 0.0f;  // this lineage's gradient terms (FP32: a few terms)
+  for (uint32_t j = 1; j <= steps; ++j) {
+    const float zj = fixed_tau ? 0.0f : z[(j - 1) * 32u];
+    const double tau = fixed_tau ? 0.0 : fma(sigma, f32_to_f64_bits(zj), mu);
     if (j == 1) {
-      S = tau * L.u_age + tau;
-      dmu = (float)(1.0 + L.u_age);
-      dsig = z * dmu;
+      R = A.t_max - fma(tau, u_age, tau);
+      dmu = (float)(1.0 + u_age);
+      dsig = zj * dmu;
     } else {
-      S = S + tau;
+      R = R - tau;
       dmu += 1.0f;
-      dsig += z;
+      dsig += zj;
     }
-    const float x = __double2float_rn((A.t_max - S) * A.inv_h);
+    const float x = f64_to_f32_rz_any(R) * inv_h;
     float ls, l1m;
     log_sig(x, ls, l1m);
     const float w = expf(log_p + l1m);  // leaf weight of generation j - 1
     if constexpr (!Backward) {
-      acc[(j - 1) * kThreads] += weight * scale * (double)w;
+      if (w != 0.0f) acc[(j - 1) * kThreads] = fma(ws, f32_to_f64_bits(w), acc[(j - 1) * kThreads]);
+      ws = twice(ws);
     } else {
-      const double a = Ag[j - 1] * scale * (double)w;
-      g_r += a;
+      const float a = Ag2[j - 1];
+      if (a != 0.0f && w != 0.0f) {
+        const float aw = a * w;
+        f_r += aw;
+        if (!fixed_tau) {
+          const float s = expf(ls);
+          f_mu += aw * (D_mu + s * inv_h * dmu);
+          f_sig += aw * (D_sig + s * inv_h * dsig);
+        }
+      }
       if (!fixed_tau) {
-        const float s = expf(ls), one_m_s = expf(l1m);
-        g_mu += a * (double)(D_mu + s * inv_h * dmu);
-        g_sig += a * (double)(D_sig + s * inv_h * dsig);
+        const float one_m_s = expf(l1m);
         D_mu -= one_m_s * inv_h * dmu;
         D_sig -= one_m_s * inv_h * dsig;
       }
     }
     log_p += ls;
     if (log_p < kLogNegligible) break;
-    scale *= 2.0;
-    node = 2ull * node + ((L.bits >> (j - 1u)) & 1ull);
   }
-}
-
-// Fixed-order sum of rows[q][0..kThreads) for q in [0, nrows), one warp per row.
-__device__ __forceinline__ void reduce_rows(const double* rows, uint32_t nrows, double* out) {
-  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-  for (uint32_t q = warp; q < nrows; q += kThreads / 32) {
-    double v = 0.0;
-#pragma unroll
-    for (int i = 0; i < kThreads / 32; ++i) v += rows[q * kThreads + lane + 32 * i];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
-    if (lane == 0) out[q] = v;
+  if constexpr (Backward) {
+    g_r += (double)f_r;
+    g_mu += (double)f_mu;
+    g_sig += (double)f_sig;
   }
 }
 
 template <bool Backward>
 __global__ void __launch_bounds__(kThreads) k_smooth(const SmoothArgs A, const double* __restrict__ params,
-                                                     const double* __restrict__ grad_expected, uint32_t nvalues,
-                                                     const int32_t* __restrict__ vidx, double* __restrict__ out) {
-  extern __shared__ double acc[];  // forward: [rows][kThreads]; backward: [ntypes * 3][kThreads]
+                                                     uint32_t ncand, const double* __restrict__ grad_expected,
+                                                     uint32_t nvalues, const int32_t* __restrict__ vidx,
+                                                     double* __restrict__ out) {
+  // dynamic: acc [nrows][kThreads] doubles, then z [kWarps][rows][32] floats
+  extern __shared__ double acc[];
   __shared__ ZigTables Z;
-  __shared__ double prm[kSmoothMaxTypes * 3];
-  __shared__ double Ag[kSmoothMaxRows];
-  const uint32_t b = blockIdx.x, c = blockIdx.y;
+  __shared__ double prm[32][kSmoothMaxTypes * 3];
+  __shared__ float Ag2[Backward ? 32 : 1][kSmoothMaxRows];
+  __shared__ double u_age[kThreads];
+  constexpr uint32_t kWarps = kThreads / 32;
+  const uint32_t b = blockIdx.x;
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  const uint32_t c = blockIdx.y * 32u + lane;
+  const bool live = c < ncand;
   const uint32_t K = A.ntypes;
+  const uint32_t nrows = Backward ? K * 3 : A.rows;
+  float* zbuf = reinterpret_cast<float*>(acc + (size_t)nrows * kThreads) + (size_t)warp * A.rows * 32u;
   for (uint32_t i = threadIdx.x; i < sizeof(ZigTables) / 4; i += blockDim.x)
     reinterpret_cast<uint32_t*>(&Z)[i] = __ldg(reinterpret_cast<const uint32_t*>(A.zig) + i);
-  for (uint32_t i = threadIdx.x; i < K * 3; i += blockDim.x) prm[i] = params[(uint64_t)c * K * 3 + i];
-  const uint32_t nrows = Backward ? K * 3 : A.rows;
+  for (uint32_t i = threadIdx.x; i < 32u * K * 3u; i += blockDim.x) {
+    const uint32_t l = i / (K * 3u), q = i % (K * 3u);
+    const uint32_t cc = blockIdx.y * 32u + l;
+    prm[l][q] = cc < ncand ? params[(uint64_t)cc * K * 3 + q] : 0.0;
+  }
   for (uint32_t i = 0; i < nrows; ++i) acc[i * kThreads + threadIdx.x] = 0.0;
   const uint32_t cap = __ldg(A.bin_cap + b);
+  const uint32_t steps = cap + 1u;
   if constexpr (Backward) {
-    for (uint32_t g = threadIdx.x; g < kSmoothMaxRows; g += blockDim.x) {
+    for (uint32_t i = threadIdx.x; i < 32u * kSmoothMaxRows; i += blockDim.x) {
+      const uint32_t l = i / kSmoothMaxRows, g = i % kSmoothMaxRows;
+      const uint32_t cc = blockIdx.y * 32u + l;
       double a = 0.0;
-      if (g < A.rows && g <= cap) {
+      if (cc < ncand && g < A.rows && g <= cap) {
         const int32_t v = vidx[(uint64_t)b * A.rows + g];
-        if (v >= 0) a = grad_expected[(uint64_t)c * nvalues + v];
+        if (v >= 0) a = ldexp(grad_expected[(uint64_t)cc * nvalues + v], (int)g);
       }
-      Ag[g] = a;
+      Ag2[l][g] = (float)a;
     }
   }
   __syncthreads();
   const uint64_t r0 = __ldg(A.bin_start + b), r1 = __ldg(A.bin_start + b + 1);
   const double inv_paths = 1.0 / (double)A.paths;
   double* my = acc + threadIdx.x;
-  for (uint64_t r = r0 + threadIdx.x; r < r1; r += kThreads) {
-    Lineage L;
-    L.root = (uint32_t)r;
-    L.steps = cap + 1u;
-    const u32x4 R = philox(u32x4{0u, 0u, L.root, kPurposeRoot}, A.k0, A.k1);
-    L.u_age = unit53_open_closed(R.z, R.w);
-    for (uint32_t m = 0; m < A.paths; ++m) {
-      const u32x4 B = philox(u32x4{m, 0u, L.root, kPurposePath}, A.k0, A.k1);
-      L.bits = (uint64_t)B.x | ((uint64_t)B.y << 32);
-      for (uint32_t k = 0; k < K; ++k) {
-        const double ratio = prm[3 * k], mu = prm[3 * k + 1], sd = prm[3 * k + 2];
-        double g_r = 0.0, g_mu = 0.0, g_sig = 0.0;
-        if (mu < 0.0) {
-          // quiescent type: a leaf at generation 0 (cell.cu:69-75)
-          if constexpr (Backward)
-            g_r = Ag[0];
-          else
-            my[0] += ratio * inv_paths;
-        } else {
-          walk<Backward>(A, Z, L, mu, sd, mu == 0.0, ratio * inv_paths, my, Ag, g_r, g_mu, g_sig);
-        }
-        if constexpr (Backward) {
-          my[(3 * k) * kThreads] += g_r * inv_paths;
-          my[(3 * k + 1) * kThreads] += g_mu * ratio * inv_paths;
-          my[(3 * k + 2) * kThreads] += g_sig * ratio * inv_paths;
+  const double* my_prm = prm[lane];
+  const float* my_ag = Backward ? Ag2[lane] : nullptr;
+  // lineage i of the bin: initial cell r0 + i / paths, path i % paths
+  const uint64_t nlin = (r1 - r0) * A.paths;
+  for (uint64_t base = (uint64_t)warp * 32u; base < nlin; base += 32u * kWarps) {
+    // this lane draws lineage base + lane
+    const uint64_t i = base + lane;
+    if (i < nlin) {
+      const uint32_t root = (uint32_t)(r0 + i / A.paths);
+      const uint32_t m = (uint32_t)(i % A.paths);
+      const u32x4 R = philox(u32x4{0u, 0u, root, kPurposeRoot}, A.k0, A.k1);
+      u_age[threadIdx.x] = unit53_open_closed(R.z, R.w);
+      const u32x4 B = philox(u32x4{m, 0u, root, kPurposePath}, A.k0, A.k1);
+      const uint64_t bits = (uint64_t)B.x | ((uint64_t)B.y << 32);
+      uint64_t node = 1;
+      for (uint32_t j = 0; j < steps; ++j) {
+        zbuf[j * 32u + lane] = node_z(node, root, A.k0, A.k1, Z, A.error);
+        node = 2ull * node + ((bits >> j) & 1ull);
+      }
+    }
+    __syncwarp();
+    const uint32_t n = (uint32_t)((nlin - base) < 32u ? (nlin - base) : 32u);
+    if (live) {
+      for (uint32_t ii = 0; ii < n; ++ii) {
+        const float* z = zbuf + ii;
+        const double ua = u_age[warp * 32u + ii];
+        for (uint32_t k = 0; k < K; ++k) {
+          const double ratio = my_prm[3 * k], mu = my_prm[3 * k + 1], sd = my_prm[3 * k + 2];
+          double g_r = 0.0, g_mu = 0.0, g_sig = 0.0;
+          if (mu < 0.0) {
+            // quiescent type: a leaf at generation 0 (cell.cu:69-75)
+            if constexpr (Backward)
+              g_r = my_ag[0];
+            else
+              my[0] += ratio * inv_paths;
+          } else if (Backward || ratio != 0.0) {
+            walk<Backward>(A, z, ua, steps, mu, sd, mu == 0.0, ratio * inv_paths, my, my_ag, g_r, g_mu, g_sig);
+          }
+          if constexpr (Backward) {
+            my[(3 * k) * kThreads] += g_r * inv_paths;
+            my[(3 * k + 1) * kThreads] += g_mu * ratio * inv_paths;
+            my[(3 * k + 2) * kThreads] += g_sig * ratio * inv_paths;
+          }
         }
       }
     }
+    __syncwarp();
   }
   __syncthreads();
-  reduce_rows(acc, nrows, out + ((uint64_t)c * A.nbins + b) * nrows);
+  // out[c][b][row] = sum over the warps, in warp order
+  if (warp == 0 && live) {
+    double* o = out + ((uint64_t)c * A.nbins + b) * nrows;
+    for (uint32_t q = 0; q < nrows; ++q) {
+      double v = 0.0;
+#pragma unroll
+      for (uint32_t w = 0; w < kWarps; ++w) v += acc[q * kThreads + w * 32u + lane];
+      o[q] = v;
+    }
+  }
 }
 
 __global__ void k_smooth_merge(const double* __restrict__ e_raw, uint32_t ncand, uint32_t per_cand,
@@ -233,19 +286,21 @@ __global__ void k_smooth_grad_sum(const double* __restrict__ part, uint32_t ncan
   grad[i] = s;
 }
 
-int smem_bytes(uint32_t rows) { return (int)(rows * kThreads * sizeof(double)); }
+// acc rows x kThreads doubles + the lineage draws (kThreads floats per generation row)
+int smem_bytes(uint32_t acc_rows, uint32_t rows) {
+  return (int)(acc_rows * kThreads * sizeof(double) + rows * kThreads * sizeof(float));
+}
 
 template <bool Backward>
 int launch_smooth_t(const SmoothArgs& A, const double* params, uint32_t ncand, const double* grad_expected,
                     uint32_t nvalues, const int32_t* vidx, double* out, cudaStream_t st) {
-  const uint32_t rows = Backward ? A.ntypes * 3u : A.rows;
-  const int smem = smem_bytes(rows);
-  if (smem > 48 * 1024) {
-    const cudaError_t e = cudaFuncSetAttribute(k_smooth<Backward>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e != cudaSuccess) return (int)e;
-  }
-  const dim3 grid(A.nbins, ncand);
-  k_smooth<Backward><<<grid, kThreads, smem, st>>>(A, params, grad_expected, nvalues, vidx, out);
+  const uint32_t acc_rows = Backward ? A.ntypes * 3u : A.rows;
+  const int smem = smem_bytes(acc_rows, A.rows);
+  // static shared memory plus `smem` may exceed the default 48 KB: always opt in
+  const cudaError_t e = cudaFuncSetAttribute(k_smooth<Backward>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return (int)e;
+  const dim3 grid(A.nbins, (ncand + 31u) / 32u);
+  k_smooth<Backward><<<grid, kThreads, smem, st>>>(A, params, ncand, grad_expected, nvalues, vidx, out);
   return (int)cudaGetLastError();
 }
 
