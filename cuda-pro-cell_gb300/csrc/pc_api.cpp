@@ -1383,6 +1383,7 @@ SmoothArgs smooth_args(const pc_context* ctx, const pc_smooth* s) {
   A.rows = s->rows;
   A.ntypes = s->ntypes;
   A.paths = s->paths;
+  A.ncells = (uint32_t)s->I.roots;
   A.t_max = s->I.t_max;
   A.inv_h = 1.0 / s->h;
   A.bin_start = s->bin_start_dev;
@@ -1426,6 +1427,10 @@ int pc_smooth_create(pc_context* ctx, const pc_bin* bins, uint64_t n_bins, uint3
   if (rc == PC_OK && s->I.gmax + 1 > (uint32_t)kSmoothMaxRows) {
     rc = PC_ERR_UNSUPPORTED;
     msg = "the smoothed form supports at most 63 generations per bin";
+  }
+  if (rc == PC_OK && (uint64_t)s->I.roots * paths_per_cell > 0xFFFFFFFFull) {
+    rc = PC_ERR_UNSUPPORTED;
+    msg = "initial cells x paths_per_cell must stay below 2^32";
   }
   if (rc != PC_OK) {
     delete s;

@@ -174,7 +174,8 @@ constexpr int kSmoothMaxRows = 64;  // generations per bin (cap + 1)
 struct SmoothArgs {
   uint32_t k0, k1;            // seed
   uint32_t nbins, rows;       // rows = max cap + 1 (generation rows per bin)
-  uint32_t ntypes, paths;     // paths sampled per initial cell
+  uint32_t ntypes, paths;     // lineages sampled per initial cell (independent replicas)
+  uint32_t ncells;            // initial cells; replica m of cell r draws as cell r + m * ncells
   double t_max, inv_h;
   const uint64_t* bin_start;  // [nbins + 1]
   const uint32_t* bin_cap;    // [nbins]

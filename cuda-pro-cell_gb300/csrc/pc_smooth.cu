@@ -12,6 +12,10 @@
 // generation-g leaves of one initial cell is E_g = sum_k ratio_k 2^g E[w_g], 0 <= g <= cap_b,
 // estimated by `paths` lineages sampled per initial cell (uniform random left/right
 // choices; at g = cap_b only "not due" survives, due cells vanish as in the plain form).
+// Each sampled lineage is an independent replica of its initial cell: replica m of cell r
+// takes every draw (initial age, normals, path) from the plain form's counters of cell
+// r + m * ncells, so the estimate converges to the expectation over all randomness, and
+// replica 0 shares its draws with the plain form run on the same seed.
 // Types enter analytically through ratio_k, so d/d ratio is exact. Weights are products of
 // sigmoids evaluated in log space (FP32; due times accumulate in FP64), never negative, and a
 // lineage stops once its survival product is below e^-100.
@@ -206,17 +210,17 @@ __global__ void __launch_bounds__(kThreads) k_smooth(const SmoothArgs A, const d
   double* my = acc + threadIdx.x;
   const double* my_prm = prm[lane];
   const float* my_ag = Backward ? Ag2[lane] : nullptr;
-  // lineage i of the bin: initial cell r0 + i / paths, path i % paths
+  // lineage i of the bin: initial cell r0 + i / paths, replica i % paths
   const uint64_t nlin = (r1 - r0) * A.paths;
   for (uint64_t base = (uint64_t)warp * 32u; base < nlin; base += 32u * kWarps) {
     // this lane draws lineage base + lane
     const uint64_t i = base + lane;
     if (i < nlin) {
-      const uint32_t root = (uint32_t)(r0 + i / A.paths);
       const uint32_t m = (uint32_t)(i % A.paths);
+      const uint32_t root = (uint32_t)(r0 + i / A.paths) + m * A.ncells;  // replica m
       const u32x4 R = philox(u32x4{0u, 0u, root, kPurposeRoot}, A.k0, A.k1);
       u_age[threadIdx.x] = unit53_open_closed(R.z, R.w);
-      const u32x4 B = philox(u32x4{m, 0u, root, kPurposePath}, A.k0, A.k1);
+      const u32x4 B = philox(u32x4{0u, 0u, root, kPurposePath}, A.k0, A.k1);
       const uint64_t bits = (uint64_t)B.x | ((uint64_t)B.y << 32);
       uint64_t node = 1;
       for (uint32_t j = 0; j < steps; ++j) {

@@ -3,7 +3,8 @@
     PYTHONPATH=cuda-pro-cell_gb300 python -m procell medium --runs 2 --budget 2e9
 
 Workloads are those of procell.configs (small, medium, large). --budget limits the device
-memory of the level buffers (memory_budget_bytes), e.g. to keep a profiler capture small.
+memory of the level buffers (memory_budget_bytes), e.g. to keep a profiler capture small;
+--driver and --config select the driver and the compiled sweep configuration.
 """
 import argparse
 import json
@@ -19,11 +20,15 @@ def main():
     ap.add_argument("--runs", type=int, default=1)
     ap.add_argument("--budget", type=float, default=0.0)
     ap.add_argument("--seed", type=int, default=None)
+    ap.add_argument("--driver", type=int, default=0, help="0: one launch per sweep, 1: persistent")
+    ap.add_argument("--config", type=int, default=4, help="compiled sweep configuration 0-7")
     a = ap.parse_args()
     w = configs.by_name(a.workload)
     eng = Engine(0)
     if a.budget > 0:
         eng.set_option("memory_budget_bytes", a.budget)
+    eng.set_option("driver", a.driver)
+    eng.set_option("sweep_config", a.config)
     plan = eng.plan(w.bins, w.types, w.t_max, w.phi, w.seed if a.seed is None else a.seed)
     for i in range(a.runs):
         t = time.perf_counter()

@@ -145,13 +145,13 @@ def time_to(trace, level):
     return None
 
 
-def compare(engine, candidates=256, seed=7, gd_iters=300, pso_seconds=40.0):
+def compare(engine, candidates=256, seed=7, gd_iters=300, pso_seconds=40.0, paths=2):
     """Both searches from the same population; time to reach a sequence of loss levels.
 
-    The headline level is the particle swarm's best loss at the end of its budget when
-    gradient descent reaches it, else the loss of the hidden parameters themselves (a fit
-    as good as the truth)."""
-    prob = Problem(engine, seed=seed)
+    The headline level is the particle swarm's best loss at the end of its budget plus 0.1%
+    when gradient descent reaches it, else the loss of the hidden parameters themselves (a
+    fit as good as the truth)."""
+    prob = Problem(engine, seed=seed, paths=paths)
     theta0 = prob.start(candidates, seed)
     gradient_descent(prob, theta0, iters=3)  # warm-up of both code paths
     particle_swarm(prob, theta0, iters=3)
@@ -162,24 +162,27 @@ def compare(engine, candidates=256, seed=7, gd_iters=300, pso_seconds=40.0):
         E = prob.smooth.forward(hidden)
         l_true = float(((torch.log1p(E) - torch.log1p(prob.target)) ** 2).sum())
     gd_final, ps_final = gd[-1][1], ps[-1][1]
-    levels = sorted({round(x, 6) for x in (2 * l_true, 1.25 * l_true, 1.1 * l_true, 1.05 * l_true, l_true,
-                                           ps_final, gd_final)}, reverse=True)
+    levels = sorted({x for x in (2 * l_true, 1.25 * l_true, 1.1 * l_true, 1.05 * l_true, l_true,
+                                 ps_final * 1.01, ps_final * 1.001, ps_final, gd_final)}, reverse=True)
     table = []
     for L in levels:
         tg, tp = time_to(gd, L), time_to(ps, L)
         table.append({"loss": L, "gd_seconds": tg, "pso_seconds": tp,
                       "ratio": (tp / tg) if (tg and tp) else None})
-    head = ps_final if time_to(gd, ps_final) is not None else l_true
+    # the swarm's final loss, 0.1% up (its last, tiny improvements would otherwise set the
+    # clock), or the loss of the hidden parameters when descent does not reach that
+    head = ps_final * 1.001 if time_to(gd, ps_final * 1.001) is not None else l_true
     tg, tp = time_to(gd, head), time_to(ps, head)
     return {
         "candidates": candidates,
+        "lineages_per_cell": paths,
         "hidden": prob.hidden,
         "loss_at_hidden": l_true,
         "gd": {"iters": len(gd), "seconds": gd[-1][0], "best_loss": gd_final, "method": "Adam, cosine lr 0.1 -> 0.002"},
         "pso": {"iters": len(ps) - 1, "seconds": ps[-1][0], "best_loss": ps_final,
                 "method": "particle swarm, constriction coefficients, ring neighbourhood"},
         "equal_loss": head,
-        "equal_loss_is": "swarm final" if head == ps_final else "loss at the hidden parameters",
+        "equal_loss_is": "swarm final + 0.1%" if head != l_true else "loss at the hidden parameters",
         "gd_seconds_to_equal_loss": tg,
         "pso_seconds_to_equal_loss": tp,
         "speedup": (tp / tg) if (tg and tp) else None,
@@ -193,10 +196,11 @@ def main():
     ap.add_argument("--seed", type=int, default=7)
     ap.add_argument("--gd-iters", type=int, default=300)
     ap.add_argument("--pso-seconds", type=float, default=40.0)
+    ap.add_argument("--paths", type=int, default=2)
     a = ap.parse_args()
     from . import Engine
     eng = Engine(0)
-    print(json.dumps(compare(eng, a.candidates, a.seed, a.gd_iters, a.pso_seconds)))
+    print(json.dumps(compare(eng, a.candidates, a.seed, a.gd_iters, a.pso_seconds, a.paths)))
 
 
 if __name__ == "__main__":

@@ -3,9 +3,10 @@
 Test infrastructure, like the rest of oracle/: it checks the sm_103a smoothed-form kernels
 and is never part of the product path. It follows the model stated in
 cuda-pro-cell_gb300/csrc/pc_smooth.cu independently of that code: the lineage of an initial
-cell (root index r, path m) visits heap nodes 1, 2*1+b_1, ...; node n's standard normal is
-the oracle's ziggurat draw for child (n & 1) of parent (n >> 1) (oracle_normals, without the
-truncation); the initial age U and the path bits come from the oracle's Philox. Everything
+cell r, replica m, draws as initial cell r + m * (number of cells): it visits heap nodes
+1, 2*1+b_1, ...; node n's standard normal is the oracle's ziggurat draw for child (n & 1) of
+parent (n >> 1) (oracle_normals, without the truncation); the initial age U and the path
+bits come from the oracle's Philox. Everything
 is evaluated in FP64 (the kernels use FP32 log-sigmoids), and the adjoint is obtained by
 forward-mode differentiation of the same loop, written separately from the kernel's.
 
@@ -59,6 +60,7 @@ def forward_backward(bins, t_max, phi, h, paths, seed, params, grad_expected=Non
     """Expected counts [C][V] for params [C][K][3], and, with grad_expected [C][V], the
     gradient [C][K][3] of sum(grad_expected * expected)."""
     rows, values, thr = prepare(bins, phi)
+    ncells = sum(f for _, f, _, _ in rows)
     vindex = {v: i for i, v in enumerate(values)}
     P = np.asarray(params, dtype=np.float64)
     C, K = P.shape[0], P.shape[1]
@@ -72,16 +74,17 @@ def forward_backward(bins, t_max, phi, h, paths, seed, params, grad_expected=Non
             vi.append(vindex.get(x, -1) if (g > 0 or v >= thr) else -1)
             x = x / 2
         for r in range(r0, r0 + f):
-            R = oracle.philox([0, 0, r, PURPOSE_ROOT], [k0, k1])
-            U = _unit53_open_closed(R[2], R[3])
             for m in range(paths):
-                B = oracle.philox([m, 0, r, PURPOSE_PATH], [k0, k1])
+                vr = r + m * ncells  # replica m draws as initial cell r + m * ncells
+                R = oracle.philox([0, 0, vr, PURPOSE_ROOT], [k0, k1])
+                U = _unit53_open_closed(R[2], R[3])
+                B = oracle.philox([0, 0, vr, PURPOSE_PATH], [k0, k1])
                 bits = B[0] | (B[1] << 32)
                 nodes, node = [], 1
                 for j in range(cap + 1):
                     nodes.append(node)
                     node = 2 * node + ((bits >> j) & 1)
-                zs = [float(oracle.normals(seed, r, n >> 1, 2)[n & 1]) for n in nodes]
+                zs = [float(oracle.normals(seed, vr, n >> 1, 2)[n & 1]) for n in nodes]
                 for c in range(C):
                     for k in range(K):
                         ratio, mu, sd = P[c, k]

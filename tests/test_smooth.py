@@ -188,3 +188,22 @@ def test_matches_cpu_restatement(engine):
     sm.close()
     assert np.allclose(E, E_ref, rtol=2e-5, atol=1e-9 * np.abs(E_ref).max()), np.abs(E - E_ref).max()
     assert np.allclose(G, G_ref, rtol=2e-5, atol=1e-7 * np.abs(G_ref).max()), (G, G_ref)
+
+
+def test_converges_to_plain_expectation(engine):
+    """With many lineages per cell (independent replicas) and a small h, the expected counts
+    approach the plain form's histogram averaged over seeds."""
+    from procell.smooth import Smooth
+    bins = [(100.0, 300), (37.5, 200), (700.0, 100)]
+    types = [(0.6, 40.0, 8.0), (0.4, 55.0, 5.5)]
+    T, phi = 168.0, 1.0
+    runs = 64
+    avg = sum(engine.simulate(bins, types, T, phi, 9000 + s).totals.astype(np.float64) for s in range(runs)) / runs
+    sm = Smooth(engine, bins, n_types=2, t_max=T, phi=phi, h=0.05, paths=256, seed=4)
+    E = sm.forward(params_tensor([types]))[0].cpu().numpy()
+    sm.sync()
+    sm.close()
+    assert abs(E.sum() - avg.sum()) <= 0.01 * avg.sum()
+    big = avg > 0.05 * avg.max()
+    # Monte Carlo error of both sides is a few percent at these counts
+    assert np.all(np.abs(E[big] - avg[big]) <= 0.06 * avg[big] + 5.0), np.c_[E[big], avg[big]]
