@@ -289,7 +289,8 @@ def run_ours(args):
     launches = max(1, args.steps if persistent else sweeps)  # launches of the dominant kernel
     achieved = alg_bytes / (divide_ms * 1e-3) / 1e9 if divide_ms > 0 else None
     traffic = None
-    tpath = os.path.join(ROOT, "profiles", "traffic_per_division.txt")
+    tpath = os.path.join(ROOT, "profiles", "traffic_per_division_persistent.txt" if persistent
+                         else "traffic_per_division.txt")
     if os.path.exists(tpath):
         try:
             per_div = float(open(tpath).read().split()[0])
