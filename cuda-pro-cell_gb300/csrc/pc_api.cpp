@@ -493,6 +493,10 @@ int prepare_instance(const pc_bin* bins, uint64_t n_bins, const pc_cell_type* ty
   I.t_hi = std::nextafter((float)(I.t_max + margin), INFINITY);
   I.t_lo = std::nextafter((float)(I.t_max - margin), -INFINITY);
   I.est_ok = est_ok ? 1 : 0;
+  if (!est_ok) {  // the estimate decides nothing: every test is exact
+    I.t_hi = INFINITY;
+    I.t_lo = -INFINITY;
+  }
   return PC_OK;
 }
 
@@ -568,7 +572,6 @@ int finalize_plan(pc_context* ctx, pc_plan* p) {
         bt.k0 = (uint32_t)I.seed;
         bt.k1 = (uint32_t)(I.seed >> 32);
         bt.root_begin = I.root_begin;
-        bt.est_ok = I.est_ok;
         bt.instance = i;
         btypes.push_back(bt);
       }

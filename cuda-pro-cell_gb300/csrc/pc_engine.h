@@ -44,25 +44,29 @@ constexpr int kWarpsPerBlock = kBlock / 32;
 enum TypeMode : int32_t { kModeNormal = 0, kModeQuiescent = 1, kModeZeroMean = 2 };
 
 // One cell type, in the descending-ratio order the reference samples in.
-struct TypeDev {
-  double mu, sigma, cum;
+// The division sweep reads bytes 0-31 as one double2 and one float4.
+struct alignas(16) TypeDev {
+  double mu, sigma;
   float mu_f, sigma_f;
   float zlo, zhi;  // the FP32 z range for which fma(sigma, z, mu) > 0 (the truncation)
+  double cum;
   int32_t mode;
   int32_t pad;
 };
 
 // Batched form: the parameters of one type together with its instance's (one table
 // entry per type of every instance, in instance order).
-struct BatchType {
-  TypeDev t;
-  double t_max;
-  float t_hi, t_lo;
-  uint32_t k0, k1;      // the instance's seed
-  uint64_t root_begin;  // the instance's first initial cell in the batch
-  int32_t est_ok;
+// The division sweep reads bytes 0-31 (type) and 48-79 (instance) as four 16-byte loads.
+struct alignas(16) BatchType {
+  TypeDev t;            // bytes 0-47
+  double t_max;         // 48
+  float t_hi, t_lo;     // 56: FP32 band around t_max (+-inf: estimate never decides)
+  uint32_t k0, k1;      // 64: the instance's seed
+  uint64_t root_begin;  // 72: the instance's first initial cell in the batch
   uint32_t instance;
+  uint32_t pad;
 };
+static_assert(sizeof(TypeDev) == 48 && sizeof(BatchType) == 96, "layout read by the division sweep");
 
 struct InstanceDev {
   uint32_t type_begin, ntypes, fallback, pad;
@@ -75,7 +79,8 @@ struct RunArgs {
   uint32_t k0, k1;           // seed
   uint32_t ks[20];           // Philox key schedule of the seed
   double t_max;
-  float t_hi, t_lo;          // FP32 band around t_max for the estimate
+  float t_hi, t_lo;          // FP32 band around t_max (+-inf when the inputs leave the
+                             // FP32 estimate's range: the estimate then never decides)
   int32_t est_ok;            // FP32 estimate allowed (inputs in range)
   uint32_t ntypes, nbins, fallback;
   uint32_t hist_gens;

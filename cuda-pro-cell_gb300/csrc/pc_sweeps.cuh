@@ -97,7 +97,7 @@ __device__ __forceinline__ void stage(Smem& s, const RunArgs& a) {
 constexpr uint32_t kRoundBudget = 1u << 16;
 
 __device__ __noinline__ float slow_z(uint32_t j, uint32_t layer, uint32_t wedge, uint64_t node,
-                                     uint32_t root, uint32_t k0, uint32_t k1, const TypeDev& T,
+                                     uint32_t root, uint32_t k0, uint32_t k1, float zlo, float zhi,
                                      const ZigTables& Z, uint32_t* error) {
   ChildStream cs = child_stream(node, root, k0, k1);
   uint32_t budget = kRoundBudget;
@@ -105,7 +105,7 @@ __device__ __noinline__ float slow_z(uint32_t j, uint32_t layer, uint32_t wedge,
   while (budget > 0u) {
     const float z = zig_normal(j, layer, have_wedge, wedge, cs, Z, budget);
     if (budget == 0u) break;
-    if (z >= T.zlo && z <= T.zhi) return z;
+    if (z >= zlo && z <= zhi) return z;
     have_wedge = false;
     j = cs.next();
     layer = cs.next() & 255u;
@@ -117,15 +117,15 @@ __device__ __noinline__ float slow_z(uint32_t j, uint32_t layer, uint32_t wedge,
 
 // First-attempt fast path (about 98.5% of draws): one strip test, one FP32 multiply.
 __device__ __forceinline__ float draw_z(uint32_t j, uint32_t layer, uint32_t wedge, uint64_t node,
-                                        uint32_t root, uint32_t k0, uint32_t k1, const TypeDev& T,
+                                        uint32_t root, uint32_t k0, uint32_t k1, float zlo, float zhi,
                                         const ZigTables& Z, uint32_t* error) {
   const uint32_t mag = j & 0x7FFFFFFFu;
   if (mag < Z.k[layer]) {
     const float x = __fmul_rn((float)mag, Z.w[layer]);
     const float z = (j >> 31) ? -x : x;
-    if (z >= T.zlo && z <= T.zhi) return z;
+    if (z >= zlo && z <= zhi) return z;
   }
-  return slow_z(j, layer, wedge, node, root, k0, k1, T, Z, error);
+  return slow_z(j, layer, wedge, node, root, k0, k1, zlo, zhi, Z, error);
 }
 
 enum Fate : int { kNone = 0, kLeaf = 1, kEmit = 2, kVanish = 3 };
@@ -143,7 +143,8 @@ __device__ __forceinline__ double f32_to_f64(float z) {
 }
 
 // A non-negative double truncated to FP32 (values below 2^-126 become 0; the estimate's
-// error band covers both truncations). Valid while d < 2^128, which est_ok guarantees.
+// error band covers both truncations). Valid while d < 2^128; inputs that allow larger times
+// get an infinite band, so that the estimate is never used.
 __device__ __forceinline__ float f64_to_f32_rz(double d) {
   const uint32_t hi = (uint32_t)__double2hiint(d), lo = (uint32_t)__double2loint(d);
   if (hi < (897u << 20)) return 0.0f;
@@ -157,33 +158,48 @@ __device__ __forceinline__ bool gt_nonneg(double a, double b) {
 
 // What a cell's type, and in the batched form its instance, supplies to the sweeps.
 struct TypeCtx {
-  const TypeDev* t;  // mu, sigma, truncation bounds (shared memory or the batch table)
+  double mu, sigma;     // tau = fma(sigma, z, mu)
+  float mu_f, sigma_f;  // the same in FP32, for the estimate
+  float zlo, zhi;       // truncation bounds on z
   double t_max;
-  float t_hi, t_lo;
-  bool eok;
+  float t_hi, t_lo;     // FP32 band around t_max (+-inf: the estimate never decides)
   uint64_t root_begin;  // batch index of the instance's first initial cell
   uint32_t k0, k1;      // the instance's seed
 };
 
+// The type's parameters from shared memory (plain form) or the batch table (batched form,
+// one entry per type of every instance), in four 16-byte loads at most.
 template <bool Batched>
 __device__ __forceinline__ TypeCtx type_ctx(const RunArgs& a, const TypeDev* smem_types, uint32_t ty) {
   TypeCtx c;
   if (Batched) {
-    const BatchType* b = a.btypes + ty;
-    c.t = &b->t;
-    c.t_max = __ldg(&b->t_max);
-    c.t_hi = __ldg(&b->t_hi);
-    c.t_lo = __ldg(&b->t_lo);
-    c.eok = __ldg(&b->est_ok) != 0;
-    c.root_begin = __ldg(&b->root_begin);
-    c.k0 = __ldg(&b->k0);
-    c.k1 = __ldg(&b->k1);
+    const uint4* q = reinterpret_cast<const uint4*>(a.btypes + ty);
+    const uint4 q0 = __ldg(q), q1 = __ldg(q + 1), q3 = __ldg(q + 3), q4 = __ldg(q + 4);
+    c.mu = __hiloint2double((int)q0.y, (int)q0.x);
+    c.sigma = __hiloint2double((int)q0.w, (int)q0.z);
+    c.mu_f = __uint_as_float(q1.x);
+    c.sigma_f = __uint_as_float(q1.y);
+    c.zlo = __uint_as_float(q1.z);
+    c.zhi = __uint_as_float(q1.w);
+    c.t_max = __hiloint2double((int)q3.y, (int)q3.x);
+    c.t_hi = __uint_as_float(q3.z);
+    c.t_lo = __uint_as_float(q3.w);
+    c.k0 = q4.x;
+    c.k1 = q4.y;
+    c.root_begin = ((uint64_t)q4.w << 32) | q4.z;
   } else {
-    c.t = smem_types + ty;
+    const TypeDev* t = smem_types + ty;
+    const double2 ms = *reinterpret_cast<const double2*>(&t->mu);
+    const float4 fz = *reinterpret_cast<const float4*>(&t->mu_f);
+    c.mu = ms.x;
+    c.sigma = ms.y;
+    c.mu_f = fz.x;
+    c.sigma_f = fz.y;
+    c.zlo = fz.z;
+    c.zhi = fz.w;
     c.t_max = a.t_max;
     c.t_hi = a.t_hi;
     c.t_lo = a.t_lo;
-    c.eok = a.est_ok != 0;
     c.root_begin = 0;
     c.k0 = a.k0;
     c.k1 = a.k1;
@@ -202,17 +218,14 @@ __device__ __forceinline__ bool rec_clamped(unsigned long long r) { return ((r >
 // birth + fma(sigma, z, mu), the reference's t + timer.
 __device__ __forceinline__ int fate(double birth, float birth_f, float z, const TypeCtx& c,
                                     bool can_divide, double& due) {
-  const TypeDev& T = *c.t;
   bool exact = true;
-  if (c.eok) {
-    const float est = __fadd_rn(birth_f, __fadd_rn(T.mu_f, __fmul_rn(T.sigma_f, z)));
-    if (est > c.t_hi) return kLeaf;
-    if (est < c.t_lo) {
-      if (!can_divide) return kVanish;
-      exact = false;
-    }
+  const float est = __fadd_rn(birth_f, __fadd_rn(c.mu_f, __fmul_rn(c.sigma_f, z)));
+  if (est > c.t_hi) return kLeaf;
+  if (est < c.t_lo) {
+    if (!can_divide) return kVanish;
+    exact = false;
   }
-  due = birth + fma(T.sigma, f32_to_f64(z), T.mu);
+  due = birth + fma(c.sigma, f32_to_f64(z), c.mu);
   if (exact && gt_nonneg(due, c.t_max)) return kLeaf;
   return can_divide ? kEmit : kVanish;
 }
@@ -379,7 +392,7 @@ __device__ void root_body(const RunArgs& a, const uint64_t root_base, const uint
       } else {
         const u32x4 P = Batched ? philox(u32x4{0u, 0u, root, kPurposePair}, k0, k1)
                                 : philox_ks(u32x4{0u, 0u, root, kPurposePair}, a.ks);
-        const float z = draw_z(P.y, (P.z >> 8) & 255u, pair_wedge_bits(P, 1u), 1ull, root, k0, k1, T,
+        const float z = draw_z(P.y, (P.z >> 8) & 255u, pair_wedge_bits(P, 1u), 1ull, root, k0, k1, T.zlo, T.zhi,
                                s.zig_or(a), a.error);
         const double tau = fma(T.sigma, f32_to_f64(z), T.mu);  // 0 for zero-mean types
         d0 = tau * u_age + tau;  // t = tau * U (cell.cu:124-143), due = t + timer
@@ -482,7 +495,6 @@ __device__ __forceinline__ CellDraw classify(const ulonglong2 c, bool act, uint3
   const uint32_t cap = rec_cap(rec);
   const bool can_divide = g1 < cap;
   const TypeCtx tc = type_ctx<Batched>(a, s.types, rec_type(rec));
-  const TypeDev& T = *tc.t;
   const uint32_t root = (uint32_t)(root_base + rl - tc.root_begin);
   const u32x4 P = Batched ? philox(u32x4{(uint32_t)node, (uint32_t)(node >> 32), root, kPurposePair}, tc.k0, tc.k1)
                           : philox_ks(u32x4{(uint32_t)node, (uint32_t)(node >> 32), root, kPurposePair}, a.ks);
@@ -494,22 +506,19 @@ __device__ __forceinline__ CellDraw classify(const ulonglong2 c, bool act, uint3
   float z1 = __fmul_rn((float)(P.y & 0x7FFFFFFFu), Z.w[l1]);
   z0 = (P.x >> 31) ? -z0 : z0;
   z1 = (P.y >> 31) ? -z1 : z1;
-  const float zlo = T.zlo, zhi = T.zhi;
+  const float zlo = tc.zlo, zhi = tc.zhi;
   const bool ok0 = act && (P.x & 0x7FFFFFFFu) < Z.k[l0] && z0 >= zlo && z0 <= zhi;
   const bool ok1 = act && (P.y & 0x7FFFFFFFu) < Z.k[l1] && z1 >= zlo && z1 <= zhi;
   // FP32 estimates settle clear leaves and clear non-leaves; the exact FP64 due times
   // decide the band and are what gets stored
   const float df = f64_to_f32_rz(d);
-  const float mu_f = T.mu_f, sigma_f = T.sigma_f;
-  const float est0 = __fadd_rn(df, __fadd_rn(mu_f, __fmul_rn(sigma_f, z0)));
-  const float est1 = __fadd_rn(df, __fadd_rn(mu_f, __fmul_rn(sigma_f, z1)));
-  const bool eok = tc.eok;
-  const bool sure0 = eok && est0 < tc.t_lo, sure1 = eok && est1 < tc.t_lo;
-  const double mu = T.mu, sigma = T.sigma;
-  r.due0 = d + fma(sigma, f32_to_f64(z0), mu);
-  r.due1 = d + fma(sigma, f32_to_f64(z1), mu);
-  const bool leaf0 = ok0 && ((eok && est0 > tc.t_hi) || (!sure0 && gt_nonneg(r.due0, tc.t_max)));
-  const bool leaf1 = ok1 && ((eok && est1 > tc.t_hi) || (!sure1 && gt_nonneg(r.due1, tc.t_max)));
+  const float est0 = __fadd_rn(df, __fadd_rn(tc.mu_f, __fmul_rn(tc.sigma_f, z0)));
+  const float est1 = __fadd_rn(df, __fadd_rn(tc.mu_f, __fmul_rn(tc.sigma_f, z1)));
+  const bool sure0 = est0 < tc.t_lo, sure1 = est1 < tc.t_lo;
+  r.due0 = d + fma(tc.sigma, f32_to_f64(z0), tc.mu);
+  r.due1 = d + fma(tc.sigma, f32_to_f64(z1), tc.mu);
+  const bool leaf0 = ok0 && (est0 > tc.t_hi || (!sure0 && gt_nonneg(r.due0, tc.t_max)));
+  const bool leaf1 = ok1 && (est1 > tc.t_hi || (!sure1 && gt_nonneg(r.due1, tc.t_max)));
   r.em0 = ok0 && !leaf0 && can_divide;
   r.em1 = ok1 && !leaf1 && can_divide;
   const bool van0 = ok0 && !leaf0 && !can_divide, van1 = ok1 && !leaf1 && !can_divide;
@@ -656,7 +665,7 @@ __device__ void divide_body(const RunArgs& a, const uint64_t root_base, const Le
       const uint32_t ch = (uint32_t)(node & 1ull);
       const u32x4 P = philox(u32x4{(uint32_t)parent, (uint32_t)(parent >> 32), root, kPurposePair}, tc.k0, tc.k1);
       const float z = slow_z(ch ? P.y : P.x, (P.z >> (8u * ch)) & 255u, pair_wedge_bits(P, ch), node, root,
-                             tc.k0, tc.k1, *tc.t, s.zig_or(a), a.error);
+                             tc.k0, tc.k1, tc.zlo, tc.zhi, s.zig_or(a), a.error);
       f = fate(birth, f64_to_f32_rz(birth), z, tc, g1 < cap, due);
       if (f == kLeaf) {
         if constexpr (C::kGlobalHist)

@@ -171,3 +171,47 @@ def test_threads_and_shards_are_deterministic(oracle_lib):
                                  root_begin=lo, root_end=hi)
              for lo, hi in ((0, n // 3), (n // 3, n - 5), (n - 5, n))]
     assert np.array_equal(sum(p.per_type for p in parts), a.per_type)
+
+
+def test_smooth_restatement_adjoint_matches_central_differences(oracle_lib):
+    """The CPU restatement of the smoothed form is itself differentiated correctly: its
+    forward-mode gradient agrees with central differences of its own forward."""
+    import smooth_ref
+    bins = [(640.0, 12), (37.0, 9), (3.0, 5)]
+    params = np.array([[[0.6, 30.0, 6.0], [0.4, 45.0, 18.0]]])
+    nv = len(smooth_ref.prepare(bins, 1.0)[1])
+    gE = np.random.default_rng(1).normal(size=(1, nv))
+    E, G, vals = smooth_ref.forward_backward(bins, 150.0, 1.0, 0.5, 3, 99, params, gE)
+    for k in range(2):
+        for q in range(3):
+            d = 1e-6 * abs(params[0, k, q])
+            P1, P2 = params.copy(), params.copy()
+            P1[0, k, q] += d
+            P2[0, k, q] -= d
+            E1, _, _ = smooth_ref.forward_backward(bins, 150.0, 1.0, 0.5, 3, 99, P1)
+            E2, _, _ = smooth_ref.forward_backward(bins, 150.0, 1.0, 0.5, 3, 99, P2)
+            fd = float((gE * (E1 - E2)).sum() / (2 * d))
+            assert abs(G[0, k, q] - fd) <= 1e-5 * max(1.0, abs(fd)), (k, q, G[0, k, q], fd)
+
+
+def test_smooth_restatement_replica_zero_is_the_plain_tree(oracle_lib):
+    """With one lineage per cell and h -> 0, a cell's smoothed weight is an unbiased estimate
+    of its own plain-form tree: enumerating every path reproduces the oracle's counts."""
+    import smooth_ref
+    T, mu, sd, seed, cap = 168.0, 40.0, 8.0, 1234, 6
+    res = oracle_lib.simulate([(100.0, 20)], [(1.0, mu, sd)], T, 1.0, seed=seed, nthreads=1)
+    total = np.zeros(cap + 1)
+    for r in range(20):
+        R = oracle_lib.philox([0, 0, r, smooth_ref.PURPOSE_ROOT], [seed & 0xFFFFFFFF, seed >> 32])
+        U = smooth_ref._unit53_open_closed(R[2], R[3])
+        for bits in range(2 ** (cap + 1)):
+            node, S = 1, 0.0
+            for j in range(1, cap + 2):
+                z = float(oracle_lib.normals(seed, r, node >> 1, 2)[node & 1])
+                tau = sd * z + mu
+                S = tau * U + tau if j == 1 else S + tau
+                if S > T:
+                    total[j - 1] += 2.0 ** (j - 1) / 2 ** (cap + 1)
+                    break
+                node = 2 * node + ((bits >> (j - 1)) & 1)
+    assert np.allclose(total, res.per_type[::-1, 0], atol=1e-9)
