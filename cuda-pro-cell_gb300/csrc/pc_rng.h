@@ -61,15 +61,12 @@ constexpr uint32_t kPurposePair = 0x10000000u;
 constexpr uint32_t kPurposeChild = 0x20000000u;
 constexpr uint32_t kPurposePath = 0x40000000u;  // smoothed form: lineage path choices
 
+// One 32x32 -> 64-bit product (a single wide multiply on the GPU, which issues once where
+// separate low and high halves would issue twice).
 PC_HD void mulhilo32(uint32_t a, uint32_t b, uint32_t& hi, uint32_t& lo) {
-#if defined(__CUDA_ARCH__)
-  lo = a * b;
-  hi = __umulhi(a, b);
-#else
   const uint64_t p = (uint64_t)a * (uint64_t)b;
   lo = (uint32_t)p;
   hi = (uint32_t)(p >> 32);
-#endif
 }
 
 // Ten Philox rounds; the key is bumped by the Weyl constants between rounds.
