@@ -502,7 +502,7 @@ def run_batched(args):
         "e2e": {"value": e2e_value, "unit": "instances/s", "h2d_bytes_per_step": h2d // args.steps,
                 "d2h_bytes_per_step": d2h // args.steps},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": (achieved / hbm) if achieved else None, "traffic": None,
+                     "frac": (achieved / hbm) if achieved else None, "traffic": batched_traffic(divisions, launches),
                      "peak_source": peak_kind, "kernel": "k_persist" if persistent else "k_divide",
                      "launches_per_step": launches / args.steps,
                      "alg_bytes_per_launch": alg_bytes / launches},
@@ -622,7 +622,7 @@ def run_calibration(args):
     clk = clocks.stop()
     h2d = host_theta.numel() * 8
     d2h = (out_g.numel() + out_l.numel()) * 8
-    comp = cb.compare(eng, candidates=C, seed=7)
+    comp = cb.compare(eng, candidates=C, seed=7, pso_seconds=30.0)
     cpu = None
     if not args.no_cpu_baseline:
         cpu = cpu_smooth_sample(prob.bins, prob.phi, prob.t_max, prob.smooth_h, prob.smooth_paths,
@@ -665,6 +665,16 @@ def run_calibration(args):
         line["cpu_baseline"] = cpu
     print(json.dumps(line), flush=True)
     return 0
+
+
+def batched_traffic(divisions, launches):
+    """Measured DRAM bytes per division of the batched sweeps (ncu, profiles/) x divisions
+    per launch."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic_per_division_batched.txt")) as fh:
+            return float(fh.read().split()[0]) * divisions / max(1, launches)
+    except (OSError, ValueError, IndexError):
+        return None
 
 
 def cpu_batched_sample(instances, seconds):

@@ -5,6 +5,7 @@
 // at the first token that does not convert. The output is written with an
 // std::ostream at precision(10) in the default float format, tab separated, one row per
 // value with a nonzero total, followed by std::endl (parser.cu:187-217).
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <fstream>
@@ -83,5 +84,40 @@ int pc_write_histogram(const char* path, const pc_histogram* h, int track_ratio)
 }
 
 void pc_free(void* p) { std::free(p); }
+
+// Logarithmic bin edges as the reference's utils::log_space (src/utils/util.cu:90-111):
+// exponents ceil(log_base(start)) .. ceil(log_base(end)) in n equally spaced steps (its
+// linear_space, util.cu:76-88), each edge base^exponent, the last one exactly base^end.
+int pc_log_space(double start, double end, uint64_t n, double base, double* edges) {
+  if (!edges || n < 2 || !(start > 0.0) || !(end > 0.0) || !(base > 0.0) || base == 1.0 ||
+      !std::isfinite(start) || !std::isfinite(end) || !std::isfinite(base))
+    return PC_ERR_INVALID;
+  const double e0 = std::ceil(std::log(start) / std::log(base));
+  const double e1 = std::ceil(std::log(end) / std::log(base));
+  const double delta = (e1 - e0) / (double)(n - 1);
+  for (uint64_t i = 0; i + 1 < n; ++i) edges[i] = std::pow(base, e0 + delta * (double)i);
+  edges[n - 1] = std::pow(base, e1);
+  return PC_OK;
+}
+
+// The reference's utils::rebin (util.cu:113-138): counts of an ascending histogram summed
+// into the bins of log_space(lower, upper, n_bins, 10), a value landing in the first bin
+// whose edge is >= the value. The reference walks past its array for values above the
+// last edge; here that is an error.
+int pc_rebin(const double* values, const uint64_t* counts, uint64_t n_values, double lower, double upper,
+             uint64_t n_bins, double* edges_out, uint64_t* counts_out) {
+  if ((n_values && (!values || !counts)) || !edges_out || !counts_out) return PC_ERR_INVALID;
+  const int rc = pc_log_space(lower, upper, n_bins, 10.0, edges_out);
+  if (rc != PC_OK) return rc;
+  for (uint64_t i = 0; i < n_bins; ++i) counts_out[i] = 0;
+  uint64_t pos = 0;
+  for (uint64_t i = 0; i < n_values; ++i) {
+    if (i > 0 && values[i] < values[i - 1]) return PC_ERR_INVALID;  // not ascending
+    while (pos < n_bins && values[i] > edges_out[pos]) ++pos;
+    if (pos == n_bins) return PC_ERR_INVALID;  // above the last edge
+    counts_out[pos] += counts[i];
+  }
+  return PC_OK;
+}
 
 }  // extern "C"

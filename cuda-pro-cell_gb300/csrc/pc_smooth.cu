@@ -79,6 +79,15 @@ __device__ __forceinline__ float node_z(uint64_t node, uint32_t root, uint32_t k
   return node_z_slow(j, layer, pair_wedge_bits(P, c), node, root, k0, k1, Z, error);
 }
 
+// Compensated (Kahan) addition into sum = p[0], compensation = p[kThreads].
+__device__ __forceinline__ void kahan_add(float* p, float x) {
+  const float sum = p[0], c = p[kThreads];
+  const float y = __fsub_rn(x, c);
+  const float t = __fadd_rn(sum, y);
+  p[kThreads] = __fsub_rn(__fsub_rn(t, sum), y);
+  p[0] = t;
+}
+
 // log sigmoid(x) and log(1 - sigmoid(x)) = log sigmoid(-x).
 __device__ __forceinline__ void log_sig(float x, float& ls, float& l1m) {
   const float L = log1pf(expf(-fabsf(x)));
@@ -109,14 +118,13 @@ constexpr float kLogNegligible = -100.0f;  // e^-100 * 2^63 < 1e-24
 template <bool Backward>
 __device__ __forceinline__ void walk(const SmoothArgs& A, const float* z, double u_age, uint32_t steps, double mu,
                                      double sigma, bool fixed_tau, double weight, double* acc, const float* Ag2,
-                                     double& g_r, double& g_mu, double& g_sig) {
+                                     float& f_r, float& f_mu, float& f_sig) {
   double R = 0.0;                 // T - S_j
   float log_p = 0.0f;             // log s_1 ... s_{j-1}
   float dmu = 0.0f, dsig = 0.0f;  // dS_j / d(mean, sd)
   float D_mu = 0.0f, D_sig = 0.0f;
   const float inv_h = (float)A.inv_h;
   double ws = weight;  // weight * 2^(j-1)
-  float f_r = 0.0f, f_mu = 0.0f, f_sig = 0.0f;  // this lineage's gradient terms (FP32: a few terms)
   for (uint32_t j = 1; j <= steps; ++j) {
     const float zj = fixed_tau ? 0.0f : z[(j - 1) * 32u];
     const double tau = fixed_tau ? 0.0 : fma(sigma, f32_to_f64_bits(zj), mu);
@@ -156,11 +164,6 @@ __device__ __forceinline__ void walk(const SmoothArgs& A, const float* z, double
     log_p += ls;
     if (log_p < kLogNegligible) break;
   }
-  if constexpr (Backward) {
-    g_r += (double)f_r;
-    g_mu += (double)f_mu;
-    g_sig += (double)f_sig;
-  }
 }
 
 template <bool Backward>
@@ -168,8 +171,10 @@ __global__ void __launch_bounds__(kThreads) k_smooth(const SmoothArgs A, const d
                                                      uint32_t ncand, const double* __restrict__ grad_expected,
                                                      uint32_t nvalues, const int32_t* __restrict__ vidx,
                                                      double* __restrict__ out) {
-  // dynamic: acc [nrows][kThreads] doubles, then z [kWarps][rows][32] floats
+  // dynamic: forward acc [rows][kThreads] doubles / backward [ntypes * 3][kThreads] floats,
+  // then the lineage draws z [kWarps][rows][32] floats
   extern __shared__ double acc[];
+  float* facc = reinterpret_cast<float*>(acc);
   __shared__ ZigTables Z;
   __shared__ double prm[32][kSmoothMaxTypes * 3];
   __shared__ float Ag2[Backward ? 32 : 1][kSmoothMaxRows];
@@ -180,8 +185,10 @@ __global__ void __launch_bounds__(kThreads) k_smooth(const SmoothArgs A, const d
   const uint32_t c = blockIdx.y * 32u + lane;
   const bool live = c < ncand;
   const uint32_t K = A.ntypes;
-  const uint32_t nrows = Backward ? K * 3 : A.rows;
-  float* zbuf = reinterpret_cast<float*>(acc + (size_t)nrows * kThreads) + (size_t)warp * A.rows * 32u;
+  const uint32_t nrows = Backward ? K * 3 : A.rows;             // output rows
+  const uint32_t arows = Backward ? K * 6 : A.rows;             // accumulator rows
+  float* zbuf = Backward ? facc + (size_t)arows * kThreads + (size_t)warp * A.rows * 32u
+                         : reinterpret_cast<float*>(acc + (size_t)arows * kThreads) + (size_t)warp * A.rows * 32u;
   for (uint32_t i = threadIdx.x; i < sizeof(ZigTables) / 4; i += blockDim.x)
     reinterpret_cast<uint32_t*>(&Z)[i] = __ldg(reinterpret_cast<const uint32_t*>(A.zig) + i);
   for (uint32_t i = threadIdx.x; i < 32u * K * 3u; i += blockDim.x) {
@@ -189,7 +196,12 @@ __global__ void __launch_bounds__(kThreads) k_smooth(const SmoothArgs A, const d
     const uint32_t cc = blockIdx.y * 32u + l;
     prm[l][q] = cc < ncand ? params[(uint64_t)cc * K * 3 + q] : 0.0;
   }
-  for (uint32_t i = 0; i < nrows; ++i) acc[i * kThreads + threadIdx.x] = 0.0;
+  for (uint32_t i = 0; i < arows; ++i) {
+    if constexpr (Backward)
+      facc[i * kThreads + threadIdx.x] = 0.0f;
+    else
+      acc[i * kThreads + threadIdx.x] = 0.0;
+  }
   const uint32_t cap = __ldg(A.bin_cap + b);
   const uint32_t steps = cap + 1u;
   if constexpr (Backward) {
@@ -208,6 +220,7 @@ __global__ void __launch_bounds__(kThreads) k_smooth(const SmoothArgs A, const d
   const uint64_t r0 = __ldg(A.bin_start + b), r1 = __ldg(A.bin_start + b + 1);
   const double inv_paths = 1.0 / (double)A.paths;
   double* my = acc + threadIdx.x;
+  float* fmy = facc + threadIdx.x;
   const double* my_prm = prm[lane];
   const float* my_ag = Backward ? Ag2[lane] : nullptr;
   // lineage i of the bin: initial cell r0 + i / paths, replica i % paths
@@ -236,20 +249,22 @@ __global__ void __launch_bounds__(kThreads) k_smooth(const SmoothArgs A, const d
         const double ua = u_age[warp * 32u + ii];
         for (uint32_t k = 0; k < K; ++k) {
           const double ratio = my_prm[3 * k], mu = my_prm[3 * k + 1], sd = my_prm[3 * k + 2];
-          double g_r = 0.0, g_mu = 0.0, g_sig = 0.0;
+          float f_r = 0.0f, f_mu = 0.0f, f_sig = 0.0f;  // this lineage's adjoint terms
           if (mu < 0.0) {
             // quiescent type: a leaf at generation 0 (cell.cu:69-75)
             if constexpr (Backward)
-              g_r = my_ag[0];
+              f_r = my_ag[0];
             else
               my[0] += ratio * inv_paths;
           } else if (Backward || ratio != 0.0) {
-            walk<Backward>(A, z, ua, steps, mu, sd, mu == 0.0, ratio * inv_paths, my, my_ag, g_r, g_mu, g_sig);
+            walk<Backward>(A, z, ua, steps, mu, sd, mu == 0.0, ratio * inv_paths, my, my_ag, f_r, f_mu, f_sig);
           }
           if constexpr (Backward) {
-            my[(3 * k) * kThreads] += g_r * inv_paths;
-            my[(3 * k + 1) * kThreads] += g_mu * ratio * inv_paths;
-            my[(3 * k + 2) * kThreads] += g_sig * ratio * inv_paths;
+            // per-thread compensated FP32 sums (terms of either sign cancel); scaled by
+            // ratio / paths once, at the end
+            kahan_add(fmy + (6 * k) * kThreads, f_r);
+            kahan_add(fmy + (6 * k + 2) * kThreads, f_mu);
+            kahan_add(fmy + (6 * k + 4) * kThreads, f_sig);
           }
         }
       }
@@ -257,13 +272,20 @@ __global__ void __launch_bounds__(kThreads) k_smooth(const SmoothArgs A, const d
     __syncwarp();
   }
   __syncthreads();
-  // out[c][b][row] = sum over the warps, in warp order
+  // out[c][b][row] = sum over the warps, in warp order (adjoint rows scaled by
+  // 1 / paths, and those of mean and sd by the ratio)
   if (warp == 0 && live) {
     double* o = out + ((uint64_t)c * A.nbins + b) * nrows;
     for (uint32_t q = 0; q < nrows; ++q) {
       double v = 0.0;
 #pragma unroll
-      for (uint32_t w = 0; w < kWarps; ++w) v += acc[q * kThreads + w * 32u + lane];
+      for (uint32_t w = 0; w < kWarps; ++w) {
+        if constexpr (Backward)
+          v += (double)facc[2 * q * kThreads + w * 32u + lane] - (double)facc[(2 * q + 1) * kThreads + w * 32u + lane];
+        else
+          v += acc[q * kThreads + w * 32u + lane];
+      }
+      if constexpr (Backward) v *= (q % 3u == 0u ? 1.0 : my_prm[q - q % 3u]) * inv_paths;
       o[q] = v;
     }
   }
@@ -291,15 +313,15 @@ __global__ void k_smooth_grad_sum(const double* __restrict__ part, uint32_t ncan
 }
 
 // acc rows x kThreads doubles + the lineage draws (kThreads floats per generation row)
-int smem_bytes(uint32_t acc_rows, uint32_t rows) {
-  return (int)(acc_rows * kThreads * sizeof(double) + rows * kThreads * sizeof(float));
+int smem_bytes(uint32_t acc_rows, size_t acc_elem, uint32_t rows) {
+  return (int)(acc_rows * kThreads * acc_elem + rows * kThreads * sizeof(float));
 }
 
 template <bool Backward>
 int launch_smooth_t(const SmoothArgs& A, const double* params, uint32_t ncand, const double* grad_expected,
                     uint32_t nvalues, const int32_t* vidx, double* out, cudaStream_t st) {
-  const uint32_t acc_rows = Backward ? A.ntypes * 3u : A.rows;
-  const int smem = smem_bytes(acc_rows, A.rows);
+  const uint32_t acc_rows = Backward ? A.ntypes * 6u : A.rows;
+  const int smem = smem_bytes(acc_rows, Backward ? sizeof(float) : sizeof(double), A.rows);
   // static shared memory plus `smem` may exceed the default 48 KB: always opt in
   const cudaError_t e = cudaFuncSetAttribute(k_smooth<Backward>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return (int)e;

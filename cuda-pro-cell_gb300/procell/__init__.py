@@ -18,7 +18,7 @@ import numpy as np
 from . import _lib
 from ._lib import ProcellError
 
-__all__ = ["Engine", "Batch", "Result", "ProcellError", "format_histogram"]
+__all__ = ["Engine", "Batch", "Result", "log_space", "rebin", "ProcellError", "format_histogram"]
 
 
 @dataclass
@@ -235,6 +235,31 @@ class Engine:
             self.close()
         except Exception:
             pass
+
+
+def log_space(start: float, end: float, n: int, base: float = 10.0) -> np.ndarray:
+    """pc_log_space: the reference's logarithmic bin edges."""
+    L = _lib.load()
+    e = np.zeros(int(n), np.float64)
+    rc = L.pc_log_space(float(start), float(end), int(n), float(base), e.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+    if rc != 0:
+        raise ProcellError(rc, "invalid log_space arguments")
+    return e
+
+
+def rebin(values, counts, lower: float, upper: float, n_bins: int):
+    """pc_rebin: an ascending histogram summed into log_space(lower, upper, n_bins, 10)."""
+    L = _lib.load()
+    v = np.ascontiguousarray(values, np.float64)
+    c = np.ascontiguousarray(counts, np.uint64)
+    e = np.zeros(int(n_bins), np.float64)
+    out = np.zeros(int(n_bins), np.uint64)
+    rc = L.pc_rebin(v.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), c.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
+                    len(v), float(lower), float(upper), int(n_bins), e.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                    out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)))
+    if rc != 0:
+        raise ProcellError(rc, "rebin: values out of order or above the last edge, or invalid edges")
+    return e, out
 
 
 def format_histogram(values, totals, per_type, track_ratio: bool) -> str:

@@ -100,6 +100,10 @@ SIGNATURES = [
     ("pc_smooth_backward", ctypes.c_int, [VP, VP, VP, ctypes.c_uint32, VP, VP]),
     ("pc_smooth_sync", ctypes.c_int, [VP]),
     ("pc_smooth_destroy", None, [VP]),
+    ("pc_log_space", ctypes.c_int, [ctypes.c_double, ctypes.c_double, ctypes.c_uint64, ctypes.c_double,
+                                    ctypes.POINTER(ctypes.c_double)]),
+    ("pc_rebin", ctypes.c_int, [ctypes.POINTER(ctypes.c_double), U64P, ctypes.c_uint64, ctypes.c_double,
+                                ctypes.c_double, ctypes.c_uint64, ctypes.POINTER(ctypes.c_double), U64P]),
     ("pc_load_histogram", ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(ctypes.POINTER(Bin)), U64P]),
     ("pc_load_cell_types", ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(ctypes.POINTER(CellType)), U32P]),
     ("pc_write_histogram", ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(Histogram), ctypes.c_int]),

@@ -1,14 +1,19 @@
 """Calibration harness: recover cell-type parameters from an output histogram.
 
 A target histogram is produced by the plain (stochastic, exact) form at hidden parameters
-drawn from a seed. Candidates are scored with the smoothed form, loss
+drawn from a seed. Candidates are scored by
     L = sum_v (log(1 + E_v) - log(1 + C_v))^2
-(E expected counts of the candidate, C the target counts), and searched two ways from the
-same random starting population:
-  * gradient descent: Adam on unconstrained coordinates, gradients from the smoothed
-    form's adjoint kernel through procell.smooth.expected_counts (torch.autograd);
-  * particle swarm: the same population as particles, forward passes only.
-Both track the best loss over the population against wall time.
+(E the candidate's counts, C the target counts), and searched three ways from the same
+random starting population:
+  * gradient descent on the smoothed form: Adam on unconstrained coordinates, gradients
+    from the smoothed form's adjoint kernel through procell.smooth.expected_counts;
+  * a particle swarm on the smoothed form (forward passes only);
+  * a particle swarm on the plain simulator itself: every iteration runs all candidates as
+    the instances of one batch (pc_simulate_batch), the search a practitioner without a
+    differentiable model would run.
+Each search keeps its best parameters over time; afterwards every snapshot is scored with
+one accurate common loss (the smoothed form with many lineages per cell, another seed), so
+the searches are compared on the same scale.
 
     python -m procell.calibrate [--candidates 256] [--seed 7] [--gd-iters 300] [--pso-seconds 40]
 """
@@ -53,7 +58,26 @@ class Problem:
         self.smooth_h, self.smooth_paths, self.smooth_seed = h, paths, seed + 2000
         self.smooth = Smooth(engine, self.bins, n_types, t_max, self.phi, h=h, paths=paths, seed=seed + 2000)
         assert np.array_equal(res.values, self.smooth.values)
-        self.target = torch.tensor(res.totals.astype(np.float64), device="cuda")
+        self.engine = engine
+        self.target_np = res.totals.astype(np.float64)
+        self.target = torch.tensor(self.target_np, device="cuda")
+        self.plain_seed = seed + 3000
+        from . import _lib
+        self._bins_np = _lib.bins_numpy(self.bins)
+        self._accurate = None
+
+    def loss_accurate(self, theta, paths=32):
+        """The common yardstick: the smoothed form with many lineages per cell (another
+        seed), i.e. close to the plain model's expectation."""
+        if self._accurate is None:
+            self._accurate = Smooth(self.engine, self.bins, self.n_types, self.t_max, self.phi, h=self.smooth_h,
+                                    paths=paths, seed=self.smooth_seed + 5000)
+        with torch.no_grad():
+            out = []
+            for chunk in torch.split(theta, 256):
+                E = self._accurate.forward(self.params(chunk))
+                out.append(((torch.log1p(E) - torch.log1p(self.target)) ** 2).sum(dim=1))
+            return torch.cat(out)
 
     def params(self, theta):
         """theta [C, K, 3] = (ratio logit, log mean, log cv) -> (ratio, mean, sd)."""
@@ -65,6 +89,36 @@ class Problem:
     def loss(self, theta):
         E = expected_counts(self.smooth, self.params(theta))
         return ((torch.log1p(E) - torch.log1p(self.target)) ** 2).sum(dim=1)
+
+    def loss_plain(self, theta, seed=None):
+        """Loss of every candidate under the plain simulator: the candidates run as the
+        instances of one batch (one seed for all: common random numbers)."""
+        import ctypes
+        from . import _lib
+        P = self.params(theta).detach().cpu().numpy()
+        seed = self.plain_seed if seed is None else seed
+        n = P.shape[0]
+        keep = [self._bins_np]
+        arr = (_lib.Instance * n)()
+        for i in range(n):
+            t = _lib.types_numpy([tuple(row) for row in P[i]])
+            keep.append(t)
+            arr[i].bins = self._bins_np.ctypes.data_as(ctypes.POINTER(_lib.Bin))
+            arr[i].n_bins = len(self._bins_np)
+            arr[i].types = t.ctypes.data_as(ctypes.POINTER(_lib.CellType))
+            arr[i].n_types = len(t)
+            arr[i].t_max, arr[i].phi, arr[i].seed = self.t_max, self.phi, seed
+        hs = (_lib.Histogram * n)()
+        eng = self.engine
+        eng._check(eng.L.pc_simulate_batch(eng.ctx, arr, n, hs))
+        tgt = np.log1p(self.target_np)
+        out = np.empty(n)
+        for i in range(n):
+            h = hs[i]
+            tot = np.ctypeslib.as_array(h.totals, shape=(int(h.n_values),)).astype(np.float64)
+            out[i] = ((np.log1p(tot) - tgt) ** 2).sum()
+            eng.L.pc_histogram_free(ctypes.byref(h))
+        return torch.tensor(out, dtype=torch.float64, device=theta.device)
 
     def box(self):
         lo = torch.tensor([-3.0, math.log(MEAN_RANGE[0]), math.log(CV_RANGE[0])], dtype=torch.float64, device="cuda")
@@ -85,24 +139,30 @@ def gradient_descent(prob, theta0, iters=150, lr=0.1, lr_end=0.002, time_limit=N
     trace, best = [], float("inf")
     torch.cuda.synchronize()
     t0 = time.perf_counter()
+    snaps = []
     for it in range(iters):
         for group in opt.param_groups:
             group["lr"] = lr_end + 0.5 * (lr - lr_end) * (1.0 + math.cos(math.pi * it / max(1, iters - 1)))
         opt.zero_grad(set_to_none=True)
         L = prob.loss(theta)
         L.sum().backward()
-        best = min(best, float(L.detach().min()))
+        i = int(torch.argmin(L.detach()))
+        if float(L[i]) < best:
+            best = float(L[i])
+            snaps.append((time.perf_counter() - t0, theta.detach()[i].clone()))
         opt.step()
         trace.append((time.perf_counter() - t0, best))
         if time_limit and trace[-1][0] > time_limit:
             break
-    return trace, theta.detach()
+    return trace, snaps
 
 
-def particle_swarm(prob, theta0, iters=150, w=0.7298, c1=1.49618, c2=1.49618, seed=1, time_limit=None):
+def particle_swarm(prob, theta0, iters=150, w=0.7298, c1=1.49618, c2=1.49618, seed=1, time_limit=None,
+                   loss=None):
     """Particle swarm with constriction coefficients and a ring neighbourhood (each particle
     follows the best of itself and its two neighbours), the standard choice for multimodal
     objectives; particles stay in the search box."""
+    loss = loss or prob.loss
     g = torch.Generator(device="cuda").manual_seed(seed)
     lo, hi = prob.box()
     x = theta0.clone()
@@ -111,10 +171,11 @@ def particle_swarm(prob, theta0, iters=150, w=0.7298, c1=1.49618, c2=1.49618, se
     with torch.no_grad():
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        fx = prob.loss(x)
+        fx = loss(x)
         pbest, pf = x.clone(), fx.clone()
         gf = float(pf.min())
         trace = [(time.perf_counter() - t0, gf)]
+        snaps = [(trace[0][0], pbest[int(torch.argmin(pf))].clone())]
         for it in range(iters):
             # best personal best among each particle's ring neighbourhood {i-1, i, i+1}
             cand = torch.stack([pf.roll(1), pf, pf.roll(-1)])
@@ -126,19 +187,30 @@ def particle_swarm(prob, theta0, iters=150, w=0.7298, c1=1.49618, c2=1.49618, se
             vel = w * vel + c1 * r1 * (pbest - x) + c2 * r2 * (nb - x)
             vel = torch.minimum(torch.maximum(vel, -vmax), vmax)
             x = torch.minimum(torch.maximum(x + vel, lo), hi)
-            fx = prob.loss(x)
+            fx = loss(x)
             better = fx < pf
             pbest[better] = x[better]
             pf = torch.where(better, fx, pf)
-            gf = min(gf, float(pf.min()))
+            gi = int(torch.argmin(pf))
+            if float(pf[gi]) < gf:
+                gf = float(pf[gi])
+                snaps.append((time.perf_counter() - t0, pbest[gi].clone()))
             trace.append((time.perf_counter() - t0, gf))
             if time_limit and trace[-1][0] > time_limit:
                 break
-        gi = int(torch.argmin(pf))
-    return trace, pbest[gi].clone()
+    return trace, snaps
 
 
-def time_to(trace, level):
+def accurate_trace(prob, snaps):
+    """(time, accurate loss of the search's best parameters so far) for each snapshot."""
+    if not snaps:
+        return []
+    L = prob.loss_accurate(torch.stack([th for _, th in snaps])).cpu().numpy()
+    return [(t, float(v)) for (t, _), v in zip(snaps, L)]
+
+
+def first_below(trace, level):
+    """First time a (time, loss) trace is at or below `level` (losses need not decrease)."""
     for t, l in trace:
         if l <= level:
             return t
@@ -146,43 +218,53 @@ def time_to(trace, level):
 
 
 def compare(engine, candidates=256, seed=7, gd_iters=300, pso_seconds=40.0, paths=2):
-    """Both searches from the same population; time to reach a sequence of loss levels.
-
-    The headline level is the particle swarm's best loss at the end of its budget plus 0.1%
-    when gradient descent reaches it, else the loss of the hidden parameters themselves (a
-    fit as good as the truth)."""
+    """Gradient descent on the smoothed form against particle swarms (on the smoothed form
+    and on the plain simulator through the batched form), all from one population, all
+    scored afterwards with the same accurate loss. The headline level is the worse of the
+    plain-simulator swarm's and gradient descent's final accurate losses (a level both
+    reach); the ratio is the swarm's time to reach it over gradient descent's."""
     prob = Problem(engine, seed=seed, paths=paths)
     theta0 = prob.start(candidates, seed)
-    gradient_descent(prob, theta0, iters=3)  # warm-up of both code paths
+    gradient_descent(prob, theta0, iters=3)  # warm-up of every code path
     particle_swarm(prob, theta0, iters=3)
-    gd, _ = gradient_descent(prob, theta0, iters=gd_iters)
-    ps, _ = particle_swarm(prob, theta0, iters=1_000_000, time_limit=pso_seconds)
+    particle_swarm(prob, theta0, iters=2, loss=prob.loss_plain)
+    gd, gd_snaps = gradient_descent(prob, theta0, iters=gd_iters)
+    ps, ps_snaps = particle_swarm(prob, theta0, iters=1_000_000, time_limit=pso_seconds)
+    pp, pp_snaps = particle_swarm(prob, theta0, iters=1_000_000, time_limit=pso_seconds, loss=prob.loss_plain)
+    acc_gd, acc_ps, acc_pp = (accurate_trace(prob, x) for x in (gd_snaps, ps_snaps, pp_snaps))
     with torch.no_grad():
         hidden = torch.tensor([prob.hidden], dtype=torch.float64, device="cuda")
-        E = prob.smooth.forward(hidden)
-        l_true = float(((torch.log1p(E) - torch.log1p(prob.target)) ** 2).sum())
-    gd_final, ps_final = gd[-1][1], ps[-1][1]
-    levels = sorted({x for x in (2 * l_true, 1.25 * l_true, 1.1 * l_true, 1.05 * l_true, l_true,
-                                 ps_final * 1.01, ps_final * 1.001, ps_final, gd_final)}, reverse=True)
+        th_h = torch.stack([torch.log(hidden[0, :, 0]), torch.log(hidden[0, :, 1]),
+                            torch.log(hidden[0, :, 2] / hidden[0, :, 1])], dim=-1)[None]
+        l_true = float(prob.loss_accurate(th_h)[0])
+
+    def best_final(tr):
+        return min(l for _, l in tr)
+
+    head = max(best_final(acc_pp), best_final(acc_gd))
+    levels = sorted({head, 1.05 * head, 1.2 * head, 1.5 * head, l_true}, reverse=True)
     table = []
     for L in levels:
-        tg, tp = time_to(gd, L), time_to(ps, L)
-        table.append({"loss": L, "gd_seconds": tg, "pso_seconds": tp,
-                      "ratio": (tp / tg) if (tg and tp) else None})
-    # the swarm's final loss, 0.1% up (its last, tiny improvements would otherwise set the
-    # clock), or the loss of the hidden parameters when descent does not reach that
-    head = ps_final * 1.001 if time_to(gd, ps_final * 1.001) is not None else l_true
-    tg, tp = time_to(gd, head), time_to(ps, head)
+        tg, tp, ts = first_below(acc_gd, L), first_below(acc_pp, L), first_below(acc_ps, L)
+        table.append({"accurate_loss": L, "gd_seconds": tg, "pso_plain_seconds": tp, "pso_smooth_seconds": ts,
+                      "ratio_plain": (tp / tg) if (tg and tp) else None,
+                      "ratio_smooth": (ts / tg) if (tg and ts) else None})
+    tg, tp = first_below(acc_gd, head), first_below(acc_pp, head)
     return {
         "candidates": candidates,
         "lineages_per_cell": paths,
         "hidden": prob.hidden,
-        "loss_at_hidden": l_true,
-        "gd": {"iters": len(gd), "seconds": gd[-1][0], "best_loss": gd_final, "method": "Adam, cosine lr 0.1 -> 0.002"},
-        "pso": {"iters": len(ps) - 1, "seconds": ps[-1][0], "best_loss": ps_final,
-                "method": "particle swarm, constriction coefficients, ring neighbourhood"},
+        "accurate_loss_at_hidden": l_true,
+        "gd": {"iters": len(gd), "seconds": gd[-1][0], "best_smoothed_loss": gd[-1][1],
+               "best_accurate_loss": best_final(acc_gd), "method": "Adam on the smoothed form, cosine lr 0.1 -> 0.002"},
+        "pso_smooth": {"iters": len(ps) - 1, "seconds": ps[-1][0], "best_smoothed_loss": ps[-1][1],
+                       "best_accurate_loss": best_final(acc_ps),
+                       "method": "particle swarm on the smoothed form (constriction, ring neighbourhood)"},
+        "pso_plain": {"iters": len(pp) - 1, "seconds": pp[-1][0], "best_plain_loss": pp[-1][1],
+                      "best_accurate_loss": best_final(acc_pp),
+                      "method": "particle swarm on the plain simulator, candidates as one pc_simulate_batch"},
         "equal_loss": head,
-        "equal_loss_is": "swarm final + 0.1%" if head != l_true else "loss at the hidden parameters",
+        "equal_loss_is": "accurate loss both gradient descent and the plain-simulator swarm reach",
         "gd_seconds_to_equal_loss": tg,
         "pso_seconds_to_equal_loss": tp,
         "speedup": (tp / tg) if (tg and tp) else None,

@@ -241,6 +241,17 @@ int pc_smooth_backward(pc_context* ctx, pc_smooth* s, const double* params, uint
 int pc_smooth_sync(pc_context* ctx);
 void pc_smooth_destroy(pc_smooth* s);
 
+/* ---- Histogram rebinning (the reference's utils::log_space / utils::rebin,
+ * src/utils/util.cu:76-138, which its main path never calls) -------------------------------
+ * pc_log_space: n >= 2 edges base^e for exponents from ceil(log_base(start)) to
+ * ceil(log_base(end)) in equal steps. pc_rebin: counts of an ascending histogram summed
+ * into the bins of pc_log_space(lower, upper, n_bins, 10), each value into the first bin
+ * whose edge is >= the value; edges_out[n_bins], counts_out[n_bins]. Values above the last
+ * edge or out of order give PC_ERR_INVALID. Host only. */
+int pc_log_space(double start, double end, uint64_t n, double base, double* edges);
+int pc_rebin(const double* values, const uint64_t* counts, uint64_t n_values, double lower,
+             double upper, uint64_t n_bins, double* edges_out, uint64_t* counts_out);
+
 /* File formats of the reference (parser.cu:68-217). Loaders read with the reference's
  * `in >> a >> b` semantics (stop at the first unparsable token). The loaders allocate
  * *out with malloc; release it with pc_free. pc_load_cell_types also applies the

@@ -131,3 +131,24 @@ def test_writer_matches_reference_format(built, tmp_path):
         assert L.pc_write_histogram(str(path).encode(), ctypes.byref(h), track) == 0
         assert path.read_text() == format_histogram(vals, tot, per, bool(track))
     assert (tmp_path / "o0.txt").read_text() == "1e-05\t2\n3\t5\n1.23456789e+11\t1\n7.25\t9\n"
+
+
+def test_log_space_and_rebin_follow_the_reference(built):
+    """pc_log_space / pc_rebin against a restatement of the reference's helpers
+    (src/utils/util.cu:76-138): exponents ceil(log10(lower))..ceil(log10(upper)) in equal steps,
+    each value into the first bin whose edge is >= it."""
+    import math
+    from procell import ProcellError, log_space, rebin
+    e = log_space(3.0, 2e4, 6, 10.0)
+    lo, hi = math.ceil(math.log10(3.0)), math.ceil(math.log10(2e4))
+    want = [10.0 ** (lo + (hi - lo) / 5 * i) for i in range(5)] + [10.0 ** hi]
+    assert np.allclose(e, want, rtol=1e-15)
+    vals = np.array([0.5, 1.0, 9.9, 10.0, 10.5, 99.0, 1000.0])
+    cnts = np.array([1, 2, 3, 4, 5, 6, 7], np.uint64)
+    edges, out = rebin(vals, cnts, 1.0, 1000.0, 4)
+    assert np.allclose(edges, [1.0, 10.0, 100.0, 1000.0])
+    assert out.tolist() == [3, 7, 11, 7]  # 0.5,1 | 9.9,10 | 10.5,99 | 1000
+    with pytest.raises(ProcellError):
+        rebin(np.array([5000.0]), np.array([1], np.uint64), 1.0, 1000.0, 4)
+    with pytest.raises(ProcellError):
+        rebin(np.array([5.0, 2.0]), np.array([1, 1], np.uint64), 1.0, 1000.0, 4)
