@@ -137,6 +137,25 @@ def cpu_sample(w, target_s, nthreads, oracle):
     return r.stats["divisions"], dt, m
 
 
+def cpu_model():
+    """The host CPU as /proc/cpuinfo or lscpu names it (for the record)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for ln in out.splitlines():
+            if ln.split(":")[0].strip() in ("Model name", "Model Name"):
+                return ln.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        with open("/proc/cpuinfo") as fh:
+            for ln in fh:
+                if ln.lower().startswith("model name"):
+                    return ln.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -169,7 +188,8 @@ def run_reference(args):
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": "oracle (CPU restatement of the reference algorithm) on the first "
                                    "%d-%d of %d initial cells per step, %d threads"
-                                   % (min(samples), max(samples), w.roots, cores)},
+                                   % (min(samples), max(samples), w.roots, cores),
+                         "cpu_model": cpu_model()},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -304,9 +324,12 @@ def run_ours(args):
         oracle.build()
         cores = os.cpu_count() or 1
         d, s, m = cpu_sample(w, args.cpu_seconds, cores, oracle)
+        d1, s1, m1 = cpu_sample(w, max(2.0, args.cpu_seconds / 3), 1, oracle)
         cpu = {"value": d / s, "unit": UNIT, "cores": cores, "kind": "port",
                "sample": "oracle on the first %d of %d initial cells (%.1f s, %d divisions)"
-                         % (m, w.roots, s, d)}
+                         % (m, w.roots, s, d),
+               "single_thread": {"value": d1 / s1, "sample": "first %d initial cells, %.1f s" % (m1, s1)},
+               "cpu_model": cpu_model(), "nproc": cores}
     line = {
         "metric": METRIC,
         "value": tot_div / (elapsed_ms * 1e-3),
