@@ -394,16 +394,13 @@ int prepare_instance(const pc_bin* bins, uint64_t n_bins, const pc_cell_type* ty
   I.seed = seed;
 
   // Bins with a nonzero frequency, in file order; output value set (parser.cu:98-151):
-  // every bin's halving chain v, v/2, ... while >= phi, sorted and deduplicated. Each chain
-  // entry remembers its (bin, generation), which gives the (bin, generation) -> value index
-  // map of the result merge in the same pass.
-  struct Link {
-    double v;
-    uint32_t bin, gen;
-  };
-  std::vector<Link> chain;
+  // every bin's halving chain v, v/2, ... while >= phi, sorted and deduplicated, together
+  // with the (bin, generation) -> value index map of the result merge.
   uint64_t total = 0;
+  std::vector<uint32_t> chain_len;  // chain length per nonzero bin
+  uint64_t chain_total = 0;
   uint32_t longest = 0;
+  bool normal = threshold >= 0x1p-1000;  // halving a normal double only lowers its exponent
   for (uint64_t i = 0; i < n_bins; ++i) {
     if (bins[i].frequency == 0) continue;
     const double v = bins[i].value;
@@ -411,21 +408,22 @@ int prepare_instance(const pc_bin* bins, uint64_t n_bins, const pc_cell_type* ty
     if (bins[i].frequency > 0xFFFFFFFFull - total) return msg = "more than 2^32-1 initial cells", PC_ERR_UNSUPPORTED;
     if (I.bin_value.size() + 1 >= (1u << 24)) return msg = "at most 2^24 nonzero bins", PC_ERR_UNSUPPORTED;
     total += bins[i].frequency;
-    const uint32_t b = (uint32_t)I.bin_value.size();
     I.bin_value.push_back(v);
     I.bin_freq.push_back(bins[i].frequency);
     uint32_t g = 0;
-    for (double cur = v; cur >= threshold; cur = cur / 2) chain.push_back(Link{cur, b, g++});
+    for (double cur = v; cur >= threshold; cur = cur / 2) ++g;
+    chain_len.push_back(g);
+    chain_total += g;
     longest = std::max(longest, g);
   }
-  std::sort(chain.begin(), chain.end(), [](const Link& x, const Link& y) { return x.v < y.v; });
   I.roots = total;
 
   // Phi cap per bin: a cell of generation g divides only while its fluorescence, the bin
   // value halved g times, still satisfies `f / 2 > phi` (proliferation.cu:323).
-  I.cap.resize(I.bin_value.size());
+  const size_t nb = I.bin_value.size();
+  I.cap.resize(nb);
   I.gmax = 0;
-  for (size_t b = 0; b < I.bin_value.size(); ++b) {
+  for (size_t b = 0; b < nb; ++b) {
     uint32_t c = 0;
     for (double f = I.bin_value[b]; f / 2 > threshold && c < 4096; f = f / 2) ++c;
     I.cap[b] = c;
@@ -433,11 +431,66 @@ int prepare_instance(const pc_bin* bins, uint64_t n_bins, const pc_cell_type* ty
   }
   // Every generation a leaf can have (<= gmax) has a row; chains are never longer.
   I.vidx_stride = std::max(I.gmax, longest) + 1;
-  I.vidx.assign(I.bin_value.size() * (size_t)I.vidx_stride, -1);
+  I.vidx.assign(nb * (size_t)I.vidx_stride, -1);
   I.values.clear();
-  for (size_t i = 0; i < chain.size(); ++i) {
-    if (i == 0 || chain[i].v != chain[i - 1].v) I.values.push_back(chain[i].v);
-    I.vidx[(size_t)chain[i].bin * I.vidx_stride + chain[i].gen] = (int32_t)(I.values.size() - 1);
+
+  // The chain of a normal value keeps its mantissa and lowers its exponent by one per
+  // halving, so the value set is enumerated exponent by exponent, each exponent's values in
+  // mantissa order. Used when that grid is dense; otherwise all chain values are sorted.
+  struct Chain {
+    uint64_t mant;
+    int32_t e_hi, len;
+    uint32_t bin;
+  };
+  std::vector<Chain> ch;
+  int32_t e_min = INT32_MAX, e_max = INT32_MIN;
+  for (size_t b = 0; b < nb && normal; ++b) {
+    if (!chain_len[b]) continue;
+    uint64_t bits;
+    std::memcpy(&bits, &I.bin_value[b], sizeof(bits));
+    const int32_t e = (int32_t)((bits >> 52) & 0x7FF);
+    if (e == 0) {
+      normal = false;
+      break;
+    }
+    ch.push_back(Chain{bits & ((1ull << 52) - 1), e, (int32_t)chain_len[b], (uint32_t)b});
+    e_max = std::max(e_max, e);
+    e_min = std::min(e_min, e - (int32_t)chain_len[b] + 1);
+  }
+  if (normal && !ch.empty() && (uint64_t)(e_max - e_min + 1) * ch.size() <= 8 * chain_total + 1024) {
+    std::stable_sort(ch.begin(), ch.end(), [](const Chain& x, const Chain& y) { return x.mant < y.mant; });
+    for (int32_t E = e_min; E <= e_max; ++E) {
+      bool have = false;
+      uint64_t prev = 0;
+      for (const Chain& c : ch) {
+        if (E > c.e_hi || E <= c.e_hi - c.len) continue;
+        if (!have || c.mant != prev) {
+          const uint64_t bits = ((uint64_t)E << 52) | c.mant;
+          double v;
+          std::memcpy(&v, &bits, sizeof(v));
+          I.values.push_back(v);
+          prev = c.mant;
+          have = true;
+        }
+        I.vidx[(size_t)c.bin * I.vidx_stride + (uint32_t)(c.e_hi - E)] = (int32_t)(I.values.size() - 1);
+      }
+    }
+  } else if (nb) {
+    struct Link {
+      double v;
+      uint32_t bin, gen;
+    };
+    std::vector<Link> chain;
+    chain.reserve(chain_total);
+    for (size_t b = 0; b < nb; ++b) {
+      uint32_t g = 0;
+      for (double cur = I.bin_value[b]; g < chain_len[b]; cur = cur / 2) chain.push_back(Link{cur, (uint32_t)b, g++});
+    }
+    std::sort(chain.begin(), chain.end(), [](const Link& x, const Link& y) { return x.v < y.v; });
+    for (size_t i = 0; i < chain.size(); ++i) {
+      if (i == 0 || chain[i].v != chain[i - 1].v) I.values.push_back(chain[i].v);
+      I.vidx[(size_t)chain[i].bin * I.vidx_stride + chain[i].gen] = (int32_t)(I.values.size() - 1);
+    }
   }
 
   // Cell types: ratio-sum check, stable sort by ratio descending, cumulative ratios in

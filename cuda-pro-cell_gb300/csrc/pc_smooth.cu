@@ -105,32 +105,27 @@ __device__ __forceinline__ float f64_to_f32_rz_any(double d) {
   return __uint_as_float(sign | ((mag - (896u << 20)) << 3) | (lo >> 29));
 }
 
-// x * 2 for a positive normal double, on the integer pipe.
-__device__ __forceinline__ double twice(double x) {
-  return __longlong_as_double(__double_as_longlong(x) + (1ll << 52));
-}
-
 constexpr float kLogNegligible = -100.0f;  // e^-100 * 2^63 < 1e-24
 
 // One lineage (its normals z[j * 32], j = 0.., and initial age U) for one type of one
 // candidate. Forward: acc[g * kThreads] += weight * 2^g * w_g. Backward (Ag2[g] = 2^g dL/dE_g):
 // accumulates sum_g Ag2[g] w_g and its derivatives in mean and sd.
 template <bool Backward>
-__device__ __forceinline__ void walk(const SmoothArgs& A, const float* z, double u_age, uint32_t steps, double mu,
-                                     double sigma, bool fixed_tau, double weight, double* acc, const float* Ag2,
-                                     float& f_r, float& f_mu, float& f_sig) {
+__device__ __forceinline__ void walk(const SmoothArgs& A, const float* z, double u_age, float u1, float inv_h,
+                                     uint32_t steps, double mu, double sigma, bool fixed_tau, float w_hi,
+                                     float w_lo, float* acc, const float* Ag2, float& f_r, float& f_mu,
+                                     float& f_sig) {
   double R = 0.0;                 // T - S_j
   float log_p = 0.0f;             // log s_1 ... s_{j-1}
   float dmu = 0.0f, dsig = 0.0f;  // dS_j / d(mean, sd)
   float D_mu = 0.0f, D_sig = 0.0f;
-  const float inv_h = (float)A.inv_h;
-  double ws = weight;  // weight * 2^(j-1)
+  float wh = w_hi, wl = w_lo;     // weight * 2^(j-1) as a pair of floats
   for (uint32_t j = 1; j <= steps; ++j) {
     const float zj = fixed_tau ? 0.0f : z[(j - 1) * 32u];
     const double tau = fixed_tau ? 0.0 : fma(sigma, f32_to_f64_bits(zj), mu);
     if (j == 1) {
       R = A.t_max - fma(tau, u_age, tau);
-      dmu = (float)(1.0 + u_age);
+      dmu = u1;
       dsig = zj * dmu;
     } else {
       R = R - tau;
@@ -142,8 +137,17 @@ __device__ __forceinline__ void walk(const SmoothArgs& A, const float* z, double
     log_sig(x, ls, l1m);
     const float w = expf(log_p + l1m);  // leaf weight of generation j - 1
     if constexpr (!Backward) {
-      if (w != 0.0f) acc[(j - 1) * kThreads] = fma(ws, f32_to_f64_bits(w), acc[(j - 1) * kThreads]);
-      ws = twice(ws);
+      if (w != 0.0f) {
+        // (wh + wl) * w as t1 + t2 (t1 rounded, t2 its error plus the low part), added into
+        // the compensated pair at acc[2g] (sum) / acc[2g + 1] (compensation)
+        const float t1 = __fmul_rn(wh, w);
+        const float t2 = __fadd_rn(__fmaf_rn(wh, w, -t1), __fmul_rn(wl, w));
+        float* p = acc + 2u * (j - 1u) * kThreads;
+        kahan_add(p, t1);
+        p[kThreads] = __fsub_rn(p[kThreads], t2);
+      }
+      wh = __fmul_rn(wh, 2.0f);
+      wl = __fmul_rn(wl, 2.0f);
     } else {
       const float a = Ag2[j - 1];
       if (a != 0.0f && w != 0.0f) {
@@ -171,12 +175,12 @@ __global__ void __launch_bounds__(kThreads) k_smooth(const SmoothArgs A, const d
                                                      uint32_t ncand, const double* __restrict__ grad_expected,
                                                      uint32_t nvalues, const int32_t* __restrict__ vidx,
                                                      double* __restrict__ out) {
-  // dynamic: forward acc [rows][kThreads] doubles / backward [ntypes * 3][kThreads] floats,
-  // then the lineage draws z [kWarps][rows][32] floats
-  extern __shared__ double acc[];
-  float* facc = reinterpret_cast<float*>(acc);
+  // dynamic: compensated FP32 accumulator pairs [arows][kThreads] (forward: 2 per generation
+  // row, backward: 2 per (type, parameter)), then the lineage draws z [kWarps][rows][32]
+  extern __shared__ float facc[];
   __shared__ ZigTables Z;
   __shared__ double prm[32][kSmoothMaxTypes * 3];
+  __shared__ float wsplit[32][kSmoothMaxTypes * 2];  // ratio / paths as a pair of floats
   __shared__ float Ag2[Backward ? 32 : 1][kSmoothMaxRows];
   __shared__ double u_age[kThreads];
   constexpr uint32_t kWarps = kThreads / 32;
@@ -185,10 +189,9 @@ __global__ void __launch_bounds__(kThreads) k_smooth(const SmoothArgs A, const d
   const uint32_t c = blockIdx.y * 32u + lane;
   const bool live = c < ncand;
   const uint32_t K = A.ntypes;
-  const uint32_t nrows = Backward ? K * 3 : A.rows;             // output rows
-  const uint32_t arows = Backward ? K * 6 : A.rows;             // accumulator rows
-  float* zbuf = Backward ? facc + (size_t)arows * kThreads + (size_t)warp * A.rows * 32u
-                         : reinterpret_cast<float*>(acc + (size_t)arows * kThreads) + (size_t)warp * A.rows * 32u;
+  const uint32_t nrows = Backward ? K * 3 : A.rows;  // output rows
+  const uint32_t arows = 2u * nrows;                  // accumulator rows (sum, compensation)
+  float* zbuf = facc + (size_t)arows * kThreads + (size_t)warp * A.rows * 32u;
   for (uint32_t i = threadIdx.x; i < sizeof(ZigTables) / 4; i += blockDim.x)
     reinterpret_cast<uint32_t*>(&Z)[i] = __ldg(reinterpret_cast<const uint32_t*>(A.zig) + i);
   for (uint32_t i = threadIdx.x; i < 32u * K * 3u; i += blockDim.x) {
@@ -196,12 +199,7 @@ __global__ void __launch_bounds__(kThreads) k_smooth(const SmoothArgs A, const d
     const uint32_t cc = blockIdx.y * 32u + l;
     prm[l][q] = cc < ncand ? params[(uint64_t)cc * K * 3 + q] : 0.0;
   }
-  for (uint32_t i = 0; i < arows; ++i) {
-    if constexpr (Backward)
-      facc[i * kThreads + threadIdx.x] = 0.0f;
-    else
-      acc[i * kThreads + threadIdx.x] = 0.0;
-  }
+  for (uint32_t i = 0; i < arows; ++i) facc[i * kThreads + threadIdx.x] = 0.0f;
   const uint32_t cap = __ldg(A.bin_cap + b);
   const uint32_t steps = cap + 1u;
   if constexpr (Backward) {
@@ -217,10 +215,18 @@ __global__ void __launch_bounds__(kThreads) k_smooth(const SmoothArgs A, const d
     }
   }
   __syncthreads();
+  for (uint32_t i = threadIdx.x; i < 32u * K; i += blockDim.x) {
+    const uint32_t l = i / K, k = i % K;
+    const double wt = prm[l][3 * k] / (double)A.paths;
+    const float hi = __double2float_rn(wt);
+    wsplit[l][2 * k] = hi;
+    wsplit[l][2 * k + 1] = __double2float_rn(wt - (double)hi);
+  }
+  __syncthreads();
   const uint64_t r0 = __ldg(A.bin_start + b), r1 = __ldg(A.bin_start + b + 1);
   const double inv_paths = 1.0 / (double)A.paths;
-  double* my = acc + threadIdx.x;
   float* fmy = facc + threadIdx.x;
+  const float inv_h = (float)A.inv_h;
   const double* my_prm = prm[lane];
   const float* my_ag = Backward ? Ag2[lane] : nullptr;
   // lineage i of the bin: initial cell r0 + i / paths, replica i % paths
@@ -247,17 +253,21 @@ __global__ void __launch_bounds__(kThreads) k_smooth(const SmoothArgs A, const d
       for (uint32_t ii = 0; ii < n; ++ii) {
         const float* z = zbuf + ii;
         const double ua = u_age[warp * 32u + ii];
+        const float u1 = __double2float_rn(1.0 + ua);
         for (uint32_t k = 0; k < K; ++k) {
-          const double ratio = my_prm[3 * k], mu = my_prm[3 * k + 1], sd = my_prm[3 * k + 2];
+          const double mu = my_prm[3 * k + 1], sd = my_prm[3 * k + 2];
+          const float w_hi = wsplit[lane][2 * k], w_lo = wsplit[lane][2 * k + 1];
           float f_r = 0.0f, f_mu = 0.0f, f_sig = 0.0f;  // this lineage's adjoint terms
           if (mu < 0.0) {
             // quiescent type: a leaf at generation 0 (cell.cu:69-75)
-            if constexpr (Backward)
+            if constexpr (Backward) {
               f_r = my_ag[0];
-            else
-              my[0] += ratio * inv_paths;
-          } else if (Backward || ratio != 0.0) {
-            walk<Backward>(A, z, ua, steps, mu, sd, mu == 0.0, ratio * inv_paths, my, my_ag, f_r, f_mu, f_sig);
+            } else {
+              kahan_add(fmy, w_hi);
+              fmy[kThreads] = __fsub_rn(fmy[kThreads], w_lo);
+            }
+          } else if (Backward || w_hi != 0.0f) {
+            walk<Backward>(A, z, ua, u1, inv_h, steps, mu, sd, mu == 0.0, w_hi, w_lo, fmy, my_ag, f_r, f_mu, f_sig);
           }
           if constexpr (Backward) {
             // per-thread compensated FP32 sums (terms of either sign cancel); scaled by
@@ -279,12 +289,8 @@ __global__ void __launch_bounds__(kThreads) k_smooth(const SmoothArgs A, const d
     for (uint32_t q = 0; q < nrows; ++q) {
       double v = 0.0;
 #pragma unroll
-      for (uint32_t w = 0; w < kWarps; ++w) {
-        if constexpr (Backward)
-          v += (double)facc[2 * q * kThreads + w * 32u + lane] - (double)facc[(2 * q + 1) * kThreads + w * 32u + lane];
-        else
-          v += acc[q * kThreads + w * 32u + lane];
-      }
+      for (uint32_t w = 0; w < kWarps; ++w)
+        v += (double)facc[2 * q * kThreads + w * 32u + lane] - (double)facc[(2 * q + 1) * kThreads + w * 32u + lane];
       if constexpr (Backward) v *= (q % 3u == 0u ? 1.0 : my_prm[q - q % 3u]) * inv_paths;
       o[q] = v;
     }
@@ -313,15 +319,14 @@ __global__ void k_smooth_grad_sum(const double* __restrict__ part, uint32_t ncan
 }
 
 // acc rows x kThreads doubles + the lineage draws (kThreads floats per generation row)
-int smem_bytes(uint32_t acc_rows, size_t acc_elem, uint32_t rows) {
-  return (int)(acc_rows * kThreads * acc_elem + rows * kThreads * sizeof(float));
+int smem_bytes(uint32_t out_rows, uint32_t rows) {
+  return (int)((2u * out_rows + rows) * kThreads * sizeof(float));
 }
 
 template <bool Backward>
 int launch_smooth_t(const SmoothArgs& A, const double* params, uint32_t ncand, const double* grad_expected,
                     uint32_t nvalues, const int32_t* vidx, double* out, cudaStream_t st) {
-  const uint32_t acc_rows = Backward ? A.ntypes * 6u : A.rows;
-  const int smem = smem_bytes(acc_rows, Backward ? sizeof(float) : sizeof(double), A.rows);
+  const int smem = smem_bytes(Backward ? A.ntypes * 3u : A.rows, A.rows);
   // static shared memory plus `smem` may exceed the default 48 KB: always opt in
   const cudaError_t e = cudaFuncSetAttribute(k_smooth<Backward>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return (int)e;
