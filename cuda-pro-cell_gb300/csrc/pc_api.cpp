@@ -1055,7 +1055,8 @@ int run_persistent(pc_context* ctx, pc_plan* p, const SweepKernels& K, const int
 
   float ms = 0.f;
   PC_CUDA(ctx, cudaEventRecord(ctx->ev[0], st));
-  if (ctx->opt_graph) {
+  bool use_graph = ctx->opt_graph != 0;
+  if (use_graph) {
     const bool same = p->graph && p->graph_config == ctx->opt_config && p->graph_grid == grid &&
                       std::memcmp(&p->graph_args, &pa, sizeof(pa)) == 0;
     if (!same) {
@@ -1067,18 +1068,22 @@ int run_persistent(pc_context* ctx, pc_plan* p, const SweepKernels& K, const int
       rc = enqueue_persistent(ctx, p, K, pa, grid, cap_st);
       cudaGraph_t g = nullptr;
       const cudaError_t ee = cudaStreamEndCapture(cap_st, &g);
-      if (rc != PC_OK) {
-        if (g) cudaGraphDestroy(g);
-        return rc;
+      cudaError_t ei = cudaErrorUnknown;
+      if (rc == PC_OK && ee == cudaSuccess) ei = cudaGraphInstantiate(&p->graph, g, 0);
+      if (g) cudaGraphDestroy(g);
+      if (rc != PC_OK || ee != cudaSuccess || ei != cudaSuccess) {
+        // capture or instantiation not possible here: run the same operations directly
+        (void)cudaGetLastError();
+        p->graph = nullptr;
+        use_graph = false;
+      } else {
+        p->graph_args = pa;
+        p->graph_config = ctx->opt_config;
+        p->graph_grid = grid;
       }
-      PC_CUDA(ctx, ee);
-      const cudaError_t ei = cudaGraphInstantiate(&p->graph, g, 0);
-      cudaGraphDestroy(g);
-      PC_CUDA(ctx, ei);
-      p->graph_args = pa;
-      p->graph_config = ctx->opt_config;
-      p->graph_grid = grid;
     }
+  }
+  if (use_graph) {
     PC_CUDA(ctx, cudaGraphLaunch(p->graph, st));
   } else {
     rc = enqueue_persistent(ctx, p, K, pa, grid, st);
