@@ -1376,6 +1376,28 @@ int pc_batch_autotune(pc_context* ctx, pc_batch* b, uint32_t repeats, pc_tuning*
   return pc_autotune(ctx, b, repeats, out);
 }
 
+int pc_debug_barrier(pc_context* ctx, int starve, double timeout_ms, uint32_t* error_bits, uint32_t* passed) {
+  if (!ctx || !error_bits || !passed || !(timeout_ms > 0.0) || timeout_ms > 10000.0)
+    return fail(ctx, PC_ERR_INVALID, "timeout must be in (0, 10000] ms");
+  PC_CUDA(ctx, cudaSetDevice(ctx->device));
+  cudaStream_t st = ctx->stream;
+  uint32_t* d = nullptr;  // [0..1] barrier (arrivals, generation), [2] error bits, [3] blocks through
+  PC_CUDA(ctx, cudaMalloc(&d, 4 * sizeof(uint32_t)));
+  const uint32_t init[4] = {starve ? 0x40000000u : 0u, 0u, 0u, 0u};
+  uint32_t host[4] = {0u, 0u, 0u, 0u};
+  const int blocks = std::max(1, std::min(ctx->sms, 8));
+  cudaError_t e = cudaMemcpyAsync(d, init, sizeof(init), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess)
+    e = (cudaError_t)launch_barrier_probe(d, (unsigned long long)(timeout_ms * 1e6), d + 2, d + 3, blocks, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(host, d, sizeof(host), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cudaFree(d);
+  if (e != cudaSuccess) return fail(ctx, PC_ERR_CUDA, std::string("barrier probe: ") + cudaGetErrorString(e));
+  *error_bits = host[2];
+  *passed = host[3];
+  return PC_OK;
+}
+
 int pc_debug_philox(pc_context* ctx, const uint32_t* ctr, uint64_t n, const uint32_t key[2], uint32_t* out) {
   if (!ctx || (n && (!ctr || !out)) || !key) return PC_ERR_INVALID;
   if (n == 0) return PC_OK;

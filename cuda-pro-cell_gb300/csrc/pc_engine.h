@@ -168,6 +168,9 @@ int launch_debug_philox(const uint32_t* ctr, uint64_t n, uint32_t k0, uint32_t k
 int launch_debug_normals(const ZigTables* zig, uint32_t k0, uint32_t k1, uint32_t root,
                          uint64_t first_parent, uint64_t count, float* z, void* stream);
 int occupancy_blocks_per_sm(int* root_blocks, int* divide_blocks);
+// One grid barrier in a cooperative launch of `blocks` blocks (failure-detection test).
+int launch_barrier_probe(uint32_t* bar, unsigned long long timeout_ns, uint32_t* error, uint32_t* passed, int blocks,
+                         void* stream);
 
 // Smoothed (differentiable) form (pc_smooth.cu). For every candidate parameter set c
 // (per type k: ratio, mean, sd) and every bin b, the expected leaf count at generation g

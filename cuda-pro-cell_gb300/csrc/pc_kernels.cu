@@ -36,7 +36,29 @@ __global__ void k_debug_normals(const ZigTables* zig, uint32_t k0, uint32_t k1, 
   z[i] = zig_normal(c ? P.y : P.x, (P.z >> (8u * c)) & 255u, true, pair_wedge_bits(P, c), cs, Z, budget);
 }
 
+// One grid barrier of the persistent driver, for the failure-detection test: with
+// `starve` set, the arrival counter starts far above the grid size, so no block is ever
+// the last to arrive (a flag that nothing sets) and every block's wait runs into the
+// timeout, sets error bit 2 and returns.
+__global__ void k_barrier_probe(uint32_t* bar, unsigned long long timeout_ns, uint32_t* error, uint32_t* passed) {
+  if (grid_barrier(bar, timeout_ns, error) && threadIdx.x == 0) atomicAdd(passed, 1u);
+}
+
 }  // namespace
+
+int launch_barrier_probe(uint32_t* bar, unsigned long long timeout_ns, uint32_t* error, uint32_t* passed, int blocks,
+                         void* stream) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)blocks);
+  cfg.blockDim = dim3(128u);
+  cfg.stream = (cudaStream_t)stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return (int)cudaLaunchKernelEx(&cfg, k_barrier_probe, bar, timeout_ns, error, passed);
+}
 
 // Narrow-layout tables (pc_tuned_plain.cu, pc_tuned_batched.cu).
 const SweepKernels& tuned_plain(int config);

@@ -297,6 +297,13 @@ int pc_simulate_noalloc(const pc_bin* bins, uint64_t n_bins, const pc_cell_type*
  * pc_debug_normals: z[i] = first-attempt normal of child (i & 1) of node first_parent+i/2
  *                   under `root` (no truncation), as the division sweep computes it.
  * pc_debug_tables: the device's ziggurat tables (k[256], w bits[256], f bits[257]). */
+/* One grid barrier of the persistent driver in a cooperative launch of up to 8 blocks,
+ * with the wait limited to timeout_ms. starve = 1 presets the arrival counter so that the
+ * barrier can never complete: every block's wait runs out, error bit 2 (value 4) is set
+ * and the kernel returns, leaving the context usable (failure detection without a GPU
+ * fault). *passed = blocks that got through. */
+int pc_debug_barrier(pc_context* ctx, int starve, double timeout_ms, uint32_t* error_bits,
+                     uint32_t* passed);
 int pc_debug_philox(pc_context* ctx, const uint32_t* ctr, uint64_t n, const uint32_t key[2],
                     uint32_t* out);
 int pc_debug_normals(pc_context* ctx, uint64_t seed, uint32_t root, uint64_t first_parent,

@@ -129,3 +129,23 @@ def test_autotune_picks_a_compiled_combination(eng, small_oracle):
     r = p.result()
     assert np.array_equal(r.per_type, o.per_type)
     p.close()
+
+
+def test_barrier_timeout_is_reported_and_the_context_survives(eng, small_oracle):
+    """Failure detection of the persistent driver without a GPU fault: a grid barrier that
+    can never complete (its arrival counter preset) runs into its time limit, every block
+    returns with error bit 2 set, and the context keeps working."""
+    import ctypes
+    L = eng.L
+    err, passed = ctypes.c_uint32(), ctypes.c_uint32()
+    assert L.pc_debug_barrier(eng.ctx, 0, 100.0, ctypes.byref(err), ctypes.byref(passed)) == 0
+    assert err.value == 0 and passed.value >= 1
+    blocks = passed.value
+    assert L.pc_debug_barrier(eng.ctx, 1, 100.0, ctypes.byref(err), ctypes.byref(passed)) == 0
+    assert err.value & 4 and passed.value == 0
+    assert L.pc_debug_barrier(eng.ctx, 0, 100.0, ctypes.byref(err), ctypes.byref(passed)) == 0
+    assert err.value == 0 and passed.value == blocks
+    w, o = small_oracle
+    set_opts(eng, driver=1, graph=1)
+    g = eng.simulate(w.bins, w.types, w.t_max, w.phi, w.seed)
+    assert np.array_equal(g.per_type, o.per_type)
