@@ -147,3 +147,26 @@ def test_batch_rerun_and_invalid_instance(engine):
     bad[3] = (bad[3][0], [(0.5, 10.0, 1.0)], 10.0, None, 1)
     with pytest.raises(ProcellError, match="instance 3: ERROR: proportion"):
         engine.batch(bad)
+
+
+def test_batch_of_many_tiny_instances(engine):
+    # a thousand instances of a few cells each: bin/class/type tables with many boundaries
+    rng = np.random.default_rng(41)
+    instances = []
+    for i in range(1000):
+        nb = int(rng.integers(1, 6))
+        bins = [(float(np.exp(rng.uniform(0.0, 7.0))), int(rng.integers(0, 4))) for _ in range(nb)]
+        nt = int(rng.integers(1, 4))
+        r = rng.dirichlet(np.ones(nt))
+        r = r / r.sum()
+        types = [(float(r[k]), float(rng.uniform(5.0, 60.0)), float(rng.uniform(0.5, 10.0))) for k in range(nt)]
+        if rng.random() < 0.1:
+            types[-1] = (types[-1][0], -1.0, -1.0)
+        phi = None if any(f for _, f in bins) else 1.0  # automatic phi needs a nonzero row
+        instances.append((bins, types, float(rng.uniform(0.0, 150.0)), phi, int(rng.integers(0, 2 ** 40))))
+    b = engine.batch(instances)
+    b.run()
+    for i, x in enumerate(instances):
+        want, _ = plain_counts(engine, *x)
+        assert np.array_equal(b.raw_counts(i), want), i
+    b.close()
