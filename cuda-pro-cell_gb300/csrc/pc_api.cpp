@@ -52,6 +52,13 @@ struct pc_context {
   // resident blocks per SM of each configuration's kernels: [narrow][batched][config]
   int occ[2][2][kNumSweepConfigs][3] = {};
   uint32_t* persist_ctl = nullptr;       // [2] barrier + [8] run totals (u64 [4])
+  // the two large per-plan device buffers (root records, count table) of destroyed plans,
+  // kept for the next plan of this context (one of each, the largest)
+  void* spare_rec = nullptr;
+  size_t spare_rec_bytes = 0;
+  void* spare_hist = nullptr;
+  size_t spare_hist_bytes = 0;
+  std::vector<pc_plan*> live;  // plans created on this context and not yet destroyed
   // pinned host copy of the last count table read back (plan id and run number it holds)
   unsigned long long* stage = nullptr;
   size_t stage_elems = 0;
@@ -107,6 +114,8 @@ struct pc_plan {
   unsigned long long* hist_dev = nullptr;
   size_t hist_elems = 0;
   uint64_t id = 0, run_id = 0;                // identity of the counts in the pinned stage
+  pc_context* owner = nullptr;                // receives the large buffers on destroy
+  size_t rec_bytes = 0, hist_bytes = 0;
   cudaGraphExec_t graph = nullptr;           // persistent driver: the captured run
   PersistArgs graph_args;                    // ... and the arguments it was captured with
   int graph_config = -1, graph_grid = 0;
@@ -233,6 +242,32 @@ int grid_for(const pc_context* ctx, uint64_t n, int per_sm, int threads) {
   return (int)std::max<uint64_t>(1, std::min<uint64_t>(want, (uint64_t)max_blocks(ctx, per_sm)));
 }
 
+// A device buffer of at least `need` bytes: the context's spare one when it is large enough,
+// else a new allocation.
+cudaError_t take_spare(void** spare, size_t* spare_bytes, size_t need, void** out, size_t* out_bytes) {
+  if (*spare && *spare_bytes >= need) {
+    *out = *spare;
+    *out_bytes = *spare_bytes;
+    *spare = nullptr;
+    *spare_bytes = 0;
+    return cudaSuccess;
+  }
+  *out_bytes = need;
+  return cudaMalloc(out, need);
+}
+
+// Keep the larger of `buf` and the context's spare, free the other.
+void give_spare(void** spare, size_t* spare_bytes, void* buf, size_t bytes) {
+  if (!buf) return;
+  if (*spare && *spare_bytes >= bytes) {
+    cudaFree(buf);
+    return;
+  }
+  cudaFree(*spare);
+  *spare = buf;
+  *spare_bytes = bytes;
+}
+
 // f(i) for i in [0, n) on up to `threads` host threads (0 = all cores).
 template <class F>
 void parallel_for(uint32_t n, F&& f, unsigned threads = 0) {
@@ -319,6 +354,9 @@ void pc_destroy(pc_context* ctx) {
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   free_pool(ctx);
+  for (pc_plan* p : ctx->live) p->owner = nullptr;  // plans outliving their context free their own buffers
+  cudaFree(ctx->spare_rec);
+  cudaFree(ctx->spare_hist);
   cudaFree(ctx->zig_dev);
   cudaFree(ctx->stats_dev);
   cudaFree(ctx->error_dev);
@@ -649,8 +687,14 @@ int finalize_plan(pc_context* ctx, pc_plan* p) {
   p->upload_bytes = nb * sizeof(uint32_t) + (nb + 1) * sizeof(uint64_t);
   cudaError_t e = cudaMalloc(&p->bin_info_dev, std::max<size_t>(1, nb) * sizeof(uint32_t));
   if (e == cudaSuccess) e = cudaMalloc(&p->bin_start_dev, (nb + 1) * sizeof(uint64_t));
-  if (e == cudaSuccess) e = cudaMalloc(&p->root_rec_dev, std::max<uint64_t>(1, chunk) * sizeof(unsigned long long));
-  if (e == cudaSuccess) e = cudaMalloc(&p->hist_dev, p->hist_elems * sizeof(unsigned long long));
+  p->owner = ctx;
+  ctx->live.push_back(p);
+  if (e == cudaSuccess)
+    e = take_spare(&ctx->spare_rec, &ctx->spare_rec_bytes, std::max<uint64_t>(1, chunk) * sizeof(unsigned long long),
+                   reinterpret_cast<void**>(&p->root_rec_dev), &p->rec_bytes);
+  if (e == cudaSuccess)
+    e = take_spare(&ctx->spare_hist, &ctx->spare_hist_bytes, p->hist_elems * sizeof(unsigned long long),
+                   reinterpret_cast<void**>(&p->hist_dev), &p->hist_bytes);
   if (e == cudaSuccess && nb)
     e = cudaMemcpyAsync(p->bin_info_dev, p->bin_info.data(), nb * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess)
@@ -802,8 +846,15 @@ void pc_plan_destroy(pc_plan* p) {
   cudaFree(p->bin_class_dev);
   cudaFree(p->bin_info_dev);
   cudaFree(p->bin_start_dev);
-  cudaFree(p->root_rec_dev);
-  cudaFree(p->hist_dev);
+  if (p->owner) {
+    pc_context* ctx = p->owner;
+    ctx->live.erase(std::remove(ctx->live.begin(), ctx->live.end(), p), ctx->live.end());
+    give_spare(&ctx->spare_rec, &ctx->spare_rec_bytes, p->root_rec_dev, p->rec_bytes);
+    give_spare(&ctx->spare_hist, &ctx->spare_hist_bytes, p->hist_dev, p->hist_bytes);
+  } else {
+    cudaFree(p->root_rec_dev);
+    cudaFree(p->hist_dev);
+  }
   delete p;
 }
 
