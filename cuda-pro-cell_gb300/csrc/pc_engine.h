@@ -56,7 +56,7 @@ struct alignas(16) TypeDev {
 
 // Batched form: the parameters of one type together with its instance's (one table
 // entry per type of every instance, in instance order).
-// The division sweep reads bytes 0-31 (type) and 48-79 (instance) as four 16-byte loads.
+// The division sweep reads bytes 0-31 (type) and 48-79 (instance) as 16-byte loads.
 struct alignas(16) BatchType {
   TypeDev t;            // bytes 0-47
   double t_max;         // 48
