@@ -645,7 +645,18 @@ def run_calibration(args):
     clk = clocks.stop()
     h2d = host_theta.numel() * 8
     d2h = (out_g.numel() + out_l.numel()) * 8
+    # one pass of the forward-mode Jacobian kernel (expected counts and d/d parameters)
+    P0 = prob.params(theta)
+    prob.smooth.jacobian(P0)
+    j0, j1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    j0.record(stream)
+    for _ in range(args.steps):
+        prob.smooth.jacobian(P0)
+    j1.record(stream)
+    torch.cuda.synchronize()
+    jac_ms = j0.elapsed_time(j1) / args.steps
     comp = cb.compare(eng, candidates=C, seed=7, pso_seconds=30.0)
+    comp.pop("traces", None)
     cpu = None
     if not args.no_cpu_baseline:
         cpu = cpu_smooth_sample(prob.bins, prob.phi, prob.t_max, prob.smooth_h, prob.smooth_paths,
@@ -674,6 +685,8 @@ def run_calibration(args):
                                % (C, prob.smooth_paths),
                    "l2": "inputs (bins, parameters) are a few MB; the kernels are compute bound"},
         "calibration": comp,
+        "jacobian_pass": {"ms": jac_ms, "candidates_per_s": C / (jac_ms * 1e-3),
+                          "what": "expected counts and their Jacobian in (ratio, mean, sd) for %d candidates" % C},
         "e2e": {"value": C * args.steps / e2e_s, "unit": "grads/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "hbm", "achieved": alg / (elapsed_ms * 1e-3 / args.steps) / 1e9, "peak": hbm,

@@ -1504,6 +1504,8 @@ struct pc_smooth {
   double* e_raw_dev = nullptr;   // [cand_cap][nbins][rows]
   double* part_dev = nullptr;    // [cand_cap][nbins][ntypes * 3]
   uint32_t cand_cap = 0;
+  double* jac_raw_dev = nullptr;  // [jac_cap][nbins][rows][ntypes * 3], allocated on first use
+  uint32_t jac_cap = 0;
 };
 
 namespace {
@@ -1538,6 +1540,17 @@ int smooth_scratch(pc_context* ctx, pc_smooth* s, uint32_t ncand) {
   PC_CUDA(ctx, cudaMalloc(&s->e_raw_dev, (size_t)ncand * nb * s->rows * sizeof(double)));
   PC_CUDA(ctx, cudaMalloc(&s->part_dev, (size_t)ncand * nb * s->ntypes * 3 * sizeof(double)));
   s->cand_cap = ncand;
+  return PC_OK;
+}
+
+int jacobian_scratch(pc_context* ctx, pc_smooth* s, uint32_t ncand) {
+  if (ncand <= s->jac_cap) return PC_OK;
+  cudaFree(s->jac_raw_dev);
+  s->jac_raw_dev = nullptr;
+  s->jac_cap = 0;
+  const size_t nb = std::max<size_t>(1, s->I.bin_value.size());
+  PC_CUDA(ctx, cudaMalloc(&s->jac_raw_dev, (size_t)ncand * nb * s->rows * s->ntypes * 3 * sizeof(double)));
+  s->jac_cap = ncand;
   return PC_OK;
 }
 
@@ -1664,6 +1677,21 @@ int pc_smooth_backward(pc_context* ctx, pc_smooth* s, const double* params, uint
   return PC_OK;
 }
 
+int pc_smooth_jacobian(pc_context* ctx, pc_smooth* s, const double* params, uint32_t n_candidates,
+                       double* expected, double* jacobian) {
+  if (!ctx || !s || (n_candidates && (!params || !expected || !jacobian)))
+    return fail(ctx, PC_ERR_INVALID, "null argument");
+  if (n_candidates == 0) return PC_OK;
+  PC_CUDA(ctx, cudaSetDevice(ctx->device));
+  int rc = jacobian_scratch(ctx, s, n_candidates);
+  if (rc != PC_OK) return rc;
+  const SmoothArgs A = smooth_args(ctx, s);
+  PC_CUDA(ctx, (cudaError_t)launch_smooth_jacobian(A, params, n_candidates, s->inv_off_dev, s->inv_idx_dev,
+                                                   (uint32_t)s->I.values.size(), s->jac_raw_dev, expected,
+                                                   jacobian, ctx->stream));
+  return PC_OK;
+}
+
 int pc_smooth_sync(pc_context* ctx) {
   if (!ctx) return PC_ERR_INVALID;
   PC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -1682,6 +1710,7 @@ void pc_smooth_destroy(pc_smooth* s) {
   cudaFree(s->inv_idx_dev);
   cudaFree(s->e_raw_dev);
   cudaFree(s->part_dev);
+  cudaFree(s->jac_raw_dev);
   delete s;
 }
 

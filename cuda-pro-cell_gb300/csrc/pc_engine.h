@@ -204,6 +204,13 @@ int launch_smooth_backward(const SmoothArgs& A, const double* params, uint32_t n
                            uint32_t nvalues, const int32_t* vidx, double* grad_part, double* grad_params,
                            void* stream);
 
+// expected[c][v] as launch_smooth_merge, and jacobian[c][v][k][3] = d expected[c][v] /
+// d params[c][k][.] by forward-mode tangents along the same lineages (one walk per lineage,
+// type and candidate); jac_raw is scratch [c][b][g][k][3].
+int launch_smooth_jacobian(const SmoothArgs& A, const double* params, uint32_t ncand, const uint32_t* inv_off,
+                           const uint32_t* inv_idx, uint32_t nvalues, double* jac_raw, double* expected,
+                           double* jacobian, void* stream);
+
 // Host helpers (pc_api.cpp).
 ZigTables host_zig_tables();
 void host_truncation_bounds(double mu, double sigma, float& zlo, float& zhi);

@@ -107,6 +107,25 @@ __device__ __forceinline__ float f64_to_f32_rz_any(double d) {
 
 constexpr float kLogNegligible = -100.0f;  // e^-100 * 2^63 < 1e-24
 
+// Lineage i of a bin whose initial cells start at r0 (initial cell r0 + i / paths, replica
+// i % paths, which draws as initial cell r + replica * ncells): its initial age, and the
+// normals of the nodes it visits (heap nodes 1, 2 + b_1, ..., b_j the path bits) into
+// z[j * 32], j < steps.
+__device__ __forceinline__ void draw_lineage(const SmoothArgs& A, const ZigTables& Z, uint64_t r0, uint64_t i,
+                                             uint32_t steps, float* z, double& u_age) {
+  const uint32_t m = (uint32_t)(i % A.paths);
+  const uint32_t root = (uint32_t)(r0 + i / A.paths) + m * A.ncells;
+  const u32x4 R = philox(u32x4{0u, 0u, root, kPurposeRoot}, A.k0, A.k1);
+  u_age = unit53_open_closed(R.z, R.w);
+  const u32x4 B = philox(u32x4{0u, 0u, root, kPurposePath}, A.k0, A.k1);
+  const uint64_t bits = (uint64_t)B.x | ((uint64_t)B.y << 32);
+  uint64_t node = 1;
+  for (uint32_t j = 0; j < steps; ++j) {
+    z[j * 32u] = node_z(node, root, A.k0, A.k1, Z, A.error);
+    node = 2ull * node + ((bits >> j) & 1ull);
+  }
+}
+
 // One lineage (its normals z[j * 32], j = 0.., and initial age U) for one type of one
 // candidate. Forward: acc[g * kThreads] += weight * 2^g * w_g. Backward (Ag2[g] = 2^g dL/dE_g):
 // accumulates sum_g Ag2[g] w_g and its derivatives in mean and sd.
@@ -167,6 +186,113 @@ __device__ __forceinline__ void walk(const SmoothArgs& A, const float* z, double
     }
     log_p += ls;
     if (log_p < kLogNegligible) break;
+  }
+}
+
+// One lineage for one type, forward mode: for every generation g it reaches, acc rows
+// 3g, 3g + 1, 3g + 2 gain 2^g w_g and 2^g dw_g/d(mean, sd) (per-thread FP32 sums).
+__device__ __forceinline__ void walk_jacobian(const SmoothArgs& A, const float* z, double u_age, float u1,
+                                              float inv_h, uint32_t steps, double mu, double sigma, bool fixed_tau,
+                                              float* acc) {
+  double R = 0.0;
+  float log_p = 0.0f, dmu = 0.0f, dsig = 0.0f, D_mu = 0.0f, D_sig = 0.0f;
+  float scale = 1.0f;  // 2^(j-1)
+  for (uint32_t j = 1; j <= steps; ++j) {
+    const float zj = fixed_tau ? 0.0f : z[(j - 1) * 32u];
+    const double tau = fixed_tau ? 0.0 : fma(sigma, f32_to_f64_bits(zj), mu);
+    if (j == 1) {
+      R = A.t_max - fma(tau, u_age, tau);
+      dmu = u1;
+      dsig = zj * dmu;
+    } else {
+      R = R - tau;
+      dmu += 1.0f;
+      dsig += zj;
+    }
+    const float x = f64_to_f32_rz_any(R) * inv_h;
+    float ls, l1m;
+    log_sig(x, ls, l1m);
+    const float w = expf(log_p + l1m);  // leaf weight of generation j - 1
+    float* p = acc + 3u * (j - 1u) * kThreads;
+    if (w != 0.0f) {
+      const float ws = w * scale;
+      p[0] += ws;
+      if (!fixed_tau) {
+        const float s = expf(ls);
+        p[kThreads] += ws * (D_mu + s * inv_h * dmu);
+        p[2 * kThreads] += ws * (D_sig + s * inv_h * dsig);
+      }
+    }
+    if (!fixed_tau) {
+      const float one_m_s = expf(l1m);
+      D_mu -= one_m_s * inv_h * dmu;
+      D_sig -= one_m_s * inv_h * dsig;
+    }
+    scale *= 2.0f;
+    log_p += ls;
+    if (log_p < kLogNegligible) break;
+  }
+}
+
+// Jacobian of the expected counts: block (bin, group of 32 candidates, type k). out[c][b][g][k]
+// = (sum 2^g w_g / paths, ratio_k / paths * sum 2^g dw_g/dmean, the same for sd), i.e.
+// d E_{b,g} / d(ratio_k, mean_k, sd_k); every block draws its bin's lineages itself (the
+// draws are shared by the 32 candidates of a warp, not across types).
+__global__ void __launch_bounds__(kThreads) k_smooth_jacobian(const SmoothArgs A, const double* __restrict__ params,
+                                                              uint32_t ncand, double* __restrict__ out) {
+  // dynamic: per-thread sums [3 * rows][kThreads], then the lineage draws [kWarps][rows][32]
+  extern __shared__ float facc[];
+  __shared__ ZigTables Z;
+  __shared__ double u_age[kThreads];
+  constexpr uint32_t kWarps = kThreads / 32;
+  const uint32_t b = blockIdx.x, k = blockIdx.z;
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  const uint32_t c = blockIdx.y * 32u + lane;
+  const bool live = c < ncand;
+  const uint32_t KQ = A.ntypes * 3u;
+  float* zbuf = facc + (size_t)3u * A.rows * kThreads + (size_t)warp * A.rows * 32u;
+  for (uint32_t i = threadIdx.x; i < sizeof(ZigTables) / 4; i += blockDim.x)
+    reinterpret_cast<uint32_t*>(&Z)[i] = __ldg(reinterpret_cast<const uint32_t*>(A.zig) + i);
+  for (uint32_t i = 0; i < 3u * A.rows; ++i) facc[i * kThreads + threadIdx.x] = 0.0f;
+  double ratio = 0.0, mu = 0.0, sd = 0.0;
+  if (live) {
+    ratio = params[(uint64_t)c * KQ + 3u * k];
+    mu = params[(uint64_t)c * KQ + 3u * k + 1u];
+    sd = params[(uint64_t)c * KQ + 3u * k + 2u];
+  }
+  __syncthreads();
+  const uint32_t steps = __ldg(A.bin_cap + b) + 1u;
+  const uint64_t r0 = __ldg(A.bin_start + b), r1 = __ldg(A.bin_start + b + 1);
+  float* fmy = facc + threadIdx.x;
+  const float inv_h = (float)A.inv_h;
+  const uint64_t nlin = (r1 - r0) * A.paths;
+  for (uint64_t base = (uint64_t)warp * 32u; base < nlin; base += 32u * kWarps) {
+    if (base + lane < nlin) draw_lineage(A, Z, r0, base + lane, steps, zbuf + lane, u_age[threadIdx.x]);
+    __syncwarp();
+    const uint32_t n = (uint32_t)((nlin - base) < 32u ? (nlin - base) : 32u);
+    if (live) {
+      for (uint32_t ii = 0; ii < n; ++ii) {
+        if (mu < 0.0) {
+          fmy[0] += 1.0f;  // quiescent type: a leaf at generation 0 (cell.cu:69-75)
+        } else {
+          const double ua = u_age[warp * 32u + ii];
+          walk_jacobian(A, zbuf + ii, ua, __double2float_rn(1.0 + ua), inv_h, steps, mu, sd, mu == 0.0, fmy);
+        }
+      }
+    }
+    __syncwarp();
+  }
+  __syncthreads();
+  // sums over the warps in warp order; lane l of every warp holds candidate 32 * group + l,
+  // so the warps split the rows
+  if (!live) return;
+  const double inv_paths = 1.0 / (double)A.paths;
+  double* o = out + ((uint64_t)c * A.nbins + b) * A.rows * KQ + 3u * k;
+  for (uint32_t q = warp; q < 3u * A.rows; q += kWarps) {
+    double v = 0.0;
+#pragma unroll
+    for (uint32_t w = 0; w < kWarps; ++w) v += (double)facc[q * kThreads + w * 32u + lane];
+    o[(q / 3u) * KQ + q % 3u] = v * (q % 3u == 0u ? 1.0 : ratio) * inv_paths;
   }
 }
 
@@ -233,20 +359,7 @@ __global__ void __launch_bounds__(kThreads) k_smooth(const SmoothArgs A, const d
   const uint64_t nlin = (r1 - r0) * A.paths;
   for (uint64_t base = (uint64_t)warp * 32u; base < nlin; base += 32u * kWarps) {
     // this lane draws lineage base + lane
-    const uint64_t i = base + lane;
-    if (i < nlin) {
-      const uint32_t m = (uint32_t)(i % A.paths);
-      const uint32_t root = (uint32_t)(r0 + i / A.paths) + m * A.ncells;  // replica m
-      const u32x4 R = philox(u32x4{0u, 0u, root, kPurposeRoot}, A.k0, A.k1);
-      u_age[threadIdx.x] = unit53_open_closed(R.z, R.w);
-      const u32x4 B = philox(u32x4{0u, 0u, root, kPurposePath}, A.k0, A.k1);
-      const uint64_t bits = (uint64_t)B.x | ((uint64_t)B.y << 32);
-      uint64_t node = 1;
-      for (uint32_t j = 0; j < steps; ++j) {
-        zbuf[j * 32u + lane] = node_z(node, root, A.k0, A.k1, Z, A.error);
-        node = 2ull * node + ((bits >> j) & 1ull);
-      }
-    }
+    if (base + lane < nlin) draw_lineage(A, Z, r0, base + lane, steps, zbuf + lane, u_age[threadIdx.x]);
     __syncwarp();
     const uint32_t n = (uint32_t)((nlin - base) < 32u ? (nlin - base) : 32u);
     if (live) {
@@ -308,6 +421,26 @@ __global__ void k_smooth_merge(const double* __restrict__ e_raw, uint32_t ncand,
   expected[i] = s;
 }
 
+// expected[c][v] = sum_k ratio_k U, jacobian[c][v][k][q] = sum of jac_raw[c][b][g][k][q]
+// over the (b, g) of value v (U = the q = 0 entry, d/d ratio_k).
+__global__ void k_smooth_jacobian_merge(const double* __restrict__ jac_raw, const double* __restrict__ params,
+                                        uint32_t ncand, uint32_t per_cand, uint32_t kq,
+                                        const uint32_t* __restrict__ inv_off, const uint32_t* __restrict__ inv_idx,
+                                        uint32_t nvalues, double* __restrict__ expected, double* __restrict__ jac) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (uint64_t)ncand * nvalues) return;
+  const uint32_t c = (uint32_t)(i / nvalues), v = (uint32_t)(i % nvalues);
+  const double* src = jac_raw + (uint64_t)c * per_cand * kq;
+  double e = 0.0;
+  for (uint32_t q = 0; q < kq; ++q) {
+    double s = 0.0;
+    for (uint32_t t = inv_off[v]; t < inv_off[v + 1]; ++t) s += src[(uint64_t)inv_idx[t] * kq + q];
+    jac[i * kq + q] = s;
+    if (q % 3u == 0u) e += params[(uint64_t)c * kq + q] * s;
+  }
+  expected[i] = e;
+}
+
 __global__ void k_smooth_grad_sum(const double* __restrict__ part, uint32_t ncand, uint32_t nbins, uint32_t per_bin,
                                   double* __restrict__ grad) {
   const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -348,6 +481,28 @@ int launch_smooth_merge(const double* e_raw, uint32_t ncand, uint32_t per_cand, 
   if (n == 0) return 0;
   k_smooth_merge<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(e_raw, ncand, per_cand, inv_off,
                                                                               inv_idx, nvalues, expected);
+  return (int)cudaGetLastError();
+}
+
+int launch_smooth_jacobian(const SmoothArgs& A, const double* params, uint32_t ncand, const uint32_t* inv_off,
+                           const uint32_t* inv_idx, uint32_t nvalues, double* jac_raw, double* expected,
+                           double* jacobian, void* stream) {
+  cudaStream_t st = (cudaStream_t)stream;
+  const uint32_t kq = A.ntypes * 3u;
+  const uint64_t n = (uint64_t)ncand * nvalues;
+  if (n == 0) return 0;
+  if (A.nbins == 0) {
+    cudaError_t e = cudaMemsetAsync(expected, 0, n * sizeof(double), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(jacobian, 0, n * kq * sizeof(double), st);
+    return (int)e;
+  }
+  const int smem = (int)(4u * A.rows * kThreads * sizeof(float));
+  const cudaError_t e = cudaFuncSetAttribute(k_smooth_jacobian, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return (int)e;
+  const dim3 grid(A.nbins, (ncand + 31u) / 32u, A.ntypes);
+  k_smooth_jacobian<<<grid, kThreads, smem, st>>>(A, params, ncand, jac_raw);
+  k_smooth_jacobian_merge<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(jac_raw, params, ncand, A.nbins * A.rows, kq,
+                                                                      inv_off, inv_idx, nvalues, expected, jacobian);
   return (int)cudaGetLastError();
 }
 

@@ -3,8 +3,10 @@
 A target histogram is produced by the plain (stochastic, exact) form at hidden parameters
 drawn from a seed. Candidates are scored by
     L = sum_v (log(1 + E_v) - log(1 + C_v))^2
-(E the candidate's counts, C the target counts), and searched three ways from the same
+(E the candidate's counts, C the target counts), and searched four ways from the same
 random starting population:
+  * Levenberg-Marquardt on the smoothed form: residuals and their Jacobian from one pass of
+    the forward-mode Jacobian kernel per iteration (pc_smooth_jacobian);
   * gradient descent on the smoothed form: Adam on unconstrained coordinates, gradients
     from the smoothed form's adjoint kernel through procell.smooth.expected_counts;
   * a particle swarm on the smoothed form (forward passes only);
@@ -15,7 +17,7 @@ Each search keeps its best parameters over time; afterwards every snapshot is sc
 one accurate common loss (the smoothed form with many lineages per cell, another seed), so
 the searches are compared on the same scale.
 
-    python -m procell.calibrate [--candidates 256] [--seed 7] [--gd-iters 300] [--pso-seconds 40]
+    python -m procell.calibrate [--candidates 256] [--seed 7] [--lm-iters 40] [--gd-iters 300] [--pso-seconds 40]
 """
 from __future__ import annotations
 
@@ -157,6 +159,64 @@ def gradient_descent(prob, theta0, iters=150, lr=0.1, lr_end=0.002, time_limit=N
     return trace, snaps
 
 
+def levenberg_marquardt(prob, theta0, iters=40, lam0=1e-2, max_step=1.0, time_limit=None):
+    """Levenberg-Marquardt from every candidate at once on the residuals r_v = log(1 + E_v) -
+    log(1 + C_v) of the smoothed form. One pass of the Jacobian kernel per iteration gives
+    the residuals and their Jacobian at the trial point; a candidate keeps its step if its
+    loss falls (damping / 3) and otherwise stays where it was (damping x 4). Steps solve
+    (J^T J + lam diag(J^T J)) d = -J^T r per candidate (9 x 9 for three types)."""
+    lo, hi = prob.box()
+    n, K = theta0.shape[0], theta0.shape[1]
+    P = 3 * K
+    eye = torch.eye(P, dtype=torch.float64, device=theta0.device)
+    tgt = torch.log1p(prob.target)
+
+    def evaluate(th):
+        prm = prob.params(th)
+        E, JP = prob.smooth.jacobian(prm)
+        r_ = torch.softmax(th[..., 0], dim=1)[:, None, :]     # [n, 1, K]
+        m_, sd_ = prm[..., 1][:, None, :], prm[..., 2][:, None, :]
+        Jr = JP[..., 0]
+        Ja = r_ * (Jr - (Jr * r_).sum(-1, keepdim=True))      # through the softmax
+        Jb = JP[..., 1] * m_ + JP[..., 2] * sd_                 # mean = e^b, sd = mean e^c
+        Jc = JP[..., 2] * sd_
+        J = torch.stack([Ja, Jb, Jc], dim=-1).reshape(n, -1, P) / (1.0 + E)[..., None]
+        res = torch.log1p(E) - tgt
+        return res, J, (res * res).sum(1)
+
+    th = theta0.clone()
+    lam = torch.full((n,), lam0, dtype=torch.float64, device=th.device)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    res, J, f = evaluate(th)
+    i = int(torch.argmin(f))
+    best = float(f[i])
+    trace = [(time.perf_counter() - t0, best)]
+    snaps = [(trace[0][0], th[i].clone())]
+    for _ in range(iters):
+        A = J.transpose(1, 2) @ J
+        g = (J * res[..., None]).sum(1)
+        d = torch.diagonal(A, dim1=1, dim2=2)
+        Ad = A + torch.diag_embed(lam[:, None] * d) + 1e-12 * d.amax(1)[:, None, None] * eye
+        step = torch.linalg.solve(Ad, -g[..., None])[..., 0].clamp(-max_step, max_step)
+        th_new = torch.minimum(torch.maximum(th + step.reshape(n, K, 3), lo - 2.0), hi + 2.0)
+        res2, J2, f2 = evaluate(th_new)
+        ok = f2 < f  # NaN losses are never accepted
+        th = torch.where(ok[:, None, None], th_new, th)
+        res = torch.where(ok[:, None], res2, res)
+        J = torch.where(ok[:, None, None], J2, J)
+        f = torch.where(ok, f2, f)
+        lam = torch.where(ok, lam / 3.0, lam * 4.0).clamp(1e-7, 1e7)
+        i = int(torch.argmin(f))
+        if float(f[i]) < best:
+            best = float(f[i])
+            snaps.append((time.perf_counter() - t0, th[i].clone()))
+        trace.append((time.perf_counter() - t0, best))
+        if time_limit and trace[-1][0] > time_limit:
+            break
+    return trace, snaps
+
+
 def particle_swarm(prob, theta0, iters=150, w=0.7298, c1=1.49618, c2=1.49618, seed=1, time_limit=None,
                    loss=None):
     """Particle swarm with constriction coefficients and a ring neighbourhood (each particle
@@ -217,21 +277,24 @@ def first_below(trace, level):
     return None
 
 
-def compare(engine, candidates=256, seed=7, gd_iters=300, pso_seconds=40.0, paths=2):
-    """Gradient descent on the smoothed form against particle swarms (on the smoothed form
-    and on the plain simulator through the batched form), all from one population, all
-    scored afterwards with the same accurate loss. The headline level is the worse of the
-    plain-simulator swarm's and gradient descent's final accurate losses (a level both
-    reach); the ratio is the swarm's time to reach it over gradient descent's."""
+def compare(engine, candidates=256, seed=7, gd_iters=300, pso_seconds=40.0, paths=2, lm_iters=40):
+    """Derivative-based searches on the smoothed form (Levenberg-Marquardt with the forward-
+    mode Jacobian; Adam with the adjoint gradient) against particle swarms (on the smoothed
+    form, and on the plain simulator through the batched form), all from one population,
+    all scored afterwards with the same accurate loss. The headline level is the worse of
+    the plain-simulator swarm's and Levenberg-Marquardt's final accurate losses (a level
+    both reach); the ratio is the swarm's time to reach it over Levenberg-Marquardt's."""
     prob = Problem(engine, seed=seed, paths=paths)
     theta0 = prob.start(candidates, seed)
-    gradient_descent(prob, theta0, iters=3)  # warm-up of every code path
+    levenberg_marquardt(prob, theta0, iters=3)  # warm-up of every code path
+    gradient_descent(prob, theta0, iters=3)
     particle_swarm(prob, theta0, iters=3)
     particle_swarm(prob, theta0, iters=2, loss=prob.loss_plain)
+    lm, lm_snaps = levenberg_marquardt(prob, theta0, iters=lm_iters)
     gd, gd_snaps = gradient_descent(prob, theta0, iters=gd_iters)
     ps, ps_snaps = particle_swarm(prob, theta0, iters=1_000_000, time_limit=pso_seconds)
     pp, pp_snaps = particle_swarm(prob, theta0, iters=1_000_000, time_limit=pso_seconds, loss=prob.loss_plain)
-    acc_gd, acc_ps, acc_pp = (accurate_trace(prob, x) for x in (gd_snaps, ps_snaps, pp_snaps))
+    acc_lm, acc_gd, acc_ps, acc_pp = (accurate_trace(prob, x) for x in (lm_snaps, gd_snaps, ps_snaps, pp_snaps))
     with torch.no_grad():
         hidden = torch.tensor([prob.hidden], dtype=torch.float64, device="cuda")
         th_h = torch.stack([torch.log(hidden[0, :, 0]), torch.log(hidden[0, :, 1]),
@@ -241,20 +304,25 @@ def compare(engine, candidates=256, seed=7, gd_iters=300, pso_seconds=40.0, path
     def best_final(tr):
         return min(l for _, l in tr)
 
-    head = max(best_final(acc_pp), best_final(acc_gd))
+    head = max(best_final(acc_pp), best_final(acc_lm))
     levels = sorted({head, 1.05 * head, 1.2 * head, 1.5 * head, l_true}, reverse=True)
     table = []
     for L in levels:
-        tg, tp, ts = first_below(acc_gd, L), first_below(acc_pp, L), first_below(acc_ps, L)
-        table.append({"accurate_loss": L, "gd_seconds": tg, "pso_plain_seconds": tp, "pso_smooth_seconds": ts,
-                      "ratio_plain": (tp / tg) if (tg and tp) else None,
-                      "ratio_smooth": (ts / tg) if (tg and ts) else None})
-    tg, tp = first_below(acc_gd, head), first_below(acc_pp, head)
+        tl, tg = first_below(acc_lm, L), first_below(acc_gd, L)
+        tp, ts = first_below(acc_pp, L), first_below(acc_ps, L)
+        table.append({"accurate_loss": L, "lm_seconds": tl, "gd_seconds": tg, "pso_plain_seconds": tp,
+                      "pso_smooth_seconds": ts, "ratio_plain": (tp / tl) if (tl and tp) else None,
+                      "ratio_smooth": (ts / tl) if (tl and ts) else None})
+    tl, tp = first_below(acc_lm, head), first_below(acc_pp, head)
     return {
         "candidates": candidates,
         "lineages_per_cell": paths,
         "hidden": prob.hidden,
         "accurate_loss_at_hidden": l_true,
+        "lm": {"iters": len(lm) - 1, "seconds": lm[-1][0], "best_smoothed_loss": lm[-1][1],
+               "best_accurate_loss": best_final(acc_lm),
+               "seconds_per_iter": lm[-1][0] / max(1, len(lm) - 1),
+               "method": "Levenberg-Marquardt on the smoothed form, Jacobian kernel (one pass per iteration)"},
         "gd": {"iters": len(gd), "seconds": gd[-1][0], "best_smoothed_loss": gd[-1][1],
                "best_accurate_loss": best_final(acc_gd), "method": "Adam on the smoothed form, cosine lr 0.1 -> 0.002"},
         "pso_smooth": {"iters": len(ps) - 1, "seconds": ps[-1][0], "best_smoothed_loss": ps[-1][1],
@@ -264,11 +332,12 @@ def compare(engine, candidates=256, seed=7, gd_iters=300, pso_seconds=40.0, path
                       "best_accurate_loss": best_final(acc_pp),
                       "method": "particle swarm on the plain simulator, candidates as one pc_simulate_batch"},
         "equal_loss": head,
-        "equal_loss_is": "accurate loss both gradient descent and the plain-simulator swarm reach",
-        "gd_seconds_to_equal_loss": tg,
+        "equal_loss_is": "accurate loss both Levenberg-Marquardt and the plain-simulator swarm reach",
+        "gradient_seconds_to_equal_loss": tl,
         "pso_seconds_to_equal_loss": tp,
-        "speedup": (tp / tg) if (tg and tp) else None,
+        "speedup": (tp / tl) if (tl and tp) else None,
         "levels": table,
+        "traces": {"lm": acc_lm, "gd": acc_gd, "pso_plain": acc_pp},
     }
 
 
@@ -279,10 +348,11 @@ def main():
     ap.add_argument("--gd-iters", type=int, default=300)
     ap.add_argument("--pso-seconds", type=float, default=40.0)
     ap.add_argument("--paths", type=int, default=2)
+    ap.add_argument("--lm-iters", type=int, default=40)
     a = ap.parse_args()
     from . import Engine
     eng = Engine(0)
-    print(json.dumps(compare(eng, a.candidates, a.seed, a.gd_iters, a.pso_seconds, a.paths)))
+    print(json.dumps(compare(eng, a.candidates, a.seed, a.gd_iters, a.pso_seconds, a.paths, a.lm_iters)))
 
 
 if __name__ == "__main__":

@@ -63,6 +63,19 @@ class Smooth:
                                                             ctypes.c_void_p(out.data_ptr())))
         return out
 
+    def jacobian(self, params: torch.Tensor):
+        """(expected [C, n_values], jacobian [C, n_values, n_types, 3]) in one pass:
+        jacobian[c, v, k] = d expected[c, v] / d (ratio, mean, sd) of type k."""
+        p = params.detach().to(torch.float64).contiguous()
+        assert p.is_cuda and p.dim() == 3 and p.shape[1] == self.n_types and p.shape[2] == 3
+        E = torch.empty(p.shape[0], self.n_values, dtype=torch.float64, device=p.device)
+        J = torch.empty(p.shape[0], self.n_values, self.n_types, 3, dtype=torch.float64, device=p.device)
+        self._bind_stream()
+        self.engine._check(self.engine.L.pc_smooth_jacobian(self.engine.ctx, self.handle, ctypes.c_void_p(p.data_ptr()),
+                                                            p.shape[0], ctypes.c_void_p(E.data_ptr()),
+                                                            ctypes.c_void_p(J.data_ptr())))
+        return E, J
+
     def sync(self):
         self.engine._check(self.engine.L.pc_smooth_sync(self.engine.ctx))
 

@@ -227,7 +227,10 @@ int pc_batch_autotune(pc_context* ctx, pc_batch* batch, uint32_t repeats, pc_tun
  * grad_expected: device array [n_candidates][n_values], dL/d expected
  * grad_params:   device array [n_candidates][n_types][3], dL/d params (the adjoint: the
  *                lineages are walked again, every normal regenerated from its counter)
- * Both calls are asynchronous on the context's stream; pc_smooth_sync waits and reports. */
+ * jacobian:      device array [n_candidates][n_values][n_types][3], d expected[c][v] /
+ *                d params[c][k][.] (forward-mode tangents in the same single pass that also
+ *                writes `expected`; for Gauss-Newton / Levenberg-Marquardt searches)
+ * The calls are asynchronous on the context's stream; pc_smooth_sync waits and reports. */
 typedef struct pc_smooth pc_smooth;
 int pc_smooth_create(pc_context* ctx, const pc_bin* bins, uint64_t n_bins, uint32_t n_types,
                      double t_max, double phi, double h, uint32_t paths_per_cell, uint64_t seed,
@@ -238,6 +241,8 @@ int pc_smooth_forward(pc_context* ctx, pc_smooth* s, const double* params, uint3
                       double* expected);
 int pc_smooth_backward(pc_context* ctx, pc_smooth* s, const double* params, uint32_t n_candidates,
                        const double* grad_expected, double* grad_params);
+int pc_smooth_jacobian(pc_context* ctx, pc_smooth* s, const double* params, uint32_t n_candidates,
+                       double* expected, double* jacobian);
 int pc_smooth_sync(pc_context* ctx);
 void pc_smooth_destroy(pc_smooth* s);
 

@@ -56,9 +56,10 @@ def prepare(bins, phi):
     return out, sorted(vals), thr
 
 
-def forward_backward(bins, t_max, phi, h, paths, seed, params, grad_expected=None):
+def forward_backward(bins, t_max, phi, h, paths, seed, params, grad_expected=None, with_jacobian=False):
     """Expected counts [C][V] for params [C][K][3], and, with grad_expected [C][V], the
-    gradient [C][K][3] of sum(grad_expected * expected)."""
+    gradient [C][K][3] of sum(grad_expected * expected). with_jacobian: also the Jacobian
+    [C][V][K][3] of the expected counts (returned fourth)."""
     rows, values, thr = prepare(bins, phi)
     ncells = sum(f for _, f, _, _ in rows)
     vindex = {v: i for i, v in enumerate(values)}
@@ -66,6 +67,7 @@ def forward_backward(bins, t_max, phi, h, paths, seed, params, grad_expected=Non
     C, K = P.shape[0], P.shape[1]
     E = np.zeros((C, len(values)))
     G = np.zeros((C, K, 3))
+    J = np.zeros((C, len(values), K, 3)) if with_jacobian else None
     k0, k1 = seed & 0xFFFFFFFF, seed >> 32
     for (v, f, cap, r0) in rows:
         vi = []
@@ -93,6 +95,8 @@ def forward_backward(bins, t_max, phi, h, paths, seed, params, grad_expected=Non
                                 E[c, vi[0]] += ratio / paths
                                 if grad_expected is not None:
                                     G[c, k, 0] += grad_expected[c, vi[0]] / paths
+                                if J is not None:
+                                    J[c, vi[0], k, 0] += 1.0 / paths
                             continue
                         if mu == 0:
                             sd = 0.0
@@ -115,6 +119,10 @@ def forward_backward(bins, t_max, phi, h, paths, seed, params, grad_expected=Non
                             g = j - 1
                             if vi[g] >= 0:
                                 E[c, vi[g]] += ratio * 2.0 ** g * w / paths
+                                if J is not None:
+                                    s = math.exp(ls)
+                                    J[c, vi[g], k, 0] += 2.0 ** g * w / paths
+                                    J[c, vi[g], k, 1:] += ratio * 2.0 ** g * w / paths * (D + s / h * dS)
                                 if grad_expected is not None:
                                     a = grad_expected[c, vi[g]] * 2.0 ** g * w / paths
                                     G[c, k, 0] += a
@@ -125,4 +133,6 @@ def forward_backward(bins, t_max, phi, h, paths, seed, params, grad_expected=Non
                             logp += ls
                             if logp < -100.0:
                                 break
+    if with_jacobian:
+        return E, G, np.array(values), J
     return E, G, np.array(values)

@@ -194,6 +194,28 @@ def test_smooth_restatement_adjoint_matches_central_differences(oracle_lib):
             assert abs(G[0, k, q] - fd) <= 1e-5 * max(1.0, abs(fd)), (k, q, G[0, k, q], fd)
 
 
+def test_smooth_restatement_jacobian(oracle_lib):
+    """The restatement's Jacobian contracts to its adjoint and matches central differences
+    of its own forward, column by column."""
+    import smooth_ref
+    bins = [(640.0, 12), (37.0, 9), (3.0, 5)]
+    params = np.array([[[0.6, 30.0, 6.0], [0.4, 45.0, 18.0]]])
+    nv = len(smooth_ref.prepare(bins, 1.0)[1])
+    gE = np.random.default_rng(2).normal(size=(1, nv))
+    E, G, _, J = smooth_ref.forward_backward(bins, 150.0, 1.0, 0.5, 3, 99, params, gE, with_jacobian=True)
+    assert np.allclose(np.einsum("cv,cvkq->ckq", gE, J), G, rtol=1e-12, atol=1e-12 * np.abs(G).max())
+    for k in range(2):
+        for q in range(3):
+            d = 1e-6 * abs(params[0, k, q])
+            P1, P2 = params.copy(), params.copy()
+            P1[0, k, q] += d
+            P2[0, k, q] -= d
+            E1, _, _ = smooth_ref.forward_backward(bins, 150.0, 1.0, 0.5, 3, 99, P1)
+            E2, _, _ = smooth_ref.forward_backward(bins, 150.0, 1.0, 0.5, 3, 99, P2)
+            fd = (E1 - E2)[0] / (2 * d)
+            assert np.linalg.norm(J[0, :, k, q] - fd) <= 1e-5 * max(1.0, np.linalg.norm(fd)), (k, q)
+
+
 def test_smooth_restatement_replica_zero_is_the_plain_tree(oracle_lib):
     """With one lineage per cell and h -> 0, a cell's smoothed weight is an unbiased estimate
     of its own plain-form tree: enumerating every path reproduces the oracle's counts."""

@@ -190,6 +190,64 @@ def test_matches_cpu_restatement(engine):
     assert np.allclose(G, G_ref, rtol=2e-5, atol=1e-7 * np.abs(G_ref).max()), (G, G_ref)
 
 
+def test_jacobian_matches_cpu_restatement_and_adjoint(engine):
+    """The forward-mode Jacobian kernel: its expected counts equal the forward kernel's, its
+    contraction with any upstream gradient equals the adjoint, and it matches the FP64 CPU
+    restatement entry by entry."""
+    import smooth_ref
+    from procell.smooth import Smooth
+    bins = [(640.0, 60), (37.0, 45), (3.0, 20), (1500.0, 0), (9.5, 30), (0.7, 10)]
+    t_max, phi, h, paths, seed = 150.0, 1.0, 0.5, 2, 987654321
+    params = [[[0.5, 30.0, 6.0], [0.3, 45.0, 18.0], [0.2, -1.0, -1.0]],
+              [[0.6, 25.0, 12.0], [0.4, 0.0, 1.0], [0.0, 40.0, 4.0]]]
+    sm = Smooth(engine, bins, n_types=3, t_max=t_max, phi=phi, h=h, paths=paths, seed=seed)
+    gE = np.random.default_rng(1).normal(size=(2, sm.n_values))
+    E_ref, G_ref, vals, J_ref = smooth_ref.forward_backward(bins, t_max, phi, h, paths, seed, params, gE,
+                                                            with_jacobian=True)
+    assert np.array_equal(vals, sm.values)
+    P = params_tensor(params)
+    E, J = sm.jacobian(P)
+    E_fwd = sm.forward(P)
+    G = sm.backward(P, torch.tensor(gE, device="cuda"))
+    sm.sync()
+    sm.close()
+    E, J, E_fwd, G = (x.cpu().numpy() for x in (E, J, E_fwd, G))
+    assert np.allclose(J, J_ref, rtol=2e-5, atol=1e-7 * np.abs(J_ref).max()), np.abs(J - J_ref).max()
+    assert np.allclose(E, E_ref, rtol=2e-5, atol=1e-9 * np.abs(E_ref).max())
+    assert np.allclose(E, E_fwd, rtol=1e-5, atol=1e-9 * np.abs(E).max())
+    GJ = np.einsum("cv,cvkq->ckq", gE, J)
+    assert np.allclose(GJ, G, rtol=1e-4, atol=1e-6 * np.abs(G).max()), (GJ, G)
+    # the ratio column of a zero-ratio type is still its (unscaled) contribution
+    assert J[1, :, 2, 0].sum() > 0 and np.all(J[1, :, 2, 1:] == 0)
+
+
+def test_jacobian_matches_central_differences(smooth_setup):
+    sm, _ = smooth_setup
+    P = params_tensor(BASE)
+    E, J = sm.jacobian(P)
+    C, K = P.shape[0], P.shape[1]
+    rows, steps = [], []
+    for c in range(C):
+        for k in range(K):
+            for q in range(3):
+                d = 1e-4 * abs(float(P[c, k, q]))
+                for sgn in (1.0, -1.0):
+                    Q = P[c].clone()
+                    Q[k, q] += sgn * d
+                    rows.append(Q)
+                steps.append(d)
+    Ef = sm.forward(torch.stack(rows)).cpu().numpy()
+    sm.sync()
+    fd = ((Ef[0::2] - Ef[1::2]) / (2.0 * np.array(steps))[:, None]).reshape(C, K, 3, -1).transpose(0, 3, 1, 2)
+    J = J.cpu().numpy()
+    assert np.all(np.isfinite(J))
+    # every Jacobian column (candidate, type, parameter) against its central difference, in
+    # norm over the values (single entries of the difference carry the forward's FP32
+    # rounding divided by the step)
+    err = np.linalg.norm(J - fd, axis=1) / np.linalg.norm(fd, axis=1)
+    assert np.all(err <= 1e-3), err
+
+
 def test_converges_to_plain_expectation(engine):
     """With many lineages per cell (independent replicas) and a small h, the expected counts
     approach the plain form's histogram averaged over seeds."""
