@@ -139,7 +139,8 @@ def gradient_descent(prob, theta0, iters=150, lr=0.1, lr_end=0.002, time_limit=N
     theta = theta0.clone().requires_grad_(True)
     opt = torch.optim.Adam([theta], lr=lr)
     trace, best = [], float("inf")
-    torch.cuda.synchronize()
+    if theta.is_cuda:
+        torch.cuda.synchronize()
     t0 = time.perf_counter()
     snaps = []
     for it in range(iters):
@@ -148,15 +149,33 @@ def gradient_descent(prob, theta0, iters=150, lr=0.1, lr_end=0.002, time_limit=N
         opt.zero_grad(set_to_none=True)
         L = prob.loss(theta)
         L.sum().backward()
-        i = int(torch.argmin(L.detach()))
-        if float(L[i]) < best:
-            best = float(L[i])
+        Ld = L.detach()
+        i = int(torch.argmin(Ld))
+        if float(Ld[i]) < best:
+            best = float(Ld[i])
             snaps.append((time.perf_counter() - t0, theta.detach()[i].clone()))
         opt.step()
         trace.append((time.perf_counter() - t0, best))
         if time_limit and trace[-1][0] > time_limit:
             break
     return trace, snaps
+
+
+def residual_jacobian(prob, th):
+    """Residuals r [n, V] = log(1 + E) - log(1 + C) at theta [n, K, 3] and their Jacobian
+    [n, V, 3K] in theta (ratio logits, log mean, log cv; index 3k + q), from one pass of
+    the smoothed form's Jacobian kernel and the chain rule through prob.params."""
+    n, K = th.shape[0], th.shape[1]
+    prm = prob.params(th)
+    E, JP = prob.smooth.jacobian(prm)
+    r_ = torch.softmax(th[..., 0], dim=1)[:, None, :]     # [n, 1, K]
+    m_, sd_ = prm[..., 1][:, None, :], prm[..., 2][:, None, :]
+    Jr = JP[..., 0]
+    Ja = r_ * (Jr - (Jr * r_).sum(-1, keepdim=True))      # through the softmax
+    Jb = JP[..., 1] * m_ + JP[..., 2] * sd_                 # mean = e^b, sd = mean e^c
+    Jc = JP[..., 2] * sd_
+    J = torch.stack([Ja, Jb, Jc], dim=-1).reshape(n, -1, 3 * K) / (1.0 + E)[..., None]
+    return torch.log1p(E) - torch.log1p(prob.target), J
 
 
 def levenberg_marquardt(prob, theta0, iters=40, lam0=1e-2, max_step=1.0, time_limit=None):
@@ -169,24 +188,15 @@ def levenberg_marquardt(prob, theta0, iters=40, lam0=1e-2, max_step=1.0, time_li
     n, K = theta0.shape[0], theta0.shape[1]
     P = 3 * K
     eye = torch.eye(P, dtype=torch.float64, device=theta0.device)
-    tgt = torch.log1p(prob.target)
 
     def evaluate(th):
-        prm = prob.params(th)
-        E, JP = prob.smooth.jacobian(prm)
-        r_ = torch.softmax(th[..., 0], dim=1)[:, None, :]     # [n, 1, K]
-        m_, sd_ = prm[..., 1][:, None, :], prm[..., 2][:, None, :]
-        Jr = JP[..., 0]
-        Ja = r_ * (Jr - (Jr * r_).sum(-1, keepdim=True))      # through the softmax
-        Jb = JP[..., 1] * m_ + JP[..., 2] * sd_                 # mean = e^b, sd = mean e^c
-        Jc = JP[..., 2] * sd_
-        J = torch.stack([Ja, Jb, Jc], dim=-1).reshape(n, -1, P) / (1.0 + E)[..., None]
-        res = torch.log1p(E) - tgt
+        res, J = residual_jacobian(prob, th)
         return res, J, (res * res).sum(1)
 
     th = theta0.clone()
     lam = torch.full((n,), lam0, dtype=torch.float64, device=th.device)
-    torch.cuda.synchronize()
+    if th.is_cuda:
+        torch.cuda.synchronize()
     t0 = time.perf_counter()
     res, J, f = evaluate(th)
     i = int(torch.argmin(f))
@@ -223,13 +233,14 @@ def particle_swarm(prob, theta0, iters=150, w=0.7298, c1=1.49618, c2=1.49618, se
     follows the best of itself and its two neighbours), the standard choice for multimodal
     objectives; particles stay in the search box."""
     loss = loss or prob.loss
-    g = torch.Generator(device="cuda").manual_seed(seed)
+    g = torch.Generator(device=theta0.device).manual_seed(seed)
     lo, hi = prob.box()
     x = theta0.clone()
     vel = torch.zeros_like(x)
     vmax = 0.5 * (hi - lo)
     with torch.no_grad():
-        torch.cuda.synchronize()
+        if x.is_cuda:
+            torch.cuda.synchronize()
         t0 = time.perf_counter()
         fx = loss(x)
         pbest, pf = x.clone(), fx.clone()
