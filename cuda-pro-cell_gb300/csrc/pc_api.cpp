@@ -1501,7 +1501,7 @@ struct pc_smooth {
   int32_t* vidx_dev = nullptr;
   uint32_t* inv_off_dev = nullptr;
   uint32_t* inv_idx_dev = nullptr;
-  double* e_raw_dev = nullptr;   // [cand_cap][nbins][rows]
+  double* e_raw_dev = nullptr;   // [cand_cap][ntypes][nbins][rows]
   double* part_dev = nullptr;    // [cand_cap][nbins][ntypes * 3]
   uint32_t cand_cap = 0;
   double* jac_raw_dev = nullptr;  // [jac_cap][nbins][rows][ntypes * 3], allocated on first use
@@ -1537,7 +1537,7 @@ int smooth_scratch(pc_context* ctx, pc_smooth* s, uint32_t ncand) {
   s->part_dev = nullptr;
   s->cand_cap = 0;
   const size_t nb = std::max<size_t>(1, s->I.bin_value.size());
-  PC_CUDA(ctx, cudaMalloc(&s->e_raw_dev, (size_t)ncand * nb * s->rows * sizeof(double)));
+  PC_CUDA(ctx, cudaMalloc(&s->e_raw_dev, (size_t)ncand * s->ntypes * nb * s->rows * sizeof(double)));
   PC_CUDA(ctx, cudaMalloc(&s->part_dev, (size_t)ncand * nb * s->ntypes * 3 * sizeof(double)));
   s->cand_cap = ncand;
   return PC_OK;
@@ -1657,8 +1657,8 @@ int pc_smooth_forward(pc_context* ctx, pc_smooth* s, const double* params, uint3
   const SmoothArgs A = smooth_args(ctx, s);
   const uint32_t nv = (uint32_t)s->I.values.size();
   PC_CUDA(ctx, (cudaError_t)launch_smooth_forward(A, params, n_candidates, s->e_raw_dev, ctx->stream));
-  PC_CUDA(ctx, (cudaError_t)launch_smooth_merge(s->e_raw_dev, n_candidates, A.nbins * A.rows, s->inv_off_dev,
-                                                s->inv_idx_dev, nv, expected, ctx->stream));
+  PC_CUDA(ctx, (cudaError_t)launch_smooth_merge(s->e_raw_dev, n_candidates, A.ntypes, A.nbins * A.rows,
+                                                s->inv_off_dev, s->inv_idx_dev, nv, expected, ctx->stream));
   return PC_OK;
 }
 

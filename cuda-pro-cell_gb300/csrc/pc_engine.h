@@ -191,13 +191,14 @@ struct SmoothArgs {
   uint32_t* error;            // bit 1: sampler round budget exhausted
 };
 
-// e_raw[c][b][g] (FP64) for params[c][k][3] = (ratio, mean, sd).
+// e_raw[c][k][b][g] (FP64) for params[c][k][3] = (ratio, mean, sd): type k's part.
 int launch_smooth_forward(const SmoothArgs& A, const double* params, uint32_t ncand, double* e_raw,
                           void* stream);
-// expected[c][v] = sum of e_raw[c][b][g] over the (b, g) of value v (CSR lists inv_off/inv_idx,
-// inv_idx = b * rows + g).
-int launch_smooth_merge(const double* e_raw, uint32_t ncand, uint32_t per_cand, const uint32_t* inv_off,
-                        const uint32_t* inv_idx, uint32_t nvalues, double* expected, void* stream);
+// expected[c][v] = sum of e_raw[c][k][b][g] over the types and the (b, g) of value v (CSR
+// lists inv_off/inv_idx, inv_idx = b * rows + g; per_type = nbins * rows).
+int launch_smooth_merge(const double* e_raw, uint32_t ncand, uint32_t ntypes, uint32_t per_type,
+                        const uint32_t* inv_off, const uint32_t* inv_idx, uint32_t nvalues, double* expected,
+                        void* stream);
 // grad_params[c][k][3] = d(sum_v grad_expected[c][v] * expected[c][v]) / d params[c][k][.],
 // regenerating every normal from its Philox counter; vidx[b][g] maps rows to values (-1: none).
 int launch_smooth_backward(const SmoothArgs& A, const double* params, uint32_t ncand, const double* grad_expected,

@@ -26,14 +26,15 @@
 // gradients A_g = dL/dE_g, regenerating every z from its counter (nothing of the forward pass
 // is stored).
 //
-// Work layout: one block per (bin, group of 32 candidates); lane l of every warp is
+// Work layout: one block per (bin, group of 32 candidates, type); lane l of every warp is
 // candidate 32 * group + l, and the block's 4 warps take the bin's lineages 32 at a time:
 // first each lane draws one lineage's normals (one Philox block and ziggurat draw per
 // generation) into shared memory, then every lane walks all 32 lineages for its own
-// candidate, reading the shared draws. Each normal is thus drawn once per 32 candidates.
-// Remaining time R = T - S is carried in FP64 (three FP64 operations per step: the division
-// time, R, and the FP64 accumulation). Per-thread partial sums live in shared memory and are
-// reduced over the warps in a fixed order, so results are deterministic.
+// candidate, reading the shared draws. Each normal is thus drawn once per 32 candidates and
+// type. Remaining time R = T - S is carried in FP64 (two FP64 operations per step: the
+// division time and R; GB300's FP64 pipe bounds these kernels). Per-thread partial sums
+// (compensated FP32) live in shared memory and are reduced over the warps in a fixed order,
+// and the types are added in a fixed order by the merge, so results are deterministic.
 #include <cuda_runtime.h>
 
 #include "pc_engine.h"
@@ -244,6 +245,7 @@ __global__ void __launch_bounds__(kThreads) k_smooth_jacobian(const SmoothArgs A
   extern __shared__ float facc[];
   __shared__ ZigTables Z;
   __shared__ double u_age[kThreads];
+  __shared__ float u_one[kThreads];
   constexpr uint32_t kWarps = kThreads / 32;
   const uint32_t b = blockIdx.x, k = blockIdx.z;
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
@@ -260,6 +262,7 @@ __global__ void __launch_bounds__(kThreads) k_smooth_jacobian(const SmoothArgs A
     mu = params[(uint64_t)c * KQ + 3u * k + 1u];
     sd = params[(uint64_t)c * KQ + 3u * k + 2u];
   }
+  const bool quiescent = mu < 0.0, fixed_tau = mu == 0.0;
   __syncthreads();
   const uint32_t steps = __ldg(A.bin_cap + b) + 1u;
   const uint64_t r0 = __ldg(A.bin_start + b), r1 = __ldg(A.bin_start + b + 1);
@@ -267,16 +270,19 @@ __global__ void __launch_bounds__(kThreads) k_smooth_jacobian(const SmoothArgs A
   const float inv_h = (float)A.inv_h;
   const uint64_t nlin = (r1 - r0) * A.paths;
   for (uint64_t base = (uint64_t)warp * 32u; base < nlin; base += 32u * kWarps) {
-    if (base + lane < nlin) draw_lineage(A, Z, r0, base + lane, steps, zbuf + lane, u_age[threadIdx.x]);
+    if (base + lane < nlin) {
+      draw_lineage(A, Z, r0, base + lane, steps, zbuf + lane, u_age[threadIdx.x]);
+      u_one[threadIdx.x] = __double2float_rn(1.0 + u_age[threadIdx.x]);
+    }
     __syncwarp();
     const uint32_t n = (uint32_t)((nlin - base) < 32u ? (nlin - base) : 32u);
     if (live) {
       for (uint32_t ii = 0; ii < n; ++ii) {
-        if (mu < 0.0) {
+        if (quiescent) {
           fmy[0] += 1.0f;  // quiescent type: a leaf at generation 0 (cell.cu:69-75)
         } else {
-          const double ua = u_age[warp * 32u + ii];
-          walk_jacobian(A, zbuf + ii, ua, __double2float_rn(1.0 + ua), inv_h, steps, mu, sd, mu == 0.0, fmy);
+          walk_jacobian(A, zbuf + ii, u_age[warp * 32u + ii], u_one[warp * 32u + ii], inv_h, steps, mu, sd,
+                        fixed_tau, fmy);
         }
       }
     }
@@ -296,35 +302,31 @@ __global__ void __launch_bounds__(kThreads) k_smooth_jacobian(const SmoothArgs A
   }
 }
 
+// Forward (e_raw[c][k][b][g] = ratio_k / paths * sum 2^g w_g over the bin's lineages) and
+// adjoint (part[c][b][3k + q] = d(sum_g A_g E_g)/d(ratio_k, mean_k, sd_k)) of one type: block
+// (bin, group of 32 candidates, type k). Every block draws its bin's lineages itself.
 template <bool Backward>
 __global__ void __launch_bounds__(kThreads) k_smooth(const SmoothArgs A, const double* __restrict__ params,
                                                      uint32_t ncand, const double* __restrict__ grad_expected,
                                                      uint32_t nvalues, const int32_t* __restrict__ vidx,
                                                      double* __restrict__ out) {
   // dynamic: compensated FP32 accumulator pairs [arows][kThreads] (forward: 2 per generation
-  // row, backward: 2 per (type, parameter)), then the lineage draws z [kWarps][rows][32]
+  // row, backward: 2 per parameter), then the lineage draws z [kWarps][rows][32]
   extern __shared__ float facc[];
   __shared__ ZigTables Z;
-  __shared__ double prm[32][kSmoothMaxTypes * 3];
-  __shared__ float wsplit[32][kSmoothMaxTypes * 2];  // ratio / paths as a pair of floats
   __shared__ float Ag2[Backward ? 32 : 1][kSmoothMaxRows];
   __shared__ double u_age[kThreads];
+  __shared__ float u_one[kThreads];
   constexpr uint32_t kWarps = kThreads / 32;
-  const uint32_t b = blockIdx.x;
+  const uint32_t b = blockIdx.x, k = blockIdx.z;
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   const uint32_t c = blockIdx.y * 32u + lane;
   const bool live = c < ncand;
-  const uint32_t K = A.ntypes;
-  const uint32_t nrows = Backward ? K * 3 : A.rows;  // output rows
-  const uint32_t arows = 2u * nrows;                  // accumulator rows (sum, compensation)
+  const uint32_t KQ = A.ntypes * 3u;
+  const uint32_t arows = Backward ? 6u : 2u * A.rows;
   float* zbuf = facc + (size_t)arows * kThreads + (size_t)warp * A.rows * 32u;
   for (uint32_t i = threadIdx.x; i < sizeof(ZigTables) / 4; i += blockDim.x)
     reinterpret_cast<uint32_t*>(&Z)[i] = __ldg(reinterpret_cast<const uint32_t*>(A.zig) + i);
-  for (uint32_t i = threadIdx.x; i < 32u * K * 3u; i += blockDim.x) {
-    const uint32_t l = i / (K * 3u), q = i % (K * 3u);
-    const uint32_t cc = blockIdx.y * 32u + l;
-    prm[l][q] = cc < ncand ? params[(uint64_t)cc * K * 3 + q] : 0.0;
-  }
   for (uint32_t i = 0; i < arows; ++i) facc[i * kThreads + threadIdx.x] = 0.0f;
   const uint32_t cap = __ldg(A.bin_cap + b);
   const uint32_t steps = cap + 1u;
@@ -340,84 +342,90 @@ __global__ void __launch_bounds__(kThreads) k_smooth(const SmoothArgs A, const d
       Ag2[l][g] = (float)a;
     }
   }
-  __syncthreads();
-  for (uint32_t i = threadIdx.x; i < 32u * K; i += blockDim.x) {
-    const uint32_t l = i / K, k = i % K;
-    const double wt = prm[l][3 * k] / (double)A.paths;
-    const float hi = __double2float_rn(wt);
-    wsplit[l][2 * k] = hi;
-    wsplit[l][2 * k + 1] = __double2float_rn(wt - (double)hi);
+  const double* my_prm = params + (uint64_t)(live ? c : 0u) * KQ + 3u * k;
+  const double mu = live ? my_prm[1] : 0.0, sd = live ? my_prm[2] : 0.0;
+  // ratio / paths as a pair of floats (the forward's weight)
+  float w_hi = 0.0f, w_lo = 0.0f;
+  if (!Backward && live) {
+    const double wt = my_prm[0] / (double)A.paths;
+    w_hi = __double2float_rn(wt);
+    w_lo = __double2float_rn(wt - (double)w_hi);
   }
+  const bool quiescent = mu < 0.0, fixed_tau = mu == 0.0;
+  const bool walks = Backward || w_hi != 0.0f;
   __syncthreads();
   const uint64_t r0 = __ldg(A.bin_start + b), r1 = __ldg(A.bin_start + b + 1);
-  const double inv_paths = 1.0 / (double)A.paths;
   float* fmy = facc + threadIdx.x;
   const float inv_h = (float)A.inv_h;
-  const double* my_prm = prm[lane];
   const float* my_ag = Backward ? Ag2[lane] : nullptr;
   // lineage i of the bin: initial cell r0 + i / paths, replica i % paths
   const uint64_t nlin = (r1 - r0) * A.paths;
   for (uint64_t base = (uint64_t)warp * 32u; base < nlin; base += 32u * kWarps) {
     // this lane draws lineage base + lane
-    if (base + lane < nlin) draw_lineage(A, Z, r0, base + lane, steps, zbuf + lane, u_age[threadIdx.x]);
+    if (base + lane < nlin) {
+      draw_lineage(A, Z, r0, base + lane, steps, zbuf + lane, u_age[threadIdx.x]);
+      u_one[threadIdx.x] = __double2float_rn(1.0 + u_age[threadIdx.x]);
+    }
     __syncwarp();
     const uint32_t n = (uint32_t)((nlin - base) < 32u ? (nlin - base) : 32u);
     if (live) {
       for (uint32_t ii = 0; ii < n; ++ii) {
-        const float* z = zbuf + ii;
-        const double ua = u_age[warp * 32u + ii];
-        const float u1 = __double2float_rn(1.0 + ua);
-        for (uint32_t k = 0; k < K; ++k) {
-          const double mu = my_prm[3 * k + 1], sd = my_prm[3 * k + 2];
-          const float w_hi = wsplit[lane][2 * k], w_lo = wsplit[lane][2 * k + 1];
-          float f_r = 0.0f, f_mu = 0.0f, f_sig = 0.0f;  // this lineage's adjoint terms
-          if (mu < 0.0) {
-            // quiescent type: a leaf at generation 0 (cell.cu:69-75)
-            if constexpr (Backward) {
-              f_r = my_ag[0];
-            } else {
-              kahan_add(fmy, w_hi);
-              fmy[kThreads] = __fsub_rn(fmy[kThreads], w_lo);
-            }
-          } else if (Backward || w_hi != 0.0f) {
-            walk<Backward>(A, z, ua, u1, inv_h, steps, mu, sd, mu == 0.0, w_hi, w_lo, fmy, my_ag, f_r, f_mu, f_sig);
-          }
+        float f_r = 0.0f, f_mu = 0.0f, f_sig = 0.0f;  // this lineage's adjoint terms
+        if (quiescent) {
+          // quiescent type: a leaf at generation 0 (cell.cu:69-75)
           if constexpr (Backward) {
-            // per-thread compensated FP32 sums (terms of either sign cancel); scaled by
-            // ratio / paths once, at the end
-            kahan_add(fmy + (6 * k) * kThreads, f_r);
-            kahan_add(fmy + (6 * k + 2) * kThreads, f_mu);
-            kahan_add(fmy + (6 * k + 4) * kThreads, f_sig);
+            f_r = my_ag[0];
+          } else {
+            kahan_add(fmy, w_hi);
+            fmy[kThreads] = __fsub_rn(fmy[kThreads], w_lo);
           }
+        } else if (walks) {
+          walk<Backward>(A, zbuf + ii, u_age[warp * 32u + ii], u_one[warp * 32u + ii], inv_h, steps, mu, sd,
+                         fixed_tau, w_hi, w_lo, fmy, my_ag, f_r, f_mu, f_sig);
+        }
+        if constexpr (Backward) {
+          // per-thread compensated FP32 sums (terms of either sign cancel); scaled by
+          // ratio / paths once, at the end
+          kahan_add(fmy, f_r);
+          kahan_add(fmy + 2 * kThreads, f_mu);
+          kahan_add(fmy + 4 * kThreads, f_sig);
         }
       }
     }
     __syncwarp();
   }
   __syncthreads();
-  // out[c][b][row] = sum over the warps, in warp order (adjoint rows scaled by
-  // 1 / paths, and those of mean and sd by the ratio)
-  if (warp == 0 && live) {
-    double* o = out + ((uint64_t)c * A.nbins + b) * nrows;
-    for (uint32_t q = 0; q < nrows; ++q) {
-      double v = 0.0;
+  // sums over the warps in warp order (adjoint rows scaled by 1 / paths, and those of mean
+  // and sd by the ratio); lane l of every warp holds candidate 32 * group + l, so the warps
+  // split the rows
+  if (!live) return;
+  const double inv_paths = 1.0 / (double)A.paths, ratio = my_prm[0];
+  const uint32_t nrows = Backward ? 3u : A.rows;
+  double* o = Backward ? out + ((uint64_t)c * A.nbins + b) * KQ + 3u * k
+                       : out + (((uint64_t)c * A.ntypes + k) * A.nbins + b) * A.rows;
+  for (uint32_t q = warp; q < nrows; q += kWarps) {
+    double v = 0.0;
 #pragma unroll
-      for (uint32_t w = 0; w < kWarps; ++w)
-        v += (double)facc[2 * q * kThreads + w * 32u + lane] - (double)facc[(2 * q + 1) * kThreads + w * 32u + lane];
-      if constexpr (Backward) v *= (q % 3u == 0u ? 1.0 : my_prm[q - q % 3u]) * inv_paths;
-      o[q] = v;
-    }
+    for (uint32_t w = 0; w < kWarps; ++w)
+      v += (double)facc[2 * q * kThreads + w * 32u + lane] - (double)facc[(2 * q + 1) * kThreads + w * 32u + lane];
+    if constexpr (Backward) v *= (q == 0u ? 1.0 : ratio) * inv_paths;
+    o[q] = v;
   }
 }
 
-__global__ void k_smooth_merge(const double* __restrict__ e_raw, uint32_t ncand, uint32_t per_cand,
+// expected[c][v] = sum over types k and the (b, g) of value v of e_raw[c][k][b][g]
+// (per_type = nbins * rows).
+__global__ void k_smooth_merge(const double* __restrict__ e_raw, uint32_t ncand, uint32_t ntypes, uint32_t per_type,
                                const uint32_t* __restrict__ inv_off, const uint32_t* __restrict__ inv_idx,
                                uint32_t nvalues, double* __restrict__ expected) {
   const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= (uint64_t)ncand * nvalues) return;
   const uint32_t c = (uint32_t)(i / nvalues), v = (uint32_t)(i % nvalues);
   double s = 0.0;
-  for (uint32_t q = inv_off[v]; q < inv_off[v + 1]; ++q) s += e_raw[(uint64_t)c * per_cand + inv_idx[q]];
+  for (uint32_t k = 0; k < ntypes; ++k) {
+    const double* src = e_raw + ((uint64_t)c * ntypes + k) * per_type;
+    for (uint32_t q = inv_off[v]; q < inv_off[v + 1]; ++q) s += src[inv_idx[q]];
+  }
   expected[i] = s;
 }
 
@@ -451,7 +459,8 @@ __global__ void k_smooth_grad_sum(const double* __restrict__ part, uint32_t ncan
   grad[i] = s;
 }
 
-// acc rows x kThreads doubles + the lineage draws (kThreads floats per generation row)
+// accumulator pairs (2 floats per output row and thread) + the lineage draws (kThreads
+// floats per generation row)
 int smem_bytes(uint32_t out_rows, uint32_t rows) {
   return (int)((2u * out_rows + rows) * kThreads * sizeof(float));
 }
@@ -459,11 +468,11 @@ int smem_bytes(uint32_t out_rows, uint32_t rows) {
 template <bool Backward>
 int launch_smooth_t(const SmoothArgs& A, const double* params, uint32_t ncand, const double* grad_expected,
                     uint32_t nvalues, const int32_t* vidx, double* out, cudaStream_t st) {
-  const int smem = smem_bytes(Backward ? A.ntypes * 3u : A.rows, A.rows);
+  const int smem = smem_bytes(Backward ? 3u : A.rows, A.rows);
   // static shared memory plus `smem` may exceed the default 48 KB: always opt in
   const cudaError_t e = cudaFuncSetAttribute(k_smooth<Backward>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return (int)e;
-  const dim3 grid(A.nbins, (ncand + 31u) / 32u);
+  const dim3 grid(A.nbins, (ncand + 31u) / 32u, A.ntypes);
   k_smooth<Backward><<<grid, kThreads, smem, st>>>(A, params, ncand, grad_expected, nvalues, vidx, out);
   return (int)cudaGetLastError();
 }
@@ -475,12 +484,13 @@ int launch_smooth_forward(const SmoothArgs& A, const double* params, uint32_t nc
   return launch_smooth_t<false>(A, params, ncand, nullptr, 0, nullptr, e_raw, (cudaStream_t)stream);
 }
 
-int launch_smooth_merge(const double* e_raw, uint32_t ncand, uint32_t per_cand, const uint32_t* inv_off,
-                        const uint32_t* inv_idx, uint32_t nvalues, double* expected, void* stream) {
+int launch_smooth_merge(const double* e_raw, uint32_t ncand, uint32_t ntypes, uint32_t per_type,
+                        const uint32_t* inv_off, const uint32_t* inv_idx, uint32_t nvalues, double* expected,
+                        void* stream) {
   const uint64_t n = (uint64_t)ncand * nvalues;
   if (n == 0) return 0;
-  k_smooth_merge<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(e_raw, ncand, per_cand, inv_off,
-                                                                              inv_idx, nvalues, expected);
+  k_smooth_merge<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(e_raw, ncand, ntypes, per_type,
+                                                                              inv_off, inv_idx, nvalues, expected);
   return (int)cudaGetLastError();
 }
 
