@@ -1267,6 +1267,47 @@ int pc_simulate(pc_context* ctx, const pc_bin* bins, uint64_t n_bins, const pc_c
   return rc;
 }
 
+int pc_simulate_shard(pc_context* ctx, const pc_bin* bins, uint64_t n_bins, const pc_cell_type* types,
+                      uint32_t n_types, double t_max, double phi, uint64_t seed, uint64_t root_begin,
+                      uint64_t root_end, pc_histogram* out) {
+  pc_plan* p = nullptr;
+  int rc = pc_plan_create(ctx, bins, n_bins, types, n_types, t_max, phi, seed, &p);
+  if (rc != PC_OK) return rc;
+  rc = pc_plan_set_roots(ctx, p, root_begin, root_end);
+  if (rc == PC_OK) rc = pc_plan_run(ctx, p);
+  if (rc == PC_OK) rc = pc_plan_result(ctx, p, out);
+  pc_plan_destroy(p);
+  return rc;
+}
+
+int pc_histogram_accumulate(pc_histogram* dst, const pc_histogram* src) {
+  if (!dst || !src) return PC_ERR_INVALID;
+  if (dst->n_values != src->n_values || dst->n_types != src->n_types) return PC_ERR_INVALID;
+  const uint64_t nv = dst->n_values;
+  if (nv && (!dst->values || !src->values || !dst->totals || !src->totals || !dst->per_type || !src->per_type))
+    return PC_ERR_INVALID;
+  for (uint64_t v = 0; v < nv; ++v)
+    if (std::memcmp(&dst->values[v], &src->values[v], sizeof(double)) != 0) return PC_ERR_INVALID;
+  for (uint64_t v = 0; v < nv; ++v) dst->totals[v] += src->totals[v];
+  for (uint64_t i = 0; i < nv * dst->n_types; ++i) dst->per_type[i] += src->per_type[i];
+  pc_stats& a = dst->stats;
+  const pc_stats& b = src->stats;
+  a.roots += b.roots;
+  a.divisions += b.divisions;
+  a.leaves += b.leaves;
+  a.uncounted += b.uncounted;
+  a.vanished += b.vanished;
+  a.max_generation = std::max(a.max_generation, b.max_generation);
+  a.sweeps += b.sweeps;
+  a.root_sweeps += b.root_sweeps;
+  a.kernel_launches += b.kernel_launches;
+  a.device_ms += b.device_ms;
+  a.divide_ms += b.divide_ms;
+  a.h2d_bytes += b.h2d_bytes;
+  a.d2h_bytes += b.d2h_bytes;
+  return PC_OK;
+}
+
 int pc_batch_create(pc_context* ctx, const pc_instance* instances, uint32_t n_instances, pc_batch** out) {
   if (!ctx || !out || (n_instances && !instances)) return fail(ctx, PC_ERR_INVALID, "null argument");
   *out = nullptr;

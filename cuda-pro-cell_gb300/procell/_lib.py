@@ -80,6 +80,10 @@ SIGNATURES = [
                                    ctypes.POINTER(CellType), ctypes.c_uint32, ctypes.c_double,
                                    ctypes.c_double, ctypes.c_uint64, ctypes.POINTER(Histogram)]),
     ("pc_histogram_free", None, [ctypes.POINTER(Histogram)]),
+    ("pc_simulate_shard", ctypes.c_int, [VP, ctypes.POINTER(Bin), ctypes.c_uint64, ctypes.POINTER(CellType),
+                                         ctypes.c_uint32, ctypes.c_double, ctypes.c_double, ctypes.c_uint64,
+                                         ctypes.c_uint64, ctypes.c_uint64, ctypes.POINTER(Histogram)]),
+    ("pc_histogram_accumulate", ctypes.c_int, [ctypes.POINTER(Histogram), ctypes.POINTER(Histogram)]),
     ("pc_batch_create", ctypes.c_int, [VP, ctypes.POINTER(Instance), ctypes.c_uint32, ctypes.POINTER(VP)]),
     ("pc_batch_run", ctypes.c_int, [VP, VP]),
     ("pc_batch_stats", ctypes.c_int, [VP, VP, ctypes.POINTER(Stats)]),

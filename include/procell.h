@@ -149,6 +149,18 @@ int pc_simulate(pc_context* ctx, const pc_bin* bins, uint64_t n_bins, const pc_c
                 uint32_t n_types, double t_max, double phi, uint64_t seed, pc_histogram* out);
 void pc_histogram_free(pc_histogram* h);
 
+/* Sharding (one process or GPU per shard): pc_simulate on initial cells [root_begin,
+ * root_end) of the file order only. Every shard's histogram has the full value set, and
+ * the shards' histograms added with pc_histogram_accumulate equal the unsharded one bit for
+ * bit (the random stream is keyed by initial cell, not by shard). */
+int pc_simulate_shard(pc_context* ctx, const pc_bin* bins, uint64_t n_bins, const pc_cell_type* types,
+                      uint32_t n_types, double t_max, double phi, uint64_t seed, uint64_t root_begin,
+                      uint64_t root_end, pc_histogram* out);
+/* dst += src: totals, per-type counts and statistics (summed; max_generation the larger).
+ * Both must hold the same value set and type count (else PC_ERR_INVALID, dst unchanged).
+ * Host only. */
+int pc_histogram_accumulate(pc_histogram* dst, const pc_histogram* src);
+
 /* ---- Batched form (no counterpart in the reference, which runs one input per process) --
  * Many independent inputs ("instances": each its own histogram, cell types, t_max, phi
  * and seed) run together: their initial cells are laid end to end and every sweep

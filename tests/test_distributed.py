@@ -89,3 +89,37 @@ def test_engine_shards_sum_to_full_run(engine):
     full = engine.simulate(w.bins, w.types, w.t_max, w.phi, w.seed)
     assert np.array_equal(sum(p.per_type for p in parts), full.per_type)
     assert sum(p.stats["divisions"] for p in parts) == full.stats["divisions"]
+
+
+@pytest.mark.gpu
+def test_simulate_shard_and_accumulate_through_the_c_abi(engine):
+    """pc_simulate_shard over four uneven shards, added with pc_histogram_accumulate, equals
+    pc_simulate on the whole input bit for bit (the small workload)."""
+    import ctypes
+    import procell.configs as cfg
+    from procell import _lib
+    w = cfg.small()
+    b, t = _lib.bins_numpy(w.bins), _lib.types_numpy(w.types)
+    bp, tp = b.ctypes.data_as(ctypes.POINTER(_lib.Bin)), t.ctypes.data_as(ctypes.POINTER(_lib.CellType))
+    L = engine.L
+    full = _lib.Histogram()
+    engine._check(L.pc_simulate(engine.ctx, bp, len(b), tp, len(t), w.t_max, w.phi, w.seed, ctypes.byref(full)))
+    n = int(b["frequency"].sum())
+    cuts = [0, 1, n // 5, n // 2 + 7, n]
+    acc = None
+    for lo, hi in zip(cuts, cuts[1:]):
+        h = _lib.Histogram()
+        engine._check(L.pc_simulate_shard(engine.ctx, bp, len(b), tp, len(t), w.t_max, w.phi, w.seed, lo, hi,
+                                          ctypes.byref(h)))
+        if acc is None:
+            acc = h
+        else:
+            assert L.pc_histogram_accumulate(ctypes.byref(acc), ctypes.byref(h)) == 0
+            L.pc_histogram_free(ctypes.byref(h))
+    fv, ft, fp, fs = _lib.histogram_to_numpy(full)
+    av, at, ap, ast = _lib.histogram_to_numpy(acc)
+    L.pc_histogram_free(ctypes.byref(full))
+    L.pc_histogram_free(ctypes.byref(acc))
+    assert np.array_equal(fv, av) and np.array_equal(ft, at) and np.array_equal(fp, ap)
+    for k in ("roots", "divisions", "leaves", "uncounted", "vanished", "max_generation"):
+        assert fs[k] == ast[k], k

@@ -152,3 +152,43 @@ def test_log_space_and_rebin_follow_the_reference(built):
         rebin(np.array([5000.0]), np.array([1], np.uint64), 1.0, 1000.0, 4)
     with pytest.raises(ProcellError):
         rebin(np.array([5.0, 2.0]), np.array([1, 1], np.uint64), 1.0, 1000.0, 4)
+
+
+def _histogram(values, totals, per_type, **stats):
+    from procell import _lib
+    v = np.ascontiguousarray(values, dtype=np.float64)
+    t = np.ascontiguousarray(totals, dtype=np.uint64)
+    p = np.ascontiguousarray(per_type, dtype=np.uint64)
+    h = _lib.Histogram()
+    h.n_values, h.n_types = len(v), p.shape[1]
+    h.values = v.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    h.totals = t.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64))
+    h.per_type = p.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64))
+    for k, x in stats.items():
+        setattr(h.stats, k, x)
+    return h, (v, t, p)
+
+
+def test_histogram_accumulate(built):
+    """pc_histogram_accumulate (host only): shard histograms add element-wise; statistics
+    add (max_generation: the larger); a different value set or type count is refused and
+    leaves the destination unchanged."""
+    from procell import _lib
+    L = _lib.load()
+    vals = [1.0, 2.5, 5.0]
+    a, keep_a = _histogram(vals, [3, 0, 7], [[1, 2], [0, 0], [3, 4]], roots=5, divisions=9, leaves=10,
+                           max_generation=4, sweeps=3, device_ms=1.5)
+    b, keep_b = _histogram(vals, [2, 1, 2**40], [[2, 0], [1, 0], [2**39, 2**39]], roots=2, divisions=1, leaves=3,
+                           max_generation=7, sweeps=2, device_ms=0.25)
+    assert L.pc_histogram_accumulate(ctypes.byref(a), ctypes.byref(b)) == 0
+    assert list(keep_a[1]) == [5, 1, 7 + 2**40]
+    assert keep_a[2].tolist() == [[3, 2], [1, 0], [3 + 2**39, 4 + 2**39]]
+    assert (a.stats.roots, a.stats.divisions, a.stats.leaves, a.stats.max_generation, a.stats.sweeps) == (7, 10, 13, 7, 5)
+    assert a.stats.device_ms == 1.75
+    before = keep_a[1].copy()
+    c, keep_c = _histogram([1.0, 2.5, 5.000000001], [1, 1, 1], [[1, 0], [1, 0], [1, 0]])
+    assert L.pc_histogram_accumulate(ctypes.byref(a), ctypes.byref(c)) == 1
+    d, keep_d = _histogram(vals, [1, 1, 1], [[1], [1], [1]])
+    assert L.pc_histogram_accumulate(ctypes.byref(a), ctypes.byref(d)) == 1
+    assert np.array_equal(keep_a[1], before)
+    assert L.pc_histogram_accumulate(None, ctypes.byref(a)) == 1
