@@ -135,23 +135,16 @@ __device__ __forceinline__ void walk(const SmoothArgs& A, const float* z, double
                                      uint32_t steps, double mu, double sigma, bool fixed_tau, float w_hi,
                                      float w_lo, float* acc, const float* Ag2, float& f_r, float& f_mu,
                                      float& f_sig) {
-  double R = 0.0;                 // T - S_j
-  float log_p = 0.0f;             // log s_1 ... s_{j-1}
-  float dmu = 0.0f, dsig = 0.0f;  // dS_j / d(mean, sd)
+  // step 1 (the first division, S_1 = tau_1 (1 + U)) is peeled off the loop, so every later
+  // step costs two FP64 operations (the division time and R) and no select
+  float zj = fixed_tau ? 0.0f : z[0];
+  double tau = fixed_tau ? 0.0 : fma(sigma, f32_to_f64_bits(zj), mu);
+  double R = A.t_max - fma(tau, u_age, tau);  // T - S_j
+  float dmu = u1, dsig = zj * u1;             // dS_j / d(mean, sd)
+  float log_p = 0.0f;                         // log s_1 ... s_{j-1}
   float D_mu = 0.0f, D_sig = 0.0f;
-  float wh = w_hi, wl = w_lo;     // weight * 2^(j-1) as a pair of floats
-  for (uint32_t j = 1; j <= steps; ++j) {
-    const float zj = fixed_tau ? 0.0f : z[(j - 1) * 32u];
-    const double tau = fixed_tau ? 0.0 : fma(sigma, f32_to_f64_bits(zj), mu);
-    if (j == 1) {
-      R = A.t_max - fma(tau, u_age, tau);
-      dmu = u1;
-      dsig = zj * dmu;
-    } else {
-      R = R - tau;
-      dmu += 1.0f;
-      dsig += zj;
-    }
+  float wh = w_hi, wl = w_lo;                 // weight * 2^(j-1) as a pair of floats
+  for (uint32_t j = 1;;) {
     const float x = f64_to_f32_rz_any(R) * inv_h;
     float ls, l1m;
     log_sig(x, ls, l1m);
@@ -186,7 +179,12 @@ __device__ __forceinline__ void walk(const SmoothArgs& A, const float* z, double
       }
     }
     log_p += ls;
-    if (log_p < kLogNegligible) break;
+    if (log_p < kLogNegligible || ++j > steps) break;
+    zj = fixed_tau ? 0.0f : z[(j - 1) * 32u];
+    tau = fixed_tau ? 0.0 : fma(sigma, f32_to_f64_bits(zj), mu);
+    R = R - tau;
+    dmu += 1.0f;
+    dsig += zj;
   }
 }
 
@@ -195,21 +193,14 @@ __device__ __forceinline__ void walk(const SmoothArgs& A, const float* z, double
 __device__ __forceinline__ void walk_jacobian(const SmoothArgs& A, const float* z, double u_age, float u1,
                                               float inv_h, uint32_t steps, double mu, double sigma, bool fixed_tau,
                                               float* acc) {
-  double R = 0.0;
-  float log_p = 0.0f, dmu = 0.0f, dsig = 0.0f, D_mu = 0.0f, D_sig = 0.0f;
+  // step 1 peeled off the loop as in walk()
+  float zj = fixed_tau ? 0.0f : z[0];
+  double tau = fixed_tau ? 0.0 : fma(sigma, f32_to_f64_bits(zj), mu);
+  double R = A.t_max - fma(tau, u_age, tau);
+  float dmu = u1, dsig = zj * u1;
+  float log_p = 0.0f, D_mu = 0.0f, D_sig = 0.0f;
   float scale = 1.0f;  // 2^(j-1)
-  for (uint32_t j = 1; j <= steps; ++j) {
-    const float zj = fixed_tau ? 0.0f : z[(j - 1) * 32u];
-    const double tau = fixed_tau ? 0.0 : fma(sigma, f32_to_f64_bits(zj), mu);
-    if (j == 1) {
-      R = A.t_max - fma(tau, u_age, tau);
-      dmu = u1;
-      dsig = zj * dmu;
-    } else {
-      R = R - tau;
-      dmu += 1.0f;
-      dsig += zj;
-    }
+  for (uint32_t j = 1;;) {
     const float x = f64_to_f32_rz_any(R) * inv_h;
     float ls, l1m;
     log_sig(x, ls, l1m);
@@ -231,7 +222,12 @@ __device__ __forceinline__ void walk_jacobian(const SmoothArgs& A, const float* 
     }
     scale *= 2.0f;
     log_p += ls;
-    if (log_p < kLogNegligible) break;
+    if (log_p < kLogNegligible || ++j > steps) break;
+    zj = fixed_tau ? 0.0f : z[(j - 1) * 32u];
+    tau = fixed_tau ? 0.0 : fma(sigma, f32_to_f64_bits(zj), mu);
+    R = R - tau;
+    dmu += 1.0f;
+    dsig += zj;
   }
 }
 
