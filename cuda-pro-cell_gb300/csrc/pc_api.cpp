@@ -1547,6 +1547,8 @@ struct pc_smooth {
   uint32_t cand_cap = 0;
   double* jac_raw_dev = nullptr;  // [jac_cap][nbins][rows][ntypes * 3], allocated on first use
   uint32_t jac_cap = 0;
+  uint32_t* order_dev = nullptr;  // [ntypes][order_cap]: candidates by mean, per type
+  uint32_t order_cap = 0;
 };
 
 namespace {
@@ -1567,10 +1569,23 @@ SmoothArgs smooth_args(const pc_context* ctx, const pc_smooth* s) {
   A.bin_cap = s->bin_cap_dev;
   A.zig = ctx->zig_dev;
   A.error = ctx->error_dev;
+  A.order = s->order_dev;
   return A;
 }
 
+int order_scratch(pc_context* ctx, pc_smooth* s, uint32_t ncand) {
+  if (ncand <= s->order_cap) return PC_OK;
+  cudaFree(s->order_dev);
+  s->order_dev = nullptr;
+  s->order_cap = 0;
+  PC_CUDA(ctx, cudaMalloc(&s->order_dev, (size_t)ncand * s->ntypes * sizeof(uint32_t)));
+  s->order_cap = ncand;
+  return PC_OK;
+}
+
 int smooth_scratch(pc_context* ctx, pc_smooth* s, uint32_t ncand) {
+  const int rc = order_scratch(ctx, s, ncand);
+  if (rc != PC_OK) return rc;
   if (ncand <= s->cand_cap) return PC_OK;
   cudaFree(s->e_raw_dev);
   cudaFree(s->part_dev);
@@ -1585,6 +1600,8 @@ int smooth_scratch(pc_context* ctx, pc_smooth* s, uint32_t ncand) {
 }
 
 int jacobian_scratch(pc_context* ctx, pc_smooth* s, uint32_t ncand) {
+  const int rc = order_scratch(ctx, s, ncand);
+  if (rc != PC_OK) return rc;
   if (ncand <= s->jac_cap) return PC_OK;
   cudaFree(s->jac_raw_dev);
   s->jac_raw_dev = nullptr;
@@ -1752,6 +1769,7 @@ void pc_smooth_destroy(pc_smooth* s) {
   cudaFree(s->e_raw_dev);
   cudaFree(s->part_dev);
   cudaFree(s->jac_raw_dev);
+  cudaFree(s->order_dev);
   delete s;
 }
 

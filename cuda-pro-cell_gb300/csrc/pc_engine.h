@@ -189,6 +189,7 @@ struct SmoothArgs {
   const uint32_t* bin_cap;    // [nbins]
   const ZigTables* zig;
   uint32_t* error;            // bit 1: sampler round budget exhausted
+  uint32_t* order;            // [ntypes][ncand] scratch: the candidates of each type by mean
 };
 
 // e_raw[c][k][b][g] (FP64) for params[c][k][3] = (ratio, mean, sd): type k's part.

@@ -235,7 +235,7 @@ __device__ __forceinline__ void walk_jacobian(const SmoothArgs& A, const float* 
 // = (sum 2^g w_g / paths, ratio_k / paths * sum 2^g dw_g/dmean, the same for sd), i.e.
 // d E_{b,g} / d(ratio_k, mean_k, sd_k); every block draws its bin's lineages itself (the
 // draws are shared by the 32 candidates of a warp, not across types).
-__global__ void __launch_bounds__(kThreads) k_smooth_jacobian(const SmoothArgs A, const double* __restrict__ params,
+__global__ void __launch_bounds__(kThreads, 5) k_smooth_jacobian(const SmoothArgs A, const double* __restrict__ params,
                                                               uint32_t ncand, double* __restrict__ out) {
   // dynamic: per-thread sums [3 * rows][kThreads], then the lineage draws [kWarps][rows][32]
   extern __shared__ float facc[];
@@ -245,8 +245,9 @@ __global__ void __launch_bounds__(kThreads) k_smooth_jacobian(const SmoothArgs A
   constexpr uint32_t kWarps = kThreads / 32;
   const uint32_t b = blockIdx.x, k = blockIdx.z;
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-  const uint32_t c = blockIdx.y * 32u + lane;
-  const bool live = c < ncand;
+  const uint32_t slot = blockIdx.y * 32u + lane;
+  const bool live = slot < ncand;
+  const uint32_t c = live ? A.order[(uint64_t)k * ncand + slot] : 0u;
   const uint32_t KQ = A.ntypes * 3u;
   float* zbuf = facc + (size_t)3u * A.rows * kThreads + (size_t)warp * A.rows * 32u;
   for (uint32_t i = threadIdx.x; i < sizeof(ZigTables) / 4; i += blockDim.x)
@@ -302,7 +303,7 @@ __global__ void __launch_bounds__(kThreads) k_smooth_jacobian(const SmoothArgs A
 // adjoint (part[c][b][3k + q] = d(sum_g A_g E_g)/d(ratio_k, mean_k, sd_k)) of one type: block
 // (bin, group of 32 candidates, type k). Every block draws its bin's lineages itself.
 template <bool Backward>
-__global__ void __launch_bounds__(kThreads) k_smooth(const SmoothArgs A, const double* __restrict__ params,
+__global__ void __launch_bounds__(kThreads, 5) k_smooth(const SmoothArgs A, const double* __restrict__ params,
                                                      uint32_t ncand, const double* __restrict__ grad_expected,
                                                      uint32_t nvalues, const int32_t* __restrict__ vidx,
                                                      double* __restrict__ out) {
@@ -316,8 +317,9 @@ __global__ void __launch_bounds__(kThreads) k_smooth(const SmoothArgs A, const d
   constexpr uint32_t kWarps = kThreads / 32;
   const uint32_t b = blockIdx.x, k = blockIdx.z;
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-  const uint32_t c = blockIdx.y * 32u + lane;
-  const bool live = c < ncand;
+  const uint32_t slot = blockIdx.y * 32u + lane;
+  const bool live = slot < ncand;
+  const uint32_t c = live ? A.order[(uint64_t)k * ncand + slot] : 0u;
   const uint32_t KQ = A.ntypes * 3u;
   const uint32_t arows = Backward ? 6u : 2u * A.rows;
   float* zbuf = facc + (size_t)arows * kThreads + (size_t)warp * A.rows * 32u;
@@ -329,9 +331,10 @@ __global__ void __launch_bounds__(kThreads) k_smooth(const SmoothArgs A, const d
   if constexpr (Backward) {
     for (uint32_t i = threadIdx.x; i < 32u * kSmoothMaxRows; i += blockDim.x) {
       const uint32_t l = i / kSmoothMaxRows, g = i % kSmoothMaxRows;
-      const uint32_t cc = blockIdx.y * 32u + l;
+      const uint32_t sl = blockIdx.y * 32u + l;
+      const uint32_t cc = sl < ncand ? A.order[(uint64_t)k * ncand + sl] : 0u;
       double a = 0.0;
-      if (cc < ncand && g < A.rows && g <= cap) {
+      if (sl < ncand && g < A.rows && g <= cap) {
         const int32_t v = vidx[(uint64_t)b * A.rows + g];
         if (v >= 0) a = ldexp(grad_expected[(uint64_t)cc * nvalues + v], (int)g);
       }
@@ -409,6 +412,48 @@ __global__ void __launch_bounds__(kThreads) k_smooth(const SmoothArgs A, const d
   }
 }
 
+// A double's bits as an unsigned key in the IEEE total order (NaNs at the ends).
+__device__ __forceinline__ uint64_t order_key(double x) {
+  const uint64_t u = (uint64_t)__double_as_longlong(x);
+  return (u >> 63) ? ~u : (u | (1ull << 63));
+}
+
+// order[k][rank] = candidate: the candidates sorted by type k's mean (ties by index), so the
+// 32 lanes of a warp walk lineages of similar length. Rank by counting, through shared-memory
+// tiles of the keys; a permutation for any input. Above kOrderMax candidates: the identity.
+constexpr uint32_t kOrderMax = 8192;
+__global__ void __launch_bounds__(256) k_smooth_order(const double* __restrict__ params, uint32_t ncand,
+                                                      uint32_t ntypes, uint32_t* __restrict__ order) {
+  __shared__ uint64_t tile[256];
+  const uint32_t k = blockIdx.y;
+  const uint32_t c = blockIdx.x * 256u + threadIdx.x;
+  const uint32_t kq = ntypes * 3u;
+  if (ncand > kOrderMax) {
+    if (c < ncand) order[(uint64_t)k * ncand + c] = c;
+    return;
+  }
+  const uint64_t key = c < ncand ? order_key(params[(uint64_t)c * kq + 3u * k + 1u]) : 0ull;
+  uint32_t rank = 0;
+  for (uint32_t t0 = 0; t0 < ncand; t0 += 256u) {
+    const uint32_t d = t0 + threadIdx.x;
+    tile[threadIdx.x] = d < ncand ? order_key(params[(uint64_t)d * kq + 3u * k + 1u]) : ~0ull;
+    __syncthreads();
+    const uint32_t m = ncand - t0 < 256u ? ncand - t0 : 256u;
+    for (uint32_t j = 0; j < m; ++j) {
+      const uint64_t kd = tile[j];
+      rank += (kd < key || (kd == key && t0 + j < c)) ? 1u : 0u;
+    }
+    __syncthreads();
+  }
+  if (c < ncand) order[(uint64_t)k * ncand + rank] = c;
+}
+
+int launch_order(const SmoothArgs& A, const double* params, uint32_t ncand, cudaStream_t st) {
+  const dim3 grid((ncand + 255u) / 256u, A.ntypes);
+  k_smooth_order<<<grid, 256, 0, st>>>(params, ncand, A.ntypes, A.order);
+  return (int)cudaGetLastError();
+}
+
 // expected[c][v] = sum over types k and the (b, g) of value v of e_raw[c][k][b][g]
 // (per_type = nbins * rows).
 __global__ void k_smooth_merge(const double* __restrict__ e_raw, uint32_t ncand, uint32_t ntypes, uint32_t per_type,
@@ -468,6 +513,8 @@ int launch_smooth_t(const SmoothArgs& A, const double* params, uint32_t ncand, c
   // static shared memory plus `smem` may exceed the default 48 KB: always opt in
   const cudaError_t e = cudaFuncSetAttribute(k_smooth<Backward>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return (int)e;
+  const int eo = launch_order(A, params, ncand, st);
+  if (eo != 0) return eo;
   const dim3 grid(A.nbins, (ncand + 31u) / 32u, A.ntypes);
   k_smooth<Backward><<<grid, kThreads, smem, st>>>(A, params, ncand, grad_expected, nvalues, vidx, out);
   return (int)cudaGetLastError();
@@ -505,6 +552,8 @@ int launch_smooth_jacobian(const SmoothArgs& A, const double* params, uint32_t n
   const int smem = (int)(4u * A.rows * kThreads * sizeof(float));
   const cudaError_t e = cudaFuncSetAttribute(k_smooth_jacobian, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return (int)e;
+  const int eo = launch_order(A, params, ncand, st);
+  if (eo != 0) return eo;
   const dim3 grid(A.nbins, (ncand + 31u) / 32u, A.ntypes);
   k_smooth_jacobian<<<grid, kThreads, smem, st>>>(A, params, ncand, jac_raw);
   k_smooth_jacobian_merge<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(jac_raw, params, ncand, A.nbins * A.rows, kq,
