@@ -692,9 +692,9 @@ def run_calibration(args):
         "roofline": {"bound": "hbm", "achieved": alg / (elapsed_ms * 1e-3 / args.steps) / 1e9, "peak": hbm,
                      "unit": "GB/s", "frac": alg / (elapsed_ms * 1e-3 / args.steps) / 1e9 / hbm,
                      "traffic": None, "peak_source": peak_kind, "kernel": "k_smooth",
-                     "note": "not memory bound: per lineage step one Philox block, a ziggurat draw, an "
-                             "FP64 due time and FP32 log-sigmoids; bytes are inputs and outputs only"},
-        "gpu_launches": 4 * args.steps,
+                     "note": "not memory bound: FP64-pipe bound (due times; 78-84% of the FP64 pipe, "
+                             "profiles/k_smooth_calibration.md); bytes are inputs and outputs only"},
+        "gpu_launches": 6 * args.steps,  # per step: order, forward, merge; order, adjoint, sum
         "clocks": clk,
     }
     if cpu:

@@ -156,6 +156,28 @@ def test_autograd_function_and_determinism(smooth_setup):
     sm.sync()
 
 
+def test_candidate_order_does_not_change_results(smooth_setup):
+    """Kernels visit each type's candidates in order of that type's mean; a candidate's
+    results are the same bits wherever it sits in the batch."""
+    sm, _ = smooth_setup
+    g = torch.Generator(device="cuda").manual_seed(3)
+    n = 70  # not a multiple of 32
+    P = torch.stack([torch.rand(n, 3, generator=g, device="cuda", dtype=torch.float64) * 0.9 + 0.05,
+                     torch.rand(n, 3, generator=g, device="cuda", dtype=torch.float64) * 80.0 + 25.0,
+                     torch.rand(n, 3, generator=g, device="cuda", dtype=torch.float64) * 10.0 + 1.0], dim=-1)
+    P[5, 1, 1] = -1.0   # a quiescent type
+    P[9] = P[4]         # equal means (ties)
+    perm = torch.randperm(n, generator=g, device="cuda")
+    E, Ep = sm.forward(P), sm.forward(P[perm])
+    gE = torch.rand(n, sm.n_values, generator=g, device="cuda", dtype=torch.float64)
+    G, Gp = sm.backward(P, gE), sm.backward(P[perm], gE[perm])
+    (EJ, J), (EJp, Jp) = sm.jacobian(P), sm.jacobian(P[perm])
+    sm.sync()
+    assert torch.equal(E[perm], Ep) and torch.equal(G[perm], Gp)
+    assert torch.equal(EJ[perm], EJp) and torch.equal(J[perm], Jp)
+    assert torch.equal(E[9], E[4])
+
+
 def test_quiescent_type_counts_at_generation_zero(engine):
     from procell.smooth import Smooth
     sm = Smooth(engine, [(100.0, 1000), (0.5, 200)], n_types=2, t_max=50.0, phi=1.0, h=0.5, paths=1, seed=1)
