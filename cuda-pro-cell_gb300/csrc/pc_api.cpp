@@ -873,7 +873,6 @@ RunArgs make_args(const pc_context* ctx, const pc_plan* p) {
     a.t_max = I0.t_max;
     a.t_hi = I0.t_hi;
     a.t_lo = I0.t_lo;
-    a.est_ok = I0.est_ok;
     a.ntypes = (uint32_t)I0.types.size();
     a.fallback = I0.fallback;
     a.types = p->types_dev;

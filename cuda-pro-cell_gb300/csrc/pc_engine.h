@@ -81,7 +81,6 @@ struct RunArgs {
   double t_max;
   float t_hi, t_lo;          // FP32 band around t_max (+-inf when the inputs leave the
                              // FP32 estimate's range: the estimate then never decides)
-  int32_t est_ok;            // FP32 estimate allowed (inputs in range)
   uint32_t ntypes, nbins, fallback;
   uint32_t hist_gens;
   uint32_t g_store_max;      // deepest generation a stored key can hold

@@ -332,7 +332,6 @@ extern "C" int pc_simulate_noalloc(const pc_bin* bins, uint64_t n_bins, const pc
   a.t_max = tmax;
   a.t_hi = std::nextafter((float)(tmax + margin), INFINITY);
   a.t_lo = std::nextafter((float)(tmax - margin), -INFINITY);
-  a.est_ok = est_ok ? 1 : 0;
   if (!est_ok) {  // the estimate decides nothing: every test is exact
     a.t_hi = INFINITY;
     a.t_lo = -INFINITY;
