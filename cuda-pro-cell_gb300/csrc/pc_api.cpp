@@ -410,6 +410,74 @@ namespace {
 // layout of io::load_fluorescences (src/io/parser.cu:68-154), the type table of
 // io::load_cell_types (parser.cu:156-185), and the per-bin phi cap implied by the
 // division test `fluorescence / 2 > threshold` (proliferation.cu:323).
+// The type tables of an instance (I.t_max set): ratio-sum check, stable sort by ratio
+// descending, cumulative ratios in that order (parser.cu:46-66,184; cell.cu:81-104),
+// truncation bounds, the fallback type and the FP32 estimate band. Replaces I's type fields.
+int prepare_types(const pc_cell_type* types, uint32_t n_types, InstanceHost& I, std::string& msg) {
+  if (n_types && !types) return msg = "null argument", PC_ERR_INVALID;
+  if (n_types == 0)
+    return msg = "ERROR: proportion distribution of cell types does not sum to 1, aborting.", PC_ERR_INVALID;
+  if (n_types > (uint32_t)kMaxTypes) return msg = "at most 64 cell types are supported", PC_ERR_UNSUPPORTED;
+  I.types.clear();
+  I.sorted_to_file.clear();
+  double sum = 0.0;
+  for (uint32_t i = 0; i < n_types; ++i) {
+    if (!std::isfinite(types[i].ratio) || !std::isfinite(types[i].mean) || !std::isfinite(types[i].sd))
+      return msg = "cell type parameters must be finite", PC_ERR_INVALID;
+    sum += types[i].ratio;
+  }
+  if (std::fabs(1.0 - sum) > 1.0 / std::pow(10.0, 8.0))
+    return msg = "ERROR: proportion distribution of cell types does not sum to 1, aborting.", PC_ERR_INVALID;
+  std::vector<uint32_t> order(n_types);
+  for (uint32_t i = 0; i < n_types; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](uint32_t a, uint32_t b) { return types[a].ratio > types[b].ratio; });
+  double acc = 0.0;
+  double max_mu = 0.0, max_sig = 0.0;
+  bool est_ok = in_est_range(I.t_max);
+  for (uint32_t s = 0; s < n_types; ++s) {
+    const pc_cell_type& src = types[order[s]];
+    TypeDev t;
+    std::memset(&t, 0, sizeof(t));
+    acc += src.ratio;
+    t.cum = acc;
+    t.mu = src.mean;
+    t.sigma = src.sd;
+    t.mu_f = (float)src.mean;
+    t.sigma_f = (float)src.sd;
+    t.mode = src.mean < 0.0 ? kModeQuiescent : (src.mean == 0.0 ? kModeZeroMean : kModeNormal);
+    truncation_bounds(src.mean, src.sd, t.zlo, t.zhi);
+    if (t.mode == kModeZeroMean) {
+      // tau = 0 for every cell of the type: with sigma = mu = 0, fma(0, z, 0) = +0 for any
+      // z, so the kernels need no special case (and accept every z)
+      t.sigma = 0.0;
+      t.sigma_f = 0.0f;
+      t.zlo = -INFINITY;
+      t.zhi = INFINITY;
+    }
+    if (t.mode == kModeNormal) {
+      max_mu = std::max(max_mu, std::fabs(src.mean));
+      max_sig = std::max(max_sig, std::fabs(src.sd));
+      est_ok = est_ok && in_est_range(src.mean) && in_est_range(src.sd);
+    }
+    I.types.push_back(t);
+    I.sorted_to_file.push_back(order[s]);
+  }
+  I.fallback = 0;
+  for (uint32_t s = 0; s < n_types; ++s)
+    if (types[order[s]].ratio > 0.0) I.fallback = s;
+  // FP32 estimate band: 8x the worst-case error 2^-21 (t_max + |mu| + 9|sigma|).
+  const double margin = std::ldexp(I.t_max + max_mu + 9.0 * max_sig, -18);
+  I.t_hi = std::nextafter((float)(I.t_max + margin), INFINITY);
+  I.t_lo = std::nextafter((float)(I.t_max - margin), -INFINITY);
+  I.est_ok = est_ok ? 1 : 0;
+  if (!est_ok) {  // the estimate decides nothing: every test is exact
+    I.t_hi = INFINITY;
+    I.t_lo = -INFINITY;
+  }
+  return PC_OK;
+}
+
 int prepare_instance(const pc_bin* bins, uint64_t n_bins, const pc_cell_type* types, uint32_t n_types,
                      double t_max, double phi, uint64_t seed, InstanceHost& I, std::string& msg) {
   if ((n_bins && !bins) || (n_types && !types)) return msg = "null argument", PC_ERR_INVALID;
@@ -531,64 +599,40 @@ int prepare_instance(const pc_bin* bins, uint64_t n_bins, const pc_cell_type* ty
     }
   }
 
-  // Cell types: ratio-sum check, stable sort by ratio descending, cumulative ratios in
-  // that order (parser.cu:46-66,184; cell.cu:81-104).
-  double sum = 0.0;
-  for (uint32_t i = 0; i < n_types; ++i) {
-    if (!std::isfinite(types[i].ratio) || !std::isfinite(types[i].mean) || !std::isfinite(types[i].sd))
-      return msg = "cell type parameters must be finite", PC_ERR_INVALID;
-    sum += types[i].ratio;
-  }
-  if (std::fabs(1.0 - sum) > 1.0 / std::pow(10.0, 8.0))
-    return msg = "ERROR: proportion distribution of cell types does not sum to 1, aborting.", PC_ERR_INVALID;
-  std::vector<uint32_t> order(n_types);
-  for (uint32_t i = 0; i < n_types; ++i) order[i] = i;
-  std::stable_sort(order.begin(), order.end(),
-                   [&](uint32_t a, uint32_t b) { return types[a].ratio > types[b].ratio; });
-  double acc = 0.0;
-  double max_mu = 0.0, max_sig = 0.0;
-  bool est_ok = in_est_range(I.t_max);
-  for (uint32_t s = 0; s < n_types; ++s) {
-    const pc_cell_type& src = types[order[s]];
-    TypeDev t;
-    std::memset(&t, 0, sizeof(t));
-    acc += src.ratio;
-    t.cum = acc;
-    t.mu = src.mean;
-    t.sigma = src.sd;
-    t.mu_f = (float)src.mean;
-    t.sigma_f = (float)src.sd;
-    t.mode = src.mean < 0.0 ? kModeQuiescent : (src.mean == 0.0 ? kModeZeroMean : kModeNormal);
-    truncation_bounds(src.mean, src.sd, t.zlo, t.zhi);
-    if (t.mode == kModeZeroMean) {
-      // tau = 0 for every cell of the type: with sigma = mu = 0, fma(0, z, 0) = +0 for any
-      // z, so the kernels need no special case (and accept every z)
-      t.sigma = 0.0;
-      t.sigma_f = 0.0f;
-      t.zlo = -INFINITY;
-      t.zhi = INFINITY;
+  return prepare_types(types, n_types, I, msg);
+}
+
+// The batched form's per-type and per-instance device tables (instances already placed).
+void batch_type_tables(const pc_plan* p, std::vector<BatchType>& btypes, std::vector<InstanceDev>& idev) {
+  btypes.clear();
+  idev.clear();
+  for (uint32_t i = 0; i < (uint32_t)p->inst.size(); ++i) {
+    const InstanceHost& I = p->inst[i];
+    const uint32_t nt = (uint32_t)I.types.size();
+    for (uint32_t k = 0; k < nt; ++k) {
+      BatchType bt;
+      std::memset(&bt, 0, sizeof(bt));
+      bt.t = I.types[k];
+      bt.t_max = I.t_max;
+      bt.t_hi = I.t_hi;
+      bt.t_lo = I.t_lo;
+      bt.k0 = (uint32_t)I.seed;
+      bt.k1 = (uint32_t)(I.seed >> 32);
+      bt.root_begin = I.root_begin;
+      bt.instance = i;
+      btypes.push_back(bt);
     }
-    if (t.mode == kModeNormal) {
-      max_mu = std::max(max_mu, std::fabs(src.mean));
-      max_sig = std::max(max_sig, std::fabs(src.sd));
-      est_ok = est_ok && in_est_range(src.mean) && in_est_range(src.sd);
-    }
-    I.types.push_back(t);
-    I.sorted_to_file.push_back(order[s]);
+    InstanceDev d;
+    std::memset(&d, 0, sizeof(d));
+    d.type_begin = I.type_begin;
+    d.ntypes = nt;
+    d.fallback = I.fallback;
+    d.k0 = (uint32_t)I.seed;
+    d.k1 = (uint32_t)(I.seed >> 32);
+    d.root_begin = I.root_begin;
+    d.t_max = I.t_max;
+    idev.push_back(d);
   }
-  I.fallback = 0;
-  for (uint32_t s = 0; s < n_types; ++s)
-    if (types[order[s]].ratio > 0.0) I.fallback = s;
-  // FP32 estimate band: 8x the worst-case error 2^-21 (t_max + |mu| + 9|sigma|).
-  const double margin = std::ldexp(I.t_max + max_mu + 9.0 * max_sig, -18);
-  I.t_hi = std::nextafter((float)(I.t_max + margin), INFINITY);
-  I.t_lo = std::nextafter((float)(I.t_max - margin), -INFINITY);
-  I.est_ok = est_ok ? 1 : 0;
-  if (!est_ok) {  // the estimate decides nothing: every test is exact
-    I.t_hi = INFINITY;
-    I.t_lo = -INFINITY;
-  }
-  return PC_OK;
 }
 
 // Lays the plan's instances out one after another (initial cells, bins, types, histogram
@@ -652,32 +696,8 @@ int finalize_plan(pc_context* ctx, pc_plan* p) {
       bin_class.push_back((uint32_t)(I.class_begin + b * nt));
     }
     I.hist_gens = std::min(I.gmax, p->g_store_max + 1) + 1;
-    if (p->batched) {
-      for (uint32_t k = 0; k < nt; ++k) {
-        BatchType bt;
-        std::memset(&bt, 0, sizeof(bt));
-        bt.t = I.types[k];
-        bt.t_max = I.t_max;
-        bt.t_hi = I.t_hi;
-        bt.t_lo = I.t_lo;
-        bt.k0 = (uint32_t)I.seed;
-        bt.k1 = (uint32_t)(I.seed >> 32);
-        bt.root_begin = I.root_begin;
-        bt.instance = i;
-        btypes.push_back(bt);
-      }
-      InstanceDev d;
-      std::memset(&d, 0, sizeof(d));
-      d.type_begin = I.type_begin;
-      d.ntypes = nt;
-      d.fallback = I.fallback;
-      d.k0 = (uint32_t)I.seed;
-      d.k1 = (uint32_t)(I.seed >> 32);
-      d.root_begin = I.root_begin;
-      d.t_max = I.t_max;
-      idev.push_back(d);
-    }
   }
+  if (p->batched) batch_type_tables(p, btypes, idev);
 
   // Device copies.
   PC_CUDA(ctx, cudaSetDevice(ctx->device));
@@ -1382,6 +1402,80 @@ int pc_batch_result(pc_context* ctx, pc_batch* b, uint32_t instance, pc_histogra
   rc = instance_result(b, I, h, out, &msg);
   if (rc != PC_OK) return fail(ctx, rc, msg);
   out->stats.roots = I.roots;
+  return PC_OK;
+}
+
+int pc_batch_set_types(pc_context* ctx, pc_batch* b, const pc_cell_type* types) {
+  if (!ctx || !b || !types) return fail(ctx, PC_ERR_INVALID, "null argument");
+  if (!b->batched) return fail(ctx, PC_ERR_INVALID, "not a batch");
+  // validate every instance's new types before changing anything
+  const uint32_t n = (uint32_t)b->inst.size();
+  std::vector<InstanceHost> next(n);
+  uint64_t off = 0;
+  for (uint32_t i = 0; i < n; ++i) {
+    const uint32_t nt = (uint32_t)b->inst[i].types.size();
+    next[i].t_max = b->inst[i].t_max;
+    std::string msg;
+    const int rc = prepare_types(types + off, nt, next[i], msg);
+    if (rc != PC_OK) return fail(ctx, rc, "instance " + std::to_string(i) + ": " + msg);
+    off += nt;
+  }
+  for (uint32_t i = 0; i < n; ++i) {
+    InstanceHost& I = b->inst[i];
+    I.types.swap(next[i].types);
+    I.sorted_to_file.swap(next[i].sorted_to_file);
+    I.fallback = next[i].fallback;
+    I.t_hi = next[i].t_hi;
+    I.t_lo = next[i].t_lo;
+    I.est_ok = next[i].est_ok;
+  }
+  std::vector<BatchType> btypes;
+  std::vector<InstanceDev> idev;
+  batch_type_tables(b, btypes, idev);
+  b->ran = false;  // counts of the previous run belong to the previous types
+  PC_CUDA(ctx, cudaSetDevice(ctx->device));
+  PC_CUDA(ctx, cudaMemcpyAsync(b->btypes_dev, btypes.data(), btypes.size() * sizeof(BatchType),
+                               cudaMemcpyHostToDevice, ctx->stream));
+  PC_CUDA(ctx, cudaMemcpyAsync(b->inst_dev, idev.data(), idev.size() * sizeof(InstanceDev), cudaMemcpyHostToDevice,
+                               ctx->stream));
+  PC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));  // the host tables are temporaries
+  return PC_OK;
+}
+
+int pc_batch_totals(pc_context* ctx, pc_batch* b, uint64_t* out, uint64_t capacity, uint64_t* offsets) {
+  if (!ctx || !b) return PC_ERR_INVALID;
+  const uint32_t n = (uint32_t)b->inst.size();
+  std::vector<uint64_t> off(n + 1, 0);
+  for (uint32_t i = 0; i < n; ++i) off[i + 1] = off[i] + b->inst[i].values.size();
+  if (offsets) std::memcpy(offsets, off.data(), (n + 1) * sizeof(uint64_t));
+  if (!out) return PC_OK;
+  if (capacity < off[n]) return fail(ctx, PC_ERR_INVALID, "totals buffer too small");
+  if (!b->ran) return fail(ctx, PC_ERR_INVALID, "batch has not run");
+  const unsigned long long* h = nullptr;
+  const int rc = stage_table(ctx, b, &h);
+  if (rc != PC_OK) return rc;
+  std::vector<int> bad(n, 0);
+  parallel_for(n, [&](uint32_t i) {
+    const InstanceHost& I = b->inst[i];
+    const uint32_t nb = (uint32_t)I.bin_value.size(), nt = (uint32_t)I.types.size();
+    uint64_t* t = out + off[i];
+    std::fill(t, t + I.values.size(), 0ull);
+    for (uint32_t g = 0; g < I.hist_gens; ++g)
+      for (uint32_t bb = 0; bb < nb; ++bb) {
+        const int64_t vi = I.vidx[(uint64_t)bb * I.vidx_stride + g];
+        const unsigned long long* row = h + g * b->nclass + I.class_begin + (uint64_t)bb * nt;
+        for (uint32_t k = 0; k < nt; ++k) {
+          if (!row[k]) continue;
+          if (vi < 0) {
+            bad[i] = 1;
+            continue;
+          }
+          t[vi] += row[k];
+        }
+      }
+  });
+  for (uint32_t i = 0; i < n; ++i)
+    if (bad[i]) return fail(ctx, PC_ERR_CUDA, "internal: leaf counted outside the output value set");
   return PC_OK;
 }
 

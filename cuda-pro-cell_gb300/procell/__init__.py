@@ -133,6 +133,24 @@ class Batch:
         finally:
             self.engine.L.pc_histogram_free(ctypes.byref(h))
 
+    def set_types(self, types):
+        """New cell types for every instance: a TYPE_DTYPE array (or rows of (ratio, mean,
+        sd)) concatenated in instance order, each instance with its original type count."""
+        t = np.ascontiguousarray(types if isinstance(types, np.ndarray) and types.dtype == _lib.TYPE_DTYPE
+                                 else _lib.types_numpy(types))
+        self.engine._check(self.engine.L.pc_batch_set_types(self.engine.ctx, self.handle,
+                                                            t.ctypes.data_as(ctypes.POINTER(_lib.CellType))))
+
+    def totals(self):
+        """(offsets [n + 1], totals): instance i's merged counts are totals[offsets[i]:offsets[i + 1]]."""
+        L = self.engine.L
+        off = np.zeros(self.size + 1, np.uint64)
+        U = ctypes.POINTER(ctypes.c_uint64)
+        self.engine._check(L.pc_batch_totals(self.engine.ctx, self.handle, None, 0, off.ctypes.data_as(U)))
+        out = np.zeros(int(off[-1]), np.uint64)
+        self.engine._check(L.pc_batch_totals(self.engine.ctx, self.handle, out.ctypes.data_as(U), len(out), None))
+        return off, out
+
     def raw_counts(self, i: int) -> np.ndarray:
         L, n = self.engine.L, ctypes.c_uint64()
         dims = (ctypes.c_uint32 * 3)()

@@ -90,6 +90,8 @@ SIGNATURES = [
     ("pc_batch_size", ctypes.c_uint32, [VP]),
     ("pc_batch_result", ctypes.c_int, [VP, VP, ctypes.c_uint32, ctypes.POINTER(Histogram)]),
     ("pc_batch_raw_counts", ctypes.c_int, [VP, VP, ctypes.c_uint32, U64P, ctypes.c_uint64, U64P, U32P]),
+    ("pc_batch_set_types", ctypes.c_int, [VP, VP, ctypes.POINTER(CellType)]),
+    ("pc_batch_totals", ctypes.c_int, [VP, VP, U64P, ctypes.c_uint64, U64P]),
     ("pc_batch_destroy", None, [VP]),
     ("pc_simulate_batch", ctypes.c_int, [VP, ctypes.POINTER(Instance), ctypes.c_uint32,
                                          ctypes.POINTER(Histogram)]),
@@ -179,7 +181,9 @@ TYPE_DTYPE = np.dtype([("ratio", "<f8"), ("mean", "<f8"), ("sd", "<f8")])
 
 def bins_numpy(bins) -> np.ndarray:
     """(value, frequency) rows as a pc_bin array; accepts a list of pairs or a (values,
-    frequencies) pair of numpy arrays."""
+    frequencies) pair of numpy arrays, or a pc_bin array itself."""
+    if isinstance(bins, np.ndarray) and bins.dtype == BIN_DTYPE:
+        return np.ascontiguousarray(bins)
     if isinstance(bins, tuple) and len(bins) == 2 and isinstance(bins[0], np.ndarray):
         out = np.empty(len(bins[0]), BIN_DTYPE)
         out["value"], out["frequency"] = bins[0], bins[1]

@@ -196,6 +196,15 @@ int pc_batch_result(pc_context* ctx, pc_batch* batch, uint32_t instance, pc_hist
 /* One instance's raw counts, in the layout of pc_plan_raw_counts. */
 int pc_batch_raw_counts(pc_context* ctx, pc_batch* batch, uint32_t instance, uint64_t* host_out,
                         uint64_t capacity, uint64_t* n_elems, uint32_t dims[3]);
+/* Replace the cell types of every instance (concatenated in instance order, each instance
+ * with as many types as it was created with), keeping bins, t_max, phi and seed: the next
+ * pc_batch_run simulates the new parameters (for parameter searches). All instances are
+ * validated first; on error nothing changes. Results need a new run. */
+int pc_batch_set_types(pc_context* ctx, pc_batch* batch, const pc_cell_type* types);
+/* Merged totals of every instance after the last run, concatenated: instance i's counts per
+ * value (its value set, ascending) are out[offsets[i] .. offsets[i + 1]). offsets (host,
+ * n_instances + 1 entries) may be NULL; pass out = NULL to query the offsets only. */
+int pc_batch_totals(pc_context* ctx, pc_batch* batch, uint64_t* out, uint64_t capacity, uint64_t* offsets);
 void pc_batch_destroy(pc_batch* batch);
 /* One call: create, run, results (out[n_instances], each freed with pc_histogram_free). */
 int pc_simulate_batch(pc_context* ctx, const pc_instance* instances, uint32_t n_instances,

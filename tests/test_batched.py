@@ -170,3 +170,47 @@ def test_batch_of_many_tiny_instances(engine):
         want, _ = plain_counts(engine, *x)
         assert np.array_equal(b.raw_counts(i), want), i
     b.close()
+
+
+def test_set_types_and_totals(engine):
+    """pc_batch_set_types re-parameterises a prepared batch: the next run equals a batch
+    created with the new types, instance by instance; pc_batch_totals returns every
+    instance's merged totals at once; invalid types leave the batch unchanged."""
+    import procell.configs as cfg
+    ws = cfg.batched(n_instances=12, seed=5)
+    ws = [w for w in ws if w.roots <= 200_000][:6]
+    inst = [(w.bins, w.types, w.t_max, w.phi, w.seed) for w in ws]
+    rng = np.random.default_rng(3)
+    new_types = []
+    for w in ws:
+        k = len(w.types)
+        r = rng.dirichlet(np.ones(k))
+        new_types.append([(float(r[j]), float(rng.uniform(25, 90)) if w.types[j][1] >= 0 else -1.0,
+                           float(rng.uniform(3, 20)) if w.types[j][1] >= 0 else -1.0) for j in range(k)])
+    b = engine.batch(inst)
+    b.run()
+    before = [b.result(i).totals for i in range(len(ws))]
+    flat = [t for ts in new_types for t in ts]
+    b.set_types(flat)
+    with pytest.raises(Exception):
+        b.result(0)  # the previous counts belong to the previous types
+    b.run()
+    off, tot = b.totals()
+    ref = engine.batch([(w.bins, new_types[i], w.t_max, w.phi, w.seed) for i, w in enumerate(ws)])
+    ref.run()
+    for i in range(len(ws)):
+        r = ref.result(i)
+        assert np.array_equal(b.result(i).per_type, r.per_type), i
+        assert np.array_equal(tot[off[i]:off[i + 1]], r.totals), i
+    ref.close()
+    bad = list(flat)
+    bad[0] = (bad[0][0] + 0.5, bad[0][1], bad[0][2])  # ratios no longer sum to 1
+    with pytest.raises(Exception, match="instance 0"):
+        b.set_types(bad)
+    b.run()
+    assert np.array_equal(b.totals()[1], tot)
+    b.set_types([t for w in ws for t in w.types])
+    b.run()
+    for i in range(len(ws)):
+        assert np.array_equal(b.result(i).totals, before[i]), i
+    b.close()

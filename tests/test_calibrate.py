@@ -112,3 +112,21 @@ def test_levenberg_marquardt_on_smoothed_form(engine):
     prob.smooth.sync()
     # from uniform random starts to within 30% of the hidden parameters' own loss
     assert trace[-1][1] <= 1.3 * at_hidden, (trace[-1][1], at_hidden)
+
+
+@pytest.mark.gpu
+def test_plain_loss_matches_single_runs(engine):
+    """The particle search's plain-simulator loss (all candidates as one batch, instance
+    table reused between calls) equals the loss of each candidate's own pc_simulate."""
+    prob = cb.Problem(engine, seed=7)
+    th = prob.start(5, 3)
+    L1 = prob.loss_plain(th).cpu().numpy()
+    L2 = prob.loss_plain(th).cpu().numpy()
+    L3 = prob.loss_plain(prob.start(5, 4)).cpu().numpy()
+    P = prob.params(th).cpu().numpy()
+    tgt = np.log1p(prob.target_np)
+    for i in range(5):
+        r = engine.simulate(prob.bins, [tuple(x) for x in P[i]], prob.t_max, prob.phi, prob.plain_seed)
+        ref = ((np.log1p(r.totals.astype(np.float64)) - tgt) ** 2).sum()
+        assert L1[i] == pytest.approx(ref, rel=1e-12)
+    assert np.array_equal(L1, L2) and not np.array_equal(L1, L3)
