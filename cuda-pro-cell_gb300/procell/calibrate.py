@@ -204,11 +204,15 @@ def levenberg_marquardt(prob, theta0, iters=40, lam0=1e-2, max_step=1.0, time_li
     trace = [(time.perf_counter() - t0, best)]
     snaps = [(trace[0][0], th[i].clone())]
     for _ in range(iters):
-        A = J.transpose(1, 2) @ J
-        g = (J * res[..., None]).sum(1)
+        # J^T J and J^T r from one FP32 batched product of [J | r] with itself (the damped
+        # Gauss-Newton matrix only steers the step; acceptance uses the FP64 loss)
+        Jr = torch.cat([J, res[..., None]], dim=-1).to(torch.float32)
+        M = (Jr.transpose(1, 2) @ Jr).to(torch.float64)
+        A, g = M[:, :P, :P], M[:, :P, P]
         d = torch.diagonal(A, dim1=1, dim2=2)
-        Ad = A + torch.diag_embed(lam[:, None] * d) + 1e-12 * d.amax(1)[:, None, None] * eye
-        step = torch.linalg.solve(Ad, -g[..., None])[..., 0].clamp(-max_step, max_step)
+        Ad = A + torch.diag_embed(lam[:, None] * d) + 1e-9 * d.amax(1)[:, None, None] * eye
+        step = torch.linalg.solve_ex(Ad, -g[..., None])[0][..., 0]
+        step = torch.nan_to_num(step, nan=0.0, posinf=0.0, neginf=0.0).clamp(-max_step, max_step)
         th_new = torch.minimum(torch.maximum(th + step.reshape(n, K, 3), lo - 2.0), hi + 2.0)
         res2, J2, f2 = evaluate(th_new)
         ok = f2 < f  # NaN losses are never accepted
