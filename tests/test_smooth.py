@@ -156,6 +156,39 @@ def test_autograd_function_and_determinism(smooth_setup):
     sm.sync()
 
 
+def test_many_types_match_cpu_restatement(engine):
+    """Six types (one quiescent, one zero-mean) and 37 candidates (two partial groups of 32):
+    forward, adjoint and Jacobian of the per-type grids against the CPU restatement."""
+    import smooth_ref
+    from procell.smooth import Smooth
+    bins = [(300.0, 14), (45.0, 9), (7.5, 11), (2.2, 6)]
+    t_max, phi, h, paths, seed = 120.0, 1.0, 0.7, 2, 4242
+    rng = np.random.default_rng(8)
+    C, K = 37, 6
+    params = []
+    for c in range(C):
+        r = rng.dirichlet(np.ones(K))
+        rows = [[float(r[k]), float(rng.uniform(18, 70)), float(rng.uniform(1, 12))] for k in range(K)]
+        rows[1][1:] = [-1.0, -1.0]   # quiescent
+        rows[4][1:] = [0.0, 3.0]     # zero mean: never due
+        params.append(rows)
+    sm = Smooth(engine, bins, n_types=K, t_max=t_max, phi=phi, h=h, paths=paths, seed=seed)
+    gE = rng.normal(size=(C, sm.n_values))
+    E_ref, G_ref, vals, J_ref = smooth_ref.forward_backward(bins, t_max, phi, h, paths, seed, params, gE,
+                                                            with_jacobian=True)
+    P = params_tensor(params)
+    E = sm.forward(P).cpu().numpy()
+    G = sm.backward(P, torch.tensor(gE, device="cuda")).cpu().numpy()
+    EJ, J = (x.cpu().numpy() for x in sm.jacobian(P))
+    sm.sync()
+    sm.close()
+    assert np.array_equal(vals, sm.values)
+    assert np.allclose(E, E_ref, rtol=2e-5, atol=1e-9 * np.abs(E_ref).max())
+    assert np.allclose(EJ, E_ref, rtol=2e-5, atol=1e-9 * np.abs(E_ref).max())
+    assert np.allclose(G, G_ref, rtol=2e-5, atol=1e-7 * np.abs(G_ref).max())
+    assert np.allclose(J, J_ref, rtol=2e-5, atol=1e-7 * np.abs(J_ref).max())
+
+
 def test_candidate_order_does_not_change_results(smooth_setup):
     """Kernels visit each type's candidates in order of that type's mean; a candidate's
     results are the same bits wherever it sits in the batch."""
