@@ -52,7 +52,7 @@ def build(verbose: bool = False, out: str | None = None, defines=()) -> str:
     os.makedirs(OUT, exist_ok=True)
     cuda = _cuda_home()
     nvcc = os.path.join(cuda, "bin", "nvcc")
-    headers = [os.path.join(CSRC, h) for h in ("pc_rng.h", "pc_engine.h", "pc_sweeps.cuh")] + \
+    headers = [os.path.join(CSRC, h) for h in ("pc_rng.h", "pc_engine.h", "pc_sweeps.cuh", "pc_guard.h")] + \
         [os.path.join(INCLUDE, "procell.h")]
     host_flags = ["-O2", "-std=c++17", "-fPIC", "-pthread", "-ffp-contract=off", "-fno-fast-math", "-Wall",
                   "-I" + os.path.join(cuda, "include"), "-I" + INCLUDE]

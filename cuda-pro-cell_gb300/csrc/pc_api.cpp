@@ -15,6 +15,8 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <exception>
+#include <new>
 #include <cstring>
 #include <atomic>
 #include <chrono>
@@ -25,6 +27,7 @@
 #include <vector>
 
 #include "../../include/procell.h"
+#include "pc_guard.h"
 #include "pc_engine.h"
 
 using namespace pc;
@@ -312,6 +315,7 @@ const char* pc_last_error(const pc_context* ctx) {
 }
 
 int pc_create(pc_context** out, int device) {
+  PC_GUARD_BEGIN
   if (!out) return PC_ERR_INVALID;
   *out = nullptr;
   pc_context* ctx = new (std::nothrow) pc_context();
@@ -347,6 +351,7 @@ int pc_create(pc_context** out, int device) {
   ctx->free_at_start = fr;
   *out = ctx;
   return PC_OK;
+  PC_GUARD_END(nullptr)
 }
 
 void pc_destroy(pc_context* ctx) {
@@ -370,12 +375,15 @@ void pc_destroy(pc_context* ctx) {
 }
 
 int pc_set_stream(pc_context* ctx, void* stream) {
+  PC_GUARD_BEGIN
   if (!ctx) return PC_ERR_INVALID;
   ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
   return PC_OK;
+  PC_GUARD_END(ctx)
 }
 
 int pc_set_option(pc_context* ctx, const char* name, double value) {
+  PC_GUARD_BEGIN
   if (!ctx || !name) return PC_ERR_INVALID;
   if (!(value >= 0.0) || !std::isfinite(value)) return fail(ctx, PC_ERR_INVALID, "option value must be >= 0");
   const std::string n(name);
@@ -400,6 +408,7 @@ int pc_set_option(pc_context* ctx, const char* name, double value) {
   }
   if (n == "memory_budget_bytes" || n == "grid_blocks") free_pool(ctx);
   return PC_OK;
+  PC_GUARD_END(ctx)
 }
 
 }  // extern "C"
@@ -825,6 +834,7 @@ extern "C" {
 
 int pc_plan_create(pc_context* ctx, const pc_bin* bins, uint64_t n_bins, const pc_cell_type* types,
                    uint32_t n_types, double t_max, double phi, uint64_t seed, pc_plan** out) {
+  PC_GUARD_BEGIN
   if (!ctx || !out) return fail(ctx, PC_ERR_INVALID, "null argument");
   *out = nullptr;
   pc_plan* p = new (std::nothrow) pc_plan();
@@ -845,15 +855,18 @@ int pc_plan_create(pc_context* ctx, const pc_bin* bins, uint64_t n_bins, const p
   }
   *out = p;
   return PC_OK;
+  PC_GUARD_END(ctx)
 }
 
 int pc_plan_set_roots(pc_context* ctx, pc_plan* p, uint64_t root_begin, uint64_t root_end) {
+  PC_GUARD_BEGIN
   if (!ctx || !p) return PC_ERR_INVALID;
   if (root_begin > root_end || root_end > p->roots_total)
     return fail(ctx, PC_ERR_INVALID, "root range outside [0, number of initial cells]");
   p->root_begin = root_begin;
   p->root_end = root_end;
   return PC_OK;
+  PC_GUARD_END(ctx)
 }
 
 void pc_plan_destroy(pc_plan* p) {
@@ -1178,6 +1191,7 @@ int run_persistent(pc_context* ctx, pc_plan* p, const SweepKernels& K, const int
 extern "C" {
 
 int pc_plan_run(pc_context* ctx, pc_plan* p) {
+  PC_GUARD_BEGIN
   if (!ctx || !p) return PC_ERR_INVALID;
   PC_CUDA(ctx, cudaSetDevice(ctx->device));
   cudaStream_t st = ctx->stream;
@@ -1216,17 +1230,21 @@ int pc_plan_run(pc_context* ctx, pc_plan* p) {
   if (err & 1u)
     return fail(ctx, PC_ERR_DEPTH, "a lineage exceeded the deepest generation the key layout holds");
   return PC_OK;
+  PC_GUARD_END(ctx)
 }
 
 int pc_plan_stats(pc_context* ctx, const pc_plan* p, pc_stats* out) {
+  PC_GUARD_BEGIN
   if (!ctx || !p || !out) return PC_ERR_INVALID;
   if (!p->ran) return fail(ctx, PC_ERR_INVALID, "plan has not run");
   *out = p->stats;
   return PC_OK;
+  PC_GUARD_END(ctx)
 }
 
 int pc_plan_raw_counts(pc_context* ctx, pc_plan* p, uint64_t* host_out, uint64_t capacity,
                        uint64_t* n_elems, uint32_t dims[3]) {
+  PC_GUARD_BEGIN
   if (!ctx || !p || p->inst.empty()) return PC_ERR_INVALID;
   const InstanceHost& I = p->inst[0];
   const uint32_t nb = (uint32_t)I.bin_value.size(), nt = (uint32_t)I.types.size();
@@ -1245,9 +1263,11 @@ int pc_plan_raw_counts(pc_context* ctx, pc_plan* p, uint64_t* host_out, uint64_t
   if (rc != PC_OK) return rc;
   instance_counts(p, I, h, host_out);
   return PC_OK;
+  PC_GUARD_END(ctx)
 }
 
 int pc_plan_result(pc_context* ctx, pc_plan* p, pc_histogram* out) {
+  PC_GUARD_BEGIN
   if (!ctx || !p || !out || p->inst.empty()) return PC_ERR_INVALID;
   std::memset(out, 0, sizeof(*out));
   if (!p->ran) return fail(ctx, PC_ERR_INVALID, "plan has not run");
@@ -1262,6 +1282,7 @@ int pc_plan_result(pc_context* ctx, pc_plan* p, pc_histogram* out) {
   out->stats.leaves = leaves;
   out->stats.d2h_bytes += p->hist_elems * sizeof(unsigned long long);
   return PC_OK;
+  PC_GUARD_END(ctx)
 }
 
 void pc_histogram_free(pc_histogram* h) {
@@ -1277,6 +1298,7 @@ void pc_histogram_free(pc_histogram* h) {
 
 int pc_simulate(pc_context* ctx, const pc_bin* bins, uint64_t n_bins, const pc_cell_type* types,
                 uint32_t n_types, double t_max, double phi, uint64_t seed, pc_histogram* out) {
+  PC_GUARD_BEGIN
   pc_plan* p = nullptr;
   int rc = pc_plan_create(ctx, bins, n_bins, types, n_types, t_max, phi, seed, &p);
   if (rc != PC_OK) return rc;
@@ -1284,11 +1306,13 @@ int pc_simulate(pc_context* ctx, const pc_bin* bins, uint64_t n_bins, const pc_c
   if (rc == PC_OK) rc = pc_plan_result(ctx, p, out);
   pc_plan_destroy(p);
   return rc;
+  PC_GUARD_END(ctx)
 }
 
 int pc_simulate_shard(pc_context* ctx, const pc_bin* bins, uint64_t n_bins, const pc_cell_type* types,
                       uint32_t n_types, double t_max, double phi, uint64_t seed, uint64_t root_begin,
                       uint64_t root_end, pc_histogram* out) {
+  PC_GUARD_BEGIN
   pc_plan* p = nullptr;
   int rc = pc_plan_create(ctx, bins, n_bins, types, n_types, t_max, phi, seed, &p);
   if (rc != PC_OK) return rc;
@@ -1297,9 +1321,11 @@ int pc_simulate_shard(pc_context* ctx, const pc_bin* bins, uint64_t n_bins, cons
   if (rc == PC_OK) rc = pc_plan_result(ctx, p, out);
   pc_plan_destroy(p);
   return rc;
+  PC_GUARD_END(ctx)
 }
 
 int pc_histogram_accumulate(pc_histogram* dst, const pc_histogram* src) {
+  PC_GUARD_BEGIN
   if (!dst || !src) return PC_ERR_INVALID;
   if (dst->n_values != src->n_values || dst->n_types != src->n_types) return PC_ERR_INVALID;
   const uint64_t nv = dst->n_values;
@@ -1325,9 +1351,11 @@ int pc_histogram_accumulate(pc_histogram* dst, const pc_histogram* src) {
   a.h2d_bytes += b.h2d_bytes;
   a.d2h_bytes += b.d2h_bytes;
   return PC_OK;
+  PC_GUARD_END(nullptr)
 }
 
 int pc_batch_create(pc_context* ctx, const pc_instance* instances, uint32_t n_instances, pc_batch** out) {
+  PC_GUARD_BEGIN
   if (!ctx || !out || (n_instances && !instances)) return fail(ctx, PC_ERR_INVALID, "null argument");
   *out = nullptr;
   if (n_instances == 0) return fail(ctx, PC_ERR_INVALID, "a batch needs at least one instance");
@@ -1355,6 +1383,7 @@ int pc_batch_create(pc_context* ctx, const pc_instance* instances, uint32_t n_in
   }
   *out = b;
   return PC_OK;
+  PC_GUARD_END(ctx)
 }
 
 int pc_batch_run(pc_context* ctx, pc_batch* b) { return pc_plan_run(ctx, b); }
@@ -1371,6 +1400,7 @@ static int batch_table(pc_context* ctx, pc_batch* b, uint32_t instance, const un
 
 int pc_batch_raw_counts(pc_context* ctx, pc_batch* b, uint32_t instance, uint64_t* host_out, uint64_t capacity,
                         uint64_t* n_elems, uint32_t dims[3]) {
+  PC_GUARD_BEGIN
   if (!ctx || !b) return PC_ERR_INVALID;
   if (instance >= b->inst.size()) return fail(ctx, PC_ERR_INVALID, "instance index out of range");
   const InstanceHost& I = b->inst[instance];
@@ -1389,9 +1419,11 @@ int pc_batch_raw_counts(pc_context* ctx, pc_batch* b, uint32_t instance, uint64_
   if (rc != PC_OK) return rc;
   instance_counts(b, I, h, host_out);
   return PC_OK;
+  PC_GUARD_END(ctx)
 }
 
 int pc_batch_result(pc_context* ctx, pc_batch* b, uint32_t instance, pc_histogram* out) {
+  PC_GUARD_BEGIN
   if (!ctx || !b || !out) return PC_ERR_INVALID;
   std::memset(out, 0, sizeof(*out));
   const unsigned long long* h = nullptr;
@@ -1403,9 +1435,11 @@ int pc_batch_result(pc_context* ctx, pc_batch* b, uint32_t instance, pc_histogra
   if (rc != PC_OK) return fail(ctx, rc, msg);
   out->stats.roots = I.roots;
   return PC_OK;
+  PC_GUARD_END(ctx)
 }
 
 int pc_batch_set_types(pc_context* ctx, pc_batch* b, const pc_cell_type* types) {
+  PC_GUARD_BEGIN
   if (!ctx || !b || !types) return fail(ctx, PC_ERR_INVALID, "null argument");
   if (!b->batched) return fail(ctx, PC_ERR_INVALID, "not a batch");
   // validate every instance's new types before changing anything
@@ -1440,9 +1474,11 @@ int pc_batch_set_types(pc_context* ctx, pc_batch* b, const pc_cell_type* types) 
                                ctx->stream));
   PC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));  // the host tables are temporaries
   return PC_OK;
+  PC_GUARD_END(ctx)
 }
 
 int pc_batch_totals(pc_context* ctx, pc_batch* b, uint64_t* out, uint64_t capacity, uint64_t* offsets) {
+  PC_GUARD_BEGIN
   if (!ctx || !b) return PC_ERR_INVALID;
   const uint32_t n = (uint32_t)b->inst.size();
   std::vector<uint64_t> off(n + 1, 0);
@@ -1477,11 +1513,13 @@ int pc_batch_totals(pc_context* ctx, pc_batch* b, uint64_t* out, uint64_t capaci
   for (uint32_t i = 0; i < n; ++i)
     if (bad[i]) return fail(ctx, PC_ERR_CUDA, "internal: leaf counted outside the output value set");
   return PC_OK;
+  PC_GUARD_END(ctx)
 }
 
 void pc_batch_destroy(pc_batch* b) { pc_plan_destroy(b); }
 
 int pc_simulate_batch(pc_context* ctx, const pc_instance* instances, uint32_t n_instances, pc_histogram* out) {
+  PC_GUARD_BEGIN
   if (!ctx || !out) return fail(ctx, PC_ERR_INVALID, "null argument");
   for (uint32_t i = 0; i < n_instances; ++i) std::memset(out + i, 0, sizeof(pc_histogram));
   pc_batch* b = nullptr;
@@ -1504,9 +1542,11 @@ int pc_simulate_batch(pc_context* ctx, const pc_instance* instances, uint32_t n_
     for (uint32_t i = 0; i < n_instances; ++i) pc_histogram_free(out + i);
   pc_batch_destroy(b);
   return rc;
+  PC_GUARD_END(ctx)
 }
 
 int pc_autotune(pc_context* ctx, pc_plan* p, uint32_t repeats, pc_tuning* out) {
+  PC_GUARD_BEGIN
   if (!ctx || !p || !out) return PC_ERR_INVALID;
   std::memset(out, 0, sizeof(*out));
   repeats = std::max<uint32_t>(1, repeats);
@@ -1555,13 +1595,17 @@ int pc_autotune(pc_context* ctx, pc_plan* p, uint32_t repeats, pc_tuning* out) {
   out->ms = best;
   out->ms_default = dflt;
   return PC_OK;
+  PC_GUARD_END(ctx)
 }
 
 int pc_batch_autotune(pc_context* ctx, pc_batch* b, uint32_t repeats, pc_tuning* out) {
+  PC_GUARD_BEGIN
   return pc_autotune(ctx, b, repeats, out);
+  PC_GUARD_END(ctx)
 }
 
 int pc_debug_barrier(pc_context* ctx, int starve, double timeout_ms, uint32_t* error_bits, uint32_t* passed) {
+  PC_GUARD_BEGIN
   if (!ctx || !error_bits || !passed || !(timeout_ms > 0.0) || timeout_ms > 10000.0)
     return fail(ctx, PC_ERR_INVALID, "timeout must be in (0, 10000] ms");
   PC_CUDA(ctx, cudaSetDevice(ctx->device));
@@ -1581,9 +1625,11 @@ int pc_debug_barrier(pc_context* ctx, int starve, double timeout_ms, uint32_t* e
   *error_bits = host[2];
   *passed = host[3];
   return PC_OK;
+  PC_GUARD_END(ctx)
 }
 
 int pc_debug_philox(pc_context* ctx, const uint32_t* ctr, uint64_t n, const uint32_t key[2], uint32_t* out) {
+  PC_GUARD_BEGIN
   if (!ctx || (n && (!ctr || !out)) || !key) return PC_ERR_INVALID;
   if (n == 0) return PC_OK;
   uint32_t *dc = nullptr, *dout = nullptr;
@@ -1597,9 +1643,11 @@ int pc_debug_philox(pc_context* ctx, const uint32_t* ctr, uint64_t n, const uint
   cudaFree(dout);
   if (e != cudaSuccess) return fail(ctx, PC_ERR_CUDA, std::string("debug philox: ") + cudaGetErrorString(e));
   return PC_OK;
+  PC_GUARD_END(ctx)
 }
 
 int pc_debug_normals(pc_context* ctx, uint64_t seed, uint32_t root, uint64_t first_parent, uint64_t count, float* z) {
+  PC_GUARD_BEGIN
   if (!ctx || (count && !z)) return PC_ERR_INVALID;
   if (count == 0) return PC_OK;
   float* dz = nullptr;
@@ -1611,9 +1659,11 @@ int pc_debug_normals(pc_context* ctx, uint64_t seed, uint32_t root, uint64_t fir
   cudaFree(dz);
   if (e != cudaSuccess) return fail(ctx, PC_ERR_CUDA, std::string("debug normals: ") + cudaGetErrorString(e));
   return PC_OK;
+  PC_GUARD_END(ctx)
 }
 
 int pc_debug_tables(pc_context* ctx, uint32_t* k, uint32_t* w_bits, uint32_t* f_bits) {
+  PC_GUARD_BEGIN
   if (!ctx) return PC_ERR_INVALID;
   ZigTables t;
   PC_CUDA(ctx, cudaMemcpy(&t, ctx->zig_dev, sizeof(t), cudaMemcpyDeviceToHost));
@@ -1621,6 +1671,7 @@ int pc_debug_tables(pc_context* ctx, uint32_t* k, uint32_t* w_bits, uint32_t* f_
   if (w_bits) std::memcpy(w_bits, t.w, sizeof(t.w));
   if (f_bits) std::memcpy(f_bits, t.f, sizeof(t.f));
   return PC_OK;
+  PC_GUARD_END(ctx)
 }
 
 }  // extern "C"
@@ -1711,6 +1762,7 @@ extern "C" {
 
 int pc_smooth_create(pc_context* ctx, const pc_bin* bins, uint64_t n_bins, uint32_t n_types, double t_max,
                      double phi, double h, uint32_t paths_per_cell, uint64_t seed, pc_smooth** out) {
+  PC_GUARD_BEGIN
   if (!ctx || !out) return fail(ctx, PC_ERR_INVALID, "null argument");
   *out = nullptr;
   if (n_types == 0 || n_types > (uint32_t)kSmoothMaxTypes)
@@ -1782,24 +1834,30 @@ int pc_smooth_create(pc_context* ctx, const pc_bin* bins, uint64_t n_bins, uint3
   }
   *out = s;
   return PC_OK;
+  PC_GUARD_END(ctx)
 }
 
 int pc_smooth_info(const pc_smooth* s, uint64_t* n_values, uint32_t* n_types, uint64_t* n_cells) {
+  PC_GUARD_BEGIN
   if (!s) return PC_ERR_INVALID;
   if (n_values) *n_values = s->I.values.size();
   if (n_types) *n_types = s->ntypes;
   if (n_cells) *n_cells = s->I.roots;
   return PC_OK;
+  PC_GUARD_END(nullptr)
 }
 
 int pc_smooth_values(const pc_smooth* s, double* values) {
+  PC_GUARD_BEGIN
   if (!s || (!values && !s->I.values.empty())) return PC_ERR_INVALID;
   if (!s->I.values.empty()) std::memcpy(values, s->I.values.data(), s->I.values.size() * sizeof(double));
   return PC_OK;
+  PC_GUARD_END(nullptr)
 }
 
 int pc_smooth_forward(pc_context* ctx, pc_smooth* s, const double* params, uint32_t n_candidates,
                       double* expected) {
+  PC_GUARD_BEGIN
   if (!ctx || !s || (n_candidates && (!params || !expected))) return fail(ctx, PC_ERR_INVALID, "null argument");
   if (n_candidates == 0) return PC_OK;
   PC_CUDA(ctx, cudaSetDevice(ctx->device));
@@ -1811,10 +1869,12 @@ int pc_smooth_forward(pc_context* ctx, pc_smooth* s, const double* params, uint3
   PC_CUDA(ctx, (cudaError_t)launch_smooth_merge(s->e_raw_dev, n_candidates, A.ntypes, A.nbins * A.rows,
                                                 s->inv_off_dev, s->inv_idx_dev, nv, expected, ctx->stream));
   return PC_OK;
+  PC_GUARD_END(ctx)
 }
 
 int pc_smooth_backward(pc_context* ctx, pc_smooth* s, const double* params, uint32_t n_candidates,
                        const double* grad_expected, double* grad_params) {
+  PC_GUARD_BEGIN
   if (!ctx || !s || (n_candidates && (!params || !grad_expected || !grad_params)))
     return fail(ctx, PC_ERR_INVALID, "null argument");
   if (n_candidates == 0) return PC_OK;
@@ -1826,10 +1886,12 @@ int pc_smooth_backward(pc_context* ctx, pc_smooth* s, const double* params, uint
                                                    (uint32_t)s->I.values.size(), s->vidx_dev, s->part_dev,
                                                    grad_params, ctx->stream));
   return PC_OK;
+  PC_GUARD_END(ctx)
 }
 
 int pc_smooth_jacobian(pc_context* ctx, pc_smooth* s, const double* params, uint32_t n_candidates,
                        double* expected, double* jacobian) {
+  PC_GUARD_BEGIN
   if (!ctx || !s || (n_candidates && (!params || !expected || !jacobian)))
     return fail(ctx, PC_ERR_INVALID, "null argument");
   if (n_candidates == 0) return PC_OK;
@@ -1841,15 +1903,18 @@ int pc_smooth_jacobian(pc_context* ctx, pc_smooth* s, const double* params, uint
                                                    (uint32_t)s->I.values.size(), s->jac_raw_dev, expected,
                                                    jacobian, ctx->stream));
   return PC_OK;
+  PC_GUARD_END(ctx)
 }
 
 int pc_smooth_sync(pc_context* ctx) {
+  PC_GUARD_BEGIN
   if (!ctx) return PC_ERR_INVALID;
   PC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   uint32_t err = 0;
   PC_CUDA(ctx, cudaMemcpy(&err, ctx->error_dev, sizeof(err), cudaMemcpyDeviceToHost));
   if (err & 2u) return fail(ctx, PC_ERR_CUDA, "internal: the normal sampler exceeded its rejection budget");
   return PC_OK;
+  PC_GUARD_END(ctx)
 }
 
 void pc_smooth_destroy(pc_smooth* s) {

@@ -8,15 +8,19 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <exception>
+#include <new>
 #include <fstream>
 #include <iostream>
 #include <vector>
 
 #include "../../include/procell.h"
+#include "pc_guard.h"
 
 extern "C" {
 
 int pc_load_histogram(const char* path, pc_bin** out, uint64_t* n) {
+  PC_GUARD_BEGIN
   if (!path || !out || !n) return PC_ERR_INVALID;
   *out = nullptr;
   *n = 0;
@@ -31,9 +35,11 @@ int pc_load_histogram(const char* path, pc_bin** out, uint64_t* n) {
   for (size_t i = 0; i < rows.size(); ++i) (*out)[i] = rows[i];
   *n = rows.size();
   return PC_OK;
+  PC_GUARD_END_NOCTX
 }
 
 int pc_load_cell_types(const char* path, pc_cell_type** out, uint32_t* n) {
+  PC_GUARD_BEGIN
   if (!path || !out || !n) return PC_ERR_INVALID;
   *out = nullptr;
   *n = 0;
@@ -56,6 +62,7 @@ int pc_load_cell_types(const char* path, pc_cell_type** out, uint32_t* n) {
     return PC_ERR_INVALID;
   }
   return PC_OK;
+  PC_GUARD_END_NOCTX
 }
 
 static void write_rows(std::ostream& stream, const pc_histogram* h, int track_ratio) {
@@ -70,6 +77,7 @@ static void write_rows(std::ostream& stream, const pc_histogram* h, int track_ra
 }
 
 int pc_write_histogram(const char* path, const pc_histogram* h, int track_ratio) {
+  PC_GUARD_BEGIN
   if (!h) return PC_ERR_INVALID;
   if (!path || (path[0] == '-' && path[1] == '\0')) {
     write_rows(std::cout, h, track_ratio);
@@ -81,6 +89,7 @@ int pc_write_histogram(const char* path, const pc_histogram* h, int track_ratio)
   write_rows(stream, h, track_ratio);
   stream.close();
   return stream.fail() ? PC_ERR_IO : PC_OK;
+  PC_GUARD_END_NOCTX
 }
 
 void pc_free(void* p) { std::free(p); }
@@ -89,6 +98,7 @@ void pc_free(void* p) { std::free(p); }
 // exponents ceil(log_base(start)) .. ceil(log_base(end)) in n equally spaced steps (its
 // linear_space, util.cu:76-88), each edge base^exponent, the last one exactly base^end.
 int pc_log_space(double start, double end, uint64_t n, double base, double* edges) {
+  PC_GUARD_BEGIN
   if (!edges || n < 2 || !(start > 0.0) || !(end > 0.0) || !(base > 0.0) || base == 1.0 ||
       !std::isfinite(start) || !std::isfinite(end) || !std::isfinite(base))
     return PC_ERR_INVALID;
@@ -98,6 +108,7 @@ int pc_log_space(double start, double end, uint64_t n, double base, double* edge
   for (uint64_t i = 0; i + 1 < n; ++i) edges[i] = std::pow(base, e0 + delta * (double)i);
   edges[n - 1] = std::pow(base, e1);
   return PC_OK;
+  PC_GUARD_END_NOCTX
 }
 
 // The reference's utils::rebin (util.cu:113-138): counts of an ascending histogram summed
@@ -106,6 +117,7 @@ int pc_log_space(double start, double end, uint64_t n, double base, double* edge
 // last edge; here that is an error.
 int pc_rebin(const double* values, const uint64_t* counts, uint64_t n_values, double lower, double upper,
              uint64_t n_bins, double* edges_out, uint64_t* counts_out) {
+  PC_GUARD_BEGIN
   if ((n_values && (!values || !counts)) || !edges_out || !counts_out) return PC_ERR_INVALID;
   const int rc = pc_log_space(lower, upper, n_bins, 10.0, edges_out);
   if (rc != PC_OK) return rc;
@@ -118,6 +130,7 @@ int pc_rebin(const double* values, const uint64_t* counts, uint64_t n_values, do
     counts_out[pos] += counts[i];
   }
   return PC_OK;
+  PC_GUARD_END_NOCTX
 }
 
 }  // extern "C"

@@ -17,7 +17,7 @@ CLI_PATH = os.path.join(PKG, "build", "procell")
 
 PC_OK = 0
 ERRORS = {1: "PC_ERR_INVALID", 2: "PC_ERR_CUDA", 3: "PC_ERR_NOMEM", 4: "PC_ERR_DEPTH",
-          5: "PC_ERR_UNSUPPORTED", 6: "PC_ERR_IO"}
+          5: "PC_ERR_UNSUPPORTED", 6: "PC_ERR_IO", 7: "PC_ERR_INTERNAL"}
 
 
 class Bin(ctypes.Structure):

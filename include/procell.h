@@ -48,6 +48,7 @@ extern "C" {
 #define PC_ERR_DEPTH 4       /* a lineage went deeper than the key layout allows */
 #define PC_ERR_UNSUPPORTED 5 /* e.g. more cell types than the kernels hold */
 #define PC_ERR_IO 6          /* a file could not be opened or written */
+#define PC_ERR_INTERNAL 7    /* an unexpected internal error (message says which) */
 
 /* One histogram row, as in the reference's `fluorescence` (data_types.h:26-30). */
 typedef struct pc_bin {
