@@ -1906,6 +1906,23 @@ int pc_smooth_jacobian(pc_context* ctx, pc_smooth* s, const double* params, uint
   PC_GUARD_END(ctx)
 }
 
+int pc_smooth_gauss_newton(pc_context* ctx, pc_smooth* s, const double* params, uint32_t n_candidates,
+                           const double* target, double* loss, double* jtj, double* jtr) {
+  PC_GUARD_BEGIN
+  if (!ctx || !s || (n_candidates && (!params || !target || !loss || !jtj || !jtr)))
+    return fail(ctx, PC_ERR_INVALID, "null argument");
+  if (n_candidates == 0) return PC_OK;
+  PC_CUDA(ctx, cudaSetDevice(ctx->device));
+  int rc = jacobian_scratch(ctx, s, n_candidates);
+  if (rc != PC_OK) return rc;
+  const SmoothArgs A = smooth_args(ctx, s);
+  PC_CUDA(ctx, (cudaError_t)launch_smooth_gauss_newton(A, params, n_candidates, s->inv_off_dev, s->inv_idx_dev,
+                                                       (uint32_t)s->I.values.size(), target, s->jac_raw_dev, loss,
+                                                       jtj, jtr, ctx->stream));
+  return PC_OK;
+  PC_GUARD_END(ctx)
+}
+
 int pc_smooth_sync(pc_context* ctx) {
   PC_GUARD_BEGIN
   if (!ctx) return PC_ERR_INVALID;

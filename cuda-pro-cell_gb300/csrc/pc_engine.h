@@ -212,6 +212,13 @@ int launch_smooth_jacobian(const SmoothArgs& A, const double* params, uint32_t n
                            const uint32_t* inv_idx, uint32_t nvalues, double* jac_raw, double* expected,
                            double* jacobian, void* stream);
 
+// loss[c], jtj[c][P][P], jtr[c][P] (P = 3 ntypes): the Gauss-Newton system of
+// sum_v (log1p(E_cv) - log1p(target_v))^2 in the parameters, from one Jacobian pass whose
+// rows are reduced on the device (nothing of size [c][v][P] is written).
+int launch_smooth_gauss_newton(const SmoothArgs& A, const double* params, uint32_t ncand, const uint32_t* inv_off,
+                               const uint32_t* inv_idx, uint32_t nvalues, const double* target, double* jac_raw,
+                               double* loss, double* jtj, double* jtr, void* stream);
+
 // Host helpers (pc_api.cpp).
 ZigTables host_zig_tables();
 void host_truncation_bounds(double mu, double sigma, float& zlo, float& zhi);

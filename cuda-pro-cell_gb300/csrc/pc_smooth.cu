@@ -490,6 +490,98 @@ __global__ void k_smooth_jacobian_merge(const double* __restrict__ jac_raw, cons
   expected[i] = e;
 }
 
+// The Gauss-Newton system of the squared log-count loss, one block per candidate c: with
+// r_v = log1p(E_v) - log1p(T_v) and j_v = (dE_v / dparams) / (1 + E_v),
+//   loss[c] = sum_v r_v^2, jtj[c][p][q] = sum_v j_vp j_vq, jtr[c][p] = sum_v j_vp r_v.
+// E and dE come from the Jacobian pass's raw rows as in k_smooth_jacobian_merge (same order
+// of additions). Values go through shared memory in tiles; each thread keeps the running sums
+// of up to kGnSlots outputs (upper triangle of jtj, jtr, loss) in a fixed order.
+constexpr uint32_t kGnTile = 128;
+constexpr int kGnSlots = 3;
+static_assert(kSmoothMaxTypes * 3 * (kSmoothMaxTypes * 3 + 1) / 2 + kSmoothMaxTypes * 3 + 1 <= kGnSlots * kGnTile,
+              "outputs per candidate exceed the block's slots");
+
+__device__ __forceinline__ void gn_pair(uint32_t o, uint32_t kq, uint32_t& a, uint32_t& b) {
+  const uint32_t npair = kq * (kq + 1u) / 2u;
+  if (o < npair) {
+    a = 0;
+    while (o >= kq - a) {
+      o -= kq - a;
+      ++a;
+    }
+    b = a + o;
+  } else if (o < npair + kq) {
+    a = o - npair;
+    b = kq;  // the residual column
+  } else {
+    a = kq;
+    b = kq;
+  }
+}
+
+__global__ void __launch_bounds__(kGnTile) k_smooth_gauss_newton(
+    const double* __restrict__ jac_raw, const double* __restrict__ params, uint32_t per_cand, uint32_t kq,
+    const uint32_t* __restrict__ inv_off, const uint32_t* __restrict__ inv_idx, uint32_t nvalues,
+    const double* __restrict__ target, double* __restrict__ loss, double* __restrict__ jtj,
+    double* __restrict__ jtr) {
+  extern __shared__ double gsm[];  // [kGnTile][kq + 1]: scaled Jacobian row, then r
+  const uint32_t c = blockIdx.x;
+  const uint32_t w = kq + 1u;
+  const uint32_t nout = kq * (kq + 1u) / 2u + kq + 1u;
+  const double* src = jac_raw + (uint64_t)c * per_cand * kq;
+  const double* prm = params + (uint64_t)c * kq;
+  double acc[kGnSlots];
+#pragma unroll
+  for (int sl = 0; sl < kGnSlots; ++sl) acc[sl] = 0.0;
+  for (uint32_t v0 = 0; v0 < nvalues; v0 += kGnTile) {
+    const uint32_t v = v0 + threadIdx.x;
+    double* row = gsm + (size_t)threadIdx.x * w;
+    if (v < nvalues) {
+      double e = 0.0;
+      for (uint32_t q = 0; q < kq; ++q) {
+        double sum = 0.0;
+        for (uint32_t t = inv_off[v]; t < inv_off[v + 1]; ++t) sum += src[(uint64_t)inv_idx[t] * kq + q];
+        row[q] = sum;
+        if (q % 3u == 0u) e += prm[q] * sum;
+      }
+      const double inv = 1.0 / (1.0 + e);
+      for (uint32_t q = 0; q < kq; ++q) row[q] *= inv;
+      row[kq] = log1p(e) - log1p(target[v]);
+    } else {
+      for (uint32_t q = 0; q <= kq; ++q) row[q] = 0.0;
+    }
+    __syncthreads();
+    const uint32_t m = nvalues - v0 < kGnTile ? nvalues - v0 : kGnTile;
+#pragma unroll
+    for (int sl = 0; sl < kGnSlots; ++sl) {
+      const uint32_t o = threadIdx.x + (uint32_t)sl * kGnTile;
+      if (o < nout) {
+        uint32_t a, b;
+        gn_pair(o, kq, a, b);
+        double sum = acc[sl];
+        for (uint32_t t = 0; t < m; ++t) sum = fma(gsm[t * w + a], gsm[t * w + b], sum);
+        acc[sl] = sum;
+      }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int sl = 0; sl < kGnSlots; ++sl) {
+    const uint32_t o = threadIdx.x + (uint32_t)sl * kGnTile;
+    if (o >= nout) continue;
+    uint32_t a, b;
+    gn_pair(o, kq, a, b);
+    if (b < kq) {
+      jtj[((uint64_t)c * kq + a) * kq + b] = acc[sl];
+      jtj[((uint64_t)c * kq + b) * kq + a] = acc[sl];
+    } else if (a < kq) {
+      jtr[(uint64_t)c * kq + a] = acc[sl];
+    } else {
+      loss[c] = acc[sl];
+    }
+  }
+}
+
 __global__ void k_smooth_grad_sum(const double* __restrict__ part, uint32_t ncand, uint32_t nbins, uint32_t per_bin,
                                   double* __restrict__ grad) {
   const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -558,6 +650,30 @@ int launch_smooth_jacobian(const SmoothArgs& A, const double* params, uint32_t n
   k_smooth_jacobian<<<grid, kThreads, smem, st>>>(A, params, ncand, jac_raw);
   k_smooth_jacobian_merge<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(jac_raw, params, ncand, A.nbins * A.rows, kq,
                                                                       inv_off, inv_idx, nvalues, expected, jacobian);
+  return (int)cudaGetLastError();
+}
+
+int launch_smooth_gauss_newton(const SmoothArgs& A, const double* params, uint32_t ncand, const uint32_t* inv_off,
+                               const uint32_t* inv_idx, uint32_t nvalues, const double* target, double* jac_raw,
+                               double* loss, double* jtj, double* jtr, void* stream) {
+  cudaStream_t st = (cudaStream_t)stream;
+  const uint32_t kq = A.ntypes * 3u;
+  if (ncand == 0) return 0;
+  if (A.nbins == 0 || nvalues == 0) {
+    cudaError_t e = cudaMemsetAsync(loss, 0, (size_t)ncand * sizeof(double), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(jtj, 0, (size_t)ncand * kq * kq * sizeof(double), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(jtr, 0, (size_t)ncand * kq * sizeof(double), st);
+    return (int)e;
+  }
+  const int smem = (int)(4u * A.rows * kThreads * sizeof(float));
+  const cudaError_t e = cudaFuncSetAttribute(k_smooth_jacobian, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return (int)e;
+  const int eo = launch_order(A, params, ncand, st);
+  if (eo != 0) return eo;
+  const dim3 grid(A.nbins, (ncand + 31u) / 32u, A.ntypes);
+  k_smooth_jacobian<<<grid, kThreads, smem, st>>>(A, params, ncand, jac_raw);
+  k_smooth_gauss_newton<<<ncand, kGnTile, kGnTile * (kq + 1u) * sizeof(double), st>>>(
+      jac_raw, params, A.nbins * A.rows, kq, inv_off, inv_idx, nvalues, target, loss, jtj, jtr);
   return (int)cudaGetLastError();
 }
 

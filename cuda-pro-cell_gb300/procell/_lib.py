@@ -105,6 +105,7 @@ SIGNATURES = [
     ("pc_smooth_forward", ctypes.c_int, [VP, VP, VP, ctypes.c_uint32, VP]),
     ("pc_smooth_backward", ctypes.c_int, [VP, VP, VP, ctypes.c_uint32, VP, VP]),
     ("pc_smooth_jacobian", ctypes.c_int, [VP, VP, VP, ctypes.c_uint32, VP, VP]),
+    ("pc_smooth_gauss_newton", ctypes.c_int, [VP, VP, VP, ctypes.c_uint32, VP, VP, VP, VP]),
     ("pc_smooth_sync", ctypes.c_int, [VP]),
     ("pc_smooth_destroy", None, [VP]),
     ("pc_log_space", ctypes.c_int, [ctypes.c_double, ctypes.c_double, ctypes.c_uint64, ctypes.c_double,

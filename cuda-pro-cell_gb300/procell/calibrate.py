@@ -5,8 +5,9 @@ drawn from a seed. Candidates are scored by
     L = sum_v (log(1 + E_v) - log(1 + C_v))^2
 (E the candidate's counts, C the target counts), and searched four ways from the same
 random starting population:
-  * Levenberg-Marquardt on the smoothed form: residuals and their Jacobian from one pass of
-    the forward-mode Jacobian kernel per iteration (pc_smooth_jacobian);
+  * Levenberg-Marquardt on the smoothed form: the Gauss-Newton system (J^T J, J^T r, loss)
+    from one pass of the forward-mode Jacobian kernel per iteration, reduced on the device
+    (pc_smooth_gauss_newton);
   * gradient descent on the smoothed form: Adam on unconstrained coordinates, gradients
     from the smoothed form's adjoint kernel through procell.smooth.expected_counts;
   * a particle swarm on the smoothed form (forward passes only);
@@ -161,64 +162,64 @@ def gradient_descent(prob, theta0, iters=150, lr=0.1, lr_end=0.002, time_limit=N
     return trace, snaps
 
 
-def residual_jacobian(prob, th):
-    """Residuals r [n, V] = log(1 + E) - log(1 + C) at theta [n, K, 3] and their Jacobian
-    [n, V, 3K] in theta (ratio logits, log mean, log cv; index 3k + q), from one pass of
-    the smoothed form's Jacobian kernel and the chain rule through prob.params."""
+def param_jacobian(th, prm):
+    """dP/dtheta [n, 3K, 3K] (index 3k + q on both sides) of prob.params: ratios = softmax of
+    the logits, mean = e^b, sd = mean e^c."""
     n, K = th.shape[0], th.shape[1]
+    r = torch.softmax(th[..., 0], dim=1)
+    D = torch.zeros(n, K, 3, K, 3, dtype=th.dtype, device=th.device)
+    D[:, :, 0, :, 0] = torch.diag_embed(r) - r[:, :, None] * r[:, None, :]
+    k = torch.arange(K, device=th.device)
+    D[:, k, 1, k, 1] = prm[..., 1]
+    D[:, k, 2, k, 1] = prm[..., 2]
+    D[:, k, 2, k, 2] = prm[..., 2]
+    return D.reshape(n, 3 * K, 3 * K)
+
+
+def gauss_newton_system(prob, th):
+    """Loss [n], J^T J [n, 3K, 3K] and J^T r [n, 3K] of the residuals r_v = log(1 + E_v) -
+    log(1 + C_v) in theta (ratio logits, log mean, log cv; index 3k + q): one device pass
+    (pc_smooth_gauss_newton gives the system in (ratio, mean, sd)) and the chain rule on the
+    3K x 3K matrices."""
     prm = prob.params(th)
-    E, JP = prob.smooth.jacobian(prm)
-    r_ = torch.softmax(th[..., 0], dim=1)[:, None, :]     # [n, 1, K]
-    m_, sd_ = prm[..., 1][:, None, :], prm[..., 2][:, None, :]
-    Jr = JP[..., 0]
-    Ja = r_ * (Jr - (Jr * r_).sum(-1, keepdim=True))      # through the softmax
-    Jb = JP[..., 1] * m_ + JP[..., 2] * sd_                 # mean = e^b, sd = mean e^c
-    Jc = JP[..., 2] * sd_
-    J = torch.stack([Ja, Jb, Jc], dim=-1).reshape(n, -1, 3 * K) / (1.0 + E)[..., None]
-    return torch.log1p(E) - torch.log1p(prob.target), J
+    f, A_p, g_p = prob.smooth.gauss_newton(prm, prob.target)
+    D = param_jacobian(th, prm)
+    Dt = D.transpose(1, 2)
+    return f, Dt @ A_p @ D, (Dt @ g_p[..., None])[..., 0]
 
 
 def levenberg_marquardt(prob, theta0, iters=40, lam0=1e-2, max_step=1.0, time_limit=None):
     """Levenberg-Marquardt from every candidate at once on the residuals r_v = log(1 + E_v) -
-    log(1 + C_v) of the smoothed form. One pass of the Jacobian kernel per iteration gives
-    the residuals and their Jacobian at the trial point; a candidate keeps its step if its
-    loss falls (damping / 3) and otherwise stays where it was (damping x 4). Steps solve
-    (J^T J + lam diag(J^T J)) d = -J^T r per candidate (9 x 9 for three types)."""
+    log(1 + C_v) of the smoothed form. One Gauss-Newton pass per iteration (the Jacobian
+    kernel, reduced on the device to J^T J, J^T r and the loss) at the trial point; a
+    candidate keeps its step if its loss falls (damping / 3) and otherwise stays where it was
+    (damping x 4). Steps solve (J^T J + lam diag(J^T J)) d = -J^T r per candidate (9 x 9 for
+    three types)."""
     lo, hi = prob.box()
     n, K = theta0.shape[0], theta0.shape[1]
     P = 3 * K
     eye = torch.eye(P, dtype=torch.float64, device=theta0.device)
-
-    def evaluate(th):
-        res, J = residual_jacobian(prob, th)
-        return res, J, (res * res).sum(1)
-
     th = theta0.clone()
     lam = torch.full((n,), lam0, dtype=torch.float64, device=th.device)
     if th.is_cuda:
         torch.cuda.synchronize()
     t0 = time.perf_counter()
-    res, J, f = evaluate(th)
+    f, A, g = gauss_newton_system(prob, th)
     i = int(torch.argmin(f))
     best = float(f[i])
     trace = [(time.perf_counter() - t0, best)]
     snaps = [(trace[0][0], th[i].clone())]
     for _ in range(iters):
-        # J^T J and J^T r from one FP32 batched product of [J | r] with itself (the damped
-        # Gauss-Newton matrix only steers the step; acceptance uses the FP64 loss)
-        Jr = torch.cat([J, res[..., None]], dim=-1).to(torch.float32)
-        M = (Jr.transpose(1, 2) @ Jr).to(torch.float64)
-        A, g = M[:, :P, :P], M[:, :P, P]
         d = torch.diagonal(A, dim1=1, dim2=2)
-        Ad = A + torch.diag_embed(lam[:, None] * d) + 1e-9 * d.amax(1)[:, None, None] * eye
+        Ad = A + torch.diag_embed(lam[:, None] * d) + 1e-12 * d.amax(1)[:, None, None] * eye
         step = torch.linalg.solve_ex(Ad, -g[..., None])[0][..., 0]
         step = torch.nan_to_num(step, nan=0.0, posinf=0.0, neginf=0.0).clamp(-max_step, max_step)
         th_new = torch.minimum(torch.maximum(th + step.reshape(n, K, 3), lo - 2.0), hi + 2.0)
-        res2, J2, f2 = evaluate(th_new)
+        f2, A2, g2 = gauss_newton_system(prob, th_new)
         ok = f2 < f  # NaN losses are never accepted
         th = torch.where(ok[:, None, None], th_new, th)
-        res = torch.where(ok[:, None], res2, res)
-        J = torch.where(ok[:, None, None], J2, J)
+        A = torch.where(ok[:, None, None], A2, A)
+        g = torch.where(ok[:, None], g2, g)
         f = torch.where(ok, f2, f)
         lam = torch.where(ok, lam / 3.0, lam * 4.0).clamp(1e-7, 1e7)
         i = int(torch.argmin(f))
@@ -338,7 +339,8 @@ def compare(engine, candidates=256, seed=7, gd_iters=300, pso_seconds=40.0, path
         "lm": {"iters": len(lm) - 1, "seconds": lm[-1][0], "best_smoothed_loss": lm[-1][1],
                "best_accurate_loss": best_final(acc_lm),
                "seconds_per_iter": lm[-1][0] / max(1, len(lm) - 1),
-               "method": "Levenberg-Marquardt on the smoothed form, Jacobian kernel (one pass per iteration)"},
+               "method": "Levenberg-Marquardt on the smoothed form, one Gauss-Newton pass (Jacobian kernel "
+                         "reduced on the device) per iteration"},
         "gd": {"iters": len(gd), "seconds": gd[-1][0], "best_smoothed_loss": gd[-1][1],
                "best_accurate_loss": best_final(acc_gd), "method": "Adam on the smoothed form, cosine lr 0.1 -> 0.002"},
         "pso_smooth": {"iters": len(ps) - 1, "seconds": ps[-1][0], "best_smoothed_loss": ps[-1][1],

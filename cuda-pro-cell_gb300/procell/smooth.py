@@ -76,6 +76,24 @@ class Smooth:
                                                             ctypes.c_void_p(J.data_ptr())))
         return E, J
 
+    def gauss_newton(self, params: torch.Tensor, target: torch.Tensor):
+        """(loss [C], jtj [C, P, P], jtr [C, P]) of sum_v (log1p(E_v) - log1p(target_v))^2,
+        P = 3 n_types in the order of params' last two dimensions (type, parameter)."""
+        p = params.detach().to(torch.float64).contiguous()
+        t = target.detach().to(torch.float64).contiguous()
+        assert p.is_cuda and p.dim() == 3 and p.shape[1] == self.n_types and p.shape[2] == 3
+        assert t.is_cuda and t.numel() == self.n_values
+        C, P = p.shape[0], 3 * self.n_types
+        loss = torch.empty(C, dtype=torch.float64, device=p.device)
+        jtj = torch.empty(C, P, P, dtype=torch.float64, device=p.device)
+        jtr = torch.empty(C, P, dtype=torch.float64, device=p.device)
+        self._bind_stream()
+        V = ctypes.c_void_p
+        self.engine._check(self.engine.L.pc_smooth_gauss_newton(
+            self.engine.ctx, self.handle, V(p.data_ptr()), C, V(t.data_ptr()), V(loss.data_ptr()),
+            V(jtj.data_ptr()), V(jtr.data_ptr())))
+        return loss, jtj, jtr
+
     def sync(self):
         self.engine._check(self.engine.L.pc_smooth_sync(self.engine.ctx))
 

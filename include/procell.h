@@ -265,6 +265,14 @@ int pc_smooth_backward(pc_context* ctx, pc_smooth* s, const double* params, uint
                        const double* grad_expected, double* grad_params);
 int pc_smooth_jacobian(pc_context* ctx, pc_smooth* s, const double* params, uint32_t n_candidates,
                        double* expected, double* jacobian);
+/* The Gauss-Newton system of the squared log-count loss
+ * L_c = sum_v (log(1 + E_cv) - log(1 + target_v))^2 for every candidate, from one Jacobian
+ * pass reduced on the device: loss [n_candidates], jtj [n_candidates][P][P] and
+ * jtr [n_candidates][P] (P = 3 n_types, parameter order of params) with J_v = (dE_v / dparams)
+ * / (1 + E_v) and r_v = log(1 + E_v) - log(1 + target_v); target is a device array
+ * [n_values]. For Levenberg-Marquardt searches that need neither E nor J themselves. */
+int pc_smooth_gauss_newton(pc_context* ctx, pc_smooth* s, const double* params, uint32_t n_candidates,
+                           const double* target, double* loss, double* jtj, double* jtr);
 int pc_smooth_sync(pc_context* ctx);
 void pc_smooth_destroy(pc_smooth* s);
 

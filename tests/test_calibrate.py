@@ -1,8 +1,8 @@
 """The calibration harness (procell/calibrate.py).
 
 CPU: the searches' host logic on a stand-in problem whose expected counts are an analytic
-Gaussian mixture with an exact Jacobian: the chain rule from (ratio, mean, sd) to the
-unconstrained coordinates against torch autograd, Levenberg-Marquardt recovering the
+Gaussian mixture with an exact Jacobian: the Gauss-Newton system's chain rule from (ratio,
+mean, sd) to the unconstrained coordinates against torch autograd, Levenberg-Marquardt recovering the
 parameters of a noise-free target, the particle swarm staying in its box and improving.
 GPU: Levenberg-Marquardt on the smoothed form of the real calibration input reaches the
 loss of the hidden parameters' neighbourhood within a few Jacobian passes.
@@ -37,6 +37,13 @@ class MixtureSmooth:
         J = torch.stack([g, r * g * d / (s * s), r * g * d * d / (s * s * s)], dim=-1)
         return (r * g).sum(-1), J
 
+    def gauss_newton(self, prm, target):
+        """The same contract as procell.smooth.Smooth.gauss_newton."""
+        E, J = self.jacobian(prm)
+        J = J.reshape(J.shape[0], J.shape[1], -1) / (1.0 + E)[..., None]
+        r = torch.log1p(E) - torch.log1p(target)
+        return (r * r).sum(1), J.transpose(1, 2) @ J, (J * r[..., None]).sum(1)
+
 
 class MixtureProblem(cb.Problem):
     def __init__(self, hidden):
@@ -62,19 +69,22 @@ class MixtureProblem(cb.Problem):
 HIDDEN = [(0.5, 40.0, 6.0), (0.3, 75.0, 9.0), (0.2, 110.0, 15.0)]
 
 
-def test_residual_jacobian_chain_rule():
+def test_gauss_newton_system_chain_rule():
+    """Loss, J^T J and J^T r in theta against torch autograd of the residuals."""
     prob = MixtureProblem(HIDDEN)
     th = prob.start(4, 1)
-    res, J = cb.residual_jacobian(prob, th)
+    f, A, g = cb.gauss_newton_system(prob, th)
 
-    def f(t):
+    def res(t):
         E = prob.smooth.forward(prob.params(t[None]))[0]
         return torch.log1p(E) - torch.log1p(prob.target)
 
     for c in range(th.shape[0]):
-        ref = torch.autograd.functional.jacobian(f, th[c]).reshape(prob.smooth.n_values, -1)
-        assert torch.allclose(res[c], f(th[c]))
-        assert torch.allclose(J[c], ref, rtol=1e-10, atol=1e-12), (J[c] - ref).abs().max()
+        J = torch.autograd.functional.jacobian(res, th[c]).reshape(prob.smooth.n_values, -1)
+        r = res(th[c])
+        assert torch.allclose(f[c], (r * r).sum())
+        assert torch.allclose(A[c], J.T @ J, rtol=1e-9, atol=1e-12 * float((J.T @ J).abs().max()))
+        assert torch.allclose(g[c], J.T @ r, rtol=1e-9, atol=1e-12 * float((J.T @ r).abs().max()))
 
 
 def test_levenberg_marquardt_recovers_parameters():

@@ -189,6 +189,38 @@ def test_many_types_match_cpu_restatement(engine):
     assert np.allclose(J, J_ref, rtol=2e-5, atol=1e-7 * np.abs(J_ref).max())
 
 
+@pytest.mark.parametrize("K", [3, 8])
+def test_gauss_newton_matches_jacobian(engine, K):
+    """pc_smooth_gauss_newton (loss, J^T J, J^T r of the squared log-count loss, reduced on
+    the device) against the same quantities formed from pc_smooth_jacobian; K = 8 uses every
+    output slot of the reduction (24 parameters: 300 + 24 + 1 outputs per candidate)."""
+    from procell.smooth import Smooth
+    bins = calib_bins(n_bins=40, cells=4000, seed=9)
+    sm = Smooth(engine, bins, n_types=K, t_max=150.0, phi=None, h=0.5, paths=2, seed=21)
+    rng = np.random.default_rng(K)
+    C = 45
+    params = []
+    for c in range(C):
+        r = rng.dirichlet(np.ones(K))
+        params.append([[float(r[k]), float(rng.uniform(25, 90)), float(rng.uniform(2, 15))] for k in range(K)])
+    if K > 2:
+        params[3][1][1:] = [-1.0, -1.0]
+    P = params_tensor(params)
+    target = sm.forward(P[:1])[0] * 1.3 + 2.0
+    f, A, g = sm.gauss_newton(P, target)
+    E, J = sm.jacobian(P)
+    sm.sync()
+    sm.close()
+    Jv = J.reshape(C, sm.n_values, 3 * K) / (1.0 + E)[..., None]
+    r = torch.log1p(E) - torch.log1p(target)
+    assert torch.allclose(f, (r * r).sum(1), rtol=1e-12, atol=0)
+    A_ref = Jv.transpose(1, 2) @ Jv
+    g_ref = (Jv * r[..., None]).sum(1)
+    assert torch.allclose(A, A_ref, rtol=1e-10, atol=1e-13 * float(A_ref.abs().max()))
+    assert torch.allclose(g, g_ref, rtol=1e-10, atol=1e-13 * float(g_ref.abs().max()))
+    assert torch.equal(A, A.transpose(1, 2))
+
+
 def test_candidate_order_does_not_change_results(smooth_setup):
     """Kernels visit each type's candidates in order of that type's mean; a candidate's
     results are the same bits wherever it sits in the batch."""
