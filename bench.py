@@ -273,14 +273,17 @@ def run_ours(args):
     barrier()
     elapsed_ms = e0.elapsed_time(e1)
 
-    # end to end through the C ABI: host inputs, upload, run, histogram download + merge
+    # end to end through the C ABI: host inputs (the histogram as a pc_bin array in host
+    # memory, as pc_load_histogram returns it), upload, run, histogram download + merge
+    from procell import _lib
+    bins_host = _lib.bins_numpy(w.bins)
     e2e_t = 0.0
     h2d = d2h = 0
     e2e_div = 0
     for _ in range(args.steps):
         torch.cuda.synchronize()
         t = time.perf_counter()
-        res = eng.simulate(w.bins, w.types, w.t_max, w.phi, seed)
+        res = eng.simulate(bins_host, w.types, w.t_max, w.phi, seed)
         e2e_t += time.perf_counter() - t
         h2d += res.stats["h2d_bytes"]
         d2h += res.stats["d2h_bytes"]
