@@ -658,6 +658,14 @@ def run_calibration(args):
     j1.record(stream)
     torch.cuda.synchronize()
     jac_ms = j0.elapsed_time(j1) / args.steps
+    # loss and its gradient (plus J^T J) by forward mode: one Gauss-Newton pass
+    prob.smooth.gauss_newton(P0, prob.target)
+    j0.record(stream)
+    for _ in range(args.steps):
+        prob.smooth.gauss_newton(P0, prob.target)
+    j1.record(stream)
+    torch.cuda.synchronize()
+    gn_ms = j0.elapsed_time(j1) / args.steps
     comp = cb.compare(eng, candidates=C, seed=7, pso_seconds=30.0)
     comp.pop("traces", None)
     cpu = None
@@ -690,6 +698,9 @@ def run_calibration(args):
         "calibration": comp,
         "jacobian_pass": {"ms": jac_ms, "candidates_per_s": C / (jac_ms * 1e-3),
                           "what": "expected counts and their Jacobian in (ratio, mean, sd) for %d candidates" % C},
+        "forward_mode": {"ms": gn_ms, "grads_per_s": C / (gn_ms * 1e-3),
+                         "what": "loss, its gradient (J^T r) and J^T J of %d candidates in one forward-mode "
+                                 "pass (pc_smooth_gauss_newton); the value above is forward + adjoint" % C},
         "e2e": {"value": C * args.steps / e2e_s, "unit": "grads/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "hbm", "achieved": alg / (elapsed_ms * 1e-3 / args.steps) / 1e9, "peak": hbm,
