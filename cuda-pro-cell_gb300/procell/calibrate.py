@@ -188,40 +188,67 @@ def gauss_newton_system(prob, th):
     return f, Dt @ A_p @ D, (Dt @ g_p[..., None])[..., 0]
 
 
-def levenberg_marquardt(prob, theta0, iters=40, lam0=1e-2, max_step=1.0, time_limit=None):
+def levenberg_marquardt(prob, theta0, iters=40, lam0=1e-2, max_step=1.0, time_limit=None, graph=True):
     """Levenberg-Marquardt from every candidate at once on the residuals r_v = log(1 + E_v) -
     log(1 + C_v) of the smoothed form. One Gauss-Newton pass per iteration (the Jacobian
     kernel, reduced on the device to J^T J, J^T r and the loss) at the trial point; a
     candidate keeps its step if its loss falls (damping / 3) and otherwise stays where it was
     (damping x 4). Steps solve (J^T J + lam diag(J^T J)) d = -J^T r per candidate (9 x 9 for
-    three types)."""
+    three types). On a GPU one iteration (the pass and every small tensor operation around
+    it) is captured once into a CUDA graph before the clock starts and replayed; without a
+    GPU, or if capture fails, iterations run eagerly with the same arithmetic."""
     lo, hi = prob.box()
     n, K = theta0.shape[0], theta0.shape[1]
     P = 3 * K
     eye = torch.eye(P, dtype=torch.float64, device=theta0.device)
+    # state, updated in place by step()
     th = theta0.clone()
     lam = torch.full((n,), lam0, dtype=torch.float64, device=th.device)
+    f, A, g = gauss_newton_system(prob, th)
+
+    def step():
+        d = torch.diagonal(A, dim1=1, dim2=2)
+        Ad = A + torch.diag_embed(lam[:, None] * d) + 1e-12 * d.amax(1)[:, None, None] * eye
+        st = torch.linalg.solve_ex(Ad, -g[..., None])[0][..., 0]
+        st = torch.nan_to_num(st, nan=0.0, posinf=0.0, neginf=0.0).clamp(-max_step, max_step)
+        th_new = torch.minimum(torch.maximum(th + st.reshape(n, K, 3), lo - 2.0), hi + 2.0)
+        f2, A2, g2 = gauss_newton_system(prob, th_new)
+        ok = f2 < f  # NaN losses are never accepted
+        th.copy_(torch.where(ok[:, None, None], th_new, th))
+        A.copy_(torch.where(ok[:, None, None], A2, A))
+        g.copy_(torch.where(ok[:, None], g2, g))
+        f.copy_(torch.where(ok, f2, f))
+        lam.copy_(torch.where(ok, lam / 3.0, lam * 4.0).clamp(1e-7, 1e7))
+
+    run = step
+    if graph and th.is_cuda:
+        try:
+            side = torch.cuda.Stream()
+            side.wait_stream(torch.cuda.current_stream())
+            with torch.cuda.stream(side):
+                step()  # warm-up outside capture (library scratch, solver workspaces)
+            torch.cuda.current_stream().wait_stream(side)
+            cg = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(cg):
+                step()
+            run = cg.replay
+        except Exception:
+            run = step
+        th.copy_(theta0)
+        lam.fill_(lam0)
     if th.is_cuda:
         torch.cuda.synchronize()
     t0 = time.perf_counter()
-    f, A, g = gauss_newton_system(prob, th)
+    f0, A0, g0 = gauss_newton_system(prob, th)
+    f.copy_(f0)
+    A.copy_(A0)
+    g.copy_(g0)
     i = int(torch.argmin(f))
     best = float(f[i])
     trace = [(time.perf_counter() - t0, best)]
     snaps = [(trace[0][0], th[i].clone())]
     for _ in range(iters):
-        d = torch.diagonal(A, dim1=1, dim2=2)
-        Ad = A + torch.diag_embed(lam[:, None] * d) + 1e-12 * d.amax(1)[:, None, None] * eye
-        step = torch.linalg.solve_ex(Ad, -g[..., None])[0][..., 0]
-        step = torch.nan_to_num(step, nan=0.0, posinf=0.0, neginf=0.0).clamp(-max_step, max_step)
-        th_new = torch.minimum(torch.maximum(th + step.reshape(n, K, 3), lo - 2.0), hi + 2.0)
-        f2, A2, g2 = gauss_newton_system(prob, th_new)
-        ok = f2 < f  # NaN losses are never accepted
-        th = torch.where(ok[:, None, None], th_new, th)
-        A = torch.where(ok[:, None, None], A2, A)
-        g = torch.where(ok[:, None], g2, g)
-        f = torch.where(ok, f2, f)
-        lam = torch.where(ok, lam / 3.0, lam * 4.0).clamp(1e-7, 1e7)
+        run()
         i = int(torch.argmin(f))
         if float(f[i]) < best:
             best = float(f[i])

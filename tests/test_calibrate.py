@@ -140,3 +140,15 @@ def test_plain_loss_matches_single_runs(engine):
         ref = ((np.log1p(r.totals.astype(np.float64)) - tgt) ** 2).sum()
         assert L1[i] == pytest.approx(ref, rel=1e-12)
     assert np.array_equal(L1, L2) and not np.array_equal(L1, L3)
+
+
+@pytest.mark.gpu
+def test_levenberg_marquardt_graph_equals_eager(engine):
+    """The CUDA-graph replay of a Levenberg-Marquardt iteration computes exactly what the
+    eager iteration computes."""
+    prob = cb.Problem(engine, seed=7)
+    th0 = prob.start(48, 11)
+    ta, sa = cb.levenberg_marquardt(prob, th0, iters=6, graph=True)
+    tb, sb = cb.levenberg_marquardt(prob, th0, iters=6, graph=False)
+    assert [l for _, l in ta] == [l for _, l in tb]
+    assert torch.equal(sa[-1][1], sb[-1][1])
