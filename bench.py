@@ -357,11 +357,17 @@ def run_ours(args):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": (achieved / hbm) if achieved else None, "traffic": traffic,
                      "peak_source": peak_kind,
+                     "dram_achieved": (traffic * launches / (divide_ms * 1e-3) / 1e9)
+                     if (traffic and divide_ms > 0) else None,
+                     "dram_frac": (traffic * launches / (divide_ms * 1e-3) / 1e9 / hbm)
+                     if (traffic and divide_ms > 0) else None,
                      "kernel": "k_persist" if (tuning and tuning["driver"]) else "k_divide",
                      "launches_per_step": launches / args.steps,
                      "alg_bytes_per_launch": alg_bytes / launches,
                      "note": "alg bytes = 64 B per division (two 16-B nodes written+read); the "
-                             "kernel stores only daughters that divide again"
+                             "kernel stores only daughters that divide again, so its DRAM traffic "
+                             "(dram_achieved, from the ncu bytes per division in profiles/) is about "
+                             "half of that and the sweep is bound by instruction issue, not HBM"
                              + ("; the persistent launch also runs the root sweep" if persistent else "")},
         "gpu_launches": kernels,
         "clocks": clk,
