@@ -89,8 +89,6 @@ struct InstanceHost {
   uint32_t fallback = 0, gmax = 0;
   double t_max = 0.0, phi = 0.0;
   uint64_t seed = 0, roots = 0;
-  float t_hi = 0.f, t_lo = 0.f;
-  int est_ok = 0;
   // placement in the plan
   uint64_t root_begin = 0, class_begin = 0;
   uint32_t bin_begin = 0, type_begin = 0, hist_gens = 1;
@@ -193,7 +191,6 @@ void truncation_bounds(double mu, double sigma, float& zlo, float& zhi) {
   }
 }
 
-bool in_est_range(double x) { return x == 0.0 || (std::fabs(x) >= 1e-30 && std::fabs(x) <= 1e30); }
 
 void free_pool(pc_context* ctx) {
   for (auto& b : ctx->pool) {
@@ -303,7 +300,6 @@ ZigTables host_zig_tables() { return build_zig_tables(); }
 void host_truncation_bounds(double mu, double sigma, float& zlo, float& zhi) {
   truncation_bounds(mu, sigma, zlo, zhi);
 }
-bool host_in_est_range(double x) { return in_est_range(x); }
 }  // namespace pc
 
 extern "C" {
@@ -421,7 +417,7 @@ namespace {
 // division test `fluorescence / 2 > threshold` (proliferation.cu:323).
 // The type tables of an instance (I.t_max set): ratio-sum check, stable sort by ratio
 // descending, cumulative ratios in that order (parser.cu:46-66,184; cell.cu:81-104),
-// truncation bounds, the fallback type and the FP32 estimate band. Replaces I's type fields.
+// truncation bounds and the fallback type. Replaces I's type fields.
 int prepare_types(const pc_cell_type* types, uint32_t n_types, InstanceHost& I, std::string& msg) {
   if (n_types && !types) return msg = "null argument", PC_ERR_INVALID;
   if (n_types == 0)
@@ -442,8 +438,6 @@ int prepare_types(const pc_cell_type* types, uint32_t n_types, InstanceHost& I, 
   std::stable_sort(order.begin(), order.end(),
                    [&](uint32_t a, uint32_t b) { return types[a].ratio > types[b].ratio; });
   double acc = 0.0;
-  double max_mu = 0.0, max_sig = 0.0;
-  bool est_ok = in_est_range(I.t_max);
   for (uint32_t s = 0; s < n_types; ++s) {
     const pc_cell_type& src = types[order[s]];
     TypeDev t;
@@ -452,22 +446,15 @@ int prepare_types(const pc_cell_type* types, uint32_t n_types, InstanceHost& I, 
     t.cum = acc;
     t.mu = src.mean;
     t.sigma = src.sd;
-    t.mu_f = (float)src.mean;
-    t.sigma_f = (float)src.sd;
+    t.t_max = I.t_max;
     t.mode = src.mean < 0.0 ? kModeQuiescent : (src.mean == 0.0 ? kModeZeroMean : kModeNormal);
     truncation_bounds(src.mean, src.sd, t.zlo, t.zhi);
     if (t.mode == kModeZeroMean) {
       // tau = 0 for every cell of the type: with sigma = mu = 0, fma(0, z, 0) = +0 for any
       // z, so the kernels need no special case (and accept every z)
       t.sigma = 0.0;
-      t.sigma_f = 0.0f;
       t.zlo = -INFINITY;
       t.zhi = INFINITY;
-    }
-    if (t.mode == kModeNormal) {
-      max_mu = std::max(max_mu, std::fabs(src.mean));
-      max_sig = std::max(max_sig, std::fabs(src.sd));
-      est_ok = est_ok && in_est_range(src.mean) && in_est_range(src.sd);
     }
     I.types.push_back(t);
     I.sorted_to_file.push_back(order[s]);
@@ -475,15 +462,6 @@ int prepare_types(const pc_cell_type* types, uint32_t n_types, InstanceHost& I, 
   I.fallback = 0;
   for (uint32_t s = 0; s < n_types; ++s)
     if (types[order[s]].ratio > 0.0) I.fallback = s;
-  // FP32 estimate band: 8x the worst-case error 2^-21 (t_max + |mu| + 9|sigma|).
-  const double margin = std::ldexp(I.t_max + max_mu + 9.0 * max_sig, -18);
-  I.t_hi = std::nextafter((float)(I.t_max + margin), INFINITY);
-  I.t_lo = std::nextafter((float)(I.t_max - margin), -INFINITY);
-  I.est_ok = est_ok ? 1 : 0;
-  if (!est_ok) {  // the estimate decides nothing: every test is exact
-    I.t_hi = INFINITY;
-    I.t_lo = -INFINITY;
-  }
   return PC_OK;
 }
 
@@ -622,9 +600,6 @@ void batch_type_tables(const pc_plan* p, std::vector<BatchType>& btypes, std::ve
       BatchType bt;
       std::memset(&bt, 0, sizeof(bt));
       bt.t = I.types[k];
-      bt.t_max = I.t_max;
-      bt.t_hi = I.t_hi;
-      bt.t_lo = I.t_lo;
       bt.k0 = (uint32_t)I.seed;
       bt.k1 = (uint32_t)(I.seed >> 32);
       bt.root_begin = I.root_begin;
@@ -904,8 +879,6 @@ RunArgs make_args(const pc_context* ctx, const pc_plan* p) {
     a.k1 = (uint32_t)(I0.seed >> 32);
     philox_key_schedule(a.k0, a.k1, a.ks);
     a.t_max = I0.t_max;
-    a.t_hi = I0.t_hi;
-    a.t_lo = I0.t_lo;
     a.ntypes = (uint32_t)I0.types.size();
     a.fallback = I0.fallback;
     a.types = p->types_dev;
@@ -1459,9 +1432,6 @@ int pc_batch_set_types(pc_context* ctx, pc_batch* b, const pc_cell_type* types) 
     I.types.swap(next[i].types);
     I.sorted_to_file.swap(next[i].sorted_to_file);
     I.fallback = next[i].fallback;
-    I.t_hi = next[i].t_hi;
-    I.t_lo = next[i].t_lo;
-    I.est_ok = next[i].est_ok;
   }
   std::vector<BatchType> btypes;
   std::vector<InstanceDev> idev;

@@ -44,29 +44,28 @@ constexpr int kWarpsPerBlock = kBlock / 32;
 enum TypeMode : int32_t { kModeNormal = 0, kModeQuiescent = 1, kModeZeroMean = 2 };
 
 // One cell type, in the descending-ratio order the reference samples in.
-// The division sweep reads bytes 0-31 as one double2 and one float4.
+// The division sweep reads bytes 0-31 (mu, sigma, zlo, zhi, t_max) as two 16-byte loads.
 struct alignas(16) TypeDev {
-  double mu, sigma;
-  float mu_f, sigma_f;
-  float zlo, zhi;  // the FP32 z range for which fma(sigma, z, mu) > 0 (the truncation)
-  double cum;
-  int32_t mode;
+  double mu, sigma;  // 0, 8: tau = fma(sigma, z, mu)
+  float zlo, zhi;    // 16: the FP32 z range for which fma(sigma, z, mu) > 0 (the truncation)
+  double t_max;      // 24: its instance's t_max (read by the batched sweeps; plain: RunArgs)
+  double cum;        // 32: cumulative ratio in this order
+  int32_t mode;      // 40
   int32_t pad;
 };
 
 // Batched form: the parameters of one type together with its instance's (one table
 // entry per type of every instance, in instance order).
-// The division sweep reads bytes 0-31 (type) and 48-79 (instance) as 16-byte loads.
+// The division sweep reads bytes 0-31 (type, t_max) and 48-63 (seed, first cell) as three
+// 16-byte loads.
 struct alignas(16) BatchType {
   TypeDev t;            // bytes 0-47
-  double t_max;         // 48
-  float t_hi, t_lo;     // 56: FP32 band around t_max (+-inf: estimate never decides)
-  uint32_t k0, k1;      // 64: the instance's seed
-  uint64_t root_begin;  // 72: the instance's first initial cell in the batch
-  uint32_t instance;
-  uint32_t pad;
+  uint32_t k0, k1;      // 48: the instance's seed
+  uint64_t root_begin;  // 56: the instance's first initial cell in the batch
+  uint32_t instance;    // 64
+  uint32_t pad[3];
 };
-static_assert(sizeof(TypeDev) == 48 && sizeof(BatchType) == 96, "layout read by the division sweep");
+static_assert(sizeof(TypeDev) == 48 && sizeof(BatchType) == 80, "layout read by the division sweep");
 
 struct InstanceDev {
   uint32_t type_begin, ntypes, fallback, pad;
@@ -79,8 +78,6 @@ struct RunArgs {
   uint32_t k0, k1;           // seed
   uint32_t ks[20];           // Philox key schedule of the seed
   double t_max;
-  float t_hi, t_lo;          // FP32 band around t_max (+-inf when the inputs leave the
-                             // FP32 estimate's range: the estimate then never decides)
   uint32_t ntypes, nbins, fallback;
   uint32_t hist_gens;
   uint32_t g_store_max;      // deepest generation a stored key can hold
@@ -222,6 +219,5 @@ int launch_smooth_gauss_newton(const SmoothArgs& A, const double* params, uint32
 // Host helpers (pc_api.cpp).
 ZigTables host_zig_tables();
 void host_truncation_bounds(double mu, double sigma, float& zlo, float& zhi);
-bool host_in_est_range(double x);
 
 }  // namespace pc

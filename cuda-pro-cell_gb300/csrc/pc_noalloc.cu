@@ -183,8 +183,7 @@ extern "C" int pc_simulate_noalloc(const pc_bin* bins, uint64_t n_bins, const pc
     order[j] = o;
   }
   TypeDev tdev[kMaxTypes];
-  double acc = 0.0, max_mu = 0.0, max_sig = 0.0;
-  bool est_ok = host_in_est_range(tmax);
+  double acc = 0.0;
   uint32_t fallback = 0;
   for (uint32_t s = 0; s < n_types; ++s) {
     const pc_cell_type& src = types[order[s]];
@@ -194,24 +193,16 @@ extern "C" int pc_simulate_noalloc(const pc_bin* bins, uint64_t n_bins, const pc
     t.cum = acc;
     t.mu = src.mean;
     t.sigma = src.sd;
-    t.mu_f = (float)src.mean;
-    t.sigma_f = (float)src.sd;
+    t.t_max = tmax;
     t.mode = src.mean < 0.0 ? kModeQuiescent : (src.mean == 0.0 ? kModeZeroMean : kModeNormal);
     host_truncation_bounds(src.mean, src.sd, t.zlo, t.zhi);
     if (t.mode == kModeZeroMean) {
       t.sigma = 0.0;
-      t.sigma_f = 0.0f;
       t.zlo = -INFINITY;
       t.zhi = INFINITY;
     }
-    if (t.mode == kModeNormal) {
-      max_mu = std::max(max_mu, std::fabs(src.mean));
-      max_sig = std::max(max_sig, std::fabs(src.sd));
-      est_ok = est_ok && host_in_est_range(src.mean) && host_in_est_range(src.sd);
-    }
     if (src.ratio > 0.0) fallback = s;
   }
-  const double margin = std::ldexp(tmax + max_mu + 9.0 * max_sig, -18);
 
   // key layout (as pc_plan_create): the generation limit follows the full root count
   uint64_t key_chunk = std::max<uint64_t>(1, total);
@@ -330,12 +321,6 @@ extern "C" int pc_simulate_noalloc(const pc_bin* bins, uint64_t n_bins, const pc
   a.k1 = (uint32_t)(seed >> 32);
   philox_key_schedule(a.k0, a.k1, a.ks);
   a.t_max = tmax;
-  a.t_hi = std::nextafter((float)(tmax + margin), INFINITY);
-  a.t_lo = std::nextafter((float)(tmax - margin), -INFINITY);
-  if (!est_ok) {  // the estimate decides nothing: every test is exact
-    a.t_hi = INFINITY;
-    a.t_lo = -INFINITY;
-  }
   a.ntypes = n_types;
   a.nbins = (uint32_t)nb;
   a.nclass = (uint32_t)(nb * n_types);

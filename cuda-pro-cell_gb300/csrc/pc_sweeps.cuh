@@ -131,7 +131,7 @@ __device__ __forceinline__ float draw_z(uint32_t j, uint32_t layer, uint32_t wed
 enum Fate : int { kNone = 0, kLeaf = 1, kEmit = 2, kVanish = 3 };
 
 // GB300 runs FP64 arithmetic and every FP64<->FP32 conversion on a pipe of 2 lanes per
-// clock per SM, so the conversions and comparisons below are done on the bits instead.
+// clock per SM, so the conversion and the comparison below are done on the bits instead.
 //
 // Exact float -> double for zero or a normal float (z is never subnormal: |z| >= the
 // smallest ziggurat strip width, about 1e-10): rebias the exponent, widen the mantissa.
@@ -142,15 +142,6 @@ __device__ __forceinline__ double f32_to_f64(float z) {
   return __hiloint2double((int)hi, (int)(f << 29));
 }
 
-// A non-negative double truncated to FP32 (values below 2^-126 become 0; the estimate's
-// error band covers both truncations). Valid while d < 2^128; inputs that allow larger times
-// get an infinite band, so that the estimate is never used.
-__device__ __forceinline__ float f64_to_f32_rz(double d) {
-  const uint32_t hi = (uint32_t)__double2hiint(d), lo = (uint32_t)__double2loint(d);
-  if (hi < (897u << 20)) return 0.0f;
-  return __uint_as_float(((hi - (896u << 20)) << 3) | (lo >> 29));
-}
-
 // a > b for non-negative doubles (IEEE order equals integer order of the bit patterns).
 __device__ __forceinline__ bool gt_nonneg(double a, double b) {
   return __double_as_longlong(a) > __double_as_longlong(b);
@@ -159,47 +150,37 @@ __device__ __forceinline__ bool gt_nonneg(double a, double b) {
 // What a cell's type, and in the batched form its instance, supplies to the sweeps.
 struct TypeCtx {
   double mu, sigma;     // tau = fma(sigma, z, mu)
-  float mu_f, sigma_f;  // the same in FP32, for the estimate
   float zlo, zhi;       // truncation bounds on z
   double t_max;
-  float t_hi, t_lo;     // FP32 band around t_max (+-inf: the estimate never decides)
   uint64_t root_begin;  // batch index of the instance's first initial cell
   uint32_t k0, k1;      // the instance's seed
 };
 
 // The type's parameters from shared memory (plain form) or the batch table (batched form,
-// one entry per type of every instance), in four 16-byte loads at most.
+// one entry per type of every instance), in three 16-byte loads at most.
 template <bool Batched>
 __device__ __forceinline__ TypeCtx type_ctx(const RunArgs& a, const TypeDev* smem_types, uint32_t ty) {
   TypeCtx c;
   if (Batched) {
     const uint4* q = reinterpret_cast<const uint4*>(a.btypes + ty);
-    const uint4 q0 = __ldg(q), q1 = __ldg(q + 1), q3 = __ldg(q + 3), q4 = __ldg(q + 4);
+    const uint4 q0 = __ldg(q), q1 = __ldg(q + 1), q3 = __ldg(q + 3);
     c.mu = __hiloint2double((int)q0.y, (int)q0.x);
     c.sigma = __hiloint2double((int)q0.w, (int)q0.z);
-    c.mu_f = __uint_as_float(q1.x);
-    c.sigma_f = __uint_as_float(q1.y);
-    c.zlo = __uint_as_float(q1.z);
-    c.zhi = __uint_as_float(q1.w);
-    c.t_max = __hiloint2double((int)q3.y, (int)q3.x);
-    c.t_hi = __uint_as_float(q3.z);
-    c.t_lo = __uint_as_float(q3.w);
-    c.k0 = q4.x;
-    c.k1 = q4.y;
-    c.root_begin = ((uint64_t)q4.w << 32) | q4.z;
+    c.zlo = __uint_as_float(q1.x);
+    c.zhi = __uint_as_float(q1.y);
+    c.t_max = __hiloint2double((int)q1.w, (int)q1.z);
+    c.k0 = q3.x;
+    c.k1 = q3.y;
+    c.root_begin = ((uint64_t)q3.w << 32) | q3.z;
   } else {
     const TypeDev* t = smem_types + ty;
     const double2 ms = *reinterpret_cast<const double2*>(&t->mu);
-    const float4 fz = *reinterpret_cast<const float4*>(&t->mu_f);
+    const float2 z = *reinterpret_cast<const float2*>(&t->zlo);
     c.mu = ms.x;
     c.sigma = ms.y;
-    c.mu_f = fz.x;
-    c.sigma_f = fz.y;
-    c.zlo = fz.z;
-    c.zhi = fz.w;
+    c.zlo = z.x;
+    c.zhi = z.y;
     c.t_max = a.t_max;
-    c.t_hi = a.t_hi;
-    c.t_lo = a.t_lo;
     c.root_begin = 0;
     c.k0 = a.k0;
     c.k1 = a.k1;
@@ -212,21 +193,12 @@ __device__ __forceinline__ uint32_t rec_type(unsigned long long r) { return (uin
 __device__ __forceinline__ uint32_t rec_cap(unsigned long long r) { return (uint32_t)(r >> 48) & 0xFFu; }
 __device__ __forceinline__ bool rec_clamped(unsigned long long r) { return ((r >> 57) & 1ull) != 0ull; }
 
-// Fate of one daughter born at `birth` with normal z. The FP32 estimate decides leaves
-// and clear non-leaves without FP64 work; the band around t_max (8x the worst-case FP32
-// error) and every daughter that is stored use the exact FP64 due time
-// birth + fma(sigma, z, mu), the reference's t + timer.
-__device__ __forceinline__ int fate(double birth, float birth_f, float z, const TypeCtx& c,
-                                    bool can_divide, double& due) {
-  bool exact = true;
-  const float est = __fadd_rn(birth_f, __fadd_rn(c.mu_f, __fmul_rn(c.sigma_f, z)));
-  if (est > c.t_hi) return kLeaf;
-  if (est < c.t_lo) {
-    if (!can_divide) return kVanish;
-    exact = false;
-  }
+// Fate of one daughter born at `birth` with normal z: due = birth + fma(sigma, z, mu), the
+// reference's t + timer; a leaf if due > t_max (proliferation.cu:404-410), else it divides
+// again when its phi cap allows and vanishes when not.
+__device__ __forceinline__ int fate(double birth, float z, const TypeCtx& c, bool can_divide, double& due) {
   due = birth + fma(c.sigma, f32_to_f64(z), c.mu);
-  if (exact && gt_nonneg(due, c.t_max)) return kLeaf;
+  if (gt_nonneg(due, c.t_max)) return kLeaf;
   return can_divide ? kEmit : kVanish;
 }
 
@@ -509,16 +481,12 @@ __device__ __forceinline__ CellDraw classify(const ulonglong2 c, bool act, uint3
   const float zlo = tc.zlo, zhi = tc.zhi;
   const bool ok0 = act && (P.x & 0x7FFFFFFFu) < Z.k[l0] && z0 >= zlo && z0 <= zhi;
   const bool ok1 = act && (P.y & 0x7FFFFFFFu) < Z.k[l1] && z1 >= zlo && z1 <= zhi;
-  // FP32 estimates settle clear leaves and clear non-leaves; the exact FP64 due times
-  // decide the band and are what gets stored
-  const float df = f64_to_f32_rz(d);
-  const float est0 = __fadd_rn(df, __fadd_rn(tc.mu_f, __fmul_rn(tc.sigma_f, z0)));
-  const float est1 = __fadd_rn(df, __fadd_rn(tc.mu_f, __fmul_rn(tc.sigma_f, z1)));
-  const bool sure0 = est0 < tc.t_lo, sure1 = est1 < tc.t_lo;
+  // exact FP64 due times (the reference's t + timer): they decide leaves and are what an
+  // emitted daughter stores
   r.due0 = d + fma(tc.sigma, f32_to_f64(z0), tc.mu);
   r.due1 = d + fma(tc.sigma, f32_to_f64(z1), tc.mu);
-  const bool leaf0 = ok0 && (est0 > tc.t_hi || (!sure0 && gt_nonneg(r.due0, tc.t_max)));
-  const bool leaf1 = ok1 && (est1 > tc.t_hi || (!sure1 && gt_nonneg(r.due1, tc.t_max)));
+  const bool leaf0 = ok0 && gt_nonneg(r.due0, tc.t_max);
+  const bool leaf1 = ok1 && gt_nonneg(r.due1, tc.t_max);
   r.em0 = ok0 && !leaf0 && can_divide;
   r.em1 = ok1 && !leaf1 && can_divide;
   const bool van0 = ok0 && !leaf0 && !can_divide, van1 = ok1 && !leaf1 && !can_divide;
@@ -666,7 +634,7 @@ __device__ void divide_body(const RunArgs& a, const uint64_t root_base, const Le
       const u32x4 P = philox(u32x4{(uint32_t)parent, (uint32_t)(parent >> 32), root, kPurposePair}, tc.k0, tc.k1);
       const float z = slow_z(ch ? P.y : P.x, (P.z >> (8u * ch)) & 255u, pair_wedge_bits(P, ch), node, root,
                              tc.k0, tc.k1, tc.zlo, tc.zhi, s.zig_or(a), a.error);
-      f = fate(birth, f64_to_f32_rz(birth), z, tc, g1 < cap, due);
+      f = fate(birth, z, tc, g1 < cap, due);
       if (f == kLeaf) {
         if constexpr (C::kGlobalHist)
           atomicAdd(hist_g1 + (uint32_t)rec, 1ull);
