@@ -18,7 +18,7 @@
 // replica 0 shares its draws with the plain form run on the same seed.
 // Types enter analytically through ratio_k, so d/d ratio is exact. Weights are products of
 // sigmoids evaluated in log space (FP32; due times accumulate in FP64), never negative, and a
-// lineage stops once its survival product is below e^-100.
+// lineage stops once no later generation can add more than e^-40 cells.
 //
 // Adjoint. dw_g/dtheta = w_g (D_g + s_{g+1} / h dS_{g+1}/dtheta) with the running tangent
 // D_g = -sum_{i <= g} (1 - s_i) / h dS_i/dtheta, dS_j/dmean = U + j and dS_j/dsd = z_1 (1 + U)
@@ -106,7 +106,11 @@ __device__ __forceinline__ float f64_to_f32_rz_any(double d) {
   return __uint_as_float(sign | ((mag - (896u << 20)) << 3) | (lo >> 29));
 }
 
-constexpr float kLogNegligible = -100.0f;  // e^-100 * 2^63 < 1e-24
+// A lineage stops once no later generation can add more than e^-40 cells: every later leaf
+// weight is at most s_1 ... s_j (the running product) times 2^g <= 2^(steps - 1).
+constexpr float kLogNegligible = -40.0f;
+constexpr float kLn2 = 0.693147180559945f;
+__device__ __forceinline__ float stop_level(uint32_t steps) { return kLogNegligible - kLn2 * (float)steps; }
 
 // Lineage i of a bin whose initial cells start at r0 (initial cell r0 + i / paths, replica
 // i % paths, which draws as initial cell r + replica * ncells): its initial age, and the
@@ -144,6 +148,7 @@ __device__ __forceinline__ void walk(const SmoothArgs& A, const float* z, double
   float log_p = 0.0f;                         // log s_1 ... s_{j-1}
   float D_mu = 0.0f, D_sig = 0.0f;
   float wh = w_hi, wl = w_lo;                 // weight * 2^(j-1) as a pair of floats
+  const float stop = stop_level(steps);
   for (uint32_t j = 1;;) {
     const float x = f64_to_f32_rz_any(R) * inv_h;
     float ls, l1m;
@@ -179,7 +184,7 @@ __device__ __forceinline__ void walk(const SmoothArgs& A, const float* z, double
       }
     }
     log_p += ls;
-    if (log_p < kLogNegligible || ++j > steps) break;
+    if (log_p < stop || ++j > steps) break;
     zj = fixed_tau ? 0.0f : z[(j - 1) * 32u];
     tau = fixed_tau ? 0.0 : fma(sigma, f32_to_f64_bits(zj), mu);
     R = R - tau;
@@ -200,6 +205,7 @@ __device__ __forceinline__ void walk_jacobian(const SmoothArgs& A, const float* 
   float dmu = u1, dsig = zj * u1;
   float log_p = 0.0f, D_mu = 0.0f, D_sig = 0.0f;
   float scale = 1.0f;  // 2^(j-1)
+  const float stop = stop_level(steps);
   for (uint32_t j = 1;;) {
     const float x = f64_to_f32_rz_any(R) * inv_h;
     float ls, l1m;
@@ -222,7 +228,7 @@ __device__ __forceinline__ void walk_jacobian(const SmoothArgs& A, const float* 
     }
     scale *= 2.0f;
     log_p += ls;
-    if (log_p < kLogNegligible || ++j > steps) break;
+    if (log_p < stop || ++j > steps) break;
     zj = fixed_tau ? 0.0f : z[(j - 1) * 32u];
     tau = fixed_tau ? 0.0 : fma(sigma, f32_to_f64_bits(zj), mu);
     R = R - tau;

@@ -131,7 +131,9 @@ def forward_backward(bins, t_max, phi, h, paths, seed, params, grad_expected=Non
                                     G[c, k, 1:] += ratio * a * (D + s / h * dS)
                             D = D - math.exp(l1m) / h * dS
                             logp += ls
-                            if logp < -100.0:
+                            # the kernels' stopping rule: no later generation can add more
+                            # than e^-40 cells
+                            if logp < -40.0 - math.log(2.0) * (cap + 1):
                                 break
     if with_jacobian:
         return E, G, np.array(values), J
