@@ -1,6 +1,6 @@
 /* Test infrastructure only: the CPU oracle for the proliferation path.
  *
- * This library is the checker that the GPU engine is compared against. Nothing in the
+ * This library is the CPU restatement that the GPU engine is compared against. Nothing in the
  * product (the procell library, its kernels or its CLI) links, loads or calls it; only
  * the test suite, the smoke check and the benchmark's CPU-baseline leg do.
  *

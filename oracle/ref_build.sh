@@ -1,11 +1,11 @@
 #!/bin/bash
 # Test infrastructure only: builds the reference's own CUDA sources, unmodified, into
-# oracle/_ref/procell_ref for the distribution check (run on the GPU machine; it needs nvcc
+# oracle/_ref/procell_ref for the distribution check (run on a machine with a GPU; it needs nvcc
 # and links CUDA's device runtime for the reference's dynamic parallelism).
 #
 # Sources: /root/reference/src when mounted, else a copy placed in baseline/_ref/src
 # (git-ignored) by `oracle/ref_build.sh --stage` on a machine that has /root/reference.
-# The copy is never committed; it only travels with the working tree to the GPU box.
+# The copy is never committed; it only travels with the working tree to the GPU machine.
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
 ROOT="$(dirname "$HERE")"

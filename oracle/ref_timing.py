@@ -1,7 +1,7 @@
-"""Measurement infrastructure: wall time of the reference binary against this build's CLI.
+"""Measurement infrastructure: wall time of the reference binary against this engine's CLI.
 
 Run on a GPU machine from the repository root, after `oracle/ref_build.sh` has built
-oracle/_ref/procell_ref and `__graft_entry__.build()` this build's CLI:
+oracle/_ref/procell_ref and `__graft_entry__.build()` this engine's CLI:
 
     python oracle/ref_timing.py [--runs 10] [--types two|one]
 
@@ -10,7 +10,7 @@ about 1e4 initial cells, t_max 168, phi the smallest value), the way a caller of
 binary runs them: CUDA initialisation, reading the two input files, the simulation and the
 histogram on stdout. Runs alternate between the two binaries; the medians are reported. The
 reference is seeded through the preloaded time() shim (oracle/_ref/libtimeshim.so), as in
-tests/golden/make_reference_fixtures.py. The division count of this build's run (the
+tests/golden/make_reference_fixtures.py. The division count of this engine's run (the
 reference prints none) converts both wall times into divisions per second of wall time.
 Prints one JSON line. The reference is run only on this workload: on the larger ones its
 grid-size arithmetic wraps (src/simulation/proliferation.cu:245).

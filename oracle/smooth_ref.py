@@ -10,7 +10,7 @@ bits come from the oracle's Philox. Everything
 is evaluated in FP64 (the kernels use FP32 log-sigmoids), and the adjoint is obtained by
 forward-mode differentiation of the same loop, written separately from the kernel's.
 
-The reference has no smoothed form (it is new in this build); the plain-form pieces it uses
+The reference has no smoothed form (the smoothed form is new here); the plain-form pieces it uses
 (root age U = tau_1 * U_root, cells_population.cu:124-143; the division rule
 proliferation.cu:404-410; the phi cap proliferation.cu:323) are those of the oracle.
 """

@@ -1,4 +1,4 @@
-"""CPU checks of the oracle (the checker the GPU engine is compared against).
+"""CPU checks of the oracle (the CPU restatement the GPU engine is compared against).
 
 Pins: the published Philox4x32-10 known-answer vectors (Random123 distribution), the
 ziggurat construction's invariants and the statistics of the normal it produces, and

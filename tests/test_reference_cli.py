@@ -1,7 +1,7 @@
 """The CLI's flag contract against the reference binary itself.
 
 oracle/ref_build.sh compiles the reference's unmodified sources into oracle/_ref/procell_ref
-(here, where the sources are mounted, or on a GPU box from the staged copy). Its argument
+(here, where the sources are mounted, or on a GPU machine from the staged copy). Its argument
 handling (src/io/cmdargs.cpp:11-375) and its ratio-sum check (src/io/parser.cu:46-66) run
 before any CUDA call, so both binaries can be compared on a machine without a GPU. Skipped
 when the reference binary has not been built.
