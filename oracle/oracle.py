@@ -1,7 +1,8 @@
 """Test infrastructure only: ctypes wrapper of the CPU oracle (oracle/liboracle.so).
 
-Imported by the test suite, the smoke check and the benchmark's CPU-baseline leg as the
-checker for the GPU engine; the engine itself never loads this library.
+Imported by the test suite, the smoke check and the benchmark's CPU-baseline leg, as the
+CPU restatement the GPU engine is compared against; the engine itself never loads this
+library.
 """
 from __future__ import annotations
 
