@@ -537,3 +537,177 @@ float oracle_expf(float x) { return o_expf(x); }
 float oracle_logf(float u) { return o_logf(u); }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------- smoothed form ----
+// The smoothed, differentiable form restated in FP64, step for step as oracle/smooth_ref.py
+// states it (same lineages and draws, same stopping rule), multi-threaded for the
+// benchmark's CPU baseline. The reference has no smoothed form; its plain-form pieces are
+// those of the oracle above (initial age, division rule, phi cap).
+namespace {
+
+const uint32_t kPath = 0x40000000u;
+
+void log_sig(double x, double& ls, double& l1m) {
+  const double L = std::log1p(std::exp(-std::fabs(x)));
+  ls = -(std::max(-x, 0.0) + L);
+  l1m = -(std::max(x, 0.0) + L);
+}
+
+struct SmoothBin {
+  double v;
+  uint64_t f, r0;
+  uint32_t cap;
+  std::vector<int64_t> vi;  // generation -> output value index or -1
+};
+
+}  // namespace
+
+extern "C" int oracle_smooth(const double* values, const uint64_t* freqs, uint64_t nrows, double t_max,
+                             double phi, int phi_given, double h, uint32_t paths, uint64_t seed,
+                             const double* params, uint32_t ncand, uint32_t ntypes,
+                             const double* grad_expected, double* expected, double* grad,
+                             uint64_t nvalues_cap, uint64_t* nvalues, int nthreads) {
+  std::vector<SmoothBin> bins;
+  double thr = phi_given ? phi : 0.0;
+  for (uint64_t i = 0; i < nrows; ++i)
+    if (freqs[i] > 0 && !phi_given && (thr == 0.0 || values[i] < thr)) thr = values[i];
+  std::vector<double> vals;
+  uint64_t ncells = 0;
+  for (uint64_t i = 0; i < nrows; ++i) {
+    if (freqs[i] == 0) continue;
+    SmoothBin b;
+    b.v = values[i];
+    b.f = freqs[i];
+    b.r0 = ncells;
+    ncells += freqs[i];
+    b.cap = 0;
+    for (double x = b.v; x / 2 > thr && b.cap < 4096; x = x / 2) ++b.cap;
+    for (double x = b.v; x >= thr; x = x / 2) vals.push_back(x);
+    bins.push_back(b);
+  }
+  std::sort(vals.begin(), vals.end());
+  vals.erase(std::unique(vals.begin(), vals.end()), vals.end());
+  *nvalues = vals.size();
+  if (nvalues_cap < vals.size() || ncells * paths > 0xFFFFFFFFull) return -1;
+  const uint64_t V = vals.size();
+  for (SmoothBin& b : bins) {
+    double x = b.v;
+    for (uint32_t g = 0; g <= b.cap; ++g, x = x / 2) {
+      int64_t idx = -1;
+      if (g > 0 || b.v >= thr) {
+        auto it = std::lower_bound(vals.begin(), vals.end(), x);
+        if (it != vals.end() && *it == x) idx = it - vals.begin();
+      }
+      b.vi.push_back(idx);
+    }
+  }
+  const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+  const uint32_t K = ntypes, C = ncand;
+  unsigned nt = nthreads > 0 ? (unsigned)nthreads : std::max(1u, std::thread::hardware_concurrency());
+  nt = (unsigned)std::min<uint64_t>(nt, std::max<uint64_t>(1, ncells));
+  std::vector<std::vector<double>> E(nt, std::vector<double>((size_t)C * V, 0.0));
+  std::vector<std::vector<double>> G(nt, std::vector<double>((size_t)C * K * 3, 0.0));
+  const double ln2 = std::log(2.0);
+  auto work = [&](unsigned t) {
+    double* e = E[t].data();
+    double* gr = G[t].data();
+    std::vector<uint64_t> nodes;
+    std::vector<double> zs;
+    size_t bi = 0;
+    const uint64_t lo = ncells * t / nt, hi = ncells * (t + 1) / nt;
+    for (uint64_t r = lo; r < hi; ++r) {
+      while (r >= bins[bi].r0 + bins[bi].f) ++bi;
+      const SmoothBin& b = bins[bi];
+      const double stop = -40.0 - ln2 * (b.cap + 1);
+      for (uint32_t m = 0; m < paths; ++m) {
+        const uint32_t vr = (uint32_t)(r + (uint64_t)m * ncells);
+        const uint32_t rc[4] = {0u, 0u, vr, kRoot}, pc[4] = {0u, 0u, vr, kPath};
+        uint32_t rw[4], pw[4];
+        philox_block(rc, k0, k1, rw);
+        philox_block(pc, k0, k1, pw);
+        const double U = (double)((((uint64_t)rw[2] << 21) | (rw[3] >> 11)) + 1) * 1.1102230246251565e-16;
+        const uint64_t bits = (uint64_t)pw[0] | ((uint64_t)pw[1] << 32);
+        nodes.assign(b.cap + 1, 0);
+        zs.assign(b.cap + 1, 0.0);
+        uint64_t node = 1;
+        for (uint32_t j = 0; j <= b.cap; ++j) {
+          nodes[j] = node;
+          node = 2 * node + ((bits >> j) & 1ull);
+        }
+        for (uint32_t j = 0; j <= b.cap; ++j) {
+          const uint64_t parent = nodes[j] >> 1;
+          const uint32_t c = (uint32_t)(nodes[j] & 1ull);
+          const PairDraw p = pair_draw(parent, c, vr, k0, k1);
+          NodeStream ns(2 * parent + c, vr, k0, k1);
+          zs[j] = (double)ziggurat(p.j, p.layer, true, p.wedge, ns);
+        }
+        for (uint32_t c = 0; c < C; ++c)
+          for (uint32_t k = 0; k < K; ++k) {
+            const double* P = params + ((size_t)c * K + k) * 3;
+            const double ratio = P[0], mu = P[1];
+            double sd = P[2];
+            double* gk = gr + ((size_t)c * K + k) * 3;
+            if (mu < 0) {
+              if (b.vi[0] >= 0) {
+                e[(size_t)c * V + b.vi[0]] += ratio / paths;
+                if (grad_expected) gk[0] += grad_expected[(size_t)c * V + b.vi[0]] / paths;
+              }
+              continue;
+            }
+            if (mu == 0) sd = 0.0;
+            double S = 0.0, logp = 0.0, dS0 = 0.0, dS1 = 0.0, D0 = 0.0, D1 = 0.0;
+            for (uint32_t j = 1; j <= b.cap + 1; ++j) {
+              const double z = mu != 0 ? zs[j - 1] : 0.0;
+              const double tau = sd * z + mu;
+              if (j == 1) {
+                S = tau * U + tau;
+                dS0 = 1.0 + U;
+                dS1 = z * (1.0 + U);
+              } else {
+                S += tau;
+                dS0 += 1.0;
+                dS1 += z;
+              }
+              if (mu == 0) dS0 = dS1 = 0.0;
+              double ls, l1m;
+              log_sig((t_max - S) / h, ls, l1m);
+              const double w = std::exp(logp + l1m);
+              const uint32_t g = j - 1;
+              if (b.vi[g] >= 0) {
+                const double two_g = std::ldexp(1.0, (int)g);
+                e[(size_t)c * V + b.vi[g]] += ratio * two_g * w / paths;
+                if (grad_expected) {
+                  const double a = grad_expected[(size_t)c * V + b.vi[g]] * two_g * w / paths;
+                  gk[0] += a;
+                  const double s = std::exp(ls);
+                  gk[1] += ratio * a * (D0 + s / h * dS0);
+                  gk[2] += ratio * a * (D1 + s / h * dS1);
+                }
+              }
+              const double oms = std::exp(l1m);
+              D0 = D0 - oms / h * dS0;
+              D1 = D1 - oms / h * dS1;
+              logp += ls;
+              if (logp < stop) break;
+            }
+          }
+      }
+    }
+  };
+  std::vector<std::thread> pool;
+  for (unsigned t = 1; t < nt; ++t) pool.emplace_back(work, t);
+  work(0);
+  for (auto& th : pool) th.join();
+  for (size_t i = 0; i < (size_t)C * V; ++i) {
+    double s = 0.0;
+    for (unsigned t = 0; t < nt; ++t) s += E[t][i];
+    expected[i] = s;
+  }
+  if (grad)
+    for (size_t i = 0; i < (size_t)C * K * 3; ++i) {
+      double s = 0.0;
+      for (unsigned t = 0; t < nt; ++t) s += G[t][i];
+      grad[i] = s;
+    }
+  return 0;
+}

@@ -54,6 +54,14 @@ void oracle_normals(uint64_t seed, uint32_t root, uint64_t first_parent, uint64_
 /* The division time of child c of parent node n (truncated normal, tau > 0). */
 double oracle_tau(uint64_t seed, uint32_t root, uint64_t parent, uint32_t child, double mean,
                   double sd);
+/* The smoothed form (oracle/smooth_ref.py restated in C++, FP64, `nthreads` threads; 0 =
+ * all): expected counts [ncand][V] and, with grad_expected [ncand][V], the gradient
+ * [ncand][ntypes][3] of sum(grad_expected * expected) for params [ncand][ntypes][3]. V goes
+ * to *nvalues; returns -1 (nothing computed) when V > nvalues_cap. */
+int oracle_smooth(const double* values, const uint64_t* freqs, uint64_t nrows, double t_max, double phi,
+                  int phi_given, double h, uint32_t paths, uint64_t seed, const double* params,
+                  uint32_t ncand, uint32_t ntypes, const double* grad_expected, double* expected,
+                  double* grad, uint64_t nvalues_cap, uint64_t* nvalues, int nthreads);
 /* The FP32 exp/log helpers of the ziggurat's slow path. */
 float oracle_expf(float x);
 float oracle_logf(float u);

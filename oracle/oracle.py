@@ -52,6 +52,11 @@ def lib() -> ctypes.CDLL:
         L.oracle_tau.restype = ctypes.c_double
         L.oracle_tau.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint64,
                                  ctypes.c_uint32, ctypes.c_double, ctypes.c_double]
+        L.oracle_smooth.restype = ctypes.c_int
+        L.oracle_smooth.argtypes = [c_dp, c_u64p, ctypes.c_uint64, ctypes.c_double, ctypes.c_double,
+                                    ctypes.c_int, ctypes.c_double, ctypes.c_uint32, ctypes.c_uint64, c_dp,
+                                    ctypes.c_uint32, ctypes.c_uint32, c_dp, c_dp, c_dp, ctypes.c_uint64,
+                                    c_u64p, ctypes.c_int]
         L.oracle_expf.restype = ctypes.c_float
         L.oracle_expf.argtypes = [ctypes.c_float]
         L.oracle_logf.restype = ctypes.c_float
@@ -107,6 +112,32 @@ def simulate(bins, types, t_max, phi=None, seed=0, root_begin=0, root_end=None,
         L.oracle_result_free(h)
     keys = ["roots", "divisions", "leaves", "uncounted", "vanished", "max_gen"]
     return OracleResult(vals, tot, per, {k: int(v) for k, v in zip(keys, st)})
+
+
+def smooth(bins, t_max, phi, h, paths, seed, params, grad_expected=None, nthreads=0):
+    """The smoothed form in C++ (the restatement of smooth_ref.forward_backward, FP64,
+    multi-threaded): (expected [C][V], gradient [C][K][3] or None, values [V])."""
+    L = lib()
+    b = np.asarray(bins, dtype=np.float64).reshape(-1, 2) if len(bins) else np.zeros((0, 2))
+    values = np.ascontiguousarray(b[:, 0], dtype=np.float64)
+    freqs = np.ascontiguousarray([int(f) for _, f in bins] if len(bins) else [], dtype=np.uint64)
+    P = np.ascontiguousarray(params, dtype=np.float64)
+    C, K = P.shape[0], P.shape[1]
+    nv = ctypes.c_uint64()
+    args = (_ptr(values, ctypes.c_double), _ptr(freqs, ctypes.c_uint64), len(values), float(t_max),
+            float(phi) if phi else 0.0, 1 if phi else 0, float(h), int(paths), int(seed),
+            _ptr(P, ctypes.c_double), C, K)
+    dummy = np.zeros(1)
+    L.oracle_smooth(*args, None, _ptr(dummy, ctypes.c_double), None, 0, ctypes.byref(nv), 1)
+    V = int(nv.value)
+    E = np.zeros((C, V))
+    G = np.zeros((C, K, 3)) if grad_expected is not None else None
+    gE = None if grad_expected is None else np.ascontiguousarray(grad_expected, dtype=np.float64)
+    rc = L.oracle_smooth(*args, None if gE is None else _ptr(gE, ctypes.c_double), _ptr(E, ctypes.c_double),
+                         None if G is None else _ptr(G, ctypes.c_double), V, ctypes.byref(nv), int(nthreads))
+    if rc != 0:
+        raise OracleError("oracle_smooth: value set larger than expected or too many lineages")
+    return E, G
 
 
 def philox(ctr, key):

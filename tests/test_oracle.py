@@ -216,6 +216,26 @@ def test_smooth_restatement_jacobian(oracle_lib):
             assert np.linalg.norm(J[0, :, k, q] - fd) <= 1e-5 * max(1.0, np.linalg.norm(fd)), (k, q)
 
 
+def test_smooth_restatement_in_cpp_matches_python(oracle_lib):
+    """The C++ restatement of the smoothed form (the benchmark's CPU baseline) equals the
+    Python one: bit for bit on one thread, to summation order on several."""
+    import smooth_ref
+    bins = [(640.0, 30), (37.0, 25), (3.0, 12), (1500.0, 0), (9.5, 17), (0.7, 6)]
+    params = [[[0.5, 30.0, 6.0], [0.3, 45.0, 18.0], [0.2, -1.0, -1.0]],
+              [[0.6, 25.0, 12.0], [0.4, 0.0, 1.0], [0.0, 40.0, 4.0]]]
+    nv = len(smooth_ref.prepare(bins, 1.0)[1])
+    gE = np.random.default_rng(3).normal(size=(2, nv))
+    E0, G0, _ = smooth_ref.forward_backward(bins, 150.0, 1.0, 0.5, 2, 987654321, params, gE)
+    E1, G1 = oracle_lib.smooth(bins, 150.0, 1.0, 0.5, 2, 987654321, params, gE, nthreads=1)
+    assert np.array_equal(E0, E1) and np.array_equal(G0, G1)
+    E2, G2 = oracle_lib.smooth(bins, 150.0, 1.0, 0.5, 2, 987654321, params, gE, nthreads=4)
+    assert np.allclose(E2, E0, rtol=1e-13, atol=1e-13 * np.abs(E0).max())
+    assert np.allclose(G2, G0, rtol=1e-12, atol=1e-12 * np.abs(G0).max())
+    E3, G3 = oracle_lib.smooth(bins, 150.0, None, 0.5, 1, 5, params[:1], nthreads=1)
+    E4, _, _ = smooth_ref.forward_backward(bins, 150.0, None, 0.5, 1, 5, params[:1])
+    assert G3 is None and np.array_equal(E3, E4)
+
+
 def test_smooth_restatement_replica_zero_is_the_plain_tree(oracle_lib):
     """With one lineage per cell and h -> 0, a cell's smoothed weight is an unbiased estimate
     of its own plain-form tree: enumerating every path reproduces the oracle's counts."""
