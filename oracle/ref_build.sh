@@ -6,6 +6,8 @@
 # Sources: /root/reference/src when mounted, else a copy placed in baseline/_ref/src
 # (git-ignored) by `oracle/ref_build.sh --stage` on a machine that has /root/reference.
 # The copy is never committed; it only travels with the working tree to the GPU machine.
+# `--if-mounted` (used by the package build) builds from the mounted sources only, and only
+# when the binary is missing or stale.
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
 ROOT="$(dirname "$HERE")"
@@ -16,6 +18,15 @@ if [[ "${1:-}" == "--stage" ]]; then
   cp -r /root/reference/src "$ROOT/baseline/_ref/src"
   echo "staged reference sources in baseline/_ref/src"
   exit 0
+fi
+if [[ "${1:-}" == "--if-mounted" ]]; then
+  # called by the package build: only where the reference is mounted, and only when the
+  # binary is missing or older than the sources
+  [[ -d /root/reference/src ]] || exit 0
+  if [[ -x "$OUT/procell_ref" && -z "$(find /root/reference/src "$HERE/ref_compat.h" "$HERE/ref_timeshim.c" \
+        -newer "$OUT/procell_ref" -print -quit)" ]]; then
+    exit 0
+  fi
 fi
 if [[ -d /root/reference/src ]]; then SRC=/root/reference/src; else SRC="$ROOT/baseline/_ref/src"; fi
 [[ -d "$SRC" ]] || { echo "reference sources not found" >&2; exit 2; }
