@@ -1,11 +1,12 @@
-"""Full-size checks through properties that do not depend on size.
+"""Full-size checks: bit-exact against the oracle, and properties that do not depend on size.
 
-The oracle finishes the small and medium workloads and 1/200 of the large one (the bit-exact
-tests); at the large workload's full size (1e7 initial cells, 3.6e9 divisions) and the
-batched workload's (6e8 initial cells) the engine is checked through properties that hold
-for any size: conservation of cells, additivity over shards of the initial cells, identical
-counts under every driver and compiled configuration, and, for the batched form, per
-instance equality with the plain form.
+The large workload (4096 bins, 1e7 initial cells, 3.6e9 divisions) is compared in full with
+the oracle run on every host core (about 20 s on 16 cores), as are 64 instances of the
+4096-instance batched workload, drawn at random, at their full size. Beside that, the
+engine is checked through properties that hold for any size: conservation of cells,
+additivity over shards of the initial cells, identical counts under every driver and
+compiled configuration, and, for the batched form, per instance equality with the plain
+form.
 """
 import numpy as np
 import pytest
@@ -41,6 +42,43 @@ def test_large_conservation(large_full):
     assert st["divisions"] > 3_000_000_000
     v = res.values
     assert np.all(np.diff(v) > 0) and v[0] >= w.phi
+
+
+def assert_same(g, o):
+    assert np.array_equal(g.values, o.values)
+    assert np.array_equal(g.totals, o.totals), np.flatnonzero(g.totals != o.totals)[:10]
+    assert np.array_equal(g.per_type, o.per_type)
+    for k in ("roots", "divisions", "leaves", "uncounted", "vanished"):
+        assert g.stats[k] == o.stats[k], (k, g.stats[k], o.stats[k])
+    assert g.stats["max_generation"] == o.stats["max_gen"]
+
+
+def test_large_full_size_bit_exact_vs_oracle(oracle_lib, large_full):
+    # every one of the 1e7 initial cells: the same chunking, slicing and leaf counts as
+    # the benchmarked run, against the CPU restatement of proliferation.cu:289-410
+    w, _, _, res, _ = large_full
+    o = oracle_lib.simulate(w.bins, w.types, w.t_max, w.phi, seed=w.seed, nthreads=0)
+    assert o.stats["divisions"] > 3_000_000_000
+    assert_same(res, o)
+
+
+def test_batched_workload_instances_bit_exact_vs_oracle(engine, oracle_lib):
+    # the benchmark's 4096-instance batch in one run; 64 instances drawn at random are
+    # each compared in full with the oracle's run of that instance alone
+    ws = cfg.batched()
+    b = engine.batch([(w.bins, w.types, w.t_max, w.phi, w.seed) for w in ws])
+    try:
+        b.run()
+        pick = np.random.default_rng(2024).choice(len(ws), size=64, replace=False)
+        for i in sorted(int(x) for x in pick):
+            w = ws[i]
+            o = oracle_lib.simulate(w.bins, w.types, w.t_max, w.phi, seed=w.seed, nthreads=0)
+            g = b.result(i)
+            assert np.array_equal(g.values, o.values), i
+            assert np.array_equal(g.per_type, o.per_type), i
+            assert np.array_equal(g.totals, o.totals), i
+    finally:
+        b.close()
 
 
 def test_large_shards_add_up(engine, large_full):

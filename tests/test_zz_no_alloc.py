@@ -6,6 +6,15 @@ synchronisation, deployments with a fixed memory budget): everything lives in on
 device array shared by all calls. These checks call it through the C ABI twice in a row
 (the second call sees the first call's leftovers in that array) and require the same
 uint64 counts, bit for bit, as pc_plan_run + pc_plan_raw_counts on the same inputs and seed.
+The inputs include one of about 1e6 initial cells, larger than one root chunk of the fixed
+array (so several chunks run and levels are cut into slices), one whose cell types are
+listed in ascending ratio order (the counts must come back in file order), and one whose
+lineages are deeper than 32 generations (the wide key layout); those three are also merged
+into the output value set and compared with the oracle directly.
+
+Out-of-memory rejection is tested on an input whose tables alone exceed the array. The
+other rejection, a lineage deeper than the array's level buffers, needs more than 40
+generations of divisions in one lineage, i.e. on the order of 2^40 cells, and is left out.
 
 This file is collected last so that a failure here leaves every other test already run; it
 also passes on its own in a fresh process.
@@ -43,15 +52,46 @@ def noalloc_counts(bins, types, t_max, phi, seed, capacity):
     return rc, out, tuple(dims), st, err.value.decode()
 
 
+def merged_from_raw(raw, bins, phi):
+    """The output value set's counts from raw [generation][bin][type] counts: a leaf of
+    generation g in bin b has the value v_b / 2^g (src/io/parser.cu:126-137)."""
+    vals = np.array([v for v, f in bins if f], np.float64)
+    out = {}
+    for g in range(raw.shape[0]):
+        for b in np.flatnonzero(raw[g].sum(axis=1)):
+            v = float(np.ldexp(vals[b], -g))
+            out[v] = out.get(v, 0) + raw[g, b].astype(np.uint64)
+    return out
+
+
+def assert_matches_oracle(oracle_lib, raw, bins, types, t_max, phi, seed):
+    o = oracle_lib.simulate(bins, types, t_max, phi, seed=seed, nthreads=0)
+    got = merged_from_raw(raw, bins, phi)
+    nz = np.flatnonzero(o.totals)
+    assert sorted(got) == [float(v) for v in o.values[nz]]
+    for i in nz:
+        assert np.array_equal(got[float(o.values[i])], o.per_type[i]), o.values[i]
+    return o
+
+
+MEDIUM = cfg.medium()
 CASES = {
     "small": (lambda w: (w.bins, w.types, w.t_max, w.phi, w.seed))(cfg.small()),
     "edge": ([(1000.0, 7), (3.0, 0), (0.5, 9), (64.0, 300)],
              [(0.5, 6.0, 2.0), (0.3, 0.0, 1.0), (0.2, -1.0, -1.0)], 40.0, 1.0, 99),
+    # about 1e6 initial cells: several root chunks of the fixed array, sliced levels
+    "medium": (MEDIUM.bins, MEDIUM.types, MEDIUM.t_max, MEDIUM.phi, MEDIUM.seed),
+    # the same with the types listed in ascending ratio order (sorted order != file order)
+    "medium_types_ascending": (MEDIUM.bins, MEDIUM.types[::-1], MEDIUM.t_max, MEDIUM.phi, MEDIUM.seed + 1),
+    # phi cap above 32 generations: the wide key layout
+    "wide_keys": ([(2.0 ** 40, 5), (2.0 ** 36, 3), (5.0, 4)], [(0.6, 10.0, 2.0), (0.4, 12.0, 3.0)],
+                  200.0, 1.0, 7),
 }
+ORACLE_CASES = ("medium", "medium_types_ascending", "wide_keys")
 
 
 @pytest.mark.parametrize("name", sorted(CASES))
-def test_noalloc_matches_regular_twice(engine, name):
+def test_noalloc_matches_regular_twice(engine, oracle_lib, name):
     bins, types, t_max, phi, seed = CASES[name]
     want, want_stats = regular_counts(engine, bins, types, t_max, phi, seed)
     for _ in range(2):
@@ -61,6 +101,13 @@ def test_noalloc_matches_regular_twice(engine, name):
         assert np.array_equal(out[:want.size].reshape(want.shape), want)
         assert st.divisions == want_stats["divisions"] and st.vanished == want_stats["vanished"]
         assert st.uncounted == want_stats["uncounted"]
+    if name in ORACLE_CASES:
+        o = assert_matches_oracle(oracle_lib, out[:want.size].reshape(want.shape), bins, types, t_max, phi, seed)
+        assert st.divisions == o.stats["divisions"] and st.vanished == o.stats["vanished"]
+    if name == "medium":
+        assert st.root_sweeps >= 3 and st.divisions > st.root_sweeps * 100_000  # several chunks and slices
+    if name == "wide_keys":
+        assert dims[0] > 34 and st.max_generation > 0
 
 
 def test_noalloc_reports_sizes(built):
