@@ -1,8 +1,9 @@
 #!/usr/bin/env python3
-"""Benchmark of the plain proliferation path: cell divisions per second.
+"""Benchmark of the proliferation path: cell divisions/s, instances/s, fwd+bwd grads/s.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--workload large|medium|small]
-    python bench.py --impl reference ...     # the CPU arm (see below)
+    python bench.py --workload batched|calibration     # one of the other forms alone
+    python bench.py --impl reference ...               # the CPU arm (see below)
 
 One step = one complete simulation of the workload (root sweep + every division sweep)
 from inputs already resident in HBM (`value`), and the same through the C ABI with host
@@ -10,6 +11,15 @@ buffers, the upload and the histogram download inside the timed region (`e2e`). 
 default workload is the 1e7-cell configuration: 4096 bins, fluorescence log-uniform on
 [1, 1e6], Poisson(2500) cells per bin, five types (means U[30, 60], sd 0.3 x mean,
 Dirichlet ratios), t_max 336, phi 1; 3.55e9 divisions per step.
+
+On one GPU the default line also carries, under "forms", the two other metrics of the path,
+each measured with its own value, e2e, roofline, CPU baseline and clocks: "batched" (4096
+uneven instances in one run, instances/s, against looping the plain form, every instance
+checked bit for bit against its plain run) and "calibration" (forward + loss gradient +
+adjoint of the smoothed form for 256 candidates, grads/s; Levenberg-Marquardt on the
+smoothed form against particle swarms to equal loss on five inputs, scored on the accurate
+smoothed loss and on the plain simulator's loss averaged over 16 seeds). --no-forms skips
+them.
 
 Under torchrun each rank runs its own instance (seed + rank) of the workload on its own
 GPU: weak scaling, no collective on the data path; value = all ranks' divisions / the
@@ -37,6 +47,7 @@ sys.path.insert(0, PKG)
 METRIC = "cell divisions/s"
 UNIT = "divisions/s"
 ALG_BYTES_PER_NODE = 32  # 16-byte cell state written once and read once per tree node
+FP64_OPS_PER_DIVISION = 4  # per daughter: tau = fma(sd, z, mean) and due = birth + tau
 
 
 def peaks():
@@ -192,17 +203,26 @@ def run_reference(args):
                          "cpu_model": cpu_model()},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    if not args.no_forms:
+        # the CPU restatements of the other two forms, one bounded sample each
+        cs = max(4.0, args.cpu_seconds / 2)
+        line["forms"] = {"batched": reference_batched_line(1, 0, cs),
+                         "calibration": reference_calibration_line(1, 0, cs)}
     print(json.dumps(line), flush=True)
     return 0
 
 
 def run_reference_batched(args):
+    print(json.dumps(reference_batched_line(args.steps, args.warmup, max(2.0, args.cpu_seconds / 2))), flush=True)
+    return 0
+
+
+def reference_batched_line(steps, warmup, per_step):
     instances = batched_instances()
-    per_step = max(2.0, args.cpu_seconds / 2)
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         cpu_batched_sample(instances, per_step / 4)
     vals, secs = [], 0.0
-    for _ in range(args.steps):
+    for _ in range(steps):
         c = cpu_batched_sample(instances, per_step)
         vals.append(c)
     done = sum(float(c["sample"].split()[2]) for c in vals)
@@ -210,7 +230,7 @@ def run_reference_batched(args):
     value = done / secs
     line = {
         "impl": "reference", "metric": "instances/s (batched form)", "value": value, "unit": "instances/s",
-        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
+        "n_gpus": 1, "steps": steps, "warmup": warmup, "ms_per_step": 1e3 * secs / steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded generator, procell/configs.py batched())",
         "config": {"workload": "batched: %d instances" % len(instances),
@@ -219,8 +239,7 @@ def run_reference_batched(args):
                          "sample": "; ".join(c["sample"] for c in vals)},
         "e2e": {"value": value, "unit": "instances/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
-    print(json.dumps(line), flush=True)
-    return 0
+    return line
 
 
 def run_ours(args):
@@ -320,6 +339,22 @@ def run_ours(args):
             traffic = per_div * divisions / launches
         except (ValueError, IndexError):
             traffic = None
+    # the division sweep's other ceilings: the FP64 pipe (two FMA + two adds per division,
+    # the daughters' exact due times) against its measured peak, and instruction issue
+    # (warp instructions per division from the ncu summary in profiles/) against four
+    # issue slots per SM per cycle at the sampled SM clock
+    fp64_peak = eng.peak("fp64")
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    ipd = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "instructions_per_division.txt")) as fh:
+            ipd = float(fh.read().split()[0])
+    except (OSError, ValueError, IndexError):
+        pass
+    fp64_rate = FP64_OPS_PER_DIVISION * divisions / (divide_ms * 1e-3) if divide_ms > 0 else None
+    issue_frac = None
+    if ipd and divide_ms > 0 and clk.get("sm_mhz"):
+        issue_frac = ipd * divisions / (divide_ms * 1e-3) / (4.0 * sms * clk["sm_mhz"] * 1e6)
     cpu = None
     if not args.no_cpu_baseline and world == 1:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -364,6 +399,13 @@ def run_ours(args):
                      "kernel": "k_persist" if (tuning and tuning["driver"]) else "k_divide",
                      "launches_per_step": launches / args.steps,
                      "alg_bytes_per_launch": alg_bytes / launches,
+                     "fp64_achieved": fp64_rate, "fp64_peak": fp64_peak,
+                     "fp64_frac": (fp64_rate / fp64_peak) if (fp64_rate and fp64_peak) else None,
+                     "fp64_unit": "FP64 lane-ops/s (%d per division; peak: pc_debug_peak FMA probe)"
+                                  % FP64_OPS_PER_DIVISION,
+                     "issue_frac": issue_frac,
+                     "issue_note": "%s warp instructions per division (ncu, profiles/) x divisions / "
+                                   "(4 x %d SMs x sampled SM clock)" % (ipd, sms),
                      "note": "alg bytes = 64 B per division (two 16-B nodes written+read); the "
                              "kernel stores only daughters that divide again, so its DRAM traffic "
                              "(dram_achieved, from the ncu bytes per division in profiles/) is about "
@@ -375,6 +417,17 @@ def run_ours(args):
     }
     if cpu:
         line["cpu_baseline"] = cpu
+    if world == 1 and not args.no_forms:
+        # the other two metrics of the path, each with its own value, e2e, roofline, CPU
+        # baseline and clocks: the batched form and the smoothed form's calibration
+        plan.close()
+        cs = None if args.no_cpu_baseline else max(4.0, args.cpu_seconds / 2)
+        line["forms"] = {
+            "batched": measure_batched(eng, local, args.steps, args.warmup, not args.no_tune, cs,
+                                       min(args.steps, 5)),
+            "calibration": measure_calibration(eng, local, args.steps, args.warmup, cs, pso_seconds=15.0,
+                                               extra_seeds=(8, 9, 10, 11), extra_pso_seconds=8.0),
+        }
     print(json.dumps(line), flush=True)
     return 0
 
@@ -419,8 +472,7 @@ def simulate_batch_e2e(eng, instances):
 
 
 def run_batched(args):
-    """Batched form: instances/s of one batch run against looping the plain form."""
-    import numpy as np
+    """Batched form alone: instances/s of one batch run against looping the plain form."""
     import torch
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
@@ -429,15 +481,28 @@ def run_batched(args):
     import build as pkg_build
     pkg_build.build()
     from procell import Engine
+    eng = Engine(local)
+    line = measure_batched(eng, local, args.steps, args.warmup, not args.no_tune,
+                           None if args.no_cpu_baseline else args.cpu_seconds, args.steps)
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def measure_batched(eng, local, steps, warmup, tune, cpu_seconds, e2e_steps):
+    """The batched workload's line: `steps` timed batch runs from HBM-resident inputs,
+    `e2e_steps` pc_simulate_batch calls with host inputs and outputs, one loop of the plain
+    form over the same instances, per-instance parity against that loop, and (cpu_seconds
+    not None) the oracle's instances/s on a sample of the instances."""
+    import numpy as np
+    import torch
 
     instances = batched_instances()
     n = len(instances)
-    eng = Engine(local)
     stream = torch.cuda.current_stream()
     eng.set_stream(stream.cuda_stream)
     batch = eng.batch(instances)
-    tuning = eng.autotune(batch, repeats=1) if not args.no_tune else None
-    for _ in range(args.warmup):
+    tuning = eng.autotune(batch, repeats=1) if tune else None
+    for _ in range(warmup):
         batch.run()
     torch.cuda.synchronize()
     clocks = ClockSampler(local)
@@ -447,7 +512,7 @@ def run_batched(args):
     divisions = roots = sweeps = kernels = 0
     divide_ms = device_ms = 0.0
     e0.record(stream)
-    for _ in range(args.steps):
+    for _ in range(steps):
         batch.run()
         st = batch.stats()
         divisions += st["divisions"]
@@ -460,7 +525,7 @@ def run_batched(args):
     torch.cuda.synchronize()
     elapsed_ms = e0.elapsed_time(e1)
     e2e_t = h2d = d2h = 0
-    for _ in range(args.steps):
+    for _ in range(e2e_steps):
         dt, hb, db = simulate_batch_e2e(eng, instances)
         e2e_t += dt
         h2d += hb
@@ -495,21 +560,21 @@ def run_batched(args):
     hbm, peak_kind = peaks()
     alg_bytes = 2 * ALG_BYTES_PER_NODE * divisions
     persistent = bool(tuning and tuning["driver"])
-    launches = max(1, args.steps if persistent else sweeps)
+    launches = max(1, steps if persistent else sweeps)
     achieved = alg_bytes / (divide_ms * 1e-3) / 1e9 if divide_ms > 0 else None
-    value = n * args.steps / (elapsed_ms * 1e-3)
-    e2e_value = n * args.steps / e2e_t
+    value = n * steps / (elapsed_ms * 1e-3)
+    e2e_value = n * e2e_steps / e2e_t
     cpu = None
-    if not args.no_cpu_baseline:
-        cpu = cpu_batched_sample(instances, args.cpu_seconds)
+    if cpu_seconds:
+        cpu = cpu_batched_sample(instances, cpu_seconds)
     line = {
         "metric": "instances/s (batched form)",
         "value": value,
         "unit": "instances/s",
         "n_gpus": 1,
-        "steps": args.steps,
-        "warmup": args.warmup,
-        "ms_per_step": elapsed_ms / args.steps,
+        "steps": steps,
+        "warmup": warmup,
+        "ms_per_step": elapsed_ms / steps,
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
@@ -517,12 +582,12 @@ def run_batched(args):
         "data": "synthetic (seeded generator, procell/configs.py batched())",
         "config": {"workload": "batched: %d instances, %d initial cells, bins U[32,1024], cells "
                                "log-U[1e3,1e6], 1-4 types (+quiescent 20%%), t_max U[48,336], "
-                               "fluorescence log-U[1,1e4], phi = min nonzero bin" % (n, roots // args.steps),
-                   "divisions_per_step": divisions // args.steps,
-                   "nodes_per_step": (roots + 2 * divisions) // args.steps,
+                               "fluorescence log-U[1,1e4], phi = min nonzero bin" % (n, roots // steps),
+                   "divisions_per_step": divisions // steps,
+                   "nodes_per_step": (roots + 2 * divisions) // steps,
                    "tuning": tuning,
                    "l2": "no flush: each step streams %.0f GB of level buffers, >> 129 MB L2"
-                         % (2 * 16 * divisions / args.steps / 1e9)},
+                         % (2 * 16 * divisions / steps / 1e9)},
         "divisions_per_s": divisions / (elapsed_ms * 1e-3),
         "loop_plain": {"run_instances_per_s": n / loop_run_s,
                        "e2e_instances_per_s": n / loop_e2e_s,
@@ -531,21 +596,20 @@ def run_batched(args):
         "speedup_vs_loop_plain": value / (n / loop_run_s),
         "e2e_speedup_vs_loop_plain": e2e_value / (n / loop_e2e_s),
         "bit_exact_instances": "%d/%d" % (same, n),
-        "e2e": {"value": e2e_value, "unit": "instances/s", "h2d_bytes_per_step": h2d // args.steps,
-                "d2h_bytes_per_step": d2h // args.steps},
+        "e2e": {"value": e2e_value, "unit": "instances/s", "h2d_bytes_per_step": h2d // e2e_steps,
+                "d2h_bytes_per_step": d2h // e2e_steps, "steps": e2e_steps},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": (achieved / hbm) if achieved else None, "traffic": batched_traffic(divisions, launches),
                      "peak_source": peak_kind, "kernel": "k_persist" if persistent else "k_divide",
-                     "launches_per_step": launches / args.steps,
+                     "launches_per_step": launches / steps,
                      "alg_bytes_per_launch": alg_bytes / launches},
         "gpu_launches": kernels,
         "clocks": clk,
-        "device_ms_per_step": device_ms / args.steps,
+        "device_ms_per_step": device_ms / steps,
     }
     if cpu:
         line["cpu_baseline"] = cpu
-    print(json.dumps(line), flush=True)
-    return 0
+    return line
 
 
 def cpu_smooth_sample(bins, phi, t_max, h, paths, seed, params, seconds):
@@ -589,16 +653,21 @@ def cpu_smooth_sample(bins, phi, t_max, h, paths, seed, params, seconds):
 
 
 def run_reference_calibration(args):
+    print(json.dumps(reference_calibration_line(args.steps, args.warmup, max(2.0, args.cpu_seconds / 2))),
+          flush=True)
+    return 0
+
+
+def reference_calibration_line(steps, warmup, per_step):
     from procell import calibrate as cb
     bins, phi, hidden = cb.problem_inputs(7)
-    per_step = max(2.0, args.cpu_seconds / 2)
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         cpu_smooth_sample(bins, phi, 168.0, 0.5, 2, 7 + 2000, hidden, per_step / 4)
-    vals = [cpu_smooth_sample(bins, phi, 168.0, 0.5, 2, 7 + 2000, hidden, per_step) for _ in range(args.steps)]
+    vals = [cpu_smooth_sample(bins, phi, 168.0, 0.5, 2, 7 + 2000, hidden, per_step) for _ in range(steps)]
     value = sum(v["value"] for v in vals) / len(vals)
     line = {
         "impl": "reference", "metric": "fwd+bwd grads/s (smoothed form)", "value": value, "unit": "grads/s",
-        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / value,
+        "n_gpus": 1, "steps": steps, "warmup": warmup, "ms_per_step": 1e3 / value,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded generator, procell/calibrate.py problem_inputs)",
         "config": {"workload": "calibration: 256 bins, 1e5 cells, 3 types, t_max 168, h 0.5, 2 lineages per cell",
@@ -607,14 +676,12 @@ def run_reference_calibration(args):
                          "sample": vals[-1]["sample"]},
         "e2e": {"value": value, "unit": "grads/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
-    print(json.dumps(line), flush=True)
-    return 0
+    return line
 
 
 def run_calibration(args):
-    """Smoothed form: fwd+bwd candidate-gradients per second at 256 candidates, and
-    gradient descent against particle swarm to equal loss."""
-    import numpy as np
+    """Smoothed form alone: fwd+bwd candidate-gradients per second at 256 candidates, and
+    gradient-based calibration against particle swarms to equal loss."""
     import torch
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
@@ -623,8 +690,23 @@ def run_calibration(args):
     import build as pkg_build
     pkg_build.build()
     from procell import Engine
-    from procell import calibrate as cb
     eng = Engine(local)
+    line = measure_calibration(eng, local, args.steps, args.warmup,
+                               None if args.no_cpu_baseline else args.cpu_seconds,
+                               pso_seconds=30.0, extra_seeds=(8, 9, 10, 11), extra_pso_seconds=10.0)
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def measure_calibration(eng, local, steps, warmup, cpu_seconds, pso_seconds, extra_seeds, extra_pso_seconds):
+    """The calibration workload's line: `steps` timed forward + loss gradient + adjoint
+    passes for 256 candidates (and the same end to end from pinned host memory), one
+    Jacobian and one Gauss-Newton pass, the race to equal loss on the configured input
+    (seed 7, every search, swarm budgets of pso_seconds) and on `extra_seeds`
+    (Levenberg-Marquardt against the plain-simulator swarm only), each scored on the
+    accurate smoothed loss and on the model-neutral plain-simulator loss."""
+    import torch
+    from procell import calibrate as cb
     prob = cb.Problem(eng, seed=7)
     C = 256
     theta = prob.start(C, 7)
@@ -636,7 +718,7 @@ def run_calibration(args):
         gE = 2.0 * (torch.log1p(E) - torch.log1p(prob.target)) / (1.0 + E)
         return prob.smooth.backward(P, gE), ((torch.log1p(E) - torch.log1p(prob.target)) ** 2).sum(dim=1)
 
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         step(theta)
     torch.cuda.synchronize()
     clocks = ClockSampler(local)
@@ -644,7 +726,7 @@ def run_calibration(args):
     time.sleep(0.3)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    for _ in range(args.steps):
+    for _ in range(steps):
         g, L = step(theta)
     e1.record(stream)
     torch.cuda.synchronize()
@@ -655,7 +737,7 @@ def run_calibration(args):
     out_l = torch.empty(C, dtype=torch.float64).pin_memory()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(steps):
         th = host_theta.to("cuda", non_blocking=True)
         g, L = step(th)
         out_g.copy_(g, non_blocking=True)
@@ -670,27 +752,40 @@ def run_calibration(args):
     prob.smooth.jacobian(P0)
     j0, j1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     j0.record(stream)
-    for _ in range(args.steps):
+    for _ in range(steps):
         prob.smooth.jacobian(P0)
     j1.record(stream)
     torch.cuda.synchronize()
-    jac_ms = j0.elapsed_time(j1) / args.steps
+    jac_ms = j0.elapsed_time(j1) / steps
     # loss and its gradient (plus J^T J) by forward mode: one Gauss-Newton pass
     prob.smooth.gauss_newton(P0, prob.target)
     j0.record(stream)
-    for _ in range(args.steps):
+    for _ in range(steps):
         prob.smooth.gauss_newton(P0, prob.target)
     j1.record(stream)
     torch.cuda.synchronize()
-    gn_ms = j0.elapsed_time(j1) / args.steps
-    comp = cb.compare(eng, candidates=C, seed=7, pso_seconds=30.0)
+    gn_ms = j0.elapsed_time(j1) / steps
+    comp = cb.compare(eng, candidates=C, seed=7, pso_seconds=pso_seconds)
     comp.pop("traces", None)
+    others = []
+    for sd in extra_seeds:
+        c = cb.compare(eng, candidates=C, seed=sd, pso_seconds=extra_pso_seconds, full=False)
+        c.pop("traces", None)
+        others.append({"seed": sd, "speedup_accurate": c["speedup"], "equal_loss_accurate": c["equal_loss"],
+                       "lm_best_accurate": c["lm"]["best_accurate_loss"],
+                       "pso_plain_best_accurate": c["pso_plain"]["best_accurate_loss"],
+                       "speedup_neutral": c["model_neutral"]["speedup"],
+                       "equal_loss_neutral": c["model_neutral"]["equal_loss"],
+                       "lm_best_neutral": c["model_neutral"]["lm_best"],
+                       "pso_plain_best_neutral": c["model_neutral"]["pso_plain_best"],
+                       "neutral_at_hidden": c["model_neutral"]["plain_loss_at_hidden"],
+                       "levels_neutral": c["model_neutral"]["levels"]})
     cpu = None
-    if not args.no_cpu_baseline:
+    if cpu_seconds:
         cpu = cpu_smooth_sample(prob.bins, prob.phi, prob.t_max, prob.smooth_h, prob.smooth_paths,
                                 prob.smooth_seed, prob.params(theta[:1]).detach().cpu().numpy(),
-                                args.cpu_seconds)
-    value = C * args.steps / (elapsed_ms * 1e-3)
+                                cpu_seconds)
+    value = C * steps / (elapsed_ms * 1e-3)
     hbm, peak_kind = peaks()
     # algorithmic bytes of one forward + backward: parameters in, expected counts out and in
     # again as gradients, parameter gradients out
@@ -700,9 +795,9 @@ def run_calibration(args):
         "value": value,
         "unit": "grads/s",
         "n_gpus": 1,
-        "steps": args.steps,
-        "warmup": args.warmup,
-        "ms_per_step": elapsed_ms / args.steps,
+        "steps": steps,
+        "warmup": warmup,
+        "ms_per_step": elapsed_ms / steps,
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
@@ -713,25 +808,28 @@ def run_calibration(args):
                                % (C, prob.smooth_paths),
                    "l2": "inputs (bins, parameters) are a few MB; the kernels are compute bound"},
         "calibration": comp,
+        "calibration_other_seeds": {
+            "swarm_seconds": extra_pso_seconds, "results": others,
+            "what": "problem_inputs(seed) for each seed: Levenberg-Marquardt against the plain-simulator swarm, "
+                    "equal-loss ratio on the accurate smoothed loss and on the model-neutral plain loss"},
         "jacobian_pass": {"ms": jac_ms, "candidates_per_s": C / (jac_ms * 1e-3),
                           "what": "expected counts and their Jacobian in (ratio, mean, sd) for %d candidates" % C},
         "forward_mode": {"ms": gn_ms, "grads_per_s": C / (gn_ms * 1e-3),
                          "what": "loss, its gradient (J^T r) and J^T J of %d candidates in one forward-mode "
                                  "pass (pc_smooth_gauss_newton); the value above is forward + adjoint" % C},
-        "e2e": {"value": C * args.steps / e2e_s, "unit": "grads/s", "h2d_bytes_per_step": h2d,
+        "e2e": {"value": C * steps / e2e_s, "unit": "grads/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
-        "roofline": {"bound": "hbm", "achieved": alg / (elapsed_ms * 1e-3 / args.steps) / 1e9, "peak": hbm,
-                     "unit": "GB/s", "frac": alg / (elapsed_ms * 1e-3 / args.steps) / 1e9 / hbm,
+        "roofline": {"bound": "hbm", "achieved": alg / (elapsed_ms * 1e-3 / steps) / 1e9, "peak": hbm,
+                     "unit": "GB/s", "frac": alg / (elapsed_ms * 1e-3 / steps) / 1e9 / hbm,
                      "traffic": None, "peak_source": peak_kind, "kernel": "k_smooth",
                      "note": "not memory bound: FP64-pipe bound (due times; 78-84% of the FP64 pipe, "
                              "profiles/k_smooth_calibration.md); bytes are inputs and outputs only"},
-        "gpu_launches": 6 * args.steps,  # per step: order, forward, merge; order, adjoint, sum
+        "gpu_launches": 6 * steps,  # per step: order, forward, merge; order, adjoint, sum
         "clocks": clk,
     }
     if cpu:
         line["cpu_baseline"] = cpu
-    print(json.dumps(line), flush=True)
-    return 0
+    return line
 
 
 def batched_traffic(divisions, launches):
@@ -777,6 +875,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (default configuration)")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="plain workload only: skip the batched and calibration forms nested in its line")
     args = ap.parse_args()
     if args.warmup < 3:
         print("warning: --warmup < 3 violates the timing rules", file=sys.stderr)

@@ -1598,6 +1598,40 @@ int pc_debug_barrier(pc_context* ctx, int starve, double timeout_ms, uint32_t* e
   PC_GUARD_END(ctx)
 }
 
+int pc_debug_peak(pc_context* ctx, int kind, double* lane_ops_per_s) {
+  PC_GUARD_BEGIN
+  if (!ctx || !lane_ops_per_s || kind < 0 || kind > 2) return fail(ctx, PC_ERR_INVALID, "kind must be 0, 1 or 2");
+  PC_CUDA(ctx, cudaSetDevice(ctx->device));
+  cudaStream_t st = ctx->stream;
+  const int blocks = 4 * std::max(1, ctx->sms);
+  double* sink = nullptr;
+  PC_CUDA(ctx, cudaMalloc(&sink, 256 * sizeof(double)));
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaError_t e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  // a short launch sizes the timed one to about 30 ms
+  uint32_t iters = 256;
+  float ms = 0.0f;
+  for (int round = 0; e == cudaSuccess && round < 4; ++round) {
+    e = (cudaError_t)launch_peak_probe(kind, iters, blocks, sink, st);  // warm-up at this size
+    if (e == cudaSuccess) e = cudaEventRecord(e0, st);
+    if (e == cudaSuccess) e = (cudaError_t)launch_peak_probe(kind, iters, blocks, sink, st);
+    if (e == cudaSuccess) e = cudaEventRecord(e1, st);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    if (e != cudaSuccess || ms >= 20.0f) break;
+    const double scale = 30.0 / std::max(0.05, (double)ms);
+    iters = (uint32_t)std::min(1e8, std::max(2.0 * iters, iters * scale));
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(sink);
+  if (e != cudaSuccess) return fail(ctx, PC_ERR_CUDA, std::string("peak probe: ") + cudaGetErrorString(e));
+  *lane_ops_per_s = (double)blocks * 256.0 * 8.0 * iters / (ms * 1e-3);
+  return PC_OK;
+  PC_GUARD_END(ctx)
+}
+
 int pc_debug_philox(pc_context* ctx, const uint32_t* ctr, uint64_t n, const uint32_t key[2], uint32_t* out) {
   PC_GUARD_BEGIN
   if (!ctx || (n && (!ctr || !out)) || !key) return PC_ERR_INVALID;

@@ -164,6 +164,9 @@ int launch_debug_philox(const uint32_t* ctr, uint64_t n, uint32_t k0, uint32_t k
 int launch_debug_normals(const ZigTables* zig, uint32_t k0, uint32_t k1, uint32_t root,
                          uint64_t first_parent, uint64_t count, float* z, void* stream);
 int occupancy_blocks_per_sm(int* root_blocks, int* divide_blocks);
+// Throughput probe (roofline denominators): kind 0 FP64 FMA, 1 FP32 FMA, 2 INT32 multiply-add;
+// each of the blocks x 256 threads runs iters x 8 operations.
+int launch_peak_probe(int kind, uint32_t iters, int blocks, double* sink, void* stream);
 // One grid barrier in a cooperative launch of `blocks` blocks (failure-detection test).
 int launch_barrier_probe(uint32_t* bar, unsigned long long timeout_ns, uint32_t* error, uint32_t* passed, int blocks,
                          void* stream);

@@ -44,7 +44,60 @@ __global__ void k_barrier_probe(uint32_t* bar, unsigned long long timeout_ns, ui
   if (grid_barrier(bar, timeout_ns, error) && threadIdx.x == 0) atomicAdd(passed, 1u);
 }
 
+// Throughput probes for the roofline denominators (FP64 and FP32 fused multiply-add, INT32
+// multiply-add). Each thread runs 8 independent dependent chains, so with a few blocks per
+// SM the pipe, not the latency, bounds the launch. The chains converge to a fixed point
+// (no overflow, no subnormals); the sum is written only if it is impossible, which keeps
+// the loop from being optimised away.
+template <int Kind>
+__global__ void __launch_bounds__(256) k_peak(uint32_t iters, double* sink) {
+  constexpr int kChains = 8;
+  double acc = 0.0;
+  if constexpr (Kind == 0) {
+    double a[kChains];
+#pragma unroll
+    for (int i = 0; i < kChains; ++i) a[i] = 1.0 + 1e-7 * i + 1e-9 * threadIdx.x;
+    const double b = 0.9999999, c = 1e-7;
+    for (uint32_t it = 0; it < iters; ++it)
+#pragma unroll
+      for (int i = 0; i < kChains; ++i) a[i] = fma(a[i], b, c);
+#pragma unroll
+    for (int i = 0; i < kChains; ++i) acc += a[i];
+  } else if constexpr (Kind == 1) {
+    float a[kChains];
+#pragma unroll
+    for (int i = 0; i < kChains; ++i) a[i] = 1.0f + 1e-3f * i + 1e-6f * threadIdx.x;
+    const float b = 0.999f, c = 1e-3f;
+    for (uint32_t it = 0; it < iters; ++it)
+#pragma unroll
+      for (int i = 0; i < kChains; ++i) a[i] = __fmaf_rn(a[i], b, c);
+#pragma unroll
+    for (int i = 0; i < kChains; ++i) acc += a[i];
+  } else {
+    uint32_t a[kChains];
+#pragma unroll
+    for (int i = 0; i < kChains; ++i) a[i] = threadIdx.x + 977u * i;
+    for (uint32_t it = 0; it < iters; ++it)
+#pragma unroll
+      for (int i = 0; i < kChains; ++i) a[i] = a[i] * 0x9E3779B9u + (uint32_t)i;
+#pragma unroll
+    for (int i = 0; i < kChains; ++i) acc += (double)(a[i] & 1u);
+  }
+  if (acc == -1.0) sink[threadIdx.x] = acc;
+}
+
 }  // namespace
+
+int launch_peak_probe(int kind, uint32_t iters, int blocks, double* sink, void* stream) {
+  cudaStream_t st = (cudaStream_t)stream;
+  if (kind == 0)
+    k_peak<0><<<blocks, 256, 0, st>>>(iters, sink);
+  else if (kind == 1)
+    k_peak<1><<<blocks, 256, 0, st>>>(iters, sink);
+  else
+    k_peak<2><<<blocks, 256, 0, st>>>(iters, sink);
+  return (int)cudaGetLastError();
+}
 
 int launch_barrier_probe(uint32_t* bar, unsigned long long timeout_ns, uint32_t* error, uint32_t* passed, int blocks,
                          void* stream) {

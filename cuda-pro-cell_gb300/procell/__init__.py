@@ -221,6 +221,12 @@ class Engine:
         finally:
             p.close()
 
+    def peak(self, kind: str) -> float:
+        """Measured lane-operations/s of one pipe: "fp64" / "fp32" FMA, "int32" multiply-add."""
+        v = ctypes.c_double()
+        self._check(self.L.pc_debug_peak(self.ctx, {"fp64": 0, "fp32": 1, "int32": 2}[kind], ctypes.byref(v)))
+        return v.value
+
     def philox(self, ctrs: np.ndarray, key) -> np.ndarray:
         c = np.ascontiguousarray(ctrs, dtype=np.uint32).reshape(-1, 4)
         out = np.zeros_like(c)

@@ -17,7 +17,9 @@ random starting population:
     model would run.
 Each search keeps its best parameters over time; afterwards every snapshot is scored with
 one accurate common loss (the smoothed form with many lineages per cell, another seed), so
-the searches are compared on the same scale.
+the searches are compared on the same scale, and with a model-neutral one: the plain
+simulator's own loss averaged over independent seeds (no smoothing, and no random numbers
+shared with any search).
 
     python -m procell.calibrate [--candidates 256] [--seed 7] [--lm-iters 40] [--gd-iters 300] [--pso-seconds 40]
 """
@@ -66,6 +68,7 @@ class Problem:
         self.target_np = res.totals.astype(np.float64)
         self.target = torch.tensor(self.target_np, device="cuda")
         self.plain_seed = seed + 3000
+        self.neutral_seed = seed + 4000
         from . import _lib
         self._bins_np = _lib.bins_numpy(self.bins)
         self._accurate = None
@@ -82,6 +85,30 @@ class Problem:
                 E = self._accurate.forward(self.params(chunk))
                 out.append(((torch.log1p(E) - torch.log1p(self.target)) ** 2).sum(dim=1))
             return torch.cat(out)
+
+    def loss_plain_mean(self, theta, n_seeds=16, chunk=256):
+        """The model-neutral yardstick: the plain simulator's loss of every candidate averaged
+        over `n_seeds` independent seeds (seeds no search uses). Each chunk of candidates x
+        seeds runs as the instances of one batch. Returns a numpy array [C]."""
+        P = self.params(theta).detach().cpu().numpy()
+        V = len(self.target_np)
+        tgt = np.log1p(self.target_np)
+        out = []
+        for c0 in range(0, P.shape[0], chunk):
+            Pc = P[c0:c0 + chunk]
+            rows = [[tuple(float(x) for x in r) for r in Pc[i]] for i in range(len(Pc))]
+            inst = [(self._bins_np, rows[i], self.t_max, self.phi, self.neutral_seed + 7919 * s)
+                    for s in range(n_seeds) for i in range(len(Pc))]
+            b = self.engine.batch(inst)
+            try:
+                b.run()
+                off, tot = b.totals()
+            finally:
+                b.close()
+            assert int(off[-1]) == n_seeds * len(Pc) * V
+            C = tot.astype(np.float64).reshape(n_seeds, len(Pc), V)
+            out.append(((np.log1p(C) - tgt) ** 2).sum(axis=2).mean(axis=0))
+        return np.concatenate(out)
 
     def params(self, theta):
         """theta [C, K, 3] = (ratio logit, log mean, log cv) -> (ratio, mean, sd)."""
@@ -320,24 +347,41 @@ def first_below(trace, level):
     return None
 
 
-def compare(engine, candidates=256, seed=7, gd_iters=300, pso_seconds=40.0, paths=2, lm_iters=40):
+def neutral_trace(prob, snaps, n_seeds):
+    """(time, model-neutral loss of the search's best parameters so far) per snapshot."""
+    if not snaps:
+        return []
+    L = prob.loss_plain_mean(torch.stack([th for _, th in snaps]), n_seeds)
+    return [(t, float(v)) for (t, _), v in zip(snaps, L)]
+
+
+def compare(engine, candidates=256, seed=7, gd_iters=300, pso_seconds=40.0, paths=2, lm_iters=40,
+            full=True, neutral_seeds=16):
     """Derivative-based searches on the smoothed form (Levenberg-Marquardt with the forward-
     mode Jacobian; Adam with the adjoint gradient) against particle swarms (on the smoothed
     form, and on the plain simulator through the batched form), all from one population,
     all scored afterwards with the same accurate loss. The headline level is the worse of
     the plain-simulator swarm's and Levenberg-Marquardt's final accurate losses (a level
-    both reach); the ratio is the swarm's time to reach it over Levenberg-Marquardt's."""
+    both reach); the ratio is the swarm's time to reach it over Levenberg-Marquardt's.
+    With neutral_seeds > 0 the snapshots of those two searches are also scored with the
+    plain simulator's loss averaged over that many seeds, and the same ratio is formed on
+    that scale. full=False runs only Levenberg-Marquardt and the plain-simulator swarm."""
     prob = Problem(engine, seed=seed, paths=paths)
     theta0 = prob.start(candidates, seed)
     levenberg_marquardt(prob, theta0, iters=3)  # warm-up of every code path
-    gradient_descent(prob, theta0, iters=3)
-    particle_swarm(prob, theta0, iters=3)
+    if full:
+        gradient_descent(prob, theta0, iters=3)
+        particle_swarm(prob, theta0, iters=3)
     particle_swarm(prob, theta0, iters=2, loss=prob.loss_plain)
     lm, lm_snaps = levenberg_marquardt(prob, theta0, iters=lm_iters)
-    gd, gd_snaps = gradient_descent(prob, theta0, iters=gd_iters)
-    ps, ps_snaps = particle_swarm(prob, theta0, iters=1_000_000, time_limit=pso_seconds)
+    gd = gd_snaps = ps = ps_snaps = None
+    if full:
+        gd, gd_snaps = gradient_descent(prob, theta0, iters=gd_iters)
+        ps, ps_snaps = particle_swarm(prob, theta0, iters=1_000_000, time_limit=pso_seconds)
     pp, pp_snaps = particle_swarm(prob, theta0, iters=1_000_000, time_limit=pso_seconds, loss=prob.loss_plain)
-    acc_lm, acc_gd, acc_ps, acc_pp = (accurate_trace(prob, x) for x in (lm_snaps, gd_snaps, ps_snaps, pp_snaps))
+    acc_lm, acc_pp = accurate_trace(prob, lm_snaps), accurate_trace(prob, pp_snaps)
+    acc_gd = accurate_trace(prob, gd_snaps) if full else []
+    acc_ps = accurate_trace(prob, ps_snaps) if full else []
     with torch.no_grad():
         hidden = torch.tensor([prob.hidden], dtype=torch.float64, device="cuda")
         th_h = torch.stack([torch.log(hidden[0, :, 0]), torch.log(hidden[0, :, 1]),
@@ -345,7 +389,7 @@ def compare(engine, candidates=256, seed=7, gd_iters=300, pso_seconds=40.0, path
         l_true = float(prob.loss_accurate(th_h)[0])
 
     def best_final(tr):
-        return min(l for _, l in tr)
+        return min(l for _, l in tr) if tr else None
 
     head = max(best_final(acc_pp), best_final(acc_lm))
     # the equal loss, and fixed multiples of the hidden parameters' own loss
@@ -358,7 +402,26 @@ def compare(engine, candidates=256, seed=7, gd_iters=300, pso_seconds=40.0, path
                       "pso_smooth_seconds": ts, "ratio_plain": (tp / tl) if (tl and tp) else None,
                       "ratio_smooth": (ts / tl) if (tl and ts) else None})
     tl, tp = first_below(acc_lm, head), first_below(acc_pp, head)
+    neutral = None
+    if neutral_seeds:
+        n_lm, n_pp = neutral_trace(prob, lm_snaps, neutral_seeds), neutral_trace(prob, pp_snaps, neutral_seeds)
+        n_true = float(prob.loss_plain_mean(th_h, neutral_seeds)[0])
+        head_n = max(best_final(n_pp), best_final(n_lm))
+        tln, tpn = first_below(n_lm, head_n), first_below(n_pp, head_n)
+        nlevels = []
+        for f in (1.5, 1.25, 1.1, 1.05):
+            L = f * n_true
+            a, b = first_below(n_lm, L), first_below(n_pp, L)
+            nlevels.append({"plain_loss": L, "lm_seconds": a, "pso_plain_seconds": b,
+                            "ratio_plain": (b / a) if (a and b) else None})
+        neutral = {"seeds": neutral_seeds, "plain_loss_at_hidden": n_true,
+                   "lm_best": best_final(n_lm), "pso_plain_best": best_final(n_pp),
+                   "equal_loss": head_n, "gradient_seconds_to_equal_loss": tln,
+                   "pso_seconds_to_equal_loss": tpn, "speedup": (tpn / tln) if (tln and tpn) else None,
+                   "levels": nlevels,
+                   "what": "mean plain-simulator loss over %d independent seeds of each snapshot" % neutral_seeds}
     return {
+        "seed": seed,
         "candidates": candidates,
         "lineages_per_cell": paths,
         "hidden": prob.hidden,
@@ -368,11 +431,13 @@ def compare(engine, candidates=256, seed=7, gd_iters=300, pso_seconds=40.0, path
                "seconds_per_iter": lm[-1][0] / max(1, len(lm) - 1),
                "method": "Levenberg-Marquardt on the smoothed form, one Gauss-Newton pass (Jacobian kernel "
                          "reduced on the device) per iteration"},
-        "gd": {"iters": len(gd), "seconds": gd[-1][0], "best_smoothed_loss": gd[-1][1],
-               "best_accurate_loss": best_final(acc_gd), "method": "Adam on the smoothed form, cosine lr 0.1 -> 0.002"},
-        "pso_smooth": {"iters": len(ps) - 1, "seconds": ps[-1][0], "best_smoothed_loss": ps[-1][1],
-                       "best_accurate_loss": best_final(acc_ps),
-                       "method": "particle swarm on the smoothed form (constriction, ring neighbourhood)"},
+        "gd": None if gd is None else {
+            "iters": len(gd), "seconds": gd[-1][0], "best_smoothed_loss": gd[-1][1],
+            "best_accurate_loss": best_final(acc_gd), "method": "Adam on the smoothed form, cosine lr 0.1 -> 0.002"},
+        "pso_smooth": None if ps is None else {
+            "iters": len(ps) - 1, "seconds": ps[-1][0], "best_smoothed_loss": ps[-1][1],
+            "best_accurate_loss": best_final(acc_ps),
+            "method": "particle swarm on the smoothed form (constriction, ring neighbourhood)"},
         "pso_plain": {"iters": len(pp) - 1, "seconds": pp[-1][0], "best_plain_loss": pp[-1][1],
                       "best_accurate_loss": best_final(acc_pp),
                       "method": "particle swarm on the plain simulator, candidates as the instances of one batch "
@@ -383,6 +448,7 @@ def compare(engine, candidates=256, seed=7, gd_iters=300, pso_seconds=40.0, path
         "pso_seconds_to_equal_loss": tp,
         "speedup": (tp / tl) if (tl and tp) else None,
         "levels": table,
+        "model_neutral": neutral,
         "traces": {"lm": acc_lm, "gd": acc_gd, "pso_plain": acc_pp},
     }
 

@@ -341,6 +341,11 @@ int pc_debug_barrier(pc_context* ctx, int starve, double timeout_ms, uint32_t* e
                      uint32_t* passed);
 int pc_debug_philox(pc_context* ctx, const uint32_t* ctr, uint64_t n, const uint32_t key[2],
                     uint32_t* out);
+/* Measured throughput of one arithmetic pipe of the context's GPU, in lane-operations per
+ * second (one fused multiply-add = one operation): kind 0 FP64 FMA, 1 FP32 FMA, 2 INT32
+ * multiply-add. A microbenchmark of about 30 ms (no counterpart in the reference); the
+ * benchmark uses it as the denominator of pipe rooflines. */
+int pc_debug_peak(pc_context* ctx, int kind, double* lane_ops_per_s);
 int pc_debug_normals(pc_context* ctx, uint64_t seed, uint32_t root, uint64_t first_parent,
                      uint64_t count, float* z);
 int pc_debug_tables(pc_context* ctx, uint32_t* k, uint32_t* w_bits, uint32_t* f_bits);
