@@ -31,8 +31,10 @@
 // first each lane draws one lineage's normals (one Philox block and ziggurat draw per
 // generation) into shared memory, then every lane walks all 32 lineages for its own
 // candidate, reading the shared draws. Each normal is thus drawn once per 32 candidates and
-// type. Remaining time R = T - S is carried in FP64 (two FP64 operations per step: the
-// division time and R; GB300's FP64 pipe bounds these kernels). Per-thread partial sums
+// type. Remaining time R = T - S is carried on the FP32 pipe as a float on a fixed grid plus
+// a float remainder (RemGrid: exact grid sums, 11 FP32 operations per step; GB300's FP64
+// pipe has 2 lanes per clock per SM), or in FP64 where that form's error bound would exceed
+// 2^-22 h (RemFp64). Per-thread partial sums
 // (compensated FP32) live in shared memory and are reduced over the warps in a fixed order,
 // and the types are added in a fixed order by the merge, so results are deterministic.
 #include <cuda_runtime.h>
@@ -106,6 +108,93 @@ __device__ __forceinline__ float f64_to_f32_rz_any(double d) {
   return __uint_as_float(sign | ((mag - (896u << 20)) << 3) | (lo >> 29));
 }
 
+// The remaining time R = T - S_j of a walk, in one of two forms with the same interface:
+// first(z_1, U, 1 + U as hi/lo floats) sets R_1 = T - tau_1 (1 + U), step(z_j) subtracts
+// tau_j = mean + sd z_j, x(1/h) returns R / h in FP32.
+//
+// RemFp64: R in FP64 (two FP64 operations per step; GB300 runs FP64 on a pipe of 2 lanes
+// per clock per SM). Used only where the grid form below would not be exact enough.
+struct RemFp64 {
+  double mu, sigma, t_max, R;
+  __device__ __forceinline__ void first(float z, double u_age, float, float) {
+    const double tau = fma(sigma, f32_to_f64_bits(z), mu);
+    R = t_max - fma(tau, u_age, tau);
+  }
+  __device__ __forceinline__ void step(float z) { R = R - fma(sigma, f32_to_f64_bits(z), mu); }
+  __device__ __forceinline__ float x(float inv_h) const { return f64_to_f32_rz_any(R) * inv_h; }
+};
+
+// RemGrid: R on the FP32 pipe as Rh + Rl. Rh only ever holds multiples of the grid step
+// g = 2^(m-23) below 2^(m+1) in magnitude (at most 24 significant bits), so sums and
+// differences of such numbers are exact; Rl, a float below about 2 g per step in magnitude,
+// takes every remainder. A product p = sd z is split exactly into p_h + p_l (one FMA), p_h
+// is rounded to the grid by adding and subtracting C = 1.5 * 2^m (exact for |p_h| < 2^(m-1))
+// and its fraction goes to Rl. With |R|, |tau| and |tau (1 + U)| bounded by 2^(m-1), every
+// step is 11 FP32 operations; each step's rounding of Rl (|Rl| <= 1.25 g steps) adds at most
+// 0.6 * 2^-23 g steps to the error of R, so it stays below 0.6 * 2^-23 * g * steps^2, which
+// grid_setup keeps below 2^-19 h (a weight's relative error below 2^-18).
+struct RemGrid {
+  float C, mu_g, mu_f, sg_h, sg_l, t_g, t_f, Rh, Rl;
+  __device__ __forceinline__ void split(float p, float& on_grid, float& rest) const {
+    on_grid = __fsub_rn(__fadd_rn(p, C), C);
+    rest = __fsub_rn(p, on_grid);
+  }
+  // tau = mean + sd z as tg (on the grid) + tf
+  __device__ __forceinline__ void tau(float z, float& tg, float& tf) const {
+    const float ph = __fmul_rn(sg_h, z);
+    const float pl = __fmaf_rn(sg_l, z, __fmaf_rn(sg_h, z, -ph));
+    float pg, pf;
+    split(ph, pg, pf);
+    tg = __fadd_rn(mu_g, pg);
+    tf = __fadd_rn(__fadd_rn(mu_f, pf), pl);
+  }
+  __device__ __forceinline__ void first(float z, double, float u_hi, float u_lo) {
+    float tg, tf;
+    tau(z, tg, tf);
+    // S_1 = (tg + tf)(u_hi + u_lo): tg u_hi exactly as qh + ql, the other terms rounded
+    const float qh = __fmul_rn(tg, u_hi);
+    const float ql = __fmaf_rn(tg, u_hi, -qh);
+    const float rest = __fmaf_rn(tf, u_lo, __fmaf_rn(tg, u_lo, __fmaf_rn(tf, u_hi, ql)));
+    float qg, qf;
+    split(qh, qg, qf);
+    Rh = __fsub_rn(t_g, qg);
+    Rl = __fsub_rn(__fsub_rn(t_f, qf), rest);
+  }
+  __device__ __forceinline__ void step(float z) {
+    float tg, tf;
+    tau(z, tg, tf);
+    Rh = __fsub_rn(Rh, tg);
+    Rl = __fsub_rn(Rl, tf);
+  }
+  __device__ __forceinline__ float x(float inv_h) const { return __fmul_rn(__fadd_rn(Rh, Rl), inv_h); }
+};
+
+// The grid form for one candidate and bin, or false where its error bound would exceed
+// 2^-19 h (very large t_max or means relative to h, or very deep bins): then the caller
+// walks in FP64. |z| <= 8.25 bounds every normal the sampler returns (the ziggurat's tail
+// draw is at most r - log(2^-24) / r = 8.21), so |tau| <= |mean| + 8.25 |sd| and
+// |R_j| <= |T| + j max |tau|.
+__device__ __forceinline__ bool grid_setup(RemGrid& r, double mu, double sigma, double t_max, uint32_t steps,
+                                           double h) {
+  const double B = fabs(t_max) + (double)(steps > 2u ? steps : 2u) * (fabs(mu) + 8.25 * fabs(sigma)) + 1.0;
+  int e;
+  frexp(B, &e);  // B < 2^e
+  const int m = e + 1;
+  const double g = ldexp(1.0, m - 23);
+  if (!(g * (double)steps * (double)steps <= 16.0 * h) || m > 100) return false;
+  const double mu_g = ldexp(rint(ldexp(mu, 23 - m)), m - 23);
+  const double t_g = ldexp(rint(ldexp(t_max, 23 - m)), m - 23);
+  r.C = (float)ldexp(1.5, m);
+  r.mu_g = (float)mu_g;
+  r.mu_f = (float)(mu - mu_g);
+  r.sg_h = (float)sigma;
+  r.sg_l = (float)(sigma - (double)r.sg_h);
+  r.t_g = (float)t_g;
+  r.t_f = (float)(t_max - t_g);
+  r.Rh = r.Rl = 0.0f;
+  return true;
+}
+
 // A lineage stops once no later generation can add more than e^-40 cells: every later leaf
 // weight is at most s_1 ... s_j (the running product) times 2^g <= 2^(steps - 1).
 constexpr float kLogNegligible = -40.0f;
@@ -131,26 +220,34 @@ __device__ __forceinline__ void draw_lineage(const SmoothArgs& A, const ZigTable
   }
 }
 
-// One lineage (its normals z[j * 32], j = 0.., and initial age U) for one type of one
-// candidate. Forward: acc[g * kThreads] += weight * 2^g * w_g. Backward (Ag2[g] = 2^g dL/dE_g):
-// accumulates sum_g Ag2[g] w_g and its derivatives in mean and sd.
-template <bool Backward>
-__device__ __forceinline__ void walk(const SmoothArgs& A, const float* z, double u_age, float u1, float inv_h,
-                                     uint32_t steps, double mu, double sigma, bool fixed_tau, float w_hi,
-                                     float w_lo, float* acc, const float* Ag2, float& f_r, float& f_mu,
-                                     float& f_sig) {
-  // step 1 (the first division, S_1 = tau_1 (1 + U)) is peeled off the loop, so every later
-  // step costs two FP64 operations (the division time and R) and no select
+// A lineage's initial age U for the walks of all 32 candidates: U itself (FP64 form) and
+// 1 + U as a pair of floats hi + lo (grid form; hi is also the FP32 dS_1/dmean).
+__device__ __forceinline__ void store_lineage_u(double u, double* u_age, float* hi, float* lo) {
+  const double one = 1.0 + u;
+  const float h = __double2float_rn(one);
+  *u_age = u;
+  *hi = h;
+  *lo = __double2float_rn(one - (double)h);
+}
+
+// One lineage (its normals z[j * 32], j = 0.., and initial age U; 1 + U = u1 + u1_lo) for one
+// type of one candidate, whose remaining time R = T - S_j is carried by `r`. Forward:
+// acc[g * kThreads] += weight * 2^g * w_g. Backward (Ag2[g] = 2^g dL/dE_g): accumulates
+// sum_g Ag2[g] w_g and its derivatives in mean and sd.
+template <bool Backward, class Rem>
+__device__ __forceinline__ void walk(const float* z, double u_age, float u1, float u1_lo, float inv_h, uint32_t steps,
+                                     Rem r, bool fixed_tau, float w_hi, float w_lo, float* acc, const float* Ag2,
+                                     float& f_r, float& f_mu, float& f_sig) {
+  // step 1 (the first division, S_1 = tau_1 (1 + U)) is peeled off the loop
   float zj = fixed_tau ? 0.0f : z[0];
-  double tau = fixed_tau ? 0.0 : fma(sigma, f32_to_f64_bits(zj), mu);
-  double R = A.t_max - fma(tau, u_age, tau);  // T - S_j
-  float dmu = u1, dsig = zj * u1;             // dS_j / d(mean, sd)
+  r.first(zj, u_age, u1, u1_lo);
+  float dmu = u1, dsig = zj * u1;  // dS_j / d(mean, sd)
   float log_p = 0.0f;                         // log s_1 ... s_{j-1}
   float D_mu = 0.0f, D_sig = 0.0f;
   float wh = w_hi, wl = w_lo;                 // weight * 2^(j-1) as a pair of floats
   const float stop = stop_level(steps);
   for (uint32_t j = 1;;) {
-    const float x = f64_to_f32_rz_any(R) * inv_h;
+    const float x = r.x(inv_h);
     float ls, l1m;
     log_sig(x, ls, l1m);
     const float w = expf(log_p + l1m);  // leaf weight of generation j - 1
@@ -186,8 +283,7 @@ __device__ __forceinline__ void walk(const SmoothArgs& A, const float* z, double
     log_p += ls;
     if (log_p < stop || ++j > steps) break;
     zj = fixed_tau ? 0.0f : z[(j - 1) * 32u];
-    tau = fixed_tau ? 0.0 : fma(sigma, f32_to_f64_bits(zj), mu);
-    R = R - tau;
+    r.step(zj);
     dmu += 1.0f;
     dsig += zj;
   }
@@ -195,19 +291,18 @@ __device__ __forceinline__ void walk(const SmoothArgs& A, const float* z, double
 
 // One lineage for one type, forward mode: for every generation g it reaches, acc rows
 // 3g, 3g + 1, 3g + 2 gain 2^g w_g and 2^g dw_g/d(mean, sd) (per-thread FP32 sums).
-__device__ __forceinline__ void walk_jacobian(const SmoothArgs& A, const float* z, double u_age, float u1,
-                                              float inv_h, uint32_t steps, double mu, double sigma, bool fixed_tau,
-                                              float* acc) {
+template <class Rem>
+__device__ __forceinline__ void walk_jacobian(const float* z, double u_age, float u1, float u1_lo, float inv_h,
+                                              uint32_t steps, Rem r, bool fixed_tau, float* acc) {
   // step 1 peeled off the loop as in walk()
   float zj = fixed_tau ? 0.0f : z[0];
-  double tau = fixed_tau ? 0.0 : fma(sigma, f32_to_f64_bits(zj), mu);
-  double R = A.t_max - fma(tau, u_age, tau);
+  r.first(zj, u_age, u1, u1_lo);
   float dmu = u1, dsig = zj * u1;
   float log_p = 0.0f, D_mu = 0.0f, D_sig = 0.0f;
   float scale = 1.0f;  // 2^(j-1)
   const float stop = stop_level(steps);
   for (uint32_t j = 1;;) {
-    const float x = f64_to_f32_rz_any(R) * inv_h;
+    const float x = r.x(inv_h);
     float ls, l1m;
     log_sig(x, ls, l1m);
     const float w = expf(log_p + l1m);  // leaf weight of generation j - 1
@@ -230,8 +325,7 @@ __device__ __forceinline__ void walk_jacobian(const SmoothArgs& A, const float* 
     log_p += ls;
     if (log_p < stop || ++j > steps) break;
     zj = fixed_tau ? 0.0f : z[(j - 1) * 32u];
-    tau = fixed_tau ? 0.0 : fma(sigma, f32_to_f64_bits(zj), mu);
-    R = R - tau;
+    r.step(zj);
     dmu += 1.0f;
     dsig += zj;
   }
@@ -247,7 +341,7 @@ __global__ void __launch_bounds__(kThreads, 5) k_smooth_jacobian(const SmoothArg
   extern __shared__ float facc[];
   __shared__ ZigTables Z;
   __shared__ double u_age[kThreads];
-  __shared__ float u_one[kThreads];
+  __shared__ float u_one[kThreads], u_one_lo[kThreads];
   constexpr uint32_t kWarps = kThreads / 32;
   const uint32_t b = blockIdx.x, k = blockIdx.z;
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
@@ -271,21 +365,27 @@ __global__ void __launch_bounds__(kThreads, 5) k_smooth_jacobian(const SmoothArg
   const uint64_t r0 = __ldg(A.bin_start + b), r1 = __ldg(A.bin_start + b + 1);
   float* fmy = facc + threadIdx.x;
   const float inv_h = (float)A.inv_h;
+  RemGrid rg;
+  const bool grid = grid_setup(rg, mu, sd, A.t_max, steps, 1.0 / A.inv_h);
+  const RemFp64 rd{mu, sd, A.t_max, 0.0};
   const uint64_t nlin = (r1 - r0) * A.paths;
   for (uint64_t base = (uint64_t)warp * 32u; base < nlin; base += 32u * kWarps) {
     if (base + lane < nlin) {
-      draw_lineage(A, Z, r0, base + lane, steps, zbuf + lane, u_age[threadIdx.x]);
-      u_one[threadIdx.x] = __double2float_rn(1.0 + u_age[threadIdx.x]);
+      double u;
+      draw_lineage(A, Z, r0, base + lane, steps, zbuf + lane, u);
+      store_lineage_u(u, u_age + threadIdx.x, u_one + threadIdx.x, u_one_lo + threadIdx.x);
     }
     __syncwarp();
     const uint32_t n = (uint32_t)((nlin - base) < 32u ? (nlin - base) : 32u);
     if (live) {
       for (uint32_t ii = 0; ii < n; ++ii) {
+        const uint32_t li = warp * 32u + ii;
         if (quiescent) {
           fmy[0] += 1.0f;  // quiescent type: a leaf at generation 0 (cell.cu:69-75)
+        } else if (grid) {
+          walk_jacobian(zbuf + ii, u_age[li], u_one[li], u_one_lo[li], inv_h, steps, rg, fixed_tau, fmy);
         } else {
-          walk_jacobian(A, zbuf + ii, u_age[warp * 32u + ii], u_one[warp * 32u + ii], inv_h, steps, mu, sd,
-                        fixed_tau, fmy);
+          walk_jacobian(zbuf + ii, u_age[li], u_one[li], u_one_lo[li], inv_h, steps, rd, fixed_tau, fmy);
         }
       }
     }
@@ -319,7 +419,7 @@ __global__ void __launch_bounds__(kThreads, 5) k_smooth(const SmoothArgs A, cons
   __shared__ ZigTables Z;
   __shared__ float Ag2[Backward ? 32 : 1][kSmoothMaxRows];
   __shared__ double u_age[kThreads];
-  __shared__ float u_one[kThreads];
+  __shared__ float u_one[kThreads], u_one_lo[kThreads];
   constexpr uint32_t kWarps = kThreads / 32;
   const uint32_t b = blockIdx.x, k = blockIdx.z;
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
@@ -363,13 +463,17 @@ __global__ void __launch_bounds__(kThreads, 5) k_smooth(const SmoothArgs A, cons
   float* fmy = facc + threadIdx.x;
   const float inv_h = (float)A.inv_h;
   const float* my_ag = Backward ? Ag2[lane] : nullptr;
+  RemGrid rg;
+  const bool grid = grid_setup(rg, mu, sd, A.t_max, steps, 1.0 / A.inv_h);
+  const RemFp64 rd{mu, sd, A.t_max, 0.0};
   // lineage i of the bin: initial cell r0 + i / paths, replica i % paths
   const uint64_t nlin = (r1 - r0) * A.paths;
   for (uint64_t base = (uint64_t)warp * 32u; base < nlin; base += 32u * kWarps) {
     // this lane draws lineage base + lane
     if (base + lane < nlin) {
-      draw_lineage(A, Z, r0, base + lane, steps, zbuf + lane, u_age[threadIdx.x]);
-      u_one[threadIdx.x] = __double2float_rn(1.0 + u_age[threadIdx.x]);
+      double u;
+      draw_lineage(A, Z, r0, base + lane, steps, zbuf + lane, u);
+      store_lineage_u(u, u_age + threadIdx.x, u_one + threadIdx.x, u_one_lo + threadIdx.x);
     }
     __syncwarp();
     const uint32_t n = (uint32_t)((nlin - base) < 32u ? (nlin - base) : 32u);
@@ -385,8 +489,13 @@ __global__ void __launch_bounds__(kThreads, 5) k_smooth(const SmoothArgs A, cons
             fmy[kThreads] = __fsub_rn(fmy[kThreads], w_lo);
           }
         } else if (walks) {
-          walk<Backward>(A, zbuf + ii, u_age[warp * 32u + ii], u_one[warp * 32u + ii], inv_h, steps, mu, sd,
-                         fixed_tau, w_hi, w_lo, fmy, my_ag, f_r, f_mu, f_sig);
+          const uint32_t li = warp * 32u + ii;
+          if (grid)
+            walk<Backward>(zbuf + ii, u_age[li], u_one[li], u_one_lo[li], inv_h, steps, rg, fixed_tau, w_hi, w_lo,
+                           fmy, my_ag, f_r, f_mu, f_sig);
+          else
+            walk<Backward>(zbuf + ii, u_age[li], u_one[li], u_one_lo[li], inv_h, steps, rd, fixed_tau, w_hi, w_lo,
+                           fmy, my_ag, f_r, f_mu, f_sig);
         }
         if constexpr (Backward) {
           // per-thread compensated FP32 sums (terms of either sign cancel); scaled by
