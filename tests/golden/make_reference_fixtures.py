@@ -12,7 +12,11 @@ Variants (procell.configs.small's histogram unless stated):
                the totals, only which column a leaf is counted in;
   medium_t150  the medium workload's histogram and types (1e6 initial cells) with t_max 150,
                the largest input the reference's planner runs in one iteration
-               (oracle/ref_planner.py); 16 runs by default, wall time of each recorded.
+               (oracle/ref_planner.py); 16 runs by default, wall time of each recorded;
+  medium_t150_same_timer  the same histogram and t_max with three types that share
+               (mean, sd) = (60, 18), ratios 0.4 / 0.35 / 0.25, no quiescent type: the type
+               drawn cannot change the totals, so any loss of cells (a child grid the
+               reference failed to launch) or any extra cell would show in them.
 
 The reference seeds every random stream with time(NULL); the preloaded oracle/_ref
 libtimeshim.so returns PROCELL_REF_TIME instead, so the runs are reproducible. Run k gets the
@@ -42,7 +46,8 @@ import procell.configs as cfg  # noqa: E402
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--runs", type=int, default=64)
-    ap.add_argument("--variant", choices=["small", "single_type", "same_timer", "medium_t150"], default="small")
+    ap.add_argument("--variant", choices=["small", "single_type", "same_timer", "medium_t150", "medium_t150_same_timer"],
+                    default="small")
     ap.add_argument("--binary", choices=["sm100", "sm103a"], default="sm100")
     ap.add_argument("--out", default=None)
     a = ap.parse_args()
@@ -58,10 +63,13 @@ def main():
     elif a.variant == "same_timer":
         w.types = [(0.53, 48.33, 21.6), (0.47, 48.33, 21.6)]
         track = True
-    elif a.variant == "medium_t150":
+    elif a.variant in ("medium_t150", "medium_t150_same_timer"):
         w = cfg.medium()
         w.t_max = 150.0
         source = "procell.configs.medium, t_max 150"
+        if a.variant == "medium_t150_same_timer":
+            w.types = [(0.4, 60.0, 18.0), (0.35, 60.0, 18.0), (0.25, 60.0, 18.0)]
+            source += ", three types sharing (60, 18)"
     d = tempfile.mkdtemp()
     cfg.write_histogram(os.path.join(d, "h.txt"), w.bins)
     cfg.write_types(os.path.join(d, "c.txt"), w.types)

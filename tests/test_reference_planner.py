@@ -54,6 +54,16 @@ def test_medium_histogram_at_t150_runs_in_one_safe_iteration(oracle_lib, planner
 
 
 @pytest.mark.parametrize("free", FREE)
+def test_medium_histogram_with_shared_timers_runs_in_one_safe_iteration(oracle_lib, planner, free):
+    w = cfg.medium()
+    w.t_max = 150.0
+    w.types = [(0.4, 60.0, 18.0), (0.35, 60.0, 18.0), (0.25, 60.0, 18.0)]
+    g, nv = max_gen_and_values(oracle_lib, w)
+    a = planner.assess(w.roots, nv, g, int(free), len(w.types))
+    assert a["safe"], a["reasons"]
+
+
+@pytest.mark.parametrize("free", FREE)
 @pytest.mark.parametrize("name", ["medium", "large"])
 def test_configured_medium_and_large_need_a_second_iteration(oracle_lib, planner, free, name):
     w = cfg.by_name(name)
