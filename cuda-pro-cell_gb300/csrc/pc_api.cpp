@@ -76,6 +76,9 @@ struct pc_context {
   unsigned long long* pinned = nullptr;     // host staging for small reads
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   uint64_t free_at_start = 0;
+  // host-side fault injection (option fail_nth_call): CUDA calls the library made for this
+  // context, the call number that fails next (0: none) and the failures injected so far
+  uint64_t cuda_calls = 0, fail_at = 0, faults_injected = 0;
 };
 
 // One simulation input: a histogram, a type set, t_max, phi and a seed, prepared once.
@@ -144,6 +147,80 @@ int fail(pc_context* ctx, int code, const std::string& msg) {
                   std::string(#call) + ": " + cudaGetErrorString(e__));                       \
   } while (0)
 
+// ---- Host-side fault injection -----------------------------------------------------------
+// Every allocation, copy, memset, synchronisation, event record and kernel or graph launch
+// this file makes goes through the wrappers below. Inside an entry point that names its
+// context (FaultScope), each counts as one call of that context; when the option
+// fail_nth_call = n is set, call n from then on does not reach CUDA and returns an error
+// instead (cudaErrorMemoryAllocation for allocations, cudaErrorLaunchOutOfResources for
+// launches, cudaErrorInvalidValue otherwise), once. Live device allocations are counted
+// process-wide, so tests can check that a failed call leaks nothing.
+thread_local pc_context* t_fault_ctx = nullptr;
+std::atomic<long long> g_live_device_allocs{0};
+
+struct FaultScope {
+  pc_context* prev;
+  explicit FaultScope(pc_context* c) : prev(t_fault_ctx) { t_fault_ctx = c; }
+  ~FaultScope() { t_fault_ctx = prev; }
+};
+
+cudaError_t injected(cudaError_t code) {
+  pc_context* c = t_fault_ctx;
+  if (!c) return cudaSuccess;
+  ++c->cuda_calls;
+  if (c->fail_at != 0 && c->cuda_calls == c->fail_at) {
+    c->fail_at = 0;
+    ++c->faults_injected;
+    return code;
+  }
+  return cudaSuccess;
+}
+
+template <class T>
+cudaError_t pc_cuda_malloc(T** p, size_t bytes) {
+  if (cudaError_t f = injected(cudaErrorMemoryAllocation)) return f;
+  const cudaError_t e = cudaMalloc(p, bytes);
+  if (e == cudaSuccess) ++g_live_device_allocs;
+  return e;
+}
+cudaError_t pc_cuda_free(void* p) {
+  if (p) --g_live_device_allocs;
+  return cudaFree(p);
+}
+template <class T>
+cudaError_t pc_cuda_malloc_host(T** p, size_t bytes) {
+  if (cudaError_t f = injected(cudaErrorMemoryAllocation)) return f;
+  return cudaMallocHost(p, bytes);
+}
+cudaError_t pc_cuda_copy(void* dst, const void* src, size_t n, cudaMemcpyKind k, cudaStream_t s) {
+  if (cudaError_t f = injected(cudaErrorInvalidValue)) return f;
+  return cudaMemcpyAsync(dst, src, n, k, s);
+}
+cudaError_t pc_cuda_copy_sync(void* dst, const void* src, size_t n, cudaMemcpyKind k) {
+  if (cudaError_t f = injected(cudaErrorInvalidValue)) return f;
+  return cudaMemcpy(dst, src, n, k);
+}
+cudaError_t pc_cuda_memset(void* p, int v, size_t n, cudaStream_t s) {
+  if (cudaError_t f = injected(cudaErrorInvalidValue)) return f;
+  return cudaMemsetAsync(p, v, n, s);
+}
+cudaError_t pc_cuda_sync(cudaStream_t s) {
+  if (cudaError_t f = injected(cudaErrorInvalidValue)) return f;
+  return cudaStreamSynchronize(s);
+}
+cudaError_t pc_cuda_event_record(cudaEvent_t e, cudaStream_t s) {
+  if (cudaError_t f = injected(cudaErrorInvalidValue)) return f;
+  return cudaEventRecord(e, s);
+}
+cudaError_t pc_cuda_graph_launch(cudaGraphExec_t g, cudaStream_t s) {
+  if (cudaError_t f = injected(cudaErrorLaunchOutOfResources)) return f;
+  return cudaGraphLaunch(g, s);
+}
+// A kernel launch through one of the launch functions (they return a cudaError_t as int);
+// an injected failure skips the launch.
+#define PC_LAUNCH(expr) \
+  (injected(cudaErrorLaunchOutOfResources) != cudaSuccess ? cudaErrorLaunchOutOfResources : (cudaError_t)(expr))
+
 // Ziggurat tables for f(x) = exp(-x^2/2), 128 layers (Marsaglia & Tsang 2000): the layer
 // edges follow x_{i+1} = sqrt(-2 ln(v/x_i + f(x_i))) from x_1 = r; the base strip's
 // effective width is v/f(r).
@@ -194,10 +271,10 @@ void truncation_bounds(double mu, double sigma, float& zlo, float& zhi) {
 
 void free_pool(pc_context* ctx) {
   for (auto& b : ctx->pool) {
-    cudaFree(b.cells);
-    cudaFree(b.count);
-    cudaFree(b.prefix);
-    cudaFree(b.ticket);
+    pc_cuda_free(b.cells);
+    pc_cuda_free(b.count);
+    pc_cuda_free(b.prefix);
+    pc_cuda_free(b.ticket);
   }
   ctx->pool.clear();
   ctx->pool_cells = 0;
@@ -213,16 +290,16 @@ int acquire(pc_context* ctx, int* idx) {
     }
   }
   LevelBuf b;
-  PC_CUDA(ctx, cudaMalloc(&b.cells, ctx->pool_cells * sizeof(ulonglong2)));
-  cudaError_t e = cudaMalloc(&b.count, ctx->pool_segs * sizeof(unsigned long long));
-  if (e == cudaSuccess) e = cudaMalloc(&b.prefix, (ctx->pool_segs + 1) * sizeof(unsigned long long));
-  if (e == cudaSuccess) e = cudaMalloc(&b.ticket, sizeof(uint32_t));
-  if (e == cudaSuccess) e = cudaMemsetAsync(b.ticket, 0, sizeof(uint32_t), ctx->stream);
+  PC_CUDA(ctx, pc_cuda_malloc(&b.cells, ctx->pool_cells * sizeof(ulonglong2)));
+  cudaError_t e = pc_cuda_malloc(&b.count, ctx->pool_segs * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = pc_cuda_malloc(&b.prefix, (ctx->pool_segs + 1) * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = pc_cuda_malloc(&b.ticket, sizeof(uint32_t));
+  if (e == cudaSuccess) e = pc_cuda_memset(b.ticket, 0, sizeof(uint32_t), ctx->stream);
   if (e != cudaSuccess) {
-    cudaFree(b.cells);
-    cudaFree(b.count);
-    cudaFree(b.prefix);
-    cudaFree(b.ticket);
+    pc_cuda_free(b.cells);
+    pc_cuda_free(b.count);
+    pc_cuda_free(b.prefix);
+    pc_cuda_free(b.ticket);
     return fail(ctx, PC_ERR_NOMEM, std::string("level buffer allocation: ") + cudaGetErrorString(e));
   }
   b.busy = true;
@@ -253,17 +330,17 @@ cudaError_t take_spare(void** spare, size_t* spare_bytes, size_t need, void** ou
     return cudaSuccess;
   }
   *out_bytes = need;
-  return cudaMalloc(out, need);
+  return pc_cuda_malloc(out, need);
 }
 
 // Keep the larger of `buf` and the context's spare, free the other.
 void give_spare(void** spare, size_t* spare_bytes, void* buf, size_t bytes) {
   if (!buf) return;
   if (*spare && *spare_bytes >= bytes) {
-    cudaFree(buf);
+    pc_cuda_free(buf);
     return;
   }
-  cudaFree(*spare);
+  pc_cuda_free(*spare);
   *spare = buf;
   *spare_bytes = bytes;
 }
@@ -332,13 +409,13 @@ int pc_create(pc_context** out, int device) {
   const int oe = occupancy_blocks_per_sm(&ctx->root_bps, &ctx->div_bps);
   if (oe != 0) return bail((cudaError_t)oe, "occupancy query (is the sm_103a binary loadable?)");
   ctx->zig_host = build_zig_tables();
-  if ((e = cudaMalloc(&ctx->zig_dev, sizeof(ZigTables))) != cudaSuccess) return bail(e, "cudaMalloc");
-  if ((e = cudaMemcpy(ctx->zig_dev, &ctx->zig_host, sizeof(ZigTables), cudaMemcpyHostToDevice)) != cudaSuccess)
+  if ((e = pc_cuda_malloc(&ctx->zig_dev, sizeof(ZigTables))) != cudaSuccess) return bail(e, "cudaMalloc");
+  if ((e = pc_cuda_copy_sync(ctx->zig_dev, &ctx->zig_host, sizeof(ZigTables), cudaMemcpyHostToDevice)) != cudaSuccess)
     return bail(e, "cudaMemcpy");
-  if ((e = cudaMalloc(&ctx->stats_dev, 4 * sizeof(unsigned long long))) != cudaSuccess) return bail(e, "cudaMalloc");
-  if ((e = cudaMalloc(&ctx->error_dev, sizeof(uint32_t))) != cudaSuccess) return bail(e, "cudaMalloc");
-  if ((e = cudaMalloc(&ctx->persist_ctl, 48)) != cudaSuccess) return bail(e, "cudaMalloc");
-  if ((e = cudaMallocHost(&ctx->pinned, 64 * sizeof(unsigned long long))) != cudaSuccess)
+  if ((e = pc_cuda_malloc(&ctx->stats_dev, 4 * sizeof(unsigned long long))) != cudaSuccess) return bail(e, "cudaMalloc");
+  if ((e = pc_cuda_malloc(&ctx->error_dev, sizeof(uint32_t))) != cudaSuccess) return bail(e, "cudaMalloc");
+  if ((e = pc_cuda_malloc(&ctx->persist_ctl, 48)) != cudaSuccess) return bail(e, "cudaMalloc");
+  if ((e = pc_cuda_malloc_host(&ctx->pinned, 64 * sizeof(unsigned long long))) != cudaSuccess)
     return bail(e, "cudaMallocHost");
   for (auto& ev : ctx->ev)
     if ((e = cudaEventCreate(&ev)) != cudaSuccess) return bail(e, "cudaEventCreate");
@@ -353,15 +430,15 @@ int pc_create(pc_context** out, int device) {
 void pc_destroy(pc_context* ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
-  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  if (ctx->stream) pc_cuda_sync(ctx->stream);
   free_pool(ctx);
   for (pc_plan* p : ctx->live) p->owner = nullptr;  // plans outliving their context free their own buffers
-  cudaFree(ctx->spare_rec);
-  cudaFree(ctx->spare_hist);
-  cudaFree(ctx->zig_dev);
-  cudaFree(ctx->stats_dev);
-  cudaFree(ctx->error_dev);
-  cudaFree(ctx->persist_ctl);
+  pc_cuda_free(ctx->spare_rec);
+  pc_cuda_free(ctx->spare_hist);
+  pc_cuda_free(ctx->zig_dev);
+  pc_cuda_free(ctx->stats_dev);
+  pc_cuda_free(ctx->error_dev);
+  pc_cuda_free(ctx->persist_ctl);
   cudaFreeHost(ctx->pinned);
   cudaFreeHost(ctx->stage);
   for (auto& ev : ctx->ev)
@@ -372,6 +449,7 @@ void pc_destroy(pc_context* ctx) {
 
 int pc_set_stream(pc_context* ctx, void* stream) {
   PC_GUARD_BEGIN
+  FaultScope fault_scope__(ctx);
   if (!ctx) return PC_ERR_INVALID;
   ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
   return PC_OK;
@@ -380,6 +458,7 @@ int pc_set_stream(pc_context* ctx, void* stream) {
 
 int pc_set_option(pc_context* ctx, const char* name, double value) {
   PC_GUARD_BEGIN
+  FaultScope fault_scope__(ctx);
   if (!ctx || !name) return PC_ERR_INVALID;
   if (!(value >= 0.0) || !std::isfinite(value)) return fail(ctx, PC_ERR_INVALID, "option value must be >= 0");
   const std::string n(name);
@@ -399,6 +478,9 @@ int pc_set_option(pc_context* ctx, const char* name, double value) {
     ctx->opt_driver = (int)value;
   } else if (n == "graph") {
     ctx->opt_graph = value != 0.0 ? 1 : 0;
+  } else if (n == "fail_nth_call") {
+    // counted from the calls made so far: the n-th call after this one fails (0: none)
+    ctx->fail_at = value >= 1.0 ? ctx->cuda_calls + (uint64_t)value : 0;
   } else {
     return fail(ctx, PC_ERR_INVALID, "unknown option " + n);
   }
@@ -689,8 +771,8 @@ int finalize_plan(pc_context* ctx, pc_plan* p) {
   const size_t nb = bins;
   p->hist_elems = (size_t)p->hist_gens * std::max<uint64_t>(1, classes);
   p->upload_bytes = nb * sizeof(uint32_t) + (nb + 1) * sizeof(uint64_t);
-  cudaError_t e = cudaMalloc(&p->bin_info_dev, std::max<size_t>(1, nb) * sizeof(uint32_t));
-  if (e == cudaSuccess) e = cudaMalloc(&p->bin_start_dev, (nb + 1) * sizeof(uint64_t));
+  cudaError_t e = pc_cuda_malloc(&p->bin_info_dev, std::max<size_t>(1, nb) * sizeof(uint32_t));
+  if (e == cudaSuccess) e = pc_cuda_malloc(&p->bin_start_dev, (nb + 1) * sizeof(uint64_t));
   p->owner = ctx;
   ctx->live.push_back(p);
   if (e == cudaSuccess)
@@ -700,31 +782,31 @@ int finalize_plan(pc_context* ctx, pc_plan* p) {
     e = take_spare(&ctx->spare_hist, &ctx->spare_hist_bytes, p->hist_elems * sizeof(unsigned long long),
                    reinterpret_cast<void**>(&p->hist_dev), &p->hist_bytes);
   if (e == cudaSuccess && nb)
-    e = cudaMemcpyAsync(p->bin_info_dev, p->bin_info.data(), nb * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
+    e = pc_cuda_copy(p->bin_info_dev, p->bin_info.data(), nb * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess)
-    e = cudaMemcpyAsync(p->bin_start_dev, p->bin_start.data(), (nb + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, st);
+    e = pc_cuda_copy(p->bin_start_dev, p->bin_start.data(), (nb + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, st);
   if (!p->batched) {
     const size_t nt = p->inst[0].types.size();
-    if (e == cudaSuccess) e = cudaMalloc(&p->types_dev, nt * sizeof(TypeDev));
+    if (e == cudaSuccess) e = pc_cuda_malloc(&p->types_dev, nt * sizeof(TypeDev));
     if (e == cudaSuccess)
-      e = cudaMemcpyAsync(p->types_dev, p->inst[0].types.data(), nt * sizeof(TypeDev), cudaMemcpyHostToDevice, st);
+      e = pc_cuda_copy(p->types_dev, p->inst[0].types.data(), nt * sizeof(TypeDev), cudaMemcpyHostToDevice, st);
     p->upload_bytes += nt * sizeof(TypeDev);
   } else {
-    if (e == cudaSuccess) e = cudaMalloc(&p->btypes_dev, btypes.size() * sizeof(BatchType));
-    if (e == cudaSuccess) e = cudaMalloc(&p->inst_dev, idev.size() * sizeof(InstanceDev));
-    if (e == cudaSuccess) e = cudaMalloc(&p->bin_inst_dev, std::max<size_t>(1, nb) * sizeof(uint32_t));
-    if (e == cudaSuccess) e = cudaMalloc(&p->bin_class_dev, std::max<size_t>(1, nb) * sizeof(uint32_t));
+    if (e == cudaSuccess) e = pc_cuda_malloc(&p->btypes_dev, btypes.size() * sizeof(BatchType));
+    if (e == cudaSuccess) e = pc_cuda_malloc(&p->inst_dev, idev.size() * sizeof(InstanceDev));
+    if (e == cudaSuccess) e = pc_cuda_malloc(&p->bin_inst_dev, std::max<size_t>(1, nb) * sizeof(uint32_t));
+    if (e == cudaSuccess) e = pc_cuda_malloc(&p->bin_class_dev, std::max<size_t>(1, nb) * sizeof(uint32_t));
     if (e == cudaSuccess)
-      e = cudaMemcpyAsync(p->btypes_dev, btypes.data(), btypes.size() * sizeof(BatchType), cudaMemcpyHostToDevice, st);
+      e = pc_cuda_copy(p->btypes_dev, btypes.data(), btypes.size() * sizeof(BatchType), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess)
-      e = cudaMemcpyAsync(p->inst_dev, idev.data(), idev.size() * sizeof(InstanceDev), cudaMemcpyHostToDevice, st);
+      e = pc_cuda_copy(p->inst_dev, idev.data(), idev.size() * sizeof(InstanceDev), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess && nb)
-      e = cudaMemcpyAsync(p->bin_inst_dev, bin_inst.data(), nb * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
+      e = pc_cuda_copy(p->bin_inst_dev, bin_inst.data(), nb * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess && nb)
-      e = cudaMemcpyAsync(p->bin_class_dev, bin_class.data(), nb * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
+      e = pc_cuda_copy(p->bin_class_dev, bin_class.data(), nb * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
     p->upload_bytes += btypes.size() * sizeof(BatchType) + idev.size() * sizeof(InstanceDev) + 2 * nb * sizeof(uint32_t);
   }
-  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e == cudaSuccess) e = pc_cuda_sync(st);
   if (e != cudaSuccess)
     return fail(ctx, e == cudaErrorMemoryAllocation ? PC_ERR_NOMEM : PC_ERR_CUDA,
                 std::string("plan upload: ") + cudaGetErrorString(e));
@@ -789,13 +871,13 @@ int stage_table(pc_context* ctx, pc_plan* p, const unsigned long long** out) {
       cudaFreeHost(ctx->stage);
       ctx->stage = nullptr;
       ctx->stage_elems = 0;
-      PC_CUDA(ctx, cudaMallocHost(&ctx->stage, p->hist_elems * sizeof(unsigned long long)));
+      PC_CUDA(ctx, pc_cuda_malloc_host(&ctx->stage, p->hist_elems * sizeof(unsigned long long)));
       ctx->stage_elems = p->hist_elems;
     }
     ctx->stage_plan = 0;
-    PC_CUDA(ctx, cudaMemcpyAsync(ctx->stage, p->hist_dev, p->hist_elems * sizeof(unsigned long long),
+    PC_CUDA(ctx, pc_cuda_copy(ctx->stage, p->hist_dev, p->hist_elems * sizeof(unsigned long long),
                                  cudaMemcpyDeviceToHost, ctx->stream));
-    PC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    PC_CUDA(ctx, pc_cuda_sync(ctx->stream));
     ctx->stage_plan = p->id;
     ctx->stage_run = p->run_id;
   }
@@ -807,9 +889,27 @@ int stage_table(pc_context* ctx, pc_plan* p, const unsigned long long** out) {
 
 extern "C" {
 
+int pc_get_option(pc_context* ctx, const char* name, double* value) {
+  if (!ctx || !name || !value) return PC_ERR_INVALID;
+  const std::string n(name);
+  if (n == "cuda_calls") {
+    *value = (double)ctx->cuda_calls;
+  } else if (n == "faults_injected") {
+    *value = (double)ctx->faults_injected;
+  } else if (n == "device_allocations") {
+    *value = (double)g_live_device_allocs.load();
+  } else if (n == "level_buffers") {
+    *value = (double)ctx->pool.size();
+  } else {
+    return fail(ctx, PC_ERR_INVALID, "unknown option " + n);
+  }
+  return PC_OK;
+}
+
 int pc_plan_create(pc_context* ctx, const pc_bin* bins, uint64_t n_bins, const pc_cell_type* types,
                    uint32_t n_types, double t_max, double phi, uint64_t seed, pc_plan** out) {
   PC_GUARD_BEGIN
+  FaultScope fault_scope__(ctx);
   if (!ctx || !out) return fail(ctx, PC_ERR_INVALID, "null argument");
   *out = nullptr;
   pc_plan* p = new (std::nothrow) pc_plan();
@@ -835,6 +935,7 @@ int pc_plan_create(pc_context* ctx, const pc_bin* bins, uint64_t n_bins, const p
 
 int pc_plan_set_roots(pc_context* ctx, pc_plan* p, uint64_t root_begin, uint64_t root_end) {
   PC_GUARD_BEGIN
+  FaultScope fault_scope__(ctx);
   if (!ctx || !p) return PC_ERR_INVALID;
   if (root_begin > root_end || root_end > p->roots_total)
     return fail(ctx, PC_ERR_INVALID, "root range outside [0, number of initial cells]");
@@ -847,21 +948,21 @@ int pc_plan_set_roots(pc_context* ctx, pc_plan* p, uint64_t root_begin, uint64_t
 void pc_plan_destroy(pc_plan* p) {
   if (!p) return;
   if (p->graph) cudaGraphExecDestroy(p->graph);
-  cudaFree(p->types_dev);
-  cudaFree(p->btypes_dev);
-  cudaFree(p->inst_dev);
-  cudaFree(p->bin_inst_dev);
-  cudaFree(p->bin_class_dev);
-  cudaFree(p->bin_info_dev);
-  cudaFree(p->bin_start_dev);
+  pc_cuda_free(p->types_dev);
+  pc_cuda_free(p->btypes_dev);
+  pc_cuda_free(p->inst_dev);
+  pc_cuda_free(p->bin_inst_dev);
+  pc_cuda_free(p->bin_class_dev);
+  pc_cuda_free(p->bin_info_dev);
+  pc_cuda_free(p->bin_start_dev);
   if (p->owner) {
     pc_context* ctx = p->owner;
     ctx->live.erase(std::remove(ctx->live.begin(), ctx->live.end(), p), ctx->live.end());
     give_spare(&ctx->spare_rec, &ctx->spare_rec_bytes, p->root_rec_dev, p->rec_bytes);
     give_spare(&ctx->spare_hist, &ctx->spare_hist_bytes, p->hist_dev, p->hist_bytes);
   } else {
-    cudaFree(p->root_rec_dev);
-    cudaFree(p->hist_dev);
+    pc_cuda_free(p->root_rec_dev);
+    pc_cuda_free(p->hist_dev);
   }
   delete p;
 }
@@ -896,6 +997,7 @@ RunArgs make_args(const pc_context* ctx, const pc_plan* p) {
   a.bin_info = p->bin_info_dev;
   a.bin_start = p->bin_start_dev;
   a.root_rec = p->root_rec_dev;
+  a.rec_cap = p->rec_bytes / sizeof(unsigned long long);
   a.hist = p->hist_dev;
   a.stats = ctx->stats_dev;
   a.error = ctx->error_dev;
@@ -921,7 +1023,7 @@ int kernel_occupancy(pc_context* ctx, bool narrow, bool batched, int config, con
 // above `cap`), with count/prefix arrays for `segs` segments.
 int ensure_pool_geometry(pc_context* ctx, uint64_t want, uint64_t cap, uint32_t segs) {
   if (ctx->pool_cells < want || ctx->pool_cells > std::max(cap, want) || ctx->pool_segs < segs) {
-    PC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    PC_CUDA(ctx, pc_cuda_sync(ctx->stream));
     free_pool(ctx);
     ctx->pool_cells = want;
     ctx->pool_segs = segs;
@@ -978,11 +1080,11 @@ int run_per_sweep(pc_context* ctx, pc_plan* p, const SweepKernels& K, const int 
     const int blocks = grid_for(ctx, n, occ[0], K.threads);
     const uint32_t nseg = (uint32_t)blocks * warps;
     LevelOut o{L.cells, L.count, L.prefix, L.ticket, (n + nseg - 1) / nseg};
-    PC_CUDA(ctx, cudaEventRecord(ctx->ev[0], st));
-    PC_CUDA(ctx, (cudaError_t)K.roots(a, 0, n, o, blocks, st));
-    PC_CUDA(ctx, cudaEventRecord(ctx->ev[1], st));
-    PC_CUDA(ctx, cudaMemcpyAsync(ctx->pinned, L.prefix + nseg, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
-    PC_CUDA(ctx, cudaStreamSynchronize(st));
+    PC_CUDA(ctx, pc_cuda_event_record(ctx->ev[0], st));
+    PC_CUDA(ctx, PC_LAUNCH(K.roots(a, 0, n, o, blocks, st)));
+    PC_CUDA(ctx, pc_cuda_event_record(ctx->ev[1], st));
+    PC_CUDA(ctx, pc_cuda_copy(ctx->pinned, L.prefix + nseg, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+    PC_CUDA(ctx, pc_cuda_sync(st));
     PC_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]));
     dev_ms += ms;
     const uint64_t n0 = ctx->pinned[0];
@@ -1004,10 +1106,10 @@ int run_per_sweep(pc_context* ctx, pc_plan* p, const SweepKernels& K, const int 
       LevelIn li{In.cells, In.prefix, top.nseg, top.stride, top.pos, top.pos + len};
       LevelOut lo{Out.cells, Out.count, Out.prefix, Out.ticket, 2 * ((len + oseg - 1) / oseg)};
       const uint32_t gen = top.gen;
-      PC_CUDA(ctx, cudaEventRecord(ctx->ev[2], st));
-      PC_CUDA(ctx, (cudaError_t)K.divide(a, li, gen, lo, blocks_d, st));
-      PC_CUDA(ctx, cudaEventRecord(ctx->ev[3], st));
-      PC_CUDA(ctx, cudaMemcpyAsync(ctx->pinned, Out.prefix + oseg, sizeof(unsigned long long),
+      PC_CUDA(ctx, pc_cuda_event_record(ctx->ev[2], st));
+      PC_CUDA(ctx, PC_LAUNCH(K.divide(a, li, gen, lo, blocks_d, st)));
+      PC_CUDA(ctx, pc_cuda_event_record(ctx->ev[3], st));
+      PC_CUDA(ctx, pc_cuda_copy(ctx->pinned, Out.prefix + oseg, sizeof(unsigned long long),
                                    cudaMemcpyDeviceToHost, st));
       divisions += len;
       ++sweeps;
@@ -1017,7 +1119,7 @@ int run_per_sweep(pc_context* ctx, pc_plan* p, const SweepKernels& K, const int 
         ctx->pool[top.buf].busy = false;  // stream order protects the in-flight read
         stack.pop_back();
       }
-      PC_CUDA(ctx, cudaStreamSynchronize(st));
+      PC_CUDA(ctx, pc_cuda_sync(st));
       PC_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]));
       dev_ms += ms;
       div_ms += ms;
@@ -1029,9 +1131,9 @@ int run_per_sweep(pc_context* ctx, pc_plan* p, const SweepKernels& K, const int 
       }
     }
   }
-  PC_CUDA(ctx, cudaMemcpyAsync(ctx->pinned, ctx->stats_dev, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
-  PC_CUDA(ctx, cudaMemcpyAsync(ctx->pinned + 8, ctx->error_dev, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-  PC_CUDA(ctx, cudaStreamSynchronize(st));
+  PC_CUDA(ctx, pc_cuda_copy(ctx->pinned, ctx->stats_dev, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+  PC_CUDA(ctx, pc_cuda_copy(ctx->pinned + 8, ctx->error_dev, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+  PC_CUDA(ctx, pc_cuda_sync(st));
   p->stats.divisions = divisions;
   p->stats.sweeps = sweeps;
   p->stats.root_sweeps = chunks;
@@ -1047,14 +1149,14 @@ int run_per_sweep(pc_context* ctx, pc_plan* p, const SweepKernels& K, const int 
 // clear the counts and control words, the cooperative launch, the totals back to pinned.
 int enqueue_persistent(pc_context* ctx, pc_plan* p, const SweepKernels& K, const PersistArgs& pa, int grid,
                        cudaStream_t s) {
-  PC_CUDA(ctx, cudaMemsetAsync(p->hist_dev, 0, p->hist_elems * sizeof(unsigned long long), s));
-  PC_CUDA(ctx, cudaMemsetAsync(ctx->stats_dev, 0, 4 * sizeof(unsigned long long), s));
-  PC_CUDA(ctx, cudaMemsetAsync(ctx->error_dev, 0, sizeof(uint32_t), s));
-  PC_CUDA(ctx, cudaMemsetAsync(ctx->persist_ctl, 0, 48, s));
-  PC_CUDA(ctx, (cudaError_t)K.persist(pa, grid, s));
-  PC_CUDA(ctx, cudaMemcpyAsync(ctx->pinned, ctx->stats_dev, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
-  PC_CUDA(ctx, cudaMemcpyAsync(ctx->pinned + 8, ctx->error_dev, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
-  PC_CUDA(ctx, cudaMemcpyAsync(ctx->pinned + 16, ctx->persist_ctl + 4, 4 * sizeof(unsigned long long),
+  PC_CUDA(ctx, pc_cuda_memset(p->hist_dev, 0, p->hist_elems * sizeof(unsigned long long), s));
+  PC_CUDA(ctx, pc_cuda_memset(ctx->stats_dev, 0, 4 * sizeof(unsigned long long), s));
+  PC_CUDA(ctx, pc_cuda_memset(ctx->error_dev, 0, sizeof(uint32_t), s));
+  PC_CUDA(ctx, pc_cuda_memset(ctx->persist_ctl, 0, 48, s));
+  PC_CUDA(ctx, PC_LAUNCH(K.persist(pa, grid, s)));
+  PC_CUDA(ctx, pc_cuda_copy(ctx->pinned, ctx->stats_dev, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+  PC_CUDA(ctx, pc_cuda_copy(ctx->pinned + 8, ctx->error_dev, sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+  PC_CUDA(ctx, pc_cuda_copy(ctx->pinned + 16, ctx->persist_ctl + 4, 4 * sizeof(unsigned long long),
                                cudaMemcpyDeviceToHost, s));
   return PC_OK;
 }
@@ -1110,7 +1212,7 @@ int run_persistent(pc_context* ctx, pc_plan* p, const SweepKernels& K, const int
   pa.timeout_ns = 20000000000ull;
 
   float ms = 0.f;
-  PC_CUDA(ctx, cudaEventRecord(ctx->ev[0], st));
+  PC_CUDA(ctx, pc_cuda_event_record(ctx->ev[0], st));
   bool use_graph = ctx->opt_graph != 0;
   if (use_graph) {
     const bool same = p->graph && p->graph_config == ctx->opt_config && p->graph_grid == grid &&
@@ -1119,7 +1221,7 @@ int run_persistent(pc_context* ctx, pc_plan* p, const SweepKernels& K, const int
       if (p->graph) cudaGraphExecDestroy(p->graph);
       p->graph = nullptr;
       cudaStream_t cap_st = ctx->own_stream;
-      PC_CUDA(ctx, cudaStreamSynchronize(st));
+      PC_CUDA(ctx, pc_cuda_sync(st));
       PC_CUDA(ctx, cudaStreamBeginCapture(cap_st, cudaStreamCaptureModeThreadLocal));
       rc = enqueue_persistent(ctx, p, K, pa, grid, cap_st);
       cudaGraph_t g = nullptr;
@@ -1140,13 +1242,13 @@ int run_persistent(pc_context* ctx, pc_plan* p, const SweepKernels& K, const int
     }
   }
   if (use_graph) {
-    PC_CUDA(ctx, cudaGraphLaunch(p->graph, st));
+    PC_CUDA(ctx, pc_cuda_graph_launch(p->graph, st));
   } else {
     rc = enqueue_persistent(ctx, p, K, pa, grid, st);
     if (rc != PC_OK) return rc;
   }
-  PC_CUDA(ctx, cudaEventRecord(ctx->ev[1], st));
-  PC_CUDA(ctx, cudaStreamSynchronize(st));
+  PC_CUDA(ctx, pc_cuda_event_record(ctx->ev[1], st));
+  PC_CUDA(ctx, pc_cuda_sync(st));
   PC_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]));
   p->stats.divisions = ctx->pinned[16];
   p->stats.sweeps = (uint32_t)ctx->pinned[17];
@@ -1165,9 +1267,13 @@ extern "C" {
 
 int pc_plan_run(pc_context* ctx, pc_plan* p) {
   PC_GUARD_BEGIN
+  FaultScope fault_scope__(ctx);
   if (!ctx || !p) return PC_ERR_INVALID;
   PC_CUDA(ctx, cudaSetDevice(ctx->device));
   cudaStream_t st = ctx->stream;
+  // a run that failed part way may have left level buffers marked in use; every run is
+  // complete (or failed) when its call returns, and work in flight is ordered on the stream
+  for (auto& lb : ctx->pool) lb.busy = false;
   std::memset(&p->stats, 0, sizeof(p->stats));
   const uint64_t nroots = p->root_end - p->root_begin;
   p->stats.roots = nroots;
@@ -1183,11 +1289,11 @@ int pc_plan_run(pc_context* ctx, pc_plan* p) {
   rc = PC_ERR_UNSUPPORTED;
   if (ctx->opt_driver == 1 && nroots > 0 && p->nbins > 0) rc = run_persistent(ctx, p, K, occ, a);
   if (rc == PC_ERR_UNSUPPORTED) {
-    PC_CUDA(ctx, cudaMemsetAsync(p->hist_dev, 0, p->hist_elems * sizeof(unsigned long long), st));
-    PC_CUDA(ctx, cudaMemsetAsync(ctx->stats_dev, 0, 4 * sizeof(unsigned long long), st));
-    PC_CUDA(ctx, cudaMemsetAsync(ctx->error_dev, 0, sizeof(uint32_t), st));
+    PC_CUDA(ctx, pc_cuda_memset(p->hist_dev, 0, p->hist_elems * sizeof(unsigned long long), st));
+    PC_CUDA(ctx, pc_cuda_memset(ctx->stats_dev, 0, 4 * sizeof(unsigned long long), st));
+    PC_CUDA(ctx, pc_cuda_memset(ctx->error_dev, 0, sizeof(uint32_t), st));
     if (nroots == 0 || p->nbins == 0) {
-      PC_CUDA(ctx, cudaStreamSynchronize(st));
+      PC_CUDA(ctx, pc_cuda_sync(st));
       return PC_OK;
     }
     rc = run_per_sweep(ctx, p, K, occ, a);
@@ -1197,6 +1303,7 @@ int pc_plan_run(pc_context* ctx, pc_plan* p) {
   p->stats.uncounted = ctx->pinned[1];
   p->stats.h2d_bytes = p->upload_bytes;
   const uint32_t err = (uint32_t)(ctx->pinned[8] & 0xFFFFFFFFu);
+  if (err & 16u) return fail(ctx, PC_ERR_INTERNAL, "internal: a device bounds check failed (checked build)");
   if (err & 4u) return fail(ctx, PC_ERR_CUDA, "persistent driver: a grid barrier timed out");
   if (err & 8u) return fail(ctx, PC_ERR_CUDA, "internal: the persistent schedule ran out of level buffers");
   if (err & 2u) return fail(ctx, PC_ERR_CUDA, "internal: the normal sampler exceeded its rejection budget");
@@ -1208,6 +1315,7 @@ int pc_plan_run(pc_context* ctx, pc_plan* p) {
 
 int pc_plan_stats(pc_context* ctx, const pc_plan* p, pc_stats* out) {
   PC_GUARD_BEGIN
+  FaultScope fault_scope__(ctx);
   if (!ctx || !p || !out) return PC_ERR_INVALID;
   if (!p->ran) return fail(ctx, PC_ERR_INVALID, "plan has not run");
   *out = p->stats;
@@ -1218,6 +1326,7 @@ int pc_plan_stats(pc_context* ctx, const pc_plan* p, pc_stats* out) {
 int pc_plan_raw_counts(pc_context* ctx, pc_plan* p, uint64_t* host_out, uint64_t capacity,
                        uint64_t* n_elems, uint32_t dims[3]) {
   PC_GUARD_BEGIN
+  FaultScope fault_scope__(ctx);
   if (!ctx || !p || p->inst.empty()) return PC_ERR_INVALID;
   const InstanceHost& I = p->inst[0];
   const uint32_t nb = (uint32_t)I.bin_value.size(), nt = (uint32_t)I.types.size();
@@ -1241,6 +1350,7 @@ int pc_plan_raw_counts(pc_context* ctx, pc_plan* p, uint64_t* host_out, uint64_t
 
 int pc_plan_result(pc_context* ctx, pc_plan* p, pc_histogram* out) {
   PC_GUARD_BEGIN
+  FaultScope fault_scope__(ctx);
   if (!ctx || !p || !out || p->inst.empty()) return PC_ERR_INVALID;
   std::memset(out, 0, sizeof(*out));
   if (!p->ran) return fail(ctx, PC_ERR_INVALID, "plan has not run");
@@ -1272,6 +1382,7 @@ void pc_histogram_free(pc_histogram* h) {
 int pc_simulate(pc_context* ctx, const pc_bin* bins, uint64_t n_bins, const pc_cell_type* types,
                 uint32_t n_types, double t_max, double phi, uint64_t seed, pc_histogram* out) {
   PC_GUARD_BEGIN
+  FaultScope fault_scope__(ctx);
   pc_plan* p = nullptr;
   int rc = pc_plan_create(ctx, bins, n_bins, types, n_types, t_max, phi, seed, &p);
   if (rc != PC_OK) return rc;
@@ -1286,6 +1397,7 @@ int pc_simulate_shard(pc_context* ctx, const pc_bin* bins, uint64_t n_bins, cons
                       uint32_t n_types, double t_max, double phi, uint64_t seed, uint64_t root_begin,
                       uint64_t root_end, pc_histogram* out) {
   PC_GUARD_BEGIN
+  FaultScope fault_scope__(ctx);
   pc_plan* p = nullptr;
   int rc = pc_plan_create(ctx, bins, n_bins, types, n_types, t_max, phi, seed, &p);
   if (rc != PC_OK) return rc;
@@ -1329,6 +1441,7 @@ int pc_histogram_accumulate(pc_histogram* dst, const pc_histogram* src) {
 
 int pc_batch_create(pc_context* ctx, const pc_instance* instances, uint32_t n_instances, pc_batch** out) {
   PC_GUARD_BEGIN
+  FaultScope fault_scope__(ctx);
   if (!ctx || !out || (n_instances && !instances)) return fail(ctx, PC_ERR_INVALID, "null argument");
   *out = nullptr;
   if (n_instances == 0) return fail(ctx, PC_ERR_INVALID, "a batch needs at least one instance");
@@ -1374,6 +1487,7 @@ static int batch_table(pc_context* ctx, pc_batch* b, uint32_t instance, const un
 int pc_batch_raw_counts(pc_context* ctx, pc_batch* b, uint32_t instance, uint64_t* host_out, uint64_t capacity,
                         uint64_t* n_elems, uint32_t dims[3]) {
   PC_GUARD_BEGIN
+  FaultScope fault_scope__(ctx);
   if (!ctx || !b) return PC_ERR_INVALID;
   if (instance >= b->inst.size()) return fail(ctx, PC_ERR_INVALID, "instance index out of range");
   const InstanceHost& I = b->inst[instance];
@@ -1397,6 +1511,7 @@ int pc_batch_raw_counts(pc_context* ctx, pc_batch* b, uint32_t instance, uint64_
 
 int pc_batch_result(pc_context* ctx, pc_batch* b, uint32_t instance, pc_histogram* out) {
   PC_GUARD_BEGIN
+  FaultScope fault_scope__(ctx);
   if (!ctx || !b || !out) return PC_ERR_INVALID;
   std::memset(out, 0, sizeof(*out));
   const unsigned long long* h = nullptr;
@@ -1413,6 +1528,7 @@ int pc_batch_result(pc_context* ctx, pc_batch* b, uint32_t instance, pc_histogra
 
 int pc_batch_set_types(pc_context* ctx, pc_batch* b, const pc_cell_type* types) {
   PC_GUARD_BEGIN
+  FaultScope fault_scope__(ctx);
   if (!ctx || !b || !types) return fail(ctx, PC_ERR_INVALID, "null argument");
   if (!b->batched) return fail(ctx, PC_ERR_INVALID, "not a batch");
   // validate every instance's new types before changing anything
@@ -1438,17 +1554,18 @@ int pc_batch_set_types(pc_context* ctx, pc_batch* b, const pc_cell_type* types) 
   batch_type_tables(b, btypes, idev);
   b->ran = false;  // counts of the previous run belong to the previous types
   PC_CUDA(ctx, cudaSetDevice(ctx->device));
-  PC_CUDA(ctx, cudaMemcpyAsync(b->btypes_dev, btypes.data(), btypes.size() * sizeof(BatchType),
+  PC_CUDA(ctx, pc_cuda_copy(b->btypes_dev, btypes.data(), btypes.size() * sizeof(BatchType),
                                cudaMemcpyHostToDevice, ctx->stream));
-  PC_CUDA(ctx, cudaMemcpyAsync(b->inst_dev, idev.data(), idev.size() * sizeof(InstanceDev), cudaMemcpyHostToDevice,
+  PC_CUDA(ctx, pc_cuda_copy(b->inst_dev, idev.data(), idev.size() * sizeof(InstanceDev), cudaMemcpyHostToDevice,
                                ctx->stream));
-  PC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));  // the host tables are temporaries
+  PC_CUDA(ctx, pc_cuda_sync(ctx->stream));  // the host tables are temporaries
   return PC_OK;
   PC_GUARD_END(ctx)
 }
 
 int pc_batch_totals(pc_context* ctx, pc_batch* b, uint64_t* out, uint64_t capacity, uint64_t* offsets) {
   PC_GUARD_BEGIN
+  FaultScope fault_scope__(ctx);
   if (!ctx || !b) return PC_ERR_INVALID;
   const uint32_t n = (uint32_t)b->inst.size();
   std::vector<uint64_t> off(n + 1, 0);
@@ -1490,6 +1607,7 @@ void pc_batch_destroy(pc_batch* b) { pc_plan_destroy(b); }
 
 int pc_simulate_batch(pc_context* ctx, const pc_instance* instances, uint32_t n_instances, pc_histogram* out) {
   PC_GUARD_BEGIN
+  FaultScope fault_scope__(ctx);
   if (!ctx || !out) return fail(ctx, PC_ERR_INVALID, "null argument");
   for (uint32_t i = 0; i < n_instances; ++i) std::memset(out + i, 0, sizeof(pc_histogram));
   pc_batch* b = nullptr;
@@ -1517,13 +1635,14 @@ int pc_simulate_batch(pc_context* ctx, const pc_instance* instances, uint32_t n_
 
 int pc_autotune(pc_context* ctx, pc_plan* p, uint32_t repeats, pc_tuning* out) {
   PC_GUARD_BEGIN
+  FaultScope fault_scope__(ctx);
   if (!ctx || !p || !out) return PC_ERR_INVALID;
   std::memset(out, 0, sizeof(*out));
   repeats = std::max<uint32_t>(1, repeats);
   const bool narrow = p->gmax <= 32;
   const int saved[3] = {ctx->opt_config, ctx->opt_driver, ctx->opt_graph};
-  double best = 1e300, dflt = 0.0;
-  int best_cfg = kDefaultSweepConfig, best_drv = 0, n = 0;
+  double best = 1e300, dflt = 0.0, best_persist = 1e300;
+  int best_cfg = kDefaultSweepConfig, best_drv = 0, n = 0, persist_cfg = kDefaultSweepConfig;
   for (int drv = 0; drv < 2; ++drv)
     for (int cfg = 0; cfg < kNumSweepConfigs; ++cfg) {
       if (!narrow && cfg != kDefaultSweepConfig) continue;
@@ -1546,12 +1665,23 @@ int pc_autotune(pc_context* ctx, pc_plan* p, uint32_t repeats, pc_tuning* out) {
       }
       ++n;
       if (drv == 0 && cfg == kDefaultSweepConfig) dflt = t_best;
+      if (drv == 1 && t_best < best_persist) {
+        best_persist = t_best;
+        persist_cfg = cfg;
+      }
       if (t_best < best) {
         best = t_best;
         best_cfg = cfg;
         best_drv = drv;
       }
     }
+  // within 1% (the spread of single timings) the persistent driver wins: one graph-replayed
+  // launch per run and no host round trip per sweep
+  if (best_drv == 0 && best_persist <= 1.01 * best) {
+    best = best_persist;
+    best_cfg = persist_cfg;
+    best_drv = 1;
+  }
   ctx->opt_config = best_cfg;
   ctx->opt_driver = best_drv;
   ctx->opt_graph = best_drv;
@@ -1570,27 +1700,31 @@ int pc_autotune(pc_context* ctx, pc_plan* p, uint32_t repeats, pc_tuning* out) {
 
 int pc_batch_autotune(pc_context* ctx, pc_batch* b, uint32_t repeats, pc_tuning* out) {
   PC_GUARD_BEGIN
+  FaultScope fault_scope__(ctx);
   return pc_autotune(ctx, b, repeats, out);
   PC_GUARD_END(ctx)
 }
 
 int pc_debug_barrier(pc_context* ctx, int starve, double timeout_ms, uint32_t* error_bits, uint32_t* passed) {
   PC_GUARD_BEGIN
+  FaultScope fault_scope__(ctx);
   if (!ctx || !error_bits || !passed || !(timeout_ms > 0.0) || timeout_ms > 10000.0)
     return fail(ctx, PC_ERR_INVALID, "timeout must be in (0, 10000] ms");
+  if (starve < 0 || starve > 2) return fail(ctx, PC_ERR_INVALID, "starve must be 0, 1 or 2");
   PC_CUDA(ctx, cudaSetDevice(ctx->device));
   cudaStream_t st = ctx->stream;
   uint32_t* d = nullptr;  // [0..1] barrier (arrivals, generation), [2] error bits, [3] blocks through
-  PC_CUDA(ctx, cudaMalloc(&d, 4 * sizeof(uint32_t)));
-  const uint32_t init[4] = {starve ? 0x40000000u : 0u, 0u, 0u, 0u};
+  PC_CUDA(ctx, pc_cuda_malloc(&d, 4 * sizeof(uint32_t)));
+  const uint32_t init[4] = {starve == 1 ? 0x40000000u : 0u, 0u, 0u, 0u};
   uint32_t host[4] = {0u, 0u, 0u, 0u};
-  const int blocks = std::max(1, std::min(ctx->sms, 8));
-  cudaError_t e = cudaMemcpyAsync(d, init, sizeof(init), cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess)
-    e = (cudaError_t)launch_barrier_probe(d, (unsigned long long)(timeout_ms * 1e6), d + 2, d + 3, blocks, st);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(host, d, sizeof(host), cudaMemcpyDeviceToHost, st);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-  cudaFree(d);
+  const int blocks = std::max(starve == 2 ? 3 : 1, std::min(ctx->sms, 8));
+  const unsigned long long t_ns = (unsigned long long)(timeout_ms * 1e6);
+  const unsigned long long long_ns = std::min<unsigned long long>(100ull * t_ns, 10000000000ull);  // at most 10 s
+  cudaError_t e = pc_cuda_copy(d, init, sizeof(init), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = (cudaError_t)launch_barrier_probe(d, t_ns, long_ns, d + 2, d + 3, starve, blocks, st);
+  if (e == cudaSuccess) e = pc_cuda_copy(host, d, sizeof(host), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = pc_cuda_sync(st);
+  pc_cuda_free(d);
   if (e != cudaSuccess) return fail(ctx, PC_ERR_CUDA, std::string("barrier probe: ") + cudaGetErrorString(e));
   *error_bits = host[2];
   *passed = host[3];
@@ -1600,12 +1734,13 @@ int pc_debug_barrier(pc_context* ctx, int starve, double timeout_ms, uint32_t* e
 
 int pc_debug_peak(pc_context* ctx, int kind, double* lane_ops_per_s) {
   PC_GUARD_BEGIN
+  FaultScope fault_scope__(ctx);
   if (!ctx || !lane_ops_per_s || kind < 0 || kind > 2) return fail(ctx, PC_ERR_INVALID, "kind must be 0, 1 or 2");
   PC_CUDA(ctx, cudaSetDevice(ctx->device));
   cudaStream_t st = ctx->stream;
   const int blocks = 4 * std::max(1, ctx->sms);
   double* sink = nullptr;
-  PC_CUDA(ctx, cudaMalloc(&sink, 256 * sizeof(double)));
+  PC_CUDA(ctx, pc_cuda_malloc(&sink, 256 * sizeof(double)));
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   cudaError_t e = cudaEventCreate(&e0);
   if (e == cudaSuccess) e = cudaEventCreate(&e1);
@@ -1614,9 +1749,9 @@ int pc_debug_peak(pc_context* ctx, int kind, double* lane_ops_per_s) {
   float ms = 0.0f;
   for (int round = 0; e == cudaSuccess && round < 4; ++round) {
     e = (cudaError_t)launch_peak_probe(kind, iters, blocks, sink, st);  // warm-up at this size
-    if (e == cudaSuccess) e = cudaEventRecord(e0, st);
+    if (e == cudaSuccess) e = pc_cuda_event_record(e0, st);
     if (e == cudaSuccess) e = (cudaError_t)launch_peak_probe(kind, iters, blocks, sink, st);
-    if (e == cudaSuccess) e = cudaEventRecord(e1, st);
+    if (e == cudaSuccess) e = pc_cuda_event_record(e1, st);
     if (e == cudaSuccess) e = cudaEventSynchronize(e1);
     if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
     if (e != cudaSuccess || ms >= 20.0f) break;
@@ -1625,7 +1760,7 @@ int pc_debug_peak(pc_context* ctx, int kind, double* lane_ops_per_s) {
   }
   if (e0) cudaEventDestroy(e0);
   if (e1) cudaEventDestroy(e1);
-  cudaFree(sink);
+  pc_cuda_free(sink);
   if (e != cudaSuccess) return fail(ctx, PC_ERR_CUDA, std::string("peak probe: ") + cudaGetErrorString(e));
   *lane_ops_per_s = (double)blocks * 256.0 * 8.0 * iters / (ms * 1e-3);
   return PC_OK;
@@ -1634,17 +1769,18 @@ int pc_debug_peak(pc_context* ctx, int kind, double* lane_ops_per_s) {
 
 int pc_debug_philox(pc_context* ctx, const uint32_t* ctr, uint64_t n, const uint32_t key[2], uint32_t* out) {
   PC_GUARD_BEGIN
+  FaultScope fault_scope__(ctx);
   if (!ctx || (n && (!ctr || !out)) || !key) return PC_ERR_INVALID;
   if (n == 0) return PC_OK;
   uint32_t *dc = nullptr, *dout = nullptr;
-  PC_CUDA(ctx, cudaMalloc(&dc, n * 16));
-  cudaError_t e = cudaMalloc(&dout, n * 16);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(dc, ctr, n * 16, cudaMemcpyHostToDevice, ctx->stream);
+  PC_CUDA(ctx, pc_cuda_malloc(&dc, n * 16));
+  cudaError_t e = pc_cuda_malloc(&dout, n * 16);
+  if (e == cudaSuccess) e = pc_cuda_copy(dc, ctr, n * 16, cudaMemcpyHostToDevice, ctx->stream);
   if (e == cudaSuccess) e = (cudaError_t)launch_debug_philox(dc, n, key[0], key[1], dout, ctx->stream);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(out, dout, n * 16, cudaMemcpyDeviceToHost, ctx->stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
-  cudaFree(dc);
-  cudaFree(dout);
+  if (e == cudaSuccess) e = pc_cuda_copy(out, dout, n * 16, cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = pc_cuda_sync(ctx->stream);
+  pc_cuda_free(dc);
+  pc_cuda_free(dout);
   if (e != cudaSuccess) return fail(ctx, PC_ERR_CUDA, std::string("debug philox: ") + cudaGetErrorString(e));
   return PC_OK;
   PC_GUARD_END(ctx)
@@ -1652,15 +1788,16 @@ int pc_debug_philox(pc_context* ctx, const uint32_t* ctr, uint64_t n, const uint
 
 int pc_debug_normals(pc_context* ctx, uint64_t seed, uint32_t root, uint64_t first_parent, uint64_t count, float* z) {
   PC_GUARD_BEGIN
+  FaultScope fault_scope__(ctx);
   if (!ctx || (count && !z)) return PC_ERR_INVALID;
   if (count == 0) return PC_OK;
   float* dz = nullptr;
-  PC_CUDA(ctx, cudaMalloc(&dz, count * sizeof(float)));
+  PC_CUDA(ctx, pc_cuda_malloc(&dz, count * sizeof(float)));
   cudaError_t e = (cudaError_t)launch_debug_normals(ctx->zig_dev, (uint32_t)seed, (uint32_t)(seed >> 32), root,
                                                     first_parent, count, dz, ctx->stream);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(z, dz, count * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
-  cudaFree(dz);
+  if (e == cudaSuccess) e = pc_cuda_copy(z, dz, count * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = pc_cuda_sync(ctx->stream);
+  pc_cuda_free(dz);
   if (e != cudaSuccess) return fail(ctx, PC_ERR_CUDA, std::string("debug normals: ") + cudaGetErrorString(e));
   return PC_OK;
   PC_GUARD_END(ctx)
@@ -1668,9 +1805,10 @@ int pc_debug_normals(pc_context* ctx, uint64_t seed, uint32_t root, uint64_t fir
 
 int pc_debug_tables(pc_context* ctx, uint32_t* k, uint32_t* w_bits, uint32_t* f_bits) {
   PC_GUARD_BEGIN
+  FaultScope fault_scope__(ctx);
   if (!ctx) return PC_ERR_INVALID;
   ZigTables t;
-  PC_CUDA(ctx, cudaMemcpy(&t, ctx->zig_dev, sizeof(t), cudaMemcpyDeviceToHost));
+  PC_CUDA(ctx, pc_cuda_copy_sync(&t, ctx->zig_dev, sizeof(t), cudaMemcpyDeviceToHost));
   if (k) std::memcpy(k, t.k, sizeof(t.k));
   if (w_bits) std::memcpy(w_bits, t.w, sizeof(t.w));
   if (f_bits) std::memcpy(f_bits, t.f, sizeof(t.f));
@@ -1723,10 +1861,10 @@ SmoothArgs smooth_args(const pc_context* ctx, const pc_smooth* s) {
 
 int order_scratch(pc_context* ctx, pc_smooth* s, uint32_t ncand) {
   if (ncand <= s->order_cap) return PC_OK;
-  cudaFree(s->order_dev);
+  pc_cuda_free(s->order_dev);
   s->order_dev = nullptr;
   s->order_cap = 0;
-  PC_CUDA(ctx, cudaMalloc(&s->order_dev, (size_t)ncand * s->ntypes * sizeof(uint32_t)));
+  PC_CUDA(ctx, pc_cuda_malloc(&s->order_dev, (size_t)ncand * s->ntypes * sizeof(uint32_t)));
   s->order_cap = ncand;
   return PC_OK;
 }
@@ -1735,14 +1873,14 @@ int smooth_scratch(pc_context* ctx, pc_smooth* s, uint32_t ncand) {
   const int rc = order_scratch(ctx, s, ncand);
   if (rc != PC_OK) return rc;
   if (ncand <= s->cand_cap) return PC_OK;
-  cudaFree(s->e_raw_dev);
-  cudaFree(s->part_dev);
+  pc_cuda_free(s->e_raw_dev);
+  pc_cuda_free(s->part_dev);
   s->e_raw_dev = nullptr;
   s->part_dev = nullptr;
   s->cand_cap = 0;
   const size_t nb = std::max<size_t>(1, s->I.bin_value.size());
-  PC_CUDA(ctx, cudaMalloc(&s->e_raw_dev, (size_t)ncand * s->ntypes * nb * s->rows * sizeof(double)));
-  PC_CUDA(ctx, cudaMalloc(&s->part_dev, (size_t)ncand * nb * s->ntypes * 3 * sizeof(double)));
+  PC_CUDA(ctx, pc_cuda_malloc(&s->e_raw_dev, (size_t)ncand * s->ntypes * nb * s->rows * sizeof(double)));
+  PC_CUDA(ctx, pc_cuda_malloc(&s->part_dev, (size_t)ncand * nb * s->ntypes * 3 * sizeof(double)));
   s->cand_cap = ncand;
   return PC_OK;
 }
@@ -1751,11 +1889,11 @@ int jacobian_scratch(pc_context* ctx, pc_smooth* s, uint32_t ncand) {
   const int rc = order_scratch(ctx, s, ncand);
   if (rc != PC_OK) return rc;
   if (ncand <= s->jac_cap) return PC_OK;
-  cudaFree(s->jac_raw_dev);
+  pc_cuda_free(s->jac_raw_dev);
   s->jac_raw_dev = nullptr;
   s->jac_cap = 0;
   const size_t nb = std::max<size_t>(1, s->I.bin_value.size());
-  PC_CUDA(ctx, cudaMalloc(&s->jac_raw_dev, (size_t)ncand * nb * s->rows * s->ntypes * 3 * sizeof(double)));
+  PC_CUDA(ctx, pc_cuda_malloc(&s->jac_raw_dev, (size_t)ncand * nb * s->rows * s->ntypes * 3 * sizeof(double)));
   s->jac_cap = ncand;
   return PC_OK;
 }
@@ -1767,6 +1905,7 @@ extern "C" {
 int pc_smooth_create(pc_context* ctx, const pc_bin* bins, uint64_t n_bins, uint32_t n_types, double t_max,
                      double phi, double h, uint32_t paths_per_cell, uint64_t seed, pc_smooth** out) {
   PC_GUARD_BEGIN
+  FaultScope fault_scope__(ctx);
   if (!ctx || !out) return fail(ctx, PC_ERR_INVALID, "null argument");
   *out = nullptr;
   if (n_types == 0 || n_types > (uint32_t)kSmoothMaxTypes)
@@ -1815,22 +1954,22 @@ int pc_smooth_create(pc_context* ctx, const pc_bin* bins, uint64_t n_bins, uint3
     }
   cudaStream_t st = ctx->stream;
   cudaError_t e = cudaSetDevice(ctx->device);
-  if (e == cudaSuccess) e = cudaMalloc(&s->bin_start_dev, (nb + 1) * sizeof(uint64_t));
-  if (e == cudaSuccess) e = cudaMalloc(&s->bin_cap_dev, std::max<size_t>(1, nb) * sizeof(uint32_t));
-  if (e == cudaSuccess) e = cudaMalloc(&s->vidx_dev, std::max<size_t>(1, vidx.size()) * sizeof(int32_t));
-  if (e == cudaSuccess) e = cudaMalloc(&s->inv_off_dev, cnt.size() * sizeof(uint32_t));
-  if (e == cudaSuccess) e = cudaMalloc(&s->inv_idx_dev, std::max<size_t>(1, inv.size()) * sizeof(uint32_t));
+  if (e == cudaSuccess) e = pc_cuda_malloc(&s->bin_start_dev, (nb + 1) * sizeof(uint64_t));
+  if (e == cudaSuccess) e = pc_cuda_malloc(&s->bin_cap_dev, std::max<size_t>(1, nb) * sizeof(uint32_t));
+  if (e == cudaSuccess) e = pc_cuda_malloc(&s->vidx_dev, std::max<size_t>(1, vidx.size()) * sizeof(int32_t));
+  if (e == cudaSuccess) e = pc_cuda_malloc(&s->inv_off_dev, cnt.size() * sizeof(uint32_t));
+  if (e == cudaSuccess) e = pc_cuda_malloc(&s->inv_idx_dev, std::max<size_t>(1, inv.size()) * sizeof(uint32_t));
   if (e == cudaSuccess)
-    e = cudaMemcpyAsync(s->bin_start_dev, start.data(), (nb + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, st);
+    e = pc_cuda_copy(s->bin_start_dev, start.data(), (nb + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess && nb)
-    e = cudaMemcpyAsync(s->bin_cap_dev, I.cap.data(), nb * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
+    e = pc_cuda_copy(s->bin_cap_dev, I.cap.data(), nb * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess && !vidx.empty())
-    e = cudaMemcpyAsync(s->vidx_dev, vidx.data(), vidx.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st);
+    e = pc_cuda_copy(s->vidx_dev, vidx.data(), vidx.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess)
-    e = cudaMemcpyAsync(s->inv_off_dev, cnt.data(), cnt.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
+    e = pc_cuda_copy(s->inv_off_dev, cnt.data(), cnt.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess && !inv.empty())
-    e = cudaMemcpyAsync(s->inv_idx_dev, inv.data(), inv.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    e = pc_cuda_copy(s->inv_idx_dev, inv.data(), inv.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = pc_cuda_sync(st);
   if (e != cudaSuccess) {
     pc_smooth_destroy(s);
     return fail(ctx, e == cudaErrorMemoryAllocation ? PC_ERR_NOMEM : PC_ERR_CUDA,
@@ -1862,6 +2001,7 @@ int pc_smooth_values(const pc_smooth* s, double* values) {
 int pc_smooth_forward(pc_context* ctx, pc_smooth* s, const double* params, uint32_t n_candidates,
                       double* expected) {
   PC_GUARD_BEGIN
+  FaultScope fault_scope__(ctx);
   if (!ctx || !s || (n_candidates && (!params || !expected))) return fail(ctx, PC_ERR_INVALID, "null argument");
   if (n_candidates == 0) return PC_OK;
   PC_CUDA(ctx, cudaSetDevice(ctx->device));
@@ -1869,9 +2009,9 @@ int pc_smooth_forward(pc_context* ctx, pc_smooth* s, const double* params, uint3
   if (rc != PC_OK) return rc;
   const SmoothArgs A = smooth_args(ctx, s);
   const uint32_t nv = (uint32_t)s->I.values.size();
-  PC_CUDA(ctx, (cudaError_t)launch_smooth_forward(A, params, n_candidates, s->e_raw_dev, ctx->stream));
-  PC_CUDA(ctx, (cudaError_t)launch_smooth_merge(s->e_raw_dev, n_candidates, A.ntypes, A.nbins * A.rows,
-                                                s->inv_off_dev, s->inv_idx_dev, nv, expected, ctx->stream));
+  PC_CUDA(ctx, PC_LAUNCH(launch_smooth_forward(A, params, n_candidates, s->e_raw_dev, ctx->stream)));
+  PC_CUDA(ctx, PC_LAUNCH(launch_smooth_merge(s->e_raw_dev, n_candidates, A.ntypes, A.nbins * A.rows,
+                                                s->inv_off_dev, s->inv_idx_dev, nv, expected, ctx->stream)));
   return PC_OK;
   PC_GUARD_END(ctx)
 }
@@ -1879,6 +2019,7 @@ int pc_smooth_forward(pc_context* ctx, pc_smooth* s, const double* params, uint3
 int pc_smooth_backward(pc_context* ctx, pc_smooth* s, const double* params, uint32_t n_candidates,
                        const double* grad_expected, double* grad_params) {
   PC_GUARD_BEGIN
+  FaultScope fault_scope__(ctx);
   if (!ctx || !s || (n_candidates && (!params || !grad_expected || !grad_params)))
     return fail(ctx, PC_ERR_INVALID, "null argument");
   if (n_candidates == 0) return PC_OK;
@@ -1886,9 +2027,9 @@ int pc_smooth_backward(pc_context* ctx, pc_smooth* s, const double* params, uint
   int rc = smooth_scratch(ctx, s, n_candidates);
   if (rc != PC_OK) return rc;
   const SmoothArgs A = smooth_args(ctx, s);
-  PC_CUDA(ctx, (cudaError_t)launch_smooth_backward(A, params, n_candidates, grad_expected,
+  PC_CUDA(ctx, PC_LAUNCH(launch_smooth_backward(A, params, n_candidates, grad_expected,
                                                    (uint32_t)s->I.values.size(), s->vidx_dev, s->part_dev,
-                                                   grad_params, ctx->stream));
+                                                   grad_params, ctx->stream)));
   return PC_OK;
   PC_GUARD_END(ctx)
 }
@@ -1896,6 +2037,7 @@ int pc_smooth_backward(pc_context* ctx, pc_smooth* s, const double* params, uint
 int pc_smooth_jacobian(pc_context* ctx, pc_smooth* s, const double* params, uint32_t n_candidates,
                        double* expected, double* jacobian) {
   PC_GUARD_BEGIN
+  FaultScope fault_scope__(ctx);
   if (!ctx || !s || (n_candidates && (!params || !expected || !jacobian)))
     return fail(ctx, PC_ERR_INVALID, "null argument");
   if (n_candidates == 0) return PC_OK;
@@ -1903,9 +2045,9 @@ int pc_smooth_jacobian(pc_context* ctx, pc_smooth* s, const double* params, uint
   int rc = jacobian_scratch(ctx, s, n_candidates);
   if (rc != PC_OK) return rc;
   const SmoothArgs A = smooth_args(ctx, s);
-  PC_CUDA(ctx, (cudaError_t)launch_smooth_jacobian(A, params, n_candidates, s->inv_off_dev, s->inv_idx_dev,
+  PC_CUDA(ctx, PC_LAUNCH(launch_smooth_jacobian(A, params, n_candidates, s->inv_off_dev, s->inv_idx_dev,
                                                    (uint32_t)s->I.values.size(), s->jac_raw_dev, expected,
-                                                   jacobian, ctx->stream));
+                                                   jacobian, ctx->stream)));
   return PC_OK;
   PC_GUARD_END(ctx)
 }
@@ -1913,6 +2055,7 @@ int pc_smooth_jacobian(pc_context* ctx, pc_smooth* s, const double* params, uint
 int pc_smooth_gauss_newton(pc_context* ctx, pc_smooth* s, const double* params, uint32_t n_candidates,
                            const double* target, double* loss, double* jtj, double* jtr) {
   PC_GUARD_BEGIN
+  FaultScope fault_scope__(ctx);
   if (!ctx || !s || (n_candidates && (!params || !target || !loss || !jtj || !jtr)))
     return fail(ctx, PC_ERR_INVALID, "null argument");
   if (n_candidates == 0) return PC_OK;
@@ -1920,19 +2063,20 @@ int pc_smooth_gauss_newton(pc_context* ctx, pc_smooth* s, const double* params, 
   int rc = jacobian_scratch(ctx, s, n_candidates);
   if (rc != PC_OK) return rc;
   const SmoothArgs A = smooth_args(ctx, s);
-  PC_CUDA(ctx, (cudaError_t)launch_smooth_gauss_newton(A, params, n_candidates, s->inv_off_dev, s->inv_idx_dev,
+  PC_CUDA(ctx, PC_LAUNCH(launch_smooth_gauss_newton(A, params, n_candidates, s->inv_off_dev, s->inv_idx_dev,
                                                        (uint32_t)s->I.values.size(), target, s->jac_raw_dev, loss,
-                                                       jtj, jtr, ctx->stream));
+                                                       jtj, jtr, ctx->stream)));
   return PC_OK;
   PC_GUARD_END(ctx)
 }
 
 int pc_smooth_sync(pc_context* ctx) {
   PC_GUARD_BEGIN
+  FaultScope fault_scope__(ctx);
   if (!ctx) return PC_ERR_INVALID;
-  PC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  PC_CUDA(ctx, pc_cuda_sync(ctx->stream));
   uint32_t err = 0;
-  PC_CUDA(ctx, cudaMemcpy(&err, ctx->error_dev, sizeof(err), cudaMemcpyDeviceToHost));
+  PC_CUDA(ctx, pc_cuda_copy_sync(&err, ctx->error_dev, sizeof(err), cudaMemcpyDeviceToHost));
   if (err & 2u) return fail(ctx, PC_ERR_CUDA, "internal: the normal sampler exceeded its rejection budget");
   return PC_OK;
   PC_GUARD_END(ctx)
@@ -1940,15 +2084,15 @@ int pc_smooth_sync(pc_context* ctx) {
 
 void pc_smooth_destroy(pc_smooth* s) {
   if (!s) return;
-  cudaFree(s->bin_start_dev);
-  cudaFree(s->bin_cap_dev);
-  cudaFree(s->vidx_dev);
-  cudaFree(s->inv_off_dev);
-  cudaFree(s->inv_idx_dev);
-  cudaFree(s->e_raw_dev);
-  cudaFree(s->part_dev);
-  cudaFree(s->jac_raw_dev);
-  cudaFree(s->order_dev);
+  pc_cuda_free(s->bin_start_dev);
+  pc_cuda_free(s->bin_cap_dev);
+  pc_cuda_free(s->vidx_dev);
+  pc_cuda_free(s->inv_off_dev);
+  pc_cuda_free(s->inv_idx_dev);
+  pc_cuda_free(s->e_raw_dev);
+  pc_cuda_free(s->part_dev);
+  pc_cuda_free(s->jac_raw_dev);
+  pc_cuda_free(s->order_dev);
   delete s;
 }
 

@@ -86,10 +86,13 @@ struct RunArgs {
   const ZigTables* zig;
   const uint32_t* bin_info;  // [nbins]
   const uint64_t* bin_start; // [nbins + 1] global root offsets
-  unsigned long long* root_rec;  // [chunk]
+  unsigned long long* root_rec;  // [rec_cap]
+  uint64_t rec_cap;              // root records the buffer holds (checked build)
   unsigned long long* hist;  // [hist_gens][nbins][ntypes]
   unsigned long long* stats; // [0] vanished, [1] uncounted, [2] max generation
-  uint32_t* error;           // bit 0: depth overflow, bit 1: sampler round budget exhausted
+  uint32_t* error;           // bit 0: depth overflow, bit 1: sampler round budget exhausted,
+                             // bit 2: grid barrier timeout, bit 3: persistent schedule out of
+                             // buffers, bit 4: a bounds check of the checked build failed
   uint32_t nclass;           // histogram classes per generation
   // batched form only (null otherwise)
   const BatchType* btypes;   // [all types]
@@ -167,9 +170,10 @@ int occupancy_blocks_per_sm(int* root_blocks, int* divide_blocks);
 // Throughput probe (roofline denominators): kind 0 FP64 FMA, 1 FP32 FMA, 2 INT32 multiply-add;
 // each of the blocks x 256 threads runs iters x 8 operations.
 int launch_peak_probe(int kind, uint32_t iters, int blocks, double* sink, void* stream);
-// One grid barrier in a cooperative launch of `blocks` blocks (failure-detection test).
-int launch_barrier_probe(uint32_t* bar, unsigned long long timeout_ns, uint32_t* error, uint32_t* passed, int blocks,
-                         void* stream);
+// Grid barriers in a cooperative launch of `blocks` blocks (failure-detection tests; mode as
+// k_barrier_probe in pc_kernels.cu).
+int launch_barrier_probe(uint32_t* bar, unsigned long long timeout_ns, unsigned long long long_ns, uint32_t* error,
+                         uint32_t* passed, int mode, int blocks, void* stream);
 
 // Smoothed (differentiable) form (pc_smooth.cu). For every candidate parameter set c
 // (per type k: ratio, mean, sd) and every bin b, the expected leaf count at generation g

@@ -36,12 +36,21 @@ __global__ void k_debug_normals(const ZigTables* zig, uint32_t k0, uint32_t k1, 
   z[i] = zig_normal(c ? P.y : P.x, (P.z >> (8u * c)) & 255u, true, pair_wedge_bits(P, c), cs, Z, budget);
 }
 
-// One grid barrier of the persistent driver, for the failure-detection test: with
-// `starve` set, the arrival counter starts far above the grid size, so no block is ever
-// the last to arrive (a flag that nothing sets) and every block's wait runs into the
-// timeout, sets error bit 2 and returns.
-__global__ void k_barrier_probe(uint32_t* bar, unsigned long long timeout_ns, uint32_t* error, uint32_t* passed) {
-  if (grid_barrier(bar, timeout_ns, error) && threadIdx.x == 0) atomicAdd(passed, 1u);
+// Grid barriers of the persistent driver, for the failure-detection tests. mode 0: one
+// barrier. mode 1: the host presets the arrival counter far above the grid size, so no
+// block is ever the last to arrive (a flag that nothing sets) and every block's wait runs
+// into the timeout, sets error bit 2 and returns. mode 2: two barriers; block 1 skips the
+// second, which can then never complete; block 0 waits there with timeout_ns and every
+// other block with long_ns, so they can only leave early by seeing block 0's error bit.
+__global__ void k_barrier_probe(uint32_t* bar, unsigned long long timeout_ns, unsigned long long long_ns,
+                                uint32_t* error, uint32_t* passed, int mode) {
+  if (mode != 2) {
+    if (grid_barrier(bar, timeout_ns, error) && threadIdx.x == 0) atomicAdd(passed, 1u);
+    return;
+  }
+  if (!grid_barrier(bar, timeout_ns, error)) return;
+  if (blockIdx.x == 1) return;
+  if (grid_barrier(bar, blockIdx.x == 0 ? timeout_ns : long_ns, error) && threadIdx.x == 0) atomicAdd(passed, 1u);
 }
 
 // Throughput probes for the roofline denominators (FP64 and FP32 fused multiply-add, INT32
@@ -99,8 +108,8 @@ int launch_peak_probe(int kind, uint32_t iters, int blocks, double* sink, void* 
   return (int)cudaGetLastError();
 }
 
-int launch_barrier_probe(uint32_t* bar, unsigned long long timeout_ns, uint32_t* error, uint32_t* passed, int blocks,
-                         void* stream) {
+int launch_barrier_probe(uint32_t* bar, unsigned long long timeout_ns, unsigned long long long_ns, uint32_t* error,
+                         uint32_t* passed, int mode, int blocks, void* stream) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)blocks);
   cfg.blockDim = dim3(128u);
@@ -110,7 +119,7 @@ int launch_barrier_probe(uint32_t* bar, unsigned long long timeout_ns, uint32_t*
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  return (int)cudaLaunchKernelEx(&cfg, k_barrier_probe, bar, timeout_ns, error, passed);
+  return (int)cudaLaunchKernelEx(&cfg, k_barrier_probe, bar, timeout_ns, long_ns, error, passed, mode);
 }
 
 // Narrow-layout tables (pc_tuned_plain.cu, pc_tuned_batched.cu).

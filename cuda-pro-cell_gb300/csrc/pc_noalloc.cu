@@ -332,6 +332,7 @@ extern "C" int pc_simulate_noalloc(const pc_bin* bins, uint64_t n_bins, const pc
   a.bin_info = (const uint32_t*)(S + info_off);
   a.bin_start = (const uint64_t*)(S + start_off);
   a.root_rec = (unsigned long long*)(S + rec_off);
+  a.rec_cap = chunk;
   a.hist = (unsigned long long*)(S + hist_off);
   a.stats = stats_dev;
   a.error = error_dev;
@@ -439,6 +440,7 @@ extern "C" int pc_simulate_noalloc(const pc_bin* bins, uint64_t n_bins, const pc
     stats->h2d_bytes = 16ull * n_bins + sizeof(TypeDev) * n_types + sizeof(ZigTables);
     stats->d2h_bytes = 8ull * hist_elems + 40 + 8ull * (sweeps + (total + chunk - 1) / chunk);
   }
+  if (flags & 16u) return fail(err, err_len, PC_ERR_INTERNAL, "internal: a device bounds check failed (checked build)");
   if (flags & 2u) return fail(err, err_len, PC_ERR_CUDA, "internal: the normal sampler exceeded its rejection budget");
   if (flags & 1u)
     return fail(err, err_len, PC_ERR_DEPTH, "a lineage exceeded the deepest generation the key layout holds");

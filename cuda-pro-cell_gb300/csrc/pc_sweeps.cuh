@@ -73,6 +73,20 @@ __device__ __forceinline__ unsigned long long ld_rec(const unsigned long long* p
     return __ldg(p);
 }
 
+// Bounds checks of the checked build (compiled with PC_CHECKED, the stand-in for a memory
+// sanitizer): a failed check sets error bit 4 (value 16) and the caller skips the access or
+// uses a safe value; nothing traps. In the normal build every check is true at compile time.
+__device__ __forceinline__ bool in_bounds(bool ok, uint32_t* error) {
+#ifdef PC_CHECKED
+  if (!ok) atomicOr(error, 16u);
+  return ok;
+#else
+  (void)ok;
+  (void)error;
+  return true;
+#endif
+}
+
 struct Smem {
   ZigTables zig;
   TypeDev types[kMaxTypes];  // plain form only
@@ -354,9 +368,10 @@ __device__ void root_body(const RunArgs& a, const uint64_t root_base, const uint
       }
       const uint32_t info = __ldg(a.bin_info + bin);
       cls = Batched ? __ldg(a.bin_class + bin) + ty : bin * a.ntypes + ty;
-      a.root_rec[rl] = (unsigned long long)cls | ((unsigned long long)(type_begin + ty) << 32) |
-                       ((unsigned long long)(info & 0xFFu) << 48) |
-                       ((unsigned long long)((info >> 8) & 3u) << 56);
+      if (in_bounds(rl < a.rec_cap && bin < a.nbins, a.error))
+        a.root_rec[rl] = (unsigned long long)cls | ((unsigned long long)(type_begin + ty) << 32) |
+                         ((unsigned long long)(info & 0xFFu) << 48) |
+                         ((unsigned long long)((info >> 8) & 3u) << 56);
       const TypeDev& T = type_at(ty);
       bool leaf;
       if (T.mode == kModeQuiescent) {
@@ -381,12 +396,14 @@ __device__ void root_body(const RunArgs& a, const uint64_t root_base, const uint
         ++vanished;
       }
     }
+    if (!in_bounds(cls < a.nclass, a.error)) nleaf = 0u;
     count_leaves(a.hist, cls, nleaf, lane);
     const uint32_t em = __ballot_sync(kFull, f == kEmit);
     if (f == kEmit) {
       const uint32_t pos = __popc(em & ((1u << lane) - 1u));
       const unsigned long long key = Narrow ? ((unsigned long long)rl << 32) | 1ull : rl;
-      ob[out_n + pos] = make_ulonglong2((unsigned long long)__double_as_longlong(d0), key);
+      if (in_bounds(out_n + pos < out.stride, a.error))
+        ob[out_n + pos] = make_ulonglong2((unsigned long long)__double_as_longlong(d0), key);
     }
     out_n += __popc(em);
   }
@@ -463,7 +480,8 @@ __device__ __forceinline__ CellDraw classify(const ulonglong2 c, bool act, uint3
   const double d = __longlong_as_double((long long)c.x);
   uint64_t rl, node;
   decode<Narrow>(c.y, g, rl, node);
-  const unsigned long long rec = act ? ld_rec<Coherent>(a.root_rec + rl) : 0ull;  // consumed after Philox
+  const bool rec_ok = act && in_bounds(rl < a.rec_cap, a.error);
+  const unsigned long long rec = rec_ok ? ld_rec<Coherent>(a.root_rec + rl) : 0ull;  // consumed after Philox
   const uint32_t cap = rec_cap(rec);
   const bool can_divide = g1 < cap;
   const TypeCtx tc = type_ctx<Batched>(a, s.types, rec_type(rec));
@@ -570,6 +588,9 @@ __device__ void divide_body(const RunArgs& a, const uint64_t root_base, const Le
   const uint32_t lt = (1u << lane) - 1u;
   uint32_t front = 0, pending = 0, vanished = 0, depth_error = 0;
   unsigned long long* const hist_g1 = a.hist + (uint64_t)g1 * a.nclass;
+  // checked build: the segment holds 2n cells, and generation g + 1 has a histogram row
+  const bool seg_ok = in_bounds(2ull * n <= out.stride, a.error);
+  const bool row_ok = in_bounds(g1 < a.hist_gens, a.error);
 
   for (uint32_t i0 = 0; i0 < n; i0 += kStep) {
     CellDraw r[kCells];
@@ -583,6 +604,7 @@ __device__ void divide_body(const RunArgs& a, const uint64_t root_base, const Le
     }
 #pragma unroll
     for (int k = 0; k < kCells; ++k) {
+      if (!in_bounds(r[k].cls < a.nclass && row_ok, a.error)) r[k].nleaf = 0u;
       if constexpr (C::kGlobalHist)
         count_leaves(hist_g1, r[k].cls, r[k].nleaf, lane);
       else if (r[k].nleaf)
@@ -590,18 +612,24 @@ __device__ void divide_body(const RunArgs& a, const uint64_t root_base, const Le
       vanished += r[k].nvanish;
       if (r[k].overflow) depth_error = 1u;
       const uint32_t e0 = __ballot_sync(kFull, r[k].em0), e1 = __ballot_sync(kFull, r[k].em1);
-      ulonglong2* dst = ob + front + __popc(e0 & lt) + __popc(e1 & lt);
-      if (r[k].em0) dst[0] = make_ulonglong2((unsigned long long)__double_as_longlong(r[k].due0), r[k].kd);
-      if (r[k].em1)
+      const uint32_t at = front + __popc(e0 & lt) + __popc(e1 & lt);
+      ulonglong2* dst = ob + at;
+      const uint32_t mine = (r[k].em0 ? 1u : 0u) + (r[k].em1 ? 1u : 0u);
+      const bool dst_ok = in_bounds(seg_ok && at + mine <= 2u * n, a.error);
+      if (r[k].em0 && dst_ok) dst[0] = make_ulonglong2((unsigned long long)__double_as_longlong(r[k].due0), r[k].kd);
+      if (r[k].em1 && dst_ok)
         dst[r[k].em0 ? 1 : 0] = make_ulonglong2((unsigned long long)__double_as_longlong(r[k].due1), r[k].kd + 1ull);
       front += __popc(e0) + __popc(e1);
       // daughters the strip test did not settle: park (birth, key) at the back
       const uint32_t p0 = __ballot_sync(kFull, r[k].sl0), p1 = __ballot_sync(kFull, r[k].sl1);
       if (p0 | p1) {
-        ulonglong2* pd = back - 1u - pending - __popc(p0 & lt) - __popc(p1 & lt);
+        const uint32_t below = pending + __popc(p0 & lt) + __popc(p1 & lt);  // records after this lane's
+        ulonglong2* pd = back - 1u - below;
         const unsigned long long bb = (unsigned long long)__double_as_longlong(r[k].birth);
-        if (r[k].sl0) pd[0] = make_ulonglong2(bb, r[k].kd);
-        if (r[k].sl1) *(pd - (r[k].sl0 ? 1 : 0)) = make_ulonglong2(bb, r[k].kd + 1ull);
+        const uint32_t parked = (r[k].sl0 ? 1u : 0u) + (r[k].sl1 ? 1u : 0u);
+        const bool pd_ok = in_bounds(seg_ok && front + below + parked <= 2u * n, a.error);
+        if (r[k].sl0 && pd_ok) pd[0] = make_ulonglong2(bb, r[k].kd);
+        if (r[k].sl1 && pd_ok) *(pd - (r[k].sl0 ? 1 : 0)) = make_ulonglong2(bb, r[k].kd + 1ull);
         pending += __popc(p0) + __popc(p1);
       }
     }
@@ -619,13 +647,13 @@ __device__ void divide_body(const RunArgs& a, const uint64_t root_base, const Le
     int f = kNone;
     double due = 0.0;
     unsigned long long key = 0ull;
-    if (act) {
+    if (act && in_bounds(seg_ok && lo + lane < 2u * n, a.error)) {
       const ulonglong2 pc = back[-1 - (int64_t)(lo + lane)];
       key = pc.y;
       const double birth = __longlong_as_double((long long)pc.x);
       uint64_t rl, node;
       decode<Narrow>(key, g1, rl, node);
-      const unsigned long long rec = ld_rec<Coherent>(a.root_rec + rl);
+      const unsigned long long rec = in_bounds(rl < a.rec_cap, a.error) ? ld_rec<Coherent>(a.root_rec + rl) : 0ull;
       const uint32_t cap = rec_cap(rec);
       const TypeCtx tc = type_ctx<Batched>(a, s.types, rec_type(rec));
       const uint32_t root = (uint32_t)(root_base + rl - tc.root_begin);
@@ -635,6 +663,7 @@ __device__ void divide_body(const RunArgs& a, const uint64_t root_base, const Le
       const float z = slow_z(ch ? P.y : P.x, (P.z >> (8u * ch)) & 255u, pair_wedge_bits(P, ch), node, root,
                              tc.k0, tc.k1, tc.zlo, tc.zhi, s.zig_or(a), a.error);
       f = fate(birth, z, tc, g1 < cap, due);
+      if (f == kLeaf && !in_bounds((uint32_t)rec < a.nclass && row_ok, a.error)) f = kNone;
       if (f == kLeaf) {
         if constexpr (C::kGlobalHist)
           atomicAdd(hist_g1 + (uint32_t)rec, 1ull);
@@ -648,7 +677,8 @@ __device__ void divide_body(const RunArgs& a, const uint64_t root_base, const Le
     }
     __syncwarp();  // every parked record of this round is read before the front grows
     const uint32_t em = __ballot_sync(kFull, f == kEmit);
-    if (f == kEmit) ob[front + __popc(em & lt)] = make_ulonglong2((unsigned long long)__double_as_longlong(due), key);
+    if (f == kEmit && in_bounds(front + __popc(em & lt) < 2u * n, a.error))
+      ob[front + __popc(em & lt)] = make_ulonglong2((unsigned long long)__double_as_longlong(due), key);
     front += __popc(em);
     hi = lo;
   }
@@ -701,8 +731,10 @@ __device__ __forceinline__ unsigned long long global_ns() {
 
 // Grid-wide barrier of a cooperative launch (every block resident). Arrival is an atomic
 // on bar[0]; the last block to arrive resets it and advances the generation bar[1], which
-// the others wait for. A wait longer than timeout_ns (or 2^28 polls) sets error bit 2 and
-// makes every block leave the run at its next barrier. Returns false once that bit is set.
+// the others wait for. A wait longer than timeout_ns (or 2^28 polls) sets error bit 2;
+// every waiting block also polls that bit (every 256 polls, about 20 us), so all blocks leave
+// within one poll period of the first timeout, wherever they wait. Returns false once that
+// bit is set.
 __device__ bool grid_barrier(uint32_t* bar, unsigned long long timeout_ns, uint32_t* error) {
   __shared__ int s_ok;
   __syncthreads();
@@ -720,10 +752,16 @@ __device__ bool grid_barrier(uint32_t* bar, unsigned long long timeout_ns, uint3
       uint32_t polls = 0;
       while (*gen == g0) {
         __nanosleep(64);
-        if ((++polls & 255u) == 0u && (global_ns() - t0 > timeout_ns || polls >= (1u << 28))) {
-          atomicOr(error, 4u);
-          ok = 0;
-          break;
+        if ((++polls & 255u) == 0u) {
+          if (*(volatile uint32_t*)error & 4u) {  // another block gave up
+            ok = 0;
+            break;
+          }
+          if (global_ns() - t0 > timeout_ns || polls >= (1u << 28)) {
+            atomicOr(error, 4u);
+            ok = 0;
+            break;
+          }
         }
       }
     }

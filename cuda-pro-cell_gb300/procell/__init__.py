@@ -221,6 +221,11 @@ class Engine:
         finally:
             p.close()
 
+    def get_option(self, name: str) -> float:
+        v = ctypes.c_double()
+        self._check(self.L.pc_get_option(self.ctx, name.encode(), ctypes.byref(v)))
+        return v.value
+
     def peak(self, kind: str) -> float:
         """Measured lane-operations/s of one pipe: "fp64" / "fp32" FMA, "int32" multiply-add."""
         v = ctypes.c_double()

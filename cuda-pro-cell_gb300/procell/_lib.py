@@ -123,6 +123,7 @@ SIGNATURES = [
     ("pc_debug_barrier", ctypes.c_int, [VP, ctypes.c_int, ctypes.c_double, U32P, U32P]),
     ("pc_debug_philox", ctypes.c_int, [VP, U32P, ctypes.c_uint64, U32P, U32P]),
     ("pc_debug_peak", ctypes.c_int, [VP, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
+    ("pc_get_option", ctypes.c_int, [VP, ctypes.c_char_p, ctypes.POINTER(ctypes.c_double)]),
     ("pc_debug_normals", ctypes.c_int, [VP, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint64,
                                         ctypes.c_uint64, ctypes.POINTER(ctypes.c_float)]),
     ("pc_debug_tables", ctypes.c_int, [VP, U32P, U32P, U32P]),

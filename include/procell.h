@@ -119,8 +119,22 @@ int pc_set_stream(pc_context* ctx, void* stream);
  *                         cooperative launch per run
  *   "graph"               1: the persistent driver captures its run in a CUDA graph once
  *                         per plan and replays it
+ * Failure injection (no counterpart in the reference, which checks no CUDA status):
+ *   "fail_nth_call"       n >= 1: the n-th CUDA call the library makes for this context
+ *                         from now on (allocation, copy, memset, synchronisation, event
+ *                         record, kernel or graph launch) does not reach CUDA and fails
+ *                         once instead, as that call would (PC_ERR_NOMEM for allocations,
+ *                         PC_ERR_CUDA otherwise); 0 disarms. For tests of the error paths:
+ *                         every failure must come back as a status, leak nothing and leave
+ *                         the context usable.
  */
 int pc_set_option(pc_context* ctx, const char* name, double value);
+
+/* Counters for those tests (no counterpart in the reference): "cuda_calls" (CUDA calls the
+ * library made for this context so far), "faults_injected", "device_allocations" (device
+ * allocations of the library live in this process, all contexts), "level_buffers" (level
+ * buffers the context's pool holds). */
+int pc_get_option(pc_context* ctx, const char* name, double* value);
 
 /* phi == 0 selects the reference's automatic threshold: the smallest value with a
  * nonzero frequency (parser.cu:80-96). phi < 0 is invalid. seed keys the random stream;
@@ -218,7 +232,9 @@ int pc_simulate_batch(pc_context* ctx, const pc_instance* instances, uint32_t n_
  * launch per sweep or by one persistent cooperative launch replayed from a CUDA graph.
  * None of this changes a single count. The context options "sweep_config" (0-7),
  * "driver" (0 per sweep, 1 persistent) and "graph" (0/1) select them; pc_autotune times
- * every combination on a prepared input and leaves the context set to the fastest. */
+ * every combination on a prepared input and leaves the context set to the fastest, taking
+ * the persistent driver when its best time is within 1% of the overall best (one graph
+ * replay per run, no host round trip per sweep). */
 typedef struct pc_tuning {
   int32_t config;         /* chosen "sweep_config" */
   int32_t driver;         /* chosen "driver" (graph replay is on with the persistent one) */
@@ -332,11 +348,14 @@ int pc_simulate_noalloc(const pc_bin* bins, uint64_t n_bins, const pc_cell_type*
  * pc_debug_normals: z[i] = first-attempt normal of child (i & 1) of node first_parent+i/2
  *                   under `root` (no truncation), as the division sweep computes it.
  * pc_debug_tables: the device's ziggurat tables (k[256], w bits[256], f bits[257]). */
-/* One grid barrier of the persistent driver in a cooperative launch of up to 8 blocks,
- * with the wait limited to timeout_ms. starve = 1 presets the arrival counter so that the
- * barrier can never complete: every block's wait runs out, error bit 2 (value 4) is set
- * and the kernel returns, leaving the context usable (failure detection without a GPU
- * fault). *passed = blocks that got through. */
+/* Grid barriers of the persistent driver in a cooperative launch of up to 8 blocks, with
+ * the wait limited to timeout_ms (failure detection without a GPU fault; the context stays
+ * usable). starve = 0: one barrier. starve = 1: the arrival counter is preset so that the
+ * barrier can never complete: every block's wait runs out, error bit 2 (value 4) is set and
+ * the kernel returns. starve = 2: two barriers, one block skips the second; one block waits
+ * there with timeout_ms and the others with 100 x timeout_ms (at most 10 s), so the call
+ * returns after about timeout_ms only if waiting blocks see another block's timeout.
+ * *passed = blocks that got through every barrier. */
 int pc_debug_barrier(pc_context* ctx, int starve, double timeout_ms, uint32_t* error_bits,
                      uint32_t* passed);
 int pc_debug_philox(pc_context* ctx, const uint32_t* ctr, uint64_t n, const uint32_t key[2],

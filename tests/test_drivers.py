@@ -149,3 +149,23 @@ def test_barrier_timeout_is_reported_and_the_context_survives(eng, small_oracle)
     set_opts(eng, driver=1, graph=1)
     g = eng.simulate(w.bins, w.types, w.t_max, w.phi, w.seed)
     assert np.array_equal(g.per_type, o.per_type)
+
+
+def test_barrier_timeout_reaches_blocks_waiting_elsewhere(eng, small_oracle):
+    """Every block leaves within one poll period of the first timeout: in a second barrier
+    that can never complete (one block skips it), one block waits with a 100 ms limit and the
+    others with 10 s; the call returns long before 10 s only because the waiting blocks poll
+    the error bit that the first block's timeout sets. The context keeps working."""
+    import ctypes
+    import time
+    L = eng.L
+    err, passed = ctypes.c_uint32(), ctypes.c_uint32()
+    t0 = time.perf_counter()
+    assert L.pc_debug_barrier(eng.ctx, 2, 100.0, ctypes.byref(err), ctypes.byref(passed)) == 0
+    dt = time.perf_counter() - t0
+    assert err.value & 4 and passed.value == 0
+    assert dt < 2.0, dt
+    w, o = small_oracle
+    set_opts(eng, driver=1, graph=0)
+    g = eng.simulate(w.bins, w.types, w.t_max, w.phi, w.seed)
+    assert np.array_equal(g.per_type, o.per_type)
