@@ -243,6 +243,7 @@ def reference_batched_line(steps, warmup, per_step):
 
 
 def run_ours(args):
+    import numpy as np
     import torch
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
@@ -257,12 +258,29 @@ def run_ours(args):
     from procell import Engine
 
     w = workload(args.workload)
-    seed = w.seed + rank
+    roots_split = args.split == "roots"
+    seed = w.seed if roots_split else w.seed + rank
     eng = Engine(local)
     stream = torch.cuda.current_stream()
     eng.set_stream(stream.cuda_stream)
     plan = eng.plan(w.bins, w.types, w.t_max, w.phi, seed)
+    shard = None
+    if roots_split:
+        # one input split over the ranks: a contiguous range of initial cells per rank,
+        # balanced by expected work, and one sum of the counts per step
+        from procell.distributed import shard_range_weighted
+        shard = shard_range_weighted(w.bins, w.types, w.t_max, w.phi, rank, world)
+        plan.set_roots(*shard)
     tuning = eng.autotune(plan, repeats=1) if not args.no_tune else None
+
+    def reduce_counts():
+        # the sharded step's one exchange: an element-wise sum of the (generation, bin, type)
+        # counts over the ranks
+        if roots_split and world > 1:
+            t = torch.from_numpy(plan.raw_counts().view(np.int64)).to("cuda")
+            torch.distributed.all_reduce(t)
+            return t
+        return None
 
     def barrier():
         torch.cuda.synchronize()
@@ -281,6 +299,7 @@ def run_ours(args):
     e0.record(stream)
     for _ in range(args.steps):
         plan.run()
+        reduce_counts()
         st = plan.stats()
         divisions += st["divisions"]
         roots += st["roots"]
@@ -302,7 +321,14 @@ def run_ours(args):
     for _ in range(args.steps):
         torch.cuda.synchronize()
         t = time.perf_counter()
-        res = eng.simulate(bins_host, w.types, w.t_max, w.phi, seed)
+        if roots_split:
+            res = eng.simulate(bins_host, w.types, w.t_max, w.phi, seed, root_begin=shard[0], root_end=shard[1])
+            if world > 1:
+                tot = torch.from_numpy(res.per_type.view(np.int64)).to("cuda")
+                torch.distributed.all_reduce(tot)
+                tot.cpu()
+        else:
+            res = eng.simulate(bins_host, w.types, w.t_max, w.phi, seed)
         e2e_t += time.perf_counter() - t
         h2d += res.stats["h2d_bytes"]
         d2h += res.stats["d2h_bytes"]
@@ -377,7 +403,7 @@ def run_ours(args):
         "warmup": args.warmup,
         "ms_per_step": elapsed_ms / args.steps,
         "higher_is_better": True,
-        "scaling": "weak",
+        "scaling": "strong" if roots_split else "weak",
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic (seeded generator, procell/configs.py)",
@@ -385,7 +411,9 @@ def run_ours(args):
                    "nodes_per_step": (roots + 2 * divisions) // args.steps,
                    "l2": "no flush: each step streams %.0f GB of level buffers, >> 129 MB L2"
                          % (2 * 16 * divisions / args.steps / 1e9),
-                   "parallelism": f"one independent instance per GPU x{world}",
+                   "parallelism": (f"one input, initial cells split over {world} GPUs by expected work, "
+                                   f"one all_reduce of the counts per step" if roots_split
+                                   else f"one independent instance per GPU x{world}"),
                    "tuning": tuning},
         "e2e": {"value": tot_e2e_div / e2e_t, "unit": UNIT,
                 "h2d_bytes_per_step": h2d // args.steps, "d2h_bytes_per_step": d2h // args.steps},
@@ -875,6 +903,9 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="skip the autotuner (default configuration)")
+    ap.add_argument("--split", choices=["replicas", "roots"], default="replicas",
+                    help="N GPUs: independent replicas (weak scaling, default) or one input split by "
+                         "initial-cell ranges with one sum of the counts per step (strong scaling)")
     ap.add_argument("--no-forms", action="store_true",
                     help="plain workload only: skip the batched and calibration forms nested in its line")
     args = ap.parse_args()

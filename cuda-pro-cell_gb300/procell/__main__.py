@@ -4,7 +4,10 @@
 
 Workloads are those of procell.configs (small, medium, large). --budget limits the device
 memory of the level buffers (memory_budget_bytes), e.g. to keep a profiler capture small;
---driver and --config select the driver and the compiled sweep configuration.
+--driver and --config select the driver and the compiled sweep configuration; --t-max and
+--phi replace the workload's (a larger phi makes the trees shallower, so a given budget
+holds fewer, larger level buffers and each division sweep is longer); --root-end runs only
+the first initial cells (a prefix of the same workload, e.g. for a small profiler capture).
 """
 import argparse
 import json
@@ -22,14 +25,23 @@ def main():
     ap.add_argument("--seed", type=int, default=None)
     ap.add_argument("--driver", type=int, default=0, help="0: one launch per sweep, 1: persistent")
     ap.add_argument("--config", type=int, default=4, help="compiled sweep configuration 0-7")
+    ap.add_argument("--t-max", type=float, default=None)
+    ap.add_argument("--phi", type=float, default=None)
+    ap.add_argument("--root-end", type=int, default=None)
     a = ap.parse_args()
     w = configs.by_name(a.workload)
+    if a.t_max is not None:
+        w.t_max = a.t_max
+    if a.phi is not None:
+        w.phi = a.phi
     eng = Engine(0)
     if a.budget > 0:
         eng.set_option("memory_budget_bytes", a.budget)
     eng.set_option("driver", a.driver)
     eng.set_option("sweep_config", a.config)
     plan = eng.plan(w.bins, w.types, w.t_max, w.phi, w.seed if a.seed is None else a.seed)
+    if a.root_end is not None:
+        plan.set_roots(0, min(a.root_end, w.roots))
     for i in range(a.runs):
         t = time.perf_counter()
         plan.run()

@@ -163,7 +163,9 @@ class Problem:
 
 
 def gradient_descent(prob, theta0, iters=150, lr=0.1, lr_end=0.002, time_limit=None):
-    """Adam from every candidate at once, learning rate decaying from lr to lr_end (cosine)."""
+    """Adam from every candidate at once, learning rate decaying from lr to lr_end (cosine),
+    each step projected onto the search box that every search shares."""
+    lo, hi = prob.box()
     theta = theta0.clone().requires_grad_(True)
     opt = torch.optim.Adam([theta], lr=lr)
     trace, best = [], float("inf")
@@ -183,6 +185,8 @@ def gradient_descent(prob, theta0, iters=150, lr=0.1, lr_end=0.002, time_limit=N
             best = float(Ld[i])
             snaps.append((time.perf_counter() - t0, theta.detach()[i].clone()))
         opt.step()
+        with torch.no_grad():
+            theta.copy_(torch.minimum(torch.maximum(theta, lo), hi))
         trace.append((time.perf_counter() - t0, best))
         if time_limit and trace[-1][0] > time_limit:
             break
@@ -218,9 +222,12 @@ def gauss_newton_system(prob, th):
 def levenberg_marquardt(prob, theta0, iters=40, lam0=1e-2, max_step=1.0, time_limit=None, graph=True):
     """Levenberg-Marquardt from every candidate at once on the residuals r_v = log(1 + E_v) -
     log(1 + C_v) of the smoothed form. One Gauss-Newton pass per iteration (the Jacobian
-    kernel, reduced on the device to J^T J, J^T r and the loss) at the trial point; a
-    candidate keeps its step if its loss falls (damping / 3) and otherwise stays where it was
-    (damping x 4). Steps solve (J^T J + lam diag(J^T J)) d = -J^T r per candidate (9 x 9 for
+    kernel, reduced on the device to J^T J, J^T r and the loss) at the trial point, which is
+    kept in the search box every search shares; a candidate keeps its step if its loss falls
+    (damping / 3) and otherwise stays where it was (damping x 4). (Left free, the search
+    leaves the box towards sd/mean near 0.007: expected counts a near-deterministic type
+    fits as well, but whose cells divide in lockstep, so that single histograms of the
+    plain simulator scatter far more than the target's.) Steps solve (J^T J + lam diag(J^T J)) d = -J^T r per candidate (9 x 9 for
     three types). On a GPU one iteration (the pass and every small tensor operation around
     it) is captured once into a CUDA graph before the clock starts and replayed; without a
     GPU, or if capture fails, iterations run eagerly with the same arithmetic."""
@@ -238,7 +245,7 @@ def levenberg_marquardt(prob, theta0, iters=40, lam0=1e-2, max_step=1.0, time_li
         Ad = A + torch.diag_embed(lam[:, None] * d) + 1e-12 * d.amax(1)[:, None, None] * eye
         st = torch.linalg.solve_ex(Ad, -g[..., None])[0][..., 0]
         st = torch.nan_to_num(st, nan=0.0, posinf=0.0, neginf=0.0).clamp(-max_step, max_step)
-        th_new = torch.minimum(torch.maximum(th + st.reshape(n, K, 3), lo - 2.0), hi + 2.0)
+        th_new = torch.minimum(torch.maximum(th + st.reshape(n, K, 3), lo), hi)
         f2, A2, g2 = gauss_newton_system(prob, th_new)
         ok = f2 < f  # NaN losses are never accepted
         th.copy_(torch.where(ok[:, None, None], th_new, th))

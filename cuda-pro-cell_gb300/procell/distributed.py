@@ -6,10 +6,12 @@ histogram is bit-identical to a one-process run, whatever the number of ranks.
 
     torchrun --nproc-per-node N script.py      # each rank:
     res = simulate_sharded(engine_shard(Engine(local_rank), bins, types, t_max, phi, seed),
-                           total_cells(bins))
+                           total_cells(bins),
+                           split=lambda r, n: shard_range_weighted(bins, types, t_max, phi, r, n))
 """
 from __future__ import annotations
 
+import math
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -22,6 +24,63 @@ def shard_range(total: int, rank: int, world: int):
     lo = total * rank // world
     hi = total * (rank + 1) // world
     return lo, hi
+
+
+def phi_cap(value: float, phi: float, limit: int = 4096) -> int:
+    """Generations a cell of this bin may divide: halvings with value / 2 > phi
+    (the division test of src/simulation/proliferation.cu:323)."""
+    c, f = 0, float(value)
+    while f / 2 > phi and c < limit:
+        f /= 2
+        c += 1
+    return c
+
+
+def cell_work(bins, types, t_max, phi=None):
+    """Expected divisions per initial cell of each row of `bins` (rows with frequency 0
+    included, weight 0): sum over types of ratio * (2^min(cap, t_max // mean) - 1), the
+    full binary tree that the phi cap and the mean division time allow, plus one for the
+    root itself. An estimate for balancing shards only; results never depend on it."""
+    if phi is None:
+        phi = min(float(v) for v, f in bins if int(f) > 0)
+    gens = [(float(r), int(t_max // m) if m > 0 else 0) for r, m, _ in types]
+    out = []
+    for v, f in bins:
+        if int(f) == 0:
+            out.append(0.0)
+            continue
+        cap = phi_cap(v, phi)
+        out.append(1.0 + sum(r * (2.0 ** min(cap, g, 60) - 1.0) for r, g in gens))
+    return out
+
+
+def shard_range_weighted(bins, types, t_max, phi, rank: int, world: int):
+    """Contiguous range [lo, hi) of initial cells (numbered in file order, as pc_plan_set_roots
+    counts them) holding about 1/world of the expected work (cell_work) for `rank`. Cuts may
+    fall inside a bin; any split gives a bit-identical summed histogram."""
+    w = cell_work(bins, types, t_max, phi)
+    freqs = [int(f) for _, f in bins]
+    total_work = sum(wi * fi for wi, fi in zip(w, freqs))
+    total = sum(freqs)
+    if total_work <= 0.0:
+        return shard_range(total, rank, world)
+
+    def cut(k):  # first cell index at which the cumulative work reaches k/world of the total
+        if k <= 0:
+            return 0
+        if k >= world:
+            return total
+        target = total_work * k / world
+        acc, cell = 0.0, 0
+        for wi, fi in zip(w, freqs):
+            if fi == 0:
+                continue
+            if acc + wi * fi >= target:
+                return cell + min(fi, int(math.ceil((target - acc) / wi)) if wi > 0 else fi)
+            acc += wi * fi
+            cell += fi
+        return total
+    return cut(rank), cut(rank + 1)
 
 
 def total_cells(bins) -> int:
@@ -54,15 +113,16 @@ def engine_shard(engine, bins, types, t_max, phi, seed):
     return compute
 
 
-def simulate_sharded(compute, total: int, group=None) -> ShardResult:
+def simulate_sharded(compute, total: int, group=None, split=None) -> ShardResult:
     """Run this rank's shard with compute(lo, hi) -> ShardResult and sum all ranks' counts
     (torch.distributed all_reduce; gloo on CPU tensors, NCCL on CUDA tensors). Every rank
-    returns the full histogram."""
+    returns the full histogram. split(rank, world) -> (lo, hi) chooses the ranges (e.g. a
+    shard_range_weighted closure); by default equal numbers of initial cells."""
     import torch
     import torch.distributed as dist
     world = dist.get_world_size(group) if dist.is_initialized() else 1
     rank = dist.get_rank(group) if dist.is_initialized() else 0
-    lo, hi = shard_range(total, rank, world)
+    lo, hi = split(rank, world) if split else shard_range(total, rank, world)
     mine = compute(lo, hi)
     if world == 1:
         return mine

@@ -33,15 +33,16 @@ def _oracle_compute(bins, types, t_max, phi, seed):
     return compute
 
 
-def _rank_main(rank, world, port, case, out_dir):
+def _rank_main(rank, world, port, case, out_dir, weighted=False):
     sys.path[:0] = [os.path.join(ROOT, "cuda-pro-cell_gb300"), os.path.join(ROOT, "oracle")]
     import torch.distributed as dist
-    from procell.distributed import simulate_sharded, total_cells
+    from procell.distributed import shard_range_weighted, simulate_sharded, total_cells
     os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
     dist.init_process_group("gloo", rank=rank, world_size=world)
     try:
         bins, types, t_max, phi, seed = case
-        res = simulate_sharded(_oracle_compute(bins, types, t_max, phi, seed), total_cells(bins))
+        split = (lambda r, n: shard_range_weighted(bins, types, t_max, phi, r, n)) if weighted else None
+        res = simulate_sharded(_oracle_compute(bins, types, t_max, phi, seed), total_cells(bins), split=split)
         np.savez(os.path.join(out_dir, f"rank{rank}.npz"), values=res.values, per_type=res.per_type,
                  stats=np.array([res.stats[k] for k in ("roots", "divisions", "leaves", "uncounted", "vanished",
                                                         "max_generation")], np.int64))
@@ -53,11 +54,11 @@ CASE = ([(float(v), int(f)) for v, f in zip(np.geomspace(2.0, 5000.0, 24), [30, 
         [(0.5, 30.0, 9.0), (0.3, 45.0, 12.0), (0.2, -1.0, -1.0)], 120.0, None, 77)
 
 
-@pytest.mark.parametrize("world", [2, 3])
-def test_gloo_shards_sum_to_full_run(oracle_lib, tmp_path, world):
+@pytest.mark.parametrize("world,weighted", [(2, False), (3, False), (2, True), (3, True)])
+def test_gloo_shards_sum_to_full_run(oracle_lib, tmp_path, world, weighted):
     bins, types, t_max, phi, seed = CASE
     full = oracle_lib.simulate(bins, types, t_max, phi, seed=seed, nthreads=2)
-    mp.start_processes(_rank_main, args=(world, _free_port(), CASE, str(tmp_path)), nprocs=world,
+    mp.start_processes(_rank_main, args=(world, _free_port(), CASE, str(tmp_path), weighted), nprocs=world,
                        join=True, start_method="spawn")
     for r in range(world):
         d = np.load(tmp_path / f"rank{r}.npz")
@@ -76,6 +77,36 @@ def test_shard_ranges_cover_exactly():
             assert ranges[0][0] == 0 and ranges[-1][1] == total
             assert all(a[1] == b[0] for a, b in zip(ranges, ranges[1:]))
             assert max(h - l for l, h in ranges) - min(h - l for l, h in ranges) <= 1
+
+
+def test_weighted_shard_ranges_cover_exactly():
+    import procell.configs as cfg
+    from procell.distributed import shard_range_weighted, total_cells
+    for w in (cfg.small(), cfg.medium()):
+        for world in (1, 2, 3, 8):
+            r = [shard_range_weighted(w.bins, w.types, w.t_max, w.phi, k, world) for k in range(world)]
+            assert r[0][0] == 0 and r[-1][1] == total_cells(w.bins)
+            assert all(a[1] == b[0] and a[0] <= a[1] for a, b in zip(r, r[1:]))
+
+
+def test_weighted_split_balances_skewed_work(oracle_lib):
+    """Bins sorted by value put cells with shallow trees first and deep ones last; equal
+    numbers of initial cells then give very unequal shards, the work-weighted split does
+    not (divisions per shard counted by the oracle)."""
+    from procell.distributed import shard_range, shard_range_weighted, total_cells
+    bins = [(float(v), 300) for v in np.geomspace(2.0, 2.0 ** 12, 48)]
+    types = [(0.6, 20.0, 5.0), (0.4, 30.0, 6.0)]
+    t_max, phi, world = 160.0, 1.0, 4
+
+    def spread(ranges):
+        d = [oracle_lib.simulate(bins, types, t_max, phi, seed=3, root_begin=lo, root_end=hi,
+                                 nthreads=2).stats["divisions"] for lo, hi in ranges]
+        return max(d) / max(1, min(d))
+
+    n = total_cells(bins)
+    equal = spread([shard_range(n, k, world) for k in range(world)])
+    weighted = spread([shard_range_weighted(bins, types, t_max, phi, k, world) for k in range(world)])
+    assert weighted < 1.5 < equal, (weighted, equal)
 
 
 @pytest.mark.gpu
