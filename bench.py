@@ -807,6 +807,7 @@ def measure_calibration(eng, local, steps, warmup, cpu_seconds, pso_seconds, ext
                        "lm_best_neutral": c["model_neutral"]["lm_best"],
                        "pso_plain_best_neutral": c["model_neutral"]["pso_plain_best"],
                        "neutral_at_hidden": c["model_neutral"]["plain_loss_at_hidden"],
+                       "lm_plain_neutral": c["model_neutral"]["lm_plain"],
                        "levels_neutral": c["model_neutral"]["levels"]})
     cpu = None
     if cpu_seconds:
@@ -815,9 +816,18 @@ def measure_calibration(eng, local, steps, warmup, cpu_seconds, pso_seconds, ext
                                 cpu_seconds)
     value = C * steps / (elapsed_ms * 1e-3)
     hbm, peak_kind = peaks()
-    # algorithmic bytes of one forward + backward: parameters in, expected counts out and in
-    # again as gradients, parameter gradients out
-    alg = (C * prob.n_types * 3 * 8) * 2 + C * prob.smooth.n_values * 8 * 2
+    # the smoothed kernels are bound by instruction issue (no FP64 left in the lineage walks,
+    # a few MB of inputs and outputs): warp instructions of one forward + adjoint for these
+    # 256 candidates (ncu, profiles/) against four issue slots per SM per cycle
+    ipp = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "smooth_instructions_per_pass.txt")) as fh:
+            ipp = float(fh.read().split()[0])
+    except (OSError, ValueError, IndexError):
+        pass
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    issue_peak = 4.0 * sms * clk["sm_mhz"] * 1e6 if clk.get("sm_mhz") else None
+    issue_rate = ipp * steps / (elapsed_ms * 1e-3) if ipp else None
     line = {
         "metric": "fwd+bwd grads/s (smoothed form)",
         "value": value,
@@ -847,11 +857,14 @@ def measure_calibration(eng, local, steps, warmup, cpu_seconds, pso_seconds, ext
                                  "pass (pc_smooth_gauss_newton); the value above is forward + adjoint" % C},
         "e2e": {"value": C * steps / e2e_s, "unit": "grads/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
-        "roofline": {"bound": "hbm", "achieved": alg / (elapsed_ms * 1e-3 / steps) / 1e9, "peak": hbm,
-                     "unit": "GB/s", "frac": alg / (elapsed_ms * 1e-3 / steps) / 1e9 / hbm,
-                     "traffic": None, "peak_source": peak_kind, "kernel": "k_smooth",
-                     "note": "not memory bound: FP64-pipe bound (due times; 78-84% of the FP64 pipe, "
-                             "profiles/k_smooth_calibration.md); bytes are inputs and outputs only"},
+        "roofline": {"bound": "issue", "achieved": issue_rate, "peak": issue_peak,
+                     "unit": "warp instructions/s",
+                     "frac": (issue_rate / issue_peak) if (issue_rate and issue_peak) else None,
+                     "traffic": None, "peak_source": "4 issue slots x %d SMs x sampled SM clock" % sms,
+                     "kernel": "k_smooth",
+                     "note": "%s warp instructions per forward + adjoint of %d candidates (ncu, "
+                             "profiles/smooth_instructions_per_pass.txt); the lineage walks run on the FP32 "
+                             "pipe, inputs and outputs are a few MB" % (ipp, C)},
         "gpu_launches": 6 * steps,  # per step: order, forward, merge; order, adjoint, sum
         "clocks": clk,
     }

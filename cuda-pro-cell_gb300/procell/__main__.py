@@ -2,7 +2,8 @@
 
     PYTHONPATH=cuda-pro-cell_gb300 python -m procell medium --runs 2 --budget 2e9
 
-Workloads are those of procell.configs (small, medium, large). --budget limits the device
+Workloads are those of procell.configs (small, medium, large, and batched: the first
+--instances instances of the batched workload as one batch). --budget limits the device
 memory of the level buffers (memory_budget_bytes), e.g. to keep a profiler capture small;
 --driver and --config select the driver and the compiled sweep configuration; --t-max and
 --phi replace the workload's (a larger phi makes the trees shallower, so a given budget
@@ -19,7 +20,8 @@ from . import configs
 
 def main():
     ap = argparse.ArgumentParser(prog="python -m procell")
-    ap.add_argument("workload", choices=["small", "medium", "large"])
+    ap.add_argument("workload", choices=["small", "medium", "large", "batched"])
+    ap.add_argument("--instances", type=int, default=4096, help="batched: how many instances")
     ap.add_argument("--runs", type=int, default=1)
     ap.add_argument("--budget", type=float, default=0.0)
     ap.add_argument("--seed", type=int, default=None)
@@ -29,6 +31,8 @@ def main():
     ap.add_argument("--phi", type=float, default=None)
     ap.add_argument("--root-end", type=int, default=None)
     a = ap.parse_args()
+    if a.workload == "batched":
+        return run_batched(a)
     w = configs.by_name(a.workload)
     if a.t_max is not None:
         w.t_max = a.t_max
@@ -51,6 +55,26 @@ def main():
                           "divisions": s["divisions"], "sweeps": s["sweeps"],
                           "device_ms": round(s["device_ms"], 3)}), flush=True)
     plan.close()
+    eng.close()
+
+
+def run_batched(a):
+    ws = configs.batched()[:a.instances]
+    eng = Engine(0)
+    if a.budget > 0:
+        eng.set_option("memory_budget_bytes", a.budget)
+    eng.set_option("driver", a.driver)
+    eng.set_option("sweep_config", a.config)
+    b = eng.batch([(w.bins, w.types, w.t_max, w.phi, w.seed) for w in ws])
+    for i in range(a.runs):
+        t = time.perf_counter()
+        b.run()
+        dt = time.perf_counter() - t
+        s = b.stats()
+        print(json.dumps({"workload": "batched", "instances": len(ws), "run": i, "wall_ms": round(1e3 * dt, 3),
+                          "divisions": s["divisions"], "sweeps": s["sweeps"],
+                          "device_ms": round(s["device_ms"], 3)}), flush=True)
+    b.close()
     eng.close()
 
 

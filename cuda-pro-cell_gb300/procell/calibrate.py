@@ -293,6 +293,51 @@ def levenberg_marquardt(prob, theta0, iters=40, lam0=1e-2, max_step=1.0, time_li
     return trace, snaps
 
 
+def levenberg_marquardt_plain(prob, theta0, iters=40, lam0=1e-2, max_step=1.0, time_limit=None):
+    """Levenberg-Marquardt steps from the smoothed form's Gauss-Newton system, accepted where
+    the plain simulator's own loss (all candidates as one batch, one seed for all: common
+    random numbers) falls: a derivative-based search on the simulator's loss. Each iteration
+    is one Gauss-Newton pass and one batch run; it sees what the smoothed loss cannot, the
+    scatter of single stochastic histograms."""
+    lo, hi = prob.box()
+    n, K = theta0.shape[0], theta0.shape[1]
+    P = 3 * K
+    eye = torch.eye(P, dtype=torch.float64, device=theta0.device)
+    th = theta0.clone()
+    lam = torch.full((n,), lam0, dtype=torch.float64, device=th.device)
+    if th.is_cuda:
+        torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    f = prob.loss_plain(th)
+    _, A, g = gauss_newton_system(prob, th)
+    i = int(torch.argmin(f))
+    best = float(f[i])
+    trace = [(time.perf_counter() - t0, best)]
+    snaps = [(trace[0][0], th[i].clone())]
+    for _ in range(iters):
+        d = torch.diagonal(A, dim1=1, dim2=2)
+        Ad = A + torch.diag_embed(lam[:, None] * d) + 1e-12 * d.amax(1)[:, None, None] * eye
+        st = torch.linalg.solve_ex(Ad, -g[..., None])[0][..., 0]
+        st = torch.nan_to_num(st, nan=0.0, posinf=0.0, neginf=0.0).clamp(-max_step, max_step)
+        th_new = torch.minimum(torch.maximum(th + st.reshape(n, K, 3), lo), hi)
+        f2 = prob.loss_plain(th_new)
+        _, A2, g2 = gauss_newton_system(prob, th_new)
+        ok = f2 < f
+        th = torch.where(ok[:, None, None], th_new, th)
+        A = torch.where(ok[:, None, None], A2, A)
+        g = torch.where(ok[:, None], g2, g)
+        f = torch.where(ok, f2, f)
+        lam = torch.where(ok, lam / 3.0, lam * 4.0).clamp(1e-7, 1e7)
+        i = int(torch.argmin(f))
+        if float(f[i]) < best:
+            best = float(f[i])
+            snaps.append((time.perf_counter() - t0, th[i].clone()))
+        trace.append((time.perf_counter() - t0, best))
+        if time_limit and trace[-1][0] > time_limit:
+            break
+    return trace, snaps
+
+
 def particle_swarm(prob, theta0, iters=150, w=0.7298, c1=1.49618, c2=1.49618, seed=1, time_limit=None,
                    loss=None):
     """Particle swarm with constriction coefficients and a ring neighbourhood (each particle
@@ -380,7 +425,9 @@ def compare(engine, candidates=256, seed=7, gd_iters=300, pso_seconds=40.0, path
         gradient_descent(prob, theta0, iters=3)
         particle_swarm(prob, theta0, iters=3)
     particle_swarm(prob, theta0, iters=2, loss=prob.loss_plain)
+    levenberg_marquardt_plain(prob, theta0, iters=2)
     lm, lm_snaps = levenberg_marquardt(prob, theta0, iters=lm_iters)
+    lmp, lmp_snaps = levenberg_marquardt_plain(prob, theta0, iters=3 * lm_iters)
     gd = gd_snaps = ps = ps_snaps = None
     if full:
         gd, gd_snaps = gradient_descent(prob, theta0, iters=gd_iters)
@@ -412,9 +459,12 @@ def compare(engine, candidates=256, seed=7, gd_iters=300, pso_seconds=40.0, path
     neutral = None
     if neutral_seeds:
         n_lm, n_pp = neutral_trace(prob, lm_snaps, neutral_seeds), neutral_trace(prob, pp_snaps, neutral_seeds)
+        n_lmp = neutral_trace(prob, lmp_snaps, neutral_seeds)
         n_true = float(prob.loss_plain_mean(th_h, neutral_seeds)[0])
         head_n = max(best_final(n_pp), best_final(n_lm))
         tln, tpn = first_below(n_lm, head_n), first_below(n_pp, head_n)
+        head_p = max(best_final(n_pp), best_final(n_lmp))
+        tlp, tpp = first_below(n_lmp, head_p), first_below(n_pp, head_p)
         nlevels = []
         for f in (1.5, 1.25, 1.1, 1.05):
             L = f * n_true
@@ -426,6 +476,12 @@ def compare(engine, candidates=256, seed=7, gd_iters=300, pso_seconds=40.0, path
                    "equal_loss": head_n, "gradient_seconds_to_equal_loss": tln,
                    "pso_seconds_to_equal_loss": tpn, "speedup": (tpn / tln) if (tln and tpn) else None,
                    "levels": nlevels,
+                   "lm_plain": {"best": best_final(n_lmp), "iters": len(lmp) - 1, "seconds": lmp[-1][0],
+                                "equal_loss": head_p, "seconds_to_equal_loss": tlp,
+                                "pso_seconds_to_equal_loss": tpp,
+                                "speedup": (tpp / tlp) if (tlp and tpp) else None,
+                                "method": "Levenberg-Marquardt steps from the smoothed form's Gauss-Newton system, "
+                                          "accepted on the plain simulator's loss (one batch per iteration)"},
                    "what": "mean plain-simulator loss over %d independent seeds of each snapshot" % neutral_seeds}
     return {
         "seed": seed,
