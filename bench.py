@@ -552,6 +552,25 @@ def measure_batched(eng, local, steps, warmup, tune, cpu_seconds, e2e_steps):
     e1.record(stream)
     torch.cuda.synchronize()
     elapsed_ms = e0.elapsed_time(e1)
+    # the same batch as one persistent cooperative launch per run, replayed from a CUDA graph
+    # (the autotuner keeps whichever driver is faster; both are reported)
+    cfg_sel = tuning["config"] if tuning else 4
+    eng.set_option("sweep_config", cfg_sel)
+    eng.set_option("driver", 1)
+    eng.set_option("graph", 1)
+    for _ in range(2):
+        batch.run()
+    torch.cuda.synchronize()
+    g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    g0.record(stream)
+    for _ in range(steps):
+        batch.run()
+    g1.record(stream)
+    torch.cuda.synchronize()
+    graph_ms = g0.elapsed_time(g1) / steps
+    graph_div = batch.stats()["divisions"]
+    eng.set_option("driver", tuning["driver"] if tuning else 0)
+    eng.set_option("graph", tuning["driver"] if tuning else 0)
     e2e_t = h2d = d2h = 0
     for _ in range(e2e_steps):
         dt, hb, db = simulate_batch_e2e(eng, instances)
@@ -576,12 +595,29 @@ def measure_batched(eng, local, steps, warmup, tune, cpu_seconds, e2e_steps):
     for p in plans[:64]:
         p.run()
     torch.cuda.synchronize()
+    t_each = np.zeros(n)
     t0 = time.perf_counter()
-    for p in plans:
-        p.run()
+    for i, p in enumerate(plans):
+        ti = time.perf_counter()
+        p.run()  # returns when the run has finished
+        t_each[i] = time.perf_counter() - ti
     torch.cuda.synchronize()
     loop_run_s = time.perf_counter() - t0
+    d_each = np.array([p.stats()["divisions"] for p in plans], np.float64)
     same = sum(int(np.array_equal(p.raw_counts(), batch_counts[i])) for i, p in enumerate(plans))
+    # the loop's time split: t_i = overhead + divisions_i x cost per division (least squares);
+    # an instance is overhead-bound when the fixed part is the larger
+    A = np.stack([np.ones(n), d_each], axis=1)
+    (ovh, per_div), *_ = np.linalg.lstsq(A, t_each, rcond=None)
+    ob = ovh > per_div * d_each
+    split = {"overhead_ms_per_instance": 1e3 * ovh, "ns_per_division": 1e9 * per_div,
+             "overhead_bound_instances": int(ob.sum()),
+             "overhead_bound_time_share": float(t_each[ob].sum() / t_each.sum()),
+             "overhead_time_share": float(n * ovh / t_each.sum()),
+             "speedup_bound_at_plain_cost": float(t_each.sum() / max(1e-12, t_each.sum() - n * ovh)),
+             "what": "plain runs timed one by one, t_i = overhead + divisions_i x cost (least squares); "
+                     "overhead-bound: the fixed part is the larger; a batch removes the overhead only, so at "
+                     "the plain per-division cost its speedup is at most loop time / (loop time - n x overhead)"}
     for p in plans:
         p.close()
 
@@ -622,6 +658,12 @@ def measure_batched(eng, local, steps, warmup, tune, cpu_seconds, e2e_steps):
                        "run": "plans created beforehand, one pc_plan_run per instance",
                        "e2e": "one pc_simulate per instance (host inputs, merged histogram out)"},
         "speedup_vs_loop_plain": value / (n / loop_run_s),
+        "persistent_graph": {"ms_per_step": graph_ms, "instances_per_s": n / (graph_ms * 1e-3),
+                             "divisions_per_s": graph_div / (graph_ms * 1e-3), "launches_per_step": 1,
+                             "speedup_vs_loop_plain": (n / (graph_ms * 1e-3)) / (n / loop_run_s),
+                             "what": "the batch as one persistent cooperative launch per run, replayed from a "
+                                     "CUDA graph, configuration %d" % cfg_sel},
+        "loop_split": split,
         "e2e_speedup_vs_loop_plain": e2e_value / (n / loop_e2e_s),
         "bit_exact_instances": "%d/%d" % (same, n),
         "e2e": {"value": e2e_value, "unit": "instances/s", "h2d_bytes_per_step": h2d // e2e_steps,
