@@ -47,6 +47,11 @@ namespace {
 
 constexpr int kThreads = 128;
 constexpr uint32_t kBudget = 1u << 16;
+// Resident blocks per SM the lineage-walk kernels are compiled for (registers per thread =
+// 65536 / (128 x this)); a compile-time tuning knob, results do not depend on it.
+#ifndef PC_SMOOTH_MIN_BLOCKS
+#define PC_SMOOTH_MIN_BLOCKS 5
+#endif
 
 __device__ __forceinline__ double f32_to_f64_bits(float z) {
   const uint32_t f = __float_as_uint(z);
@@ -339,7 +344,7 @@ __device__ __forceinline__ void walk_jacobian(const float* z, double u_age, floa
 // = (sum 2^g w_g / paths, ratio_k / paths * sum 2^g dw_g/dmean, the same for sd), i.e.
 // d E_{b,g} / d(ratio_k, mean_k, sd_k); every block draws its bin's lineages itself (the
 // draws are shared by the 32 candidates of a warp, not across types).
-__global__ void __launch_bounds__(kThreads, 5) k_smooth_jacobian(const SmoothArgs A, const double* __restrict__ params,
+__global__ void __launch_bounds__(kThreads, PC_SMOOTH_MIN_BLOCKS) k_smooth_jacobian(const SmoothArgs A, const double* __restrict__ params,
                                                               uint32_t ncand, double* __restrict__ out) {
   // dynamic: per-thread sums [3 * rows][kThreads], then the lineage draws [kWarps][rows][32]
   extern __shared__ float facc[];
@@ -413,7 +418,7 @@ __global__ void __launch_bounds__(kThreads, 5) k_smooth_jacobian(const SmoothArg
 // adjoint (part[c][b][3k + q] = d(sum_g A_g E_g)/d(ratio_k, mean_k, sd_k)) of one type: block
 // (bin, group of 32 candidates, type k). Every block draws its bin's lineages itself.
 template <bool Backward>
-__global__ void __launch_bounds__(kThreads, 5) k_smooth(const SmoothArgs A, const double* __restrict__ params,
+__global__ void __launch_bounds__(kThreads, PC_SMOOTH_MIN_BLOCKS) k_smooth(const SmoothArgs A, const double* __restrict__ params,
                                                      uint32_t ncand, const double* __restrict__ grad_expected,
                                                      uint32_t nvalues, const int32_t* __restrict__ vidx,
                                                      double* __restrict__ out) {
