@@ -86,11 +86,15 @@ __global__ void __launch_bounds__(256) k_peak(uint32_t iters, double* sink) {
     uint32_t a[kChains];
 #pragma unroll
     for (int i = 0; i < kChains; ++i) a[i] = threadIdx.x + 977u * i;
+    // inline PTX, so that the compiler cannot fold the chain of multiply-adds
     for (uint32_t it = 0; it < iters; ++it)
 #pragma unroll
-      for (int i = 0; i < kChains; ++i) a[i] = a[i] * 0x9E3779B9u + (uint32_t)i;
+      for (int i = 0; i < kChains; ++i)
+        asm volatile("mad.lo.u32 %0, %0, %1, %2;" : "+r"(a[i]) : "r"(0x9E3779B9u), "r"((uint32_t)i));
+    uint32_t x = 0;
 #pragma unroll
-    for (int i = 0; i < kChains; ++i) acc += (double)(a[i] & 1u);
+    for (int i = 0; i < kChains; ++i) x ^= a[i];
+    if (x == iters + 0x5EEDu) sink[threadIdx.x] = (double)x;  // not provably false: keeps the chain
   }
   if (acc == -1.0) sink[threadIdx.x] = acc;
 }

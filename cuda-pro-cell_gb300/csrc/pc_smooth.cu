@@ -48,9 +48,11 @@ namespace {
 constexpr int kThreads = 128;
 constexpr uint32_t kBudget = 1u << 16;
 // Resident blocks per SM the lineage-walk kernels are compiled for (registers per thread =
-// 65536 / (128 x this)); a compile-time tuning knob, results do not depend on it.
+// 65536 / (128 x this)); a compile-time tuning knob, results do not depend on it. Measured on
+// the calibration input: 5 blocks (96 registers) forward 1.91 ms, adjoint 2.62 ms; 6 (80
+// registers, a few more spills) 1.75 / 2.45 ms; 8 (64 registers) 3.04 / 2.45 ms.
 #ifndef PC_SMOOTH_MIN_BLOCKS
-#define PC_SMOOTH_MIN_BLOCKS 5
+#define PC_SMOOTH_MIN_BLOCKS 6
 #endif
 
 __device__ __forceinline__ double f32_to_f64_bits(float z) {
@@ -101,10 +103,20 @@ __device__ __forceinline__ void kahan_add(float* p, float x) {
 // log intrinsics (relative errors near 2^-22) it stays near 1e-7, i.e. a weight's relative
 // error near 1e-7 (checked against the FP64 CPU restatement to 2e-5 and against central
 // differences to 1e-3). The same holds for the weights' exponentials below.
-__device__ __forceinline__ void log_sig(float x, float& ls, float& l1m) {
-  const float L = __logf(1.0f + __expf(-fabsf(x)));
+__device__ __forceinline__ void log_sig(float x, float& ls, float& l1m, float& e) {
+  e = __expf(-fabsf(x));
+  const float L = __logf(1.0f + e);
   ls = -(fmaxf(-x, 0.0f) + L);
   l1m = -(fmaxf(x, 0.0f) + L);
+}
+
+// sigmoid(x) and 1 - sigmoid(x) from e = exp(-|x|) with one reciprocal: 1 / (1 + e) is the
+// larger of the two and e / (1 + e) the smaller (for x >= 0, sigmoid(x) is the larger).
+__device__ __forceinline__ void sig_pair(float x, float e, float& s, float& one_m_s) {
+  const float q = __fdividef(1.0f, 1.0f + e);
+  const float eq = e * q;
+  s = x >= 0.0f ? q : eq;
+  one_m_s = x >= 0.0f ? eq : q;
 }
 
 // A double rounded toward zero to float on the integer pipes (GB300 runs FP64<->FP32
@@ -245,8 +257,8 @@ __device__ __forceinline__ void store_lineage_u(double u, double* u_age, float* 
 // sum_g Ag2[g] w_g and its derivatives in mean and sd.
 template <bool Backward, class Rem>
 __device__ __forceinline__ void walk(const float* z, double u_age, float u1, float u1_lo, float inv_h, uint32_t steps,
-                                     Rem r, bool fixed_tau, float w_hi, float w_lo, float* acc, const float* Ag2,
-                                     float& f_r, float& f_mu, float& f_sig) {
+                                     float stop, Rem r, bool fixed_tau, float w_hi, float w_lo, float* acc,
+                                     const float* Ag2, float& f_r, float& f_mu, float& f_sig) {
   // step 1 (the first division, S_1 = tau_1 (1 + U)) is peeled off the loop
   float zj = fixed_tau ? 0.0f : z[0];
   r.first(zj, u_age, u1, u1_lo);
@@ -254,11 +266,10 @@ __device__ __forceinline__ void walk(const float* z, double u_age, float u1, flo
   float log_p = 0.0f;                         // log s_1 ... s_{j-1}
   float D_mu = 0.0f, D_sig = 0.0f;
   float wh = w_hi, wl = w_lo;                 // weight * 2^(j-1) as a pair of floats
-  const float stop = stop_level(steps);
   for (uint32_t j = 1;;) {
     const float x = r.x(inv_h);
-    float ls, l1m;
-    log_sig(x, ls, l1m);
+    float ls, l1m, e;
+    log_sig(x, ls, l1m, e);
     const float w = __expf(log_p + l1m);  // leaf weight of generation j - 1
     if constexpr (!Backward) {
       if (w != 0.0f) {
@@ -274,17 +285,17 @@ __device__ __forceinline__ void walk(const float* z, double u_age, float u1, flo
       wl = __fmul_rn(wl, 2.0f);
     } else {
       const float a = Ag2[j - 1];
+      float s = 0.0f, one_m_s = 0.0f;
+      if (!fixed_tau) sig_pair(x, e, s, one_m_s);
       if (a != 0.0f && w != 0.0f) {
         const float aw = a * w;
         f_r += aw;
         if (!fixed_tau) {
-          const float s = __expf(ls);
           f_mu += aw * (D_mu + s * inv_h * dmu);
           f_sig += aw * (D_sig + s * inv_h * dsig);
         }
       }
       if (!fixed_tau) {
-        const float one_m_s = __expf(l1m);
         D_mu -= one_m_s * inv_h * dmu;
         D_sig -= one_m_s * inv_h * dsig;
       }
@@ -302,31 +313,30 @@ __device__ __forceinline__ void walk(const float* z, double u_age, float u1, flo
 // 3g, 3g + 1, 3g + 2 gain 2^g w_g and 2^g dw_g/d(mean, sd) (per-thread FP32 sums).
 template <class Rem>
 __device__ __forceinline__ void walk_jacobian(const float* z, double u_age, float u1, float u1_lo, float inv_h,
-                                              uint32_t steps, Rem r, bool fixed_tau, float* acc) {
+                                              uint32_t steps, float stop, Rem r, bool fixed_tau, float* acc) {
   // step 1 peeled off the loop as in walk()
   float zj = fixed_tau ? 0.0f : z[0];
   r.first(zj, u_age, u1, u1_lo);
   float dmu = u1, dsig = zj * u1;
   float log_p = 0.0f, D_mu = 0.0f, D_sig = 0.0f;
   float scale = 1.0f;  // 2^(j-1)
-  const float stop = stop_level(steps);
   for (uint32_t j = 1;;) {
     const float x = r.x(inv_h);
-    float ls, l1m;
-    log_sig(x, ls, l1m);
+    float ls, l1m, e;
+    log_sig(x, ls, l1m, e);
     const float w = __expf(log_p + l1m);  // leaf weight of generation j - 1
     float* p = acc + 3u * (j - 1u) * kThreads;
+    float s = 0.0f, one_m_s = 0.0f;
+    if (!fixed_tau) sig_pair(x, e, s, one_m_s);
     if (w != 0.0f) {
       const float ws = w * scale;
       p[0] += ws;
       if (!fixed_tau) {
-        const float s = __expf(ls);
         p[kThreads] += ws * (D_mu + s * inv_h * dmu);
         p[2 * kThreads] += ws * (D_sig + s * inv_h * dsig);
       }
     }
     if (!fixed_tau) {
-      const float one_m_s = __expf(l1m);
       D_mu -= one_m_s * inv_h * dmu;
       D_sig -= one_m_s * inv_h * dsig;
     }
@@ -338,6 +348,22 @@ __device__ __forceinline__ void walk_jacobian(const float* z, double u_age, floa
     dmu += 1.0f;
     dsig += zj;
   }
+}
+
+// The FP64 walks (candidates and bins where the grid form's error bound does not hold), kept
+// out of line so that the compiler cannot merge them into the FP32 walks as predicated code.
+template <bool Backward>
+__device__ __noinline__ float3 walk_fp64(const float* z, double u_age, float u1, float u1_lo, float inv_h,
+                                         uint32_t steps, float stop, RemFp64 r, bool fixed_tau, float w_hi, float w_lo,
+                                         float* acc, const float* Ag2) {
+  float f_r = 0.0f, f_mu = 0.0f, f_sig = 0.0f;
+  walk<Backward>(z, u_age, u1, u1_lo, inv_h, steps, stop, r, fixed_tau, w_hi, w_lo, acc, Ag2, f_r, f_mu, f_sig);
+  return make_float3(f_r, f_mu, f_sig);
+}
+
+__device__ __noinline__ void walk_jacobian_fp64(const float* z, double u_age, float u1, float u1_lo, float inv_h,
+                                                uint32_t steps, float stop, RemFp64 r, bool fixed_tau, float* acc) {
+  walk_jacobian(z, u_age, u1, u1_lo, inv_h, steps, stop, r, fixed_tau, acc);
 }
 
 // Jacobian of the expected counts: block (bin, group of 32 candidates, type k). out[c][b][g][k]
@@ -377,6 +403,7 @@ __global__ void __launch_bounds__(kThreads, PC_SMOOTH_MIN_BLOCKS) k_smooth_jacob
   RemGrid rg;
   const bool grid = grid_setup(rg, mu, sd, A.t_max, steps, 1.0 / A.inv_h);
   const RemFp64 rd{mu, sd, A.t_max, 0.0};
+  const float stop = stop_level(steps);  // once per block: the walks' stopping threshold
   const uint64_t nlin = (r1 - r0) * A.paths;
   for (uint64_t base = (uint64_t)warp * 32u; base < nlin; base += 32u * kWarps) {
     if (base + lane < nlin) {
@@ -392,9 +419,9 @@ __global__ void __launch_bounds__(kThreads, PC_SMOOTH_MIN_BLOCKS) k_smooth_jacob
         if (quiescent) {
           fmy[0] += 1.0f;  // quiescent type: a leaf at generation 0 (cell.cu:69-75)
         } else if (grid) {
-          walk_jacobian(zbuf + ii, u_age[li], u_one[li], u_one_lo[li], inv_h, steps, rg, fixed_tau, fmy);
+          walk_jacobian(zbuf + ii, u_age[li], u_one[li], u_one_lo[li], inv_h, steps, stop, rg, fixed_tau, fmy);
         } else {
-          walk_jacobian(zbuf + ii, u_age[li], u_one[li], u_one_lo[li], inv_h, steps, rd, fixed_tau, fmy);
+          walk_jacobian_fp64(zbuf + ii, u_age[li], u_one[li], u_one_lo[li], inv_h, steps, stop, rd, fixed_tau, fmy);
         }
       }
     }
@@ -475,6 +502,7 @@ __global__ void __launch_bounds__(kThreads, PC_SMOOTH_MIN_BLOCKS) k_smooth(const
   RemGrid rg;
   const bool grid = grid_setup(rg, mu, sd, A.t_max, steps, 1.0 / A.inv_h);
   const RemFp64 rd{mu, sd, A.t_max, 0.0};
+  const float stop = stop_level(steps);  // once per block: the walks' stopping threshold
   // lineage i of the bin: initial cell r0 + i / paths, replica i % paths
   const uint64_t nlin = (r1 - r0) * A.paths;
   for (uint64_t base = (uint64_t)warp * 32u; base < nlin; base += 32u * kWarps) {
@@ -500,11 +528,15 @@ __global__ void __launch_bounds__(kThreads, PC_SMOOTH_MIN_BLOCKS) k_smooth(const
         } else if (walks) {
           const uint32_t li = warp * 32u + ii;
           if (grid)
-            walk<Backward>(zbuf + ii, u_age[li], u_one[li], u_one_lo[li], inv_h, steps, rg, fixed_tau, w_hi, w_lo,
-                           fmy, my_ag, f_r, f_mu, f_sig);
-          else
-            walk<Backward>(zbuf + ii, u_age[li], u_one[li], u_one_lo[li], inv_h, steps, rd, fixed_tau, w_hi, w_lo,
-                           fmy, my_ag, f_r, f_mu, f_sig);
+            walk<Backward>(zbuf + ii, u_age[li], u_one[li], u_one_lo[li], inv_h, steps, stop, rg, fixed_tau, w_hi,
+                           w_lo, fmy, my_ag, f_r, f_mu, f_sig);
+          else {
+            const float3 f = walk_fp64<Backward>(zbuf + ii, u_age[li], u_one[li], u_one_lo[li], inv_h, steps, stop,
+                                                 rd, fixed_tau, w_hi, w_lo, fmy, my_ag);
+            f_r = f.x;
+            f_mu = f.y;
+            f_sig = f.z;
+          }
         }
         if constexpr (Backward) {
           // per-thread compensated FP32 sums (terms of either sign cancel); scaled by
