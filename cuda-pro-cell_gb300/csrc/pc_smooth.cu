@@ -16,9 +16,9 @@
 // takes every draw (initial age, normals, path) from the plain form's counters of cell
 // r + m * ncells, so the estimate converges to the expectation over all randomness, and
 // replica 0 shares its draws with the plain form run on the same seed.
-// Types enter analytically through ratio_k, so d/d ratio is exact. Weights are products of
-// sigmoids evaluated in log space (FP32; due times accumulate in FP64), never negative, and a
-// lineage stops once no later generation can add more than e^-40 cells.
+// Types enter analytically through ratio_k, so d/d ratio is exact. Weights are running
+// products of sigmoids (FP32), never negative, and a lineage stops once no later generation
+// can add more than e^-40 cells, well before such a product could leave the normal range.
 //
 // Adjoint. dw_g/dtheta = w_g (D_g + s_{g+1} / h dS_{g+1}/dtheta) with the running tangent
 // D_g = -sum_{i <= g} (1 - s_i) / h dS_i/dtheta, dS_j/dmean = U + j and dS_j/dsd = z_1 (1 + U)
@@ -98,21 +98,14 @@ __device__ __forceinline__ void kahan_add(float* p, float x) {
   p[0] = t;
 }
 
-// log sigmoid(x) and log(1 - sigmoid(x)) = log sigmoid(-x). Weights are products kept in log
-// space, so what matters is the absolute error of these logarithms: with the fast exp and
-// log intrinsics (relative errors near 2^-22) it stays near 1e-7, i.e. a weight's relative
-// error near 1e-7 (checked against the FP64 CPU restatement to 2e-5 and against central
-// differences to 1e-3). The same holds for the weights' exponentials below.
-__device__ __forceinline__ void log_sig(float x, float& ls, float& l1m, float& e) {
-  e = __expf(-fabsf(x));
-  const float L = __logf(1.0f + e);
-  ls = -(fmaxf(-x, 0.0f) + L);
-  l1m = -(fmaxf(x, 0.0f) + L);
-}
-
-// sigmoid(x) and 1 - sigmoid(x) from e = exp(-|x|) with one reciprocal: 1 / (1 + e) is the
-// larger of the two and e / (1 + e) the smaller (for x >= 0, sigmoid(x) is the larger).
-__device__ __forceinline__ void sig_pair(float x, float e, float& s, float& one_m_s) {
+// sigmoid(x) and 1 - sigmoid(x) from e = exp(-|x|) and one reciprocal: 1 / (1 + e) is the
+// larger of the two and e / (1 + e) the smaller (for x >= 0, sigmoid(x) is the larger), so
+// both keep their relative accuracy however far x is from 0. With the fast exp and
+// reciprocal intrinsics (relative errors near 2^-22) each factor of a weight is good to a few
+// 1e-7, and a weight of up to ~60 factors to about 1e-5 at worst (checked against the FP64
+// CPU restatement to 2e-5 and against central differences to 1e-3).
+__device__ __forceinline__ void sig_pair(float x, float& s, float& one_m_s) {
+  const float e = __expf(-fabsf(x));
   const float q = __fdividef(1.0f, 1.0f + e);
   const float eq = e * q;
   s = x >= 0.0f ? q : eq;
@@ -217,10 +210,11 @@ __device__ __forceinline__ bool grid_setup(RemGrid& r, double mu, double sigma, 
 }
 
 // A lineage stops once no later generation can add more than e^-40 cells: every later leaf
-// weight is at most s_1 ... s_j (the running product) times 2^g <= 2^(steps - 1).
-constexpr float kLogNegligible = -40.0f;
-constexpr float kLn2 = 0.693147180559945f;
-__device__ __forceinline__ float stop_level(uint32_t steps) { return kLogNegligible - kLn2 * (float)steps; }
+// weight is at most s_1 ... s_j (the running product) times 2^g <= 2^(steps - 1), so the walk
+// ends when that product falls below e^-40 2^-steps (above the smallest normal float for up
+// to 68 steps; deeper bins walk on, at most until the product is 0).
+constexpr float kNegligible = 4.24835426e-18f;  // e^-40
+__device__ __forceinline__ float stop_level(uint32_t steps) { return ldexpf(kNegligible, -(int)steps); }
 
 // Lineage i of a bin whose initial cells start at r0 (initial cell r0 + i / paths, replica
 // i % paths, which draws as initial cell r + replica * ncells): its initial age, and the
@@ -263,14 +257,14 @@ __device__ __forceinline__ void walk(const float* z, double u_age, float u1, flo
   float zj = fixed_tau ? 0.0f : z[0];
   r.first(zj, u_age, u1, u1_lo);
   float dmu = u1, dsig = zj * u1;  // dS_j / d(mean, sd)
-  float log_p = 0.0f;                         // log s_1 ... s_{j-1}
+  float P = 1.0f;                             // s_1 ... s_{j-1}
   float D_mu = 0.0f, D_sig = 0.0f;
   float wh = w_hi, wl = w_lo;                 // weight * 2^(j-1) as a pair of floats
   for (uint32_t j = 1;;) {
     const float x = r.x(inv_h);
-    float ls, l1m, e;
-    log_sig(x, ls, l1m, e);
-    const float w = __expf(log_p + l1m);  // leaf weight of generation j - 1
+    float s, one_m_s;
+    sig_pair(x, s, one_m_s);
+    const float w = P * one_m_s;  // leaf weight of generation j - 1
     if constexpr (!Backward) {
       if (w != 0.0f) {
         // (wh + wl) * w as t1 + t2 (t1 rounded, t2 its error plus the low part), added into
@@ -285,8 +279,6 @@ __device__ __forceinline__ void walk(const float* z, double u_age, float u1, flo
       wl = __fmul_rn(wl, 2.0f);
     } else {
       const float a = Ag2[j - 1];
-      float s = 0.0f, one_m_s = 0.0f;
-      if (!fixed_tau) sig_pair(x, e, s, one_m_s);
       if (a != 0.0f && w != 0.0f) {
         const float aw = a * w;
         f_r += aw;
@@ -300,8 +292,8 @@ __device__ __forceinline__ void walk(const float* z, double u_age, float u1, flo
         D_sig -= one_m_s * inv_h * dsig;
       }
     }
-    log_p += ls;
-    if (log_p < stop || ++j > steps) break;
+    P *= s;
+    if (P < stop || ++j > steps) break;
     zj = fixed_tau ? 0.0f : z[(j - 1) * 32u];
     r.step(zj);
     dmu += 1.0f;
@@ -318,16 +310,14 @@ __device__ __forceinline__ void walk_jacobian(const float* z, double u_age, floa
   float zj = fixed_tau ? 0.0f : z[0];
   r.first(zj, u_age, u1, u1_lo);
   float dmu = u1, dsig = zj * u1;
-  float log_p = 0.0f, D_mu = 0.0f, D_sig = 0.0f;
+  float P = 1.0f, D_mu = 0.0f, D_sig = 0.0f;  // P = s_1 ... s_{j-1}
   float scale = 1.0f;  // 2^(j-1)
   for (uint32_t j = 1;;) {
     const float x = r.x(inv_h);
-    float ls, l1m, e;
-    log_sig(x, ls, l1m, e);
-    const float w = __expf(log_p + l1m);  // leaf weight of generation j - 1
+    float s, one_m_s;
+    sig_pair(x, s, one_m_s);
+    const float w = P * one_m_s;  // leaf weight of generation j - 1
     float* p = acc + 3u * (j - 1u) * kThreads;
-    float s = 0.0f, one_m_s = 0.0f;
-    if (!fixed_tau) sig_pair(x, e, s, one_m_s);
     if (w != 0.0f) {
       const float ws = w * scale;
       p[0] += ws;
@@ -341,8 +331,8 @@ __device__ __forceinline__ void walk_jacobian(const float* z, double u_age, floa
       D_sig -= one_m_s * inv_h * dsig;
     }
     scale *= 2.0f;
-    log_p += ls;
-    if (log_p < stop || ++j > steps) break;
+    P *= s;
+    if (P < stop || ++j > steps) break;
     zj = fixed_tau ? 0.0f : z[(j - 1) * 32u];
     r.step(zj);
     dmu += 1.0f;
