@@ -66,6 +66,12 @@ struct pc_context {
   unsigned long long* stage = nullptr;
   size_t stage_elems = 0;
   uint64_t stage_plan = 0, stage_run = 0;
+  // the device merge of a plan's result: device scratch (value map, type order, merged
+  // counts) and the pinned copy of the merged counts, both grown on demand
+  void* merge_dev = nullptr;
+  size_t merge_dev_bytes = 0;
+  unsigned long long* merge_host = nullptr;
+  size_t merge_host_bytes = 0;
   ZigTables zig_host;
   ZigTables* zig_dev = nullptr;
   std::vector<LevelBuf> pool;
@@ -435,6 +441,8 @@ void pc_destroy(pc_context* ctx) {
   for (pc_plan* p : ctx->live) p->owner = nullptr;  // plans outliving their context free their own buffers
   pc_cuda_free(ctx->spare_rec);
   pc_cuda_free(ctx->spare_hist);
+  pc_cuda_free(ctx->merge_dev);
+  cudaFreeHost(ctx->merge_host);
   pc_cuda_free(ctx->zig_dev);
   pc_cuda_free(ctx->stats_dev);
   pc_cuda_free(ctx->error_dev);
@@ -726,9 +734,6 @@ int finalize_plan(pc_context* ctx, pc_plan* p) {
   p->roots_total = roots;
   p->root_begin = 0;
   p->root_end = roots;
-  p->bin_start.assign(1, 0);
-  for (const auto& I : p->inst)
-    for (uint64_t f : I.bin_freq) p->bin_start.push_back(p->bin_start.back() + f);
 
   // Root chunk and key layout: key = root_local * 2^g + path must fit 64 bits; the narrow
   // layout (root_local << 32 | heap node) needs root_local < 2^32.
@@ -743,25 +748,44 @@ int finalize_plan(pc_context* ctx, pc_plan* p) {
   p->g_store_max = std::min<uint32_t>(62u, 64u - rb);
   p->hist_gens = std::min(gmax, p->g_store_max + 1) + 1;
 
+  // Per-bin tables (first initial cell, cap and flags; in a batch also the instance and first
+  // class). Each instance fills its own slice, on host threads when there are many.
   std::vector<uint32_t> bin_inst, bin_class;
   std::vector<BatchType> btypes;
   std::vector<InstanceDev> idev;
-  p->bin_info.clear();
-  for (uint32_t i = 0; i < (uint32_t)p->inst.size(); ++i) {
+  p->bin_start.assign((size_t)bins + 1, 0);
+  p->bin_info.assign(bins, 0);
+  if (p->batched) {
+    bin_inst.assign(bins, 0);
+    bin_class.assign(bins, 0);
+  }
+  auto fill = [&](uint32_t i) {
     InstanceHost& I = p->inst[i];
     const uint32_t nt = (uint32_t)I.types.size();
+    uint64_t start = I.root_begin;
     for (size_t b = 0; b < I.bin_value.size(); ++b) {
+      const size_t at = I.bin_begin + b;
+      start += I.bin_freq[b];
+      p->bin_start[at + 1] = start;
       uint32_t c = I.cap[b];
       uint32_t clamped = 0;
       if (c > p->g_store_max + 1) {
         c = p->g_store_max + 1;
         clamped = 0x200u;
       }
-      p->bin_info.push_back(c | (I.bin_value[b] >= I.phi ? 0x100u : 0u) | clamped);
-      bin_inst.push_back(i);
-      bin_class.push_back((uint32_t)(I.class_begin + b * nt));
+      p->bin_info[at] = c | (I.bin_value[b] >= I.phi ? 0x100u : 0u) | clamped;
+      if (p->batched) {
+        bin_inst[at] = i;
+        bin_class[at] = (uint32_t)(I.class_begin + b * nt);
+      }
     }
     I.hist_gens = std::min(I.gmax, p->g_store_max + 1) + 1;
+  };
+  const uint32_t ninst = (uint32_t)p->inst.size();
+  if (ninst >= 64 && bins >= (1u << 16)) {
+    parallel_for(ninst, fill);
+  } else {
+    for (uint32_t i = 0; i < ninst; ++i) fill(i);
   }
   if (p->batched) batch_type_tables(p, btypes, idev);
 
@@ -862,6 +886,82 @@ int instance_result(const pc_plan* p, const InstanceHost& I, const unsigned long
 }
 
 std::atomic<uint64_t> g_plan_ids{1};
+
+// Device scratch of the result merge above this size is not kept: such plans merge on host
+// threads instead.
+constexpr size_t kMaxMergeScratch = size_t(256) << 20;
+
+size_t round16(size_t n) { return (n + 15) & ~size_t(15); }
+
+// The merged histogram of a single-instance plan, merged on the device from the count table
+// the run left there: the value map and type order go up (nbins x generations int32), the
+// merged counts (values x (1 + types) u64) come back, instead of the whole [generation][class]
+// table and a host loop over it. Returns PC_ERR_UNSUPPORTED when the scratch would exceed
+// kMaxMergeScratch.
+int device_result(pc_context* ctx, pc_plan* p, pc_histogram* out) {
+  const InstanceHost& I = p->inst[0];
+  const uint32_t nb = (uint32_t)I.bin_value.size(), nt = (uint32_t)I.types.size();
+  const uint64_t nv = I.values.size();
+  const size_t vidx_bytes = round16((size_t)nb * I.vidx_stride * sizeof(int32_t));
+  const size_t s2f_bytes = round16((size_t)nt * sizeof(uint32_t));
+  const size_t counts = (size_t)nv * (1u + nt) + 2u;  // totals, per_type, error word
+  const size_t need = vidx_bytes + s2f_bytes + counts * sizeof(unsigned long long);
+  if (need > kMaxMergeScratch) return PC_ERR_UNSUPPORTED;
+  cudaStream_t st = ctx->stream;
+  if (ctx->merge_dev_bytes < need) {
+    pc_cuda_free(ctx->merge_dev);
+    ctx->merge_dev = nullptr;
+    ctx->merge_dev_bytes = 0;
+    PC_CUDA(ctx, pc_cuda_malloc(&ctx->merge_dev, need));
+    ctx->merge_dev_bytes = need;
+  }
+  if (ctx->merge_host_bytes < counts * sizeof(unsigned long long)) {
+    cudaFreeHost(ctx->merge_host);
+    ctx->merge_host = nullptr;
+    ctx->merge_host_bytes = 0;
+    PC_CUDA(ctx, pc_cuda_malloc_host(&ctx->merge_host, counts * sizeof(unsigned long long)));
+    ctx->merge_host_bytes = counts * sizeof(unsigned long long);
+  }
+  char* base = static_cast<char*>(ctx->merge_dev);
+  int32_t* vidx = reinterpret_cast<int32_t*>(base);
+  uint32_t* s2f = reinterpret_cast<uint32_t*>(base + vidx_bytes);
+  unsigned long long* merged = reinterpret_cast<unsigned long long*>(base + vidx_bytes + s2f_bytes);
+  unsigned long long* totals = merged;
+  unsigned long long* per_type = merged + nv;
+  uint32_t* error = reinterpret_cast<uint32_t*>(merged + nv * (1u + nt));
+  if (nb)
+    PC_CUDA(ctx, pc_cuda_copy(vidx, I.vidx.data(), (size_t)nb * I.vidx_stride * sizeof(int32_t),
+                              cudaMemcpyHostToDevice, st));
+  PC_CUDA(ctx, pc_cuda_copy(s2f, I.sorted_to_file.data(), (size_t)nt * sizeof(uint32_t), cudaMemcpyHostToDevice, st));
+  PC_CUDA(ctx, pc_cuda_memset(merged, 0, counts * sizeof(unsigned long long), st));
+  PC_CUDA(ctx, PC_LAUNCH(launch_merge_counts(p->hist_dev, p->nclass, I.class_begin, I.hist_gens, nb, nt, vidx,
+                                             I.vidx_stride, s2f, totals, per_type, error, st)));
+  PC_CUDA(ctx, pc_cuda_copy(ctx->merge_host, merged, counts * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+  PC_CUDA(ctx, pc_cuda_sync(st));
+  const unsigned long long* hm = ctx->merge_host;
+  if (static_cast<uint32_t>(hm[nv * (1u + nt)]) & 1u)
+    return fail(ctx, PC_ERR_CUDA, "internal: leaf counted outside the output value set");
+  out->n_values = nv;
+  out->n_types = nt;
+  out->values = (double*)std::malloc(std::max<uint64_t>(1, nv) * sizeof(double));
+  out->totals = (uint64_t*)std::malloc(std::max<uint64_t>(1, nv) * sizeof(uint64_t));
+  out->per_type = (uint64_t*)std::malloc(std::max<uint64_t>(1, nv * nt) * sizeof(uint64_t));
+  if (!out->values || !out->totals || !out->per_type) {
+    pc_histogram_free(out);
+    return fail(ctx, PC_ERR_NOMEM, "host allocation");
+  }
+  if (nv) {
+    std::memcpy(out->values, I.values.data(), nv * sizeof(double));
+    std::memcpy(out->totals, hm, nv * sizeof(uint64_t));
+    std::memcpy(out->per_type, hm + nv, nv * nt * sizeof(uint64_t));
+  }
+  uint64_t leaves = 0;
+  for (uint64_t v = 0; v < nv; ++v) leaves += hm[v];
+  out->stats.leaves = leaves;
+  out->stats.h2d_bytes = (uint64_t)nb * I.vidx_stride * sizeof(int32_t) + (uint64_t)nt * sizeof(uint32_t);
+  out->stats.d2h_bytes = counts * sizeof(unsigned long long);
+  return PC_OK;
+}
 
 // The plan's count table after its last run, in the context's pinned stage (read back
 // once per run; the stage grows to the largest table and is reused).
@@ -1354,16 +1454,28 @@ int pc_plan_result(pc_context* ctx, pc_plan* p, pc_histogram* out) {
   if (!ctx || !p || !out || p->inst.empty()) return PC_ERR_INVALID;
   std::memset(out, 0, sizeof(*out));
   if (!p->ran) return fail(ctx, PC_ERR_INVALID, "plan has not run");
-  const unsigned long long* h = nullptr;
-  int rc = stage_table(ctx, p, &h);
-  if (rc != PC_OK) return rc;
-  const char* msg = "";
-  rc = instance_result(p, p->inst[0], h, out, &msg);
-  if (rc != PC_OK) return fail(ctx, rc, msg);
+  int rc = device_result(ctx, p, out);
+  uint64_t h2d = 0, d2h = 0;
+  if (rc == PC_OK) {
+    h2d = out->stats.h2d_bytes;
+    d2h = out->stats.d2h_bytes;
+  } else if (rc == PC_ERR_UNSUPPORTED) {
+    // merge scratch too large for the device: read the count table back, merge on the host
+    const unsigned long long* h = nullptr;
+    rc = stage_table(ctx, p, &h);
+    if (rc != PC_OK) return rc;
+    const char* msg = "";
+    rc = instance_result(p, p->inst[0], h, out, &msg);
+    if (rc != PC_OK) return fail(ctx, rc, msg);
+    d2h = p->hist_elems * sizeof(unsigned long long);
+  } else {
+    return rc;
+  }
   const uint64_t leaves = out->stats.leaves;
   out->stats = p->stats;
   out->stats.leaves = leaves;
-  out->stats.d2h_bytes += p->hist_elems * sizeof(unsigned long long);
+  out->stats.h2d_bytes += h2d;
+  out->stats.d2h_bytes += d2h;
   return PC_OK;
   PC_GUARD_END(ctx)
 }

@@ -167,6 +167,12 @@ int launch_debug_philox(const uint32_t* ctr, uint64_t n, uint32_t k0, uint32_t k
 int launch_debug_normals(const ZigTables* zig, uint32_t k0, uint32_t k1, uint32_t root,
                          uint64_t first_parent, uint64_t count, float* z, void* stream);
 int occupancy_blocks_per_sm(int* root_blocks, int* divide_blocks);
+// One instance's leaf counts (rows of nclass classes, hist_gens rows; its nb x nt classes from
+// class_begin) merged into totals[v] and per_type[v][nt] (file type order s2f), v = vidx[b][g];
+// both zeroed by the caller. A count outside the value set sets bit 0 of *error.
+int launch_merge_counts(const unsigned long long* hist, uint64_t nclass, uint64_t class_begin, uint32_t hist_gens,
+                        uint32_t nb, uint32_t nt, const int32_t* vidx, uint32_t vidx_stride, const uint32_t* s2f,
+                        unsigned long long* totals, unsigned long long* per_type, uint32_t* error, void* stream);
 // Throughput probe (roofline denominators): kind 0 FP64 FMA, 1 FP32 FMA, 2 INT32 multiply-add;
 // each of the blocks x 256 threads runs iters x 8 operations.
 int launch_peak_probe(int kind, uint32_t iters, int blocks, double* sink, void* stream);

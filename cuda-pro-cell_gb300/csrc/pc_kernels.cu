@@ -99,7 +99,48 @@ __global__ void __launch_bounds__(256) k_peak(uint32_t iters, double* sink) {
   if (acc == -1.0) sink[threadIdx.x] = acc;
 }
 
+// One instance's leaf counts merged into its output value histogram: thread (g, b) reads the
+// nt counts of bin b at generation g (row g of the plan's [generation][class] table, classes
+// from class_begin, b-major), adds them to per_type[v][file type] and their sum to totals[v],
+// v = vidx[b][g] the index of the bin's value halved g times in the value set. A nonzero count
+// with no value (v < 0, which the leaf rule never produces) sets bit 0 of *error.
+__global__ void __launch_bounds__(256) k_merge_counts(const unsigned long long* __restrict__ h, uint64_t nclass,
+                                                      uint64_t class_begin, uint32_t hist_gens, uint32_t nb,
+                                                      uint32_t nt, const int32_t* __restrict__ vidx,
+                                                      uint32_t vidx_stride, const uint32_t* __restrict__ s2f,
+                                                      unsigned long long* __restrict__ totals,
+                                                      unsigned long long* __restrict__ per_type, uint32_t* error) {
+  const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (uint64_t)hist_gens * nb) return;
+  const uint32_t g = (uint32_t)(i / nb), b = (uint32_t)(i % nb);
+  const unsigned long long* row = h + (uint64_t)g * nclass + class_begin + (uint64_t)b * nt;
+  const int32_t v = vidx[(uint64_t)b * vidx_stride + g];
+  unsigned long long sum = 0ull;
+  for (uint32_t k = 0; k < nt; ++k) {
+    const unsigned long long c = row[k];
+    if (c == 0ull) continue;
+    if (v < 0) {
+      atomicOr(error, 1u);
+      continue;
+    }
+    atomicAdd(per_type + (uint64_t)v * nt + s2f[k], c);
+    sum += c;
+  }
+  if (sum != 0ull) atomicAdd(totals + v, sum);
+}
+
 }  // namespace
+
+int launch_merge_counts(const unsigned long long* hist, uint64_t nclass, uint64_t class_begin, uint32_t hist_gens,
+                        uint32_t nb, uint32_t nt, const int32_t* vidx, uint32_t vidx_stride, const uint32_t* s2f,
+                        unsigned long long* totals, unsigned long long* per_type, uint32_t* error, void* stream) {
+  const uint64_t n = (uint64_t)hist_gens * nb;
+  if (n == 0 || nt == 0) return 0;
+  const unsigned blocks = (unsigned)((n + 255) / 256);
+  k_merge_counts<<<blocks, 256, 0, (cudaStream_t)stream>>>(hist, nclass, class_begin, hist_gens, nb, nt, vidx,
+                                                             vidx_stride, s2f, totals, per_type, error);
+  return (int)cudaGetLastError();
+}
 
 int launch_peak_probe(int kind, uint32_t iters, int blocks, double* sink, void* stream) {
   cudaStream_t st = (cudaStream_t)stream;

@@ -175,7 +175,7 @@ def histogram_to_numpy(h: Histogram):
     per = np.ctypeslib.as_array(h.per_type, shape=(max(1, nv * nt),))[:nv * nt].copy().reshape(nv, nt)
     st = h.stats
     stats = {k: getattr(st, k) for k, _ in Stats._fields_}
-    return values, totals.astype(np.uint64), per.astype(np.uint64), stats
+    return values, totals.astype(np.uint64, copy=False), per.astype(np.uint64, copy=False), stats
 
 
 BIN_DTYPE = np.dtype([("value", "<f8"), ("frequency", "<u8")])

@@ -149,8 +149,9 @@ int pc_plan_set_roots(pc_context* ctx, pc_plan* plan, uint64_t root_begin, uint6
 int pc_plan_run(pc_context* ctx, pc_plan* plan);
 /* Statistics of the last pc_plan_run (leaves is filled by pc_plan_result only). */
 int pc_plan_stats(pc_context* ctx, const pc_plan* plan, pc_stats* out);
-/* Copy the counts to the host and merge equal values into `out` (free with
- * pc_histogram_free). */
+/* Merge equal values of the counts into `out` (free with pc_histogram_free): on the device,
+ * reading back only the merged counts (values x (1 + types)); for plans whose merge scratch
+ * would exceed 256 MB, by reading the count table back and merging on the host. */
 int pc_plan_result(pc_context* ctx, pc_plan* plan, pc_histogram* out);
 /* The raw per-(generation, bin, type) counts as uint64 [gens][bins][types], bins in file
  * order of the nonzero rows and types in file order. *n_elems gets the element count;
