@@ -216,6 +216,12 @@ __device__ __forceinline__ bool grid_setup(RemGrid& r, double mu, double sigma, 
 constexpr float kNegligible = 4.24835426e-18f;  // e^-40
 __device__ __forceinline__ float stop_level(uint32_t steps) { return ldexpf(kNegligible, -(int)steps); }
 
+// A cell due at least 24 h before t_max (x = (T - S) / h > 24) divides with sigmoid(x), which
+// rounds to 1 in FP32, and stays a leaf with 1 - sigmoid(x) < e^-24 = 3.8e-11: its step adds
+// no leaf weight worth counting and changes neither the running product nor the tangents, so
+// the walks only advance the remaining time there (the early generations of most lineages).
+constexpr float kFar = 24.0f;
+
 // Lineage i of a bin whose initial cells start at r0 (initial cell r0 + i / paths, replica
 // i % paths, which draws as initial cell r + replica * ncells): its initial age, and the
 // normals of the nodes it visits (heap nodes 1, 2 + b_1, ..., b_j the path bits) into
@@ -253,51 +259,58 @@ template <bool Backward, class Rem>
 __device__ __forceinline__ void walk(const float* z, double u_age, float u1, float u1_lo, float inv_h, uint32_t steps,
                                      float stop, Rem r, bool fixed_tau, float w_hi, float w_lo, float* acc,
                                      const float* Ag2, float& f_r, float& f_mu, float& f_sig) {
-  // step 1 (the first division, S_1 = tau_1 (1 + U)) is peeled off the loop
+  // step 1 (the first division, S_1 = tau_1 (1 + U)) is peeled off the loop. The device code
+  // is compiled without automatic FMA contraction (the random stream must round as on the
+  // host), so the derivative updates below name their FMAs.
   float zj = fixed_tau ? 0.0f : z[0];
   r.first(zj, u_age, u1, u1_lo);
-  float dmu = u1, dsig = zj * u1;  // dS_j / d(mean, sd)
+  float dmu = u1 * inv_h, dsig = zj * dmu;    // dS_j / d(mean, sd), divided by h
   float P = 1.0f;                             // s_1 ... s_{j-1}
   float D_mu = 0.0f, D_sig = 0.0f;
   float wh = w_hi, wl = w_lo;                 // weight * 2^(j-1) as a pair of floats
   for (uint32_t j = 1;;) {
     const float x = r.x(inv_h);
-    float s, one_m_s;
-    sig_pair(x, s, one_m_s);
-    const float w = P * one_m_s;  // leaf weight of generation j - 1
-    if constexpr (!Backward) {
-      if (w != 0.0f) {
-        // (wh + wl) * w as t1 + t2 (t1 rounded, t2 its error plus the low part), added into
-        // the compensated pair at acc[2g] (sum) / acc[2g + 1] (compensation)
-        const float t1 = __fmul_rn(wh, w);
-        const float t2 = __fadd_rn(__fmaf_rn(wh, w, -t1), __fmul_rn(wl, w));
-        float* p = acc + 2u * (j - 1u) * kThreads;
-        kahan_add(p, t1);
-        p[kThreads] = __fsub_rn(p[kThreads], t2);
-      }
-      wh = __fmul_rn(wh, 2.0f);
-      wl = __fmul_rn(wl, 2.0f);
-    } else {
-      const float a = Ag2[j - 1];
-      if (a != 0.0f && w != 0.0f) {
-        const float aw = a * w;
-        f_r += aw;
+    if (x <= kFar) {
+      float s, one_m_s;
+      sig_pair(x, s, one_m_s);
+      const float w = P * one_m_s;  // leaf weight of generation j - 1
+      if constexpr (!Backward) {
+        if (w != 0.0f) {
+          // (wh + wl) * w as t1 + t2 (t1 rounded, t2 its error plus the low part), added into
+          // the compensated pair at acc[2g] (sum) / acc[2g + 1] (compensation)
+          const float t1 = __fmul_rn(wh, w);
+          const float t2 = __fmaf_rn(wl, w, __fmaf_rn(wh, w, -t1));
+          float* p = acc + 2u * (j - 1u) * kThreads;
+          kahan_add(p, t1);
+          p[kThreads] = __fsub_rn(p[kThreads], t2);
+        }
+      } else {
+        const float a = Ag2[j - 1];
+        if (a != 0.0f && w != 0.0f) {
+          const float aw = a * w;
+          f_r += aw;
+          if (!fixed_tau) {
+            f_mu = __fmaf_rn(aw, __fmaf_rn(s, dmu, D_mu), f_mu);
+            f_sig = __fmaf_rn(aw, __fmaf_rn(s, dsig, D_sig), f_sig);
+          }
+        }
         if (!fixed_tau) {
-          f_mu += aw * (D_mu + s * inv_h * dmu);
-          f_sig += aw * (D_sig + s * inv_h * dsig);
+          D_mu = __fmaf_rn(-one_m_s, dmu, D_mu);
+          D_sig = __fmaf_rn(-one_m_s, dsig, D_sig);
         }
       }
-      if (!fixed_tau) {
-        D_mu -= one_m_s * inv_h * dmu;
-        D_sig -= one_m_s * inv_h * dsig;
-      }
+      P *= s;
+      if (P < stop) break;
     }
-    P *= s;
-    if (P < stop || ++j > steps) break;
+    if constexpr (!Backward) {
+      wh = __fmul_rn(wh, 2.0f);
+      wl = __fmul_rn(wl, 2.0f);
+    }
+    if (++j > steps) break;
     zj = fixed_tau ? 0.0f : z[(j - 1) * 32u];
     r.step(zj);
-    dmu += 1.0f;
-    dsig += zj;
+    dmu += inv_h;
+    dsig = __fmaf_rn(zj, inv_h, dsig);
   }
 }
 
@@ -306,37 +319,40 @@ __device__ __forceinline__ void walk(const float* z, double u_age, float u1, flo
 template <class Rem>
 __device__ __forceinline__ void walk_jacobian(const float* z, double u_age, float u1, float u1_lo, float inv_h,
                                               uint32_t steps, float stop, Rem r, bool fixed_tau, float* acc) {
-  // step 1 peeled off the loop as in walk()
+  // step 1 peeled off the loop as in walk(), derivatives divided by h as there
   float zj = fixed_tau ? 0.0f : z[0];
   r.first(zj, u_age, u1, u1_lo);
-  float dmu = u1, dsig = zj * u1;
+  float dmu = u1 * inv_h, dsig = zj * dmu;
   float P = 1.0f, D_mu = 0.0f, D_sig = 0.0f;  // P = s_1 ... s_{j-1}
   float scale = 1.0f;  // 2^(j-1)
   for (uint32_t j = 1;;) {
     const float x = r.x(inv_h);
-    float s, one_m_s;
-    sig_pair(x, s, one_m_s);
-    const float w = P * one_m_s;  // leaf weight of generation j - 1
-    float* p = acc + 3u * (j - 1u) * kThreads;
-    if (w != 0.0f) {
-      const float ws = w * scale;
-      p[0] += ws;
-      if (!fixed_tau) {
-        p[kThreads] += ws * (D_mu + s * inv_h * dmu);
-        p[2 * kThreads] += ws * (D_sig + s * inv_h * dsig);
+    if (x <= kFar) {  // as in walk()
+      float s, one_m_s;
+      sig_pair(x, s, one_m_s);
+      const float w = P * one_m_s;  // leaf weight of generation j - 1
+      float* p = acc + 3u * (j - 1u) * kThreads;
+      if (w != 0.0f) {
+        const float ws = w * scale;
+        p[0] += ws;
+        if (!fixed_tau) {
+          p[kThreads] = __fmaf_rn(ws, __fmaf_rn(s, dmu, D_mu), p[kThreads]);
+          p[2 * kThreads] = __fmaf_rn(ws, __fmaf_rn(s, dsig, D_sig), p[2 * kThreads]);
+        }
       }
-    }
-    if (!fixed_tau) {
-      D_mu -= one_m_s * inv_h * dmu;
-      D_sig -= one_m_s * inv_h * dsig;
+      if (!fixed_tau) {
+        D_mu = __fmaf_rn(-one_m_s, dmu, D_mu);
+        D_sig = __fmaf_rn(-one_m_s, dsig, D_sig);
+      }
+      P *= s;
+      if (P < stop) break;
     }
     scale *= 2.0f;
-    P *= s;
-    if (P < stop || ++j > steps) break;
+    if (++j > steps) break;
     zj = fixed_tau ? 0.0f : z[(j - 1) * 32u];
     r.step(zj);
-    dmu += 1.0f;
-    dsig += zj;
+    dmu += inv_h;
+    dsig = __fmaf_rn(zj, inv_h, dsig);
   }
 }
 
