@@ -66,6 +66,10 @@ struct pc_context {
   unsigned long long* stage = nullptr;
   size_t stage_elems = 0;
   uint64_t stage_plan = 0, stage_run = 0;
+  // a second pinned count table: pc_simulate_batch reads one sub-batch's table back while
+  // host threads merge the previous one's
+  unsigned long long* stage2 = nullptr;
+  size_t stage2_elems = 0;
   // the device merge of a plan's result: device scratch (value map, type order, merged
   // counts) and the pinned copy of the merged counts, both grown on demand
   void* merge_dev = nullptr;
@@ -351,7 +355,8 @@ void give_spare(void** spare, size_t* spare_bytes, void* buf, size_t bytes) {
   *spare_bytes = bytes;
 }
 
-// f(i) for i in [0, n) on up to `threads` host threads (0 = all cores).
+// f(i) for i in [0, n) on up to `threads` host threads (0 = all cores), the calling thread
+// among them. A thread that cannot be started leaves its share to the others.
 template <class F>
 void parallel_for(uint32_t n, F&& f, unsigned threads = 0) {
   unsigned nt = threads ? threads : std::max(1u, std::thread::hardware_concurrency());
@@ -361,11 +366,19 @@ void parallel_for(uint32_t n, F&& f, unsigned threads = 0) {
     return;
   }
   std::atomic<uint32_t> next{0};
+  auto work = [&]() {
+    for (uint32_t i; (i = next.fetch_add(1)) < n;) f(i);
+  };
   std::vector<std::thread> pool;
-  for (unsigned t = 0; t < nt; ++t)
-    pool.emplace_back([&]() {
-      for (uint32_t i; (i = next.fetch_add(1)) < n;) f(i);
-    });
+  pool.reserve(nt - 1);
+  for (unsigned t = 0; t + 1 < nt; ++t) {
+    try {
+      pool.emplace_back(work);
+    } catch (...) {
+      break;
+    }
+  }
+  work();
   for (auto& th : pool) th.join();
 }
 
@@ -449,6 +462,7 @@ void pc_destroy(pc_context* ctx) {
   pc_cuda_free(ctx->persist_ctl);
   cudaFreeHost(ctx->pinned);
   cudaFreeHost(ctx->stage);
+  cudaFreeHost(ctx->stage2);
   for (auto& ev : ctx->ev)
     if (ev) cudaEventDestroy(ev);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
@@ -982,6 +996,26 @@ int stage_table(pc_context* ctx, pc_plan* p, const unsigned long long** out) {
     ctx->stage_run = p->run_id;
   }
   *out = ctx->stage;
+  return PC_OK;
+}
+
+// The count table of a run into pinned stage `which` (0: the stage stage_table caches, whose
+// cache this clears; 1: the second stage), without caching.
+int copy_table(pc_context* ctx, pc_plan* p, int which, const unsigned long long** out) {
+  unsigned long long** buf = which ? &ctx->stage2 : &ctx->stage;
+  size_t* cap = which ? &ctx->stage2_elems : &ctx->stage_elems;
+  if (!which) ctx->stage_plan = 0;
+  if (*cap < p->hist_elems) {
+    cudaFreeHost(*buf);
+    *buf = nullptr;
+    *cap = 0;
+    PC_CUDA(ctx, pc_cuda_malloc_host(buf, p->hist_elems * sizeof(unsigned long long)));
+    *cap = p->hist_elems;
+  }
+  PC_CUDA(ctx, pc_cuda_copy(*buf, p->hist_dev, p->hist_elems * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                            ctx->stream));
+  PC_CUDA(ctx, pc_cuda_sync(ctx->stream));
+  *out = *buf;
   return PC_OK;
 }
 
@@ -1722,25 +1756,69 @@ int pc_simulate_batch(pc_context* ctx, const pc_instance* instances, uint32_t n_
   FaultScope fault_scope__(ctx);
   if (!ctx || !out) return fail(ctx, PC_ERR_INVALID, "null argument");
   for (uint32_t i = 0; i < n_instances; ++i) std::memset(out + i, 0, sizeof(pc_histogram));
-  pc_batch* b = nullptr;
-  int rc = pc_batch_create(ctx, instances, n_instances, &b);
-  if (rc != PC_OK) return rc;
-  rc = pc_batch_run(ctx, b);
-  const unsigned long long* h = nullptr;
-  if (rc == PC_OK) rc = batch_table(ctx, b, 0, &h);
-  if (rc == PC_OK) {
-    std::vector<int> codes(n_instances, PC_OK);
-    std::vector<const char*> msgs(n_instances, "");
-    parallel_for(n_instances, [&](uint32_t i) {
-      codes[i] = instance_result(b, b->inst[i], h, out + i, &msgs[i]);
-      out[i].stats.roots = b->inst[i].roots;
+  // Large batches run as consecutive sub-batches of up to 4 parts: host threads merge one
+  // part's histograms (for 4096 instances about 0.5 GB of host output) while the device runs
+  // the next. Every instance's counts depend on that instance alone, so the split changes no
+  // result.
+  const uint32_t parts = std::min<uint32_t>(4u, std::max<uint32_t>(1u, n_instances / 1024u));
+  std::vector<int> codes(n_instances, PC_OK);
+  std::vector<const char*> msgs(n_instances, "");
+  auto merge = [&codes, &msgs, out](pc_batch* b, const unsigned long long* h, uint32_t first) {
+    parallel_for((uint32_t)b->inst.size(), [&](uint32_t i) {
+      codes[first + i] = instance_result(b, b->inst[i], h, out + first + i, &msgs[first + i]);
+      out[first + i].stats.roots = b->inst[i].roots;
     });
-    for (uint32_t i = 0; rc == PC_OK && i < n_instances; ++i)
-      if (codes[i] != PC_OK) rc = fail(ctx, codes[i], msgs[i]);
+  };
+  // the part being merged on its own thread; joined (and its batch destroyed) on every path
+  struct Merging {
+    std::thread th;
+    pc_batch* b = nullptr;
+    void finish() {
+      if (th.joinable()) th.join();
+      pc_batch_destroy(b);
+      b = nullptr;
+    }
+    ~Merging() { finish(); }
+  } merging;
+  int rc = PC_OK;
+  for (uint32_t part = 0; part < parts && rc == PC_OK; ++part) {
+    const uint32_t first = (uint32_t)((uint64_t)n_instances * part / parts);
+    const uint32_t count = (uint32_t)((uint64_t)n_instances * (part + 1) / parts) - first;
+    pc_batch* b = nullptr;
+    rc = pc_batch_create(ctx, instances + first, count, &b);
+    if (rc == PC_OK) rc = pc_batch_run(ctx, b);
+    const unsigned long long* h = nullptr;
+    if (rc == PC_OK) rc = copy_table(ctx, b, (int)(part & 1u), &h);
+    merging.finish();  // the previous part's merge read the other stage
+    if (rc != PC_OK) {
+      pc_batch_destroy(b);
+      break;
+    }
+    merging.b = b;
+    if (part + 1 == parts) {
+      merge(b, h, first);  // nothing left to overlap with
+    } else {
+      try {
+        merging.th = std::thread([merge, &codes, &msgs, b, h, first]() {
+          try {
+            merge(b, h, first);
+          } catch (...) {
+            for (uint32_t i = 0; i < (uint32_t)b->inst.size(); ++i) {
+              codes[first + i] = PC_ERR_NOMEM;
+              msgs[first + i] = "host allocation";
+            }
+          }
+        });
+      } catch (...) {
+        merge(b, h, first);  // no thread to overlap with: merge here
+      }
+    }
   }
+  merging.finish();
+  for (uint32_t i = 0; rc == PC_OK && i < n_instances; ++i)
+    if (codes[i] != PC_OK) rc = fail(ctx, codes[i], msgs[i]);
   if (rc != PC_OK)
     for (uint32_t i = 0; i < n_instances; ++i) pc_histogram_free(out + i);
-  pc_batch_destroy(b);
   return rc;
   PC_GUARD_END(ctx)
 }
@@ -1936,7 +2014,7 @@ struct pc_smooth {
   uint32_t ntypes = 0, paths = 1, rows = 1;
   double h = 0.5;
   uint64_t* bin_start_dev = nullptr;
-  uint32_t* bin_cap_dev = nullptr;
+  uint32_t* bin_cap_dev = nullptr;  // [2 nbins]: phi caps, then the bins' launch order
   int32_t* vidx_dev = nullptr;
   uint32_t* inv_off_dev = nullptr;
   uint32_t* inv_idx_dev = nullptr;
@@ -1965,6 +2043,7 @@ SmoothArgs smooth_args(const pc_context* ctx, const pc_smooth* s) {
   A.inv_h = 1.0 / s->h;
   A.bin_start = s->bin_start_dev;
   A.bin_cap = s->bin_cap_dev;
+  A.bin_order = s->bin_cap_dev + s->I.bin_value.size();
   A.zig = ctx->zig_dev;
   A.error = ctx->error_dev;
   A.order = s->order_dev;
@@ -2067,14 +2146,25 @@ int pc_smooth_create(pc_context* ctx, const pc_bin* bins, uint64_t n_bins, uint3
   cudaStream_t st = ctx->stream;
   cudaError_t e = cudaSetDevice(ctx->device);
   if (e == cudaSuccess) e = pc_cuda_malloc(&s->bin_start_dev, (nb + 1) * sizeof(uint64_t));
-  if (e == cudaSuccess) e = pc_cuda_malloc(&s->bin_cap_dev, std::max<size_t>(1, nb) * sizeof(uint32_t));
+  // caps, then the bins in the order their blocks are launched: most expensive first
+  // (initial cells x generations), so that the last blocks of a launch are short ones
+  std::vector<uint32_t> cap_order(I.cap.begin(), I.cap.end());
+  {
+    std::vector<uint32_t> order(nb);
+    for (size_t b = 0; b < nb; ++b) order[b] = (uint32_t)b;
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) {
+      return I.bin_freq[x] * (I.cap[x] + 1ull) > I.bin_freq[y] * (I.cap[y] + 1ull);
+    });
+    cap_order.insert(cap_order.end(), order.begin(), order.end());
+  }
+  if (e == cudaSuccess) e = pc_cuda_malloc(&s->bin_cap_dev, std::max<size_t>(1, 2 * nb) * sizeof(uint32_t));
   if (e == cudaSuccess) e = pc_cuda_malloc(&s->vidx_dev, std::max<size_t>(1, vidx.size()) * sizeof(int32_t));
   if (e == cudaSuccess) e = pc_cuda_malloc(&s->inv_off_dev, cnt.size() * sizeof(uint32_t));
   if (e == cudaSuccess) e = pc_cuda_malloc(&s->inv_idx_dev, std::max<size_t>(1, inv.size()) * sizeof(uint32_t));
   if (e == cudaSuccess)
     e = pc_cuda_copy(s->bin_start_dev, start.data(), (nb + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess && nb)
-    e = pc_cuda_copy(s->bin_cap_dev, I.cap.data(), nb * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
+    e = pc_cuda_copy(s->bin_cap_dev, cap_order.data(), 2 * nb * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess && !vidx.empty())
     e = pc_cuda_copy(s->vidx_dev, vidx.data(), vidx.size() * sizeof(int32_t), cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess)

@@ -196,6 +196,7 @@ struct SmoothArgs {
   double t_max, inv_h;
   const uint64_t* bin_start;  // [nbins + 1]
   const uint32_t* bin_cap;    // [nbins]
+  const uint32_t* bin_order;  // [nbins] the bins in launch order (most expensive first)
   const ZigTables* zig;
   uint32_t* error;            // bit 1: sampler round budget exhausted
   uint32_t* order;            // [ntypes][ncand] scratch: the candidates of each type by mean

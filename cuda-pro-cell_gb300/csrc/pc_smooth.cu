@@ -384,7 +384,7 @@ __global__ void __launch_bounds__(kThreads, PC_SMOOTH_MIN_BLOCKS) k_smooth_jacob
   __shared__ double u_age[kThreads];
   __shared__ float u_one[kThreads], u_one_lo[kThreads];
   constexpr uint32_t kWarps = kThreads / 32;
-  const uint32_t b = blockIdx.x, k = blockIdx.z;
+  const uint32_t b = A.bin_order[blockIdx.x], k = blockIdx.z;
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   const uint32_t slot = blockIdx.y * 32u + lane;
   const bool live = slot < ncand;
@@ -463,7 +463,7 @@ __global__ void __launch_bounds__(kThreads, PC_SMOOTH_MIN_BLOCKS) k_smooth(const
   __shared__ double u_age[kThreads];
   __shared__ float u_one[kThreads], u_one_lo[kThreads];
   constexpr uint32_t kWarps = kThreads / 32;
-  const uint32_t b = blockIdx.x, k = blockIdx.z;
+  const uint32_t b = A.bin_order[blockIdx.x], k = blockIdx.z;
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   const uint32_t slot = blockIdx.y * 32u + lane;
   const bool live = slot < ncand;

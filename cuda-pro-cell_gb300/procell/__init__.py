@@ -87,30 +87,37 @@ class Plan:
             pass
 
 
+def instance_array(instances):
+    """A pc_instance array of (bins, types, t_max, phi, seed) tuples or dicts, and the numpy
+    arrays it points into (keep them alive while the array is used)."""
+    keep = []
+    arr = (_lib.Instance * max(1, len(instances)))()
+    for i, inst in enumerate(instances):
+        if isinstance(inst, dict):
+            bins, types, t_max = inst["bins"], inst["types"], inst["t_max"]
+            phi, seed = inst.get("phi"), inst.get("seed", 0)
+        else:
+            bins, types, t_max, phi, seed = inst
+        b, t = _lib.bins_numpy(bins), _lib.types_numpy(types)
+        keep += [b, t]
+        arr[i].bins = b.ctypes.data_as(ctypes.POINTER(_lib.Bin))
+        arr[i].n_bins = len(b)
+        arr[i].types = t.ctypes.data_as(ctypes.POINTER(_lib.CellType))
+        arr[i].n_types = len(t)
+        arr[i].reserved = 0
+        arr[i].t_max = float(t_max)
+        arr[i].phi = 0.0 if phi is None else float(phi)
+        arr[i].seed = int(seed)
+    return arr, keep
+
+
 class Batch:
     """Many independent instances in one run (pc_batch). Each instance is a dict or tuple
     (bins, types, t_max, phi, seed); bins may be (values, frequencies) numpy arrays."""
 
     def __init__(self, engine: "Engine", instances):
         self.engine = engine
-        self._keep = []
-        arr = (_lib.Instance * max(1, len(instances)))()
-        for i, inst in enumerate(instances):
-            if isinstance(inst, dict):
-                bins, types, t_max = inst["bins"], inst["types"], inst["t_max"]
-                phi, seed = inst.get("phi"), inst.get("seed", 0)
-            else:
-                bins, types, t_max, phi, seed = inst
-            b, t = _lib.bins_numpy(bins), _lib.types_numpy(types)
-            self._keep += [b, t]
-            arr[i].bins = b.ctypes.data_as(ctypes.POINTER(_lib.Bin))
-            arr[i].n_bins = len(b)
-            arr[i].types = t.ctypes.data_as(ctypes.POINTER(_lib.CellType))
-            arr[i].n_types = len(t)
-            arr[i].reserved = 0
-            arr[i].t_max = float(t_max)
-            arr[i].phi = 0.0 if phi is None else float(phi)
-            arr[i].seed = int(seed)
+        arr, self._keep = instance_array(instances)
         h = ctypes.c_void_p()
         engine._check(engine.L.pc_batch_create(engine.ctx, arr, len(instances), ctypes.byref(h)))
         self.handle = h
@@ -209,6 +216,23 @@ class Engine:
 
     def batch(self, instances) -> Batch:
         return Batch(self, instances)
+
+    def simulate_batch(self, instances) -> list:
+        """pc_simulate_batch: every instance's merged histogram (host inputs in, host results
+        out), as a list of Result."""
+        arr, keep = instance_array(instances)
+        n = len(instances)
+        hs = (_lib.Histogram * max(1, n))()
+        self._check(self.L.pc_simulate_batch(self.ctx, arr, n, hs))
+        out = []
+        try:
+            for i in range(n):
+                out.append(Result(*_lib.histogram_to_numpy(hs[i])))
+        finally:
+            for i in range(n):
+                self.L.pc_histogram_free(ctypes.byref(hs[i]))
+        del keep
+        return out
 
     def simulate(self, bins, types, t_max, phi=None, seed=0, root_begin=None, root_end=None) -> Result:
         p = self.plan(bins, types, t_max, phi, seed)

@@ -172,6 +172,41 @@ def test_batch_of_many_tiny_instances(engine):
     b.close()
 
 
+def tiny_instances(n, seed):
+    rng = np.random.default_rng(seed)
+    instances = []
+    for i in range(n):
+        nb = int(rng.integers(1, 6))
+        bins = [(float(np.exp(rng.uniform(0.0, 7.0))), int(rng.integers(0, 40))) for _ in range(nb)]
+        nt = int(rng.integers(1, 4))
+        r = rng.dirichlet(np.ones(nt))
+        types = [(float(r[k]), float(rng.uniform(5.0, 60.0)), float(rng.uniform(0.5, 10.0))) for k in range(nt)]
+        phi = None if any(f for _, f in bins) else 1.0
+        instances.append((bins, types, float(rng.uniform(0.0, 150.0)), phi, int(rng.integers(0, 2 ** 40))))
+    return instances
+
+
+@pytest.mark.parametrize("n", [7, 2100])
+def test_simulate_batch_matches_one_batch(engine, n):
+    """pc_simulate_batch (host inputs in, merged histograms out) equals pc_batch_result of one
+    batch run, instance by instance. From 2048 instances on it runs the batch as sub-batches,
+    merging one on host threads while the device runs the next: results must not change."""
+    instances = small_uneven(n, seed=5) if n < 100 else tiny_instances(n, seed=77)
+    got = engine.simulate_batch(instances)
+    b = engine.batch(instances)
+    try:
+        b.run()
+        for i in range(n):
+            want = b.result(i)
+            assert np.array_equal(got[i].values, want.values), i
+            assert np.array_equal(got[i].totals, want.totals), i
+            assert np.array_equal(got[i].per_type, want.per_type), i
+            assert got[i].stats["leaves"] == want.stats["leaves"], i
+            assert got[i].stats["roots"] == want.stats["roots"], i
+    finally:
+        b.close()
+
+
 def test_set_types_and_totals(engine):
     """pc_batch_set_types re-parameterises a prepared batch: the next run equals a batch
     created with the new types, instance by instance; pc_batch_totals returns every
