@@ -253,11 +253,12 @@ __device__ __forceinline__ void store_lineage_u(double u, double* u_age, float* 
 
 // One lineage (its normals z[j * 32], j = 0.., and initial age U; 1 + U = u1 + u1_lo) for one
 // type of one candidate, whose remaining time R = T - S_j is carried by `r`. Forward:
-// acc[g * kThreads] += weight * 2^g * w_g. Backward (Ag2[g] = 2^g dL/dE_g): accumulates
-// sum_g Ag2[g] w_g and its derivatives in mean and sd.
+// acc[2g * kThreads] += w_g (compensated; the caller scales row g by ratio / paths * 2^g).
+// Backward (Ag2[g] = 2^g dL/dE_g): accumulates sum_g Ag2[g] w_g and its derivatives in mean
+// and sd.
 template <bool Backward, class Rem>
 __device__ __forceinline__ void walk(const float* z, double u_age, float u1, float u1_lo, float inv_h, uint32_t steps,
-                                     float stop, Rem r, bool fixed_tau, float w_hi, float w_lo, float* acc,
+                                     float stop, Rem r, bool fixed_tau, float* acc,
                                      const float* Ag2, float& f_r, float& f_mu, float& f_sig) {
   // step 1 (the first division, S_1 = tau_1 (1 + U)) is peeled off the loop. The device code
   // is compiled without automatic FMA contraction (the random stream must round as on the
@@ -267,7 +268,6 @@ __device__ __forceinline__ void walk(const float* z, double u_age, float u1, flo
   float dmu = u1 * inv_h, dsig = zj * dmu;    // dS_j / d(mean, sd), divided by h
   float P = 1.0f;                             // s_1 ... s_{j-1}
   float D_mu = 0.0f, D_sig = 0.0f;
-  float wh = w_hi, wl = w_lo;                 // weight * 2^(j-1) as a pair of floats
   for (uint32_t j = 1;;) {
     const float x = r.x(inv_h);
     if (x <= kFar) {
@@ -275,15 +275,9 @@ __device__ __forceinline__ void walk(const float* z, double u_age, float u1, flo
       sig_pair(x, s, one_m_s);
       const float w = P * one_m_s;  // leaf weight of generation j - 1
       if constexpr (!Backward) {
-        if (w != 0.0f) {
-          // (wh + wl) * w as t1 + t2 (t1 rounded, t2 its error plus the low part), added into
-          // the compensated pair at acc[2g] (sum) / acc[2g + 1] (compensation)
-          const float t1 = __fmul_rn(wh, w);
-          const float t2 = __fmaf_rn(wl, w, __fmaf_rn(wh, w, -t1));
-          float* p = acc + 2u * (j - 1u) * kThreads;
-          kahan_add(p, t1);
-          p[kThreads] = __fsub_rn(p[kThreads], t2);
-        }
+        // into the compensated pair at acc[2g] (sum) / acc[2g + 1] (compensation); the
+        // generation's scale ratio / paths * 2^g is applied once per row at the end
+        if (w != 0.0f) kahan_add(acc + 2u * (j - 1u) * kThreads, w);
       } else {
         const float a = Ag2[j - 1];
         if (a != 0.0f && w != 0.0f) {
@@ -302,10 +296,6 @@ __device__ __forceinline__ void walk(const float* z, double u_age, float u1, flo
       P *= s;
       if (P < stop) break;
     }
-    if constexpr (!Backward) {
-      wh = __fmul_rn(wh, 2.0f);
-      wl = __fmul_rn(wl, 2.0f);
-    }
     if (++j > steps) break;
     zj = fixed_tau ? 0.0f : z[(j - 1) * 32u];
     r.step(zj);
@@ -315,7 +305,8 @@ __device__ __forceinline__ void walk(const float* z, double u_age, float u1, flo
 }
 
 // One lineage for one type, forward mode: for every generation g it reaches, acc rows
-// 3g, 3g + 1, 3g + 2 gain 2^g w_g and 2^g dw_g/d(mean, sd) (per-thread FP32 sums).
+// 3g, 3g + 1, 3g + 2 gain w_g and dw_g/d(mean, sd) (per-thread FP32 sums; the caller scales
+// generation g's rows by 2^g).
 template <class Rem>
 __device__ __forceinline__ void walk_jacobian(const float* z, double u_age, float u1, float u1_lo, float inv_h,
                                               uint32_t steps, float stop, Rem r, bool fixed_tau, float* acc) {
@@ -324,7 +315,6 @@ __device__ __forceinline__ void walk_jacobian(const float* z, double u_age, floa
   r.first(zj, u_age, u1, u1_lo);
   float dmu = u1 * inv_h, dsig = zj * dmu;
   float P = 1.0f, D_mu = 0.0f, D_sig = 0.0f;  // P = s_1 ... s_{j-1}
-  float scale = 1.0f;  // 2^(j-1)
   for (uint32_t j = 1;;) {
     const float x = r.x(inv_h);
     if (x <= kFar) {  // as in walk()
@@ -332,12 +322,11 @@ __device__ __forceinline__ void walk_jacobian(const float* z, double u_age, floa
       sig_pair(x, s, one_m_s);
       const float w = P * one_m_s;  // leaf weight of generation j - 1
       float* p = acc + 3u * (j - 1u) * kThreads;
-      if (w != 0.0f) {
-        const float ws = w * scale;
-        p[0] += ws;
+      if (w != 0.0f) {  // generation j - 1's scale 2^(j-1) is applied per row at the end
+        p[0] += w;
         if (!fixed_tau) {
-          p[kThreads] = __fmaf_rn(ws, __fmaf_rn(s, dmu, D_mu), p[kThreads]);
-          p[2 * kThreads] = __fmaf_rn(ws, __fmaf_rn(s, dsig, D_sig), p[2 * kThreads]);
+          p[kThreads] = __fmaf_rn(w, __fmaf_rn(s, dmu, D_mu), p[kThreads]);
+          p[2 * kThreads] = __fmaf_rn(w, __fmaf_rn(s, dsig, D_sig), p[2 * kThreads]);
         }
       }
       if (!fixed_tau) {
@@ -347,7 +336,6 @@ __device__ __forceinline__ void walk_jacobian(const float* z, double u_age, floa
       P *= s;
       if (P < stop) break;
     }
-    scale *= 2.0f;
     if (++j > steps) break;
     zj = fixed_tau ? 0.0f : z[(j - 1) * 32u];
     r.step(zj);
@@ -360,10 +348,10 @@ __device__ __forceinline__ void walk_jacobian(const float* z, double u_age, floa
 // out of line so that the compiler cannot merge them into the FP32 walks as predicated code.
 template <bool Backward>
 __device__ __noinline__ float3 walk_fp64(const float* z, double u_age, float u1, float u1_lo, float inv_h,
-                                         uint32_t steps, float stop, RemFp64 r, bool fixed_tau, float w_hi, float w_lo,
-                                         float* acc, const float* Ag2) {
+                                         uint32_t steps, float stop, RemFp64 r, bool fixed_tau, float* acc,
+                                         const float* Ag2) {
   float f_r = 0.0f, f_mu = 0.0f, f_sig = 0.0f;
-  walk<Backward>(z, u_age, u1, u1_lo, inv_h, steps, stop, r, fixed_tau, w_hi, w_lo, acc, Ag2, f_r, f_mu, f_sig);
+  walk<Backward>(z, u_age, u1, u1_lo, inv_h, steps, stop, r, fixed_tau, acc, Ag2, f_r, f_mu, f_sig);
   return make_float3(f_r, f_mu, f_sig);
 }
 
@@ -434,8 +422,8 @@ __global__ void __launch_bounds__(kThreads, PC_SMOOTH_MIN_BLOCKS) k_smooth_jacob
     __syncwarp();
   }
   __syncthreads();
-  // sums over the warps in warp order; lane l of every warp holds candidate 32 * group + l,
-  // so the warps split the rows
+  // sums over the warps in warp order, generation g's rows scaled by 2^g; lane l of every
+  // warp holds candidate 32 * group + l, so the warps split the rows
   if (!live) return;
   const double inv_paths = 1.0 / (double)A.paths;
   double* o = out + ((uint64_t)c * A.nbins + b) * A.rows * KQ + 3u * k;
@@ -443,7 +431,7 @@ __global__ void __launch_bounds__(kThreads, PC_SMOOTH_MIN_BLOCKS) k_smooth_jacob
     double v = 0.0;
 #pragma unroll
     for (uint32_t w = 0; w < kWarps; ++w) v += (double)facc[q * kThreads + w * 32u + lane];
-    o[(q / 3u) * KQ + q % 3u] = v * (q % 3u == 0u ? 1.0 : ratio) * inv_paths;
+    o[(q / 3u) * KQ + q % 3u] = ldexp(v * (q % 3u == 0u ? 1.0 : ratio) * inv_paths, (int)(q / 3u));
   }
 }
 
@@ -491,15 +479,9 @@ __global__ void __launch_bounds__(kThreads, PC_SMOOTH_MIN_BLOCKS) k_smooth(const
   }
   const double* my_prm = params + (uint64_t)(live ? c : 0u) * KQ + 3u * k;
   const double mu = live ? my_prm[1] : 0.0, sd = live ? my_prm[2] : 0.0;
-  // ratio / paths as a pair of floats (the forward's weight)
-  float w_hi = 0.0f, w_lo = 0.0f;
-  if (!Backward && live) {
-    const double wt = my_prm[0] / (double)A.paths;
-    w_hi = __double2float_rn(wt);
-    w_lo = __double2float_rn(wt - (double)w_hi);
-  }
   const bool quiescent = mu < 0.0, fixed_tau = mu == 0.0;
-  const bool walks = Backward || w_hi != 0.0f;
+  // a type of ratio 0 adds nothing to the expected counts (its adjoint rows still count)
+  const bool walks = Backward || (live && my_prm[0] != 0.0);
   __syncthreads();
   const uint64_t r0 = __ldg(A.bin_start + b), r1 = __ldg(A.bin_start + b + 1);
   float* fmy = facc + threadIdx.x;
@@ -521,44 +503,43 @@ __global__ void __launch_bounds__(kThreads, PC_SMOOTH_MIN_BLOCKS) k_smooth(const
     __syncwarp();
     const uint32_t n = (uint32_t)((nlin - base) < 32u ? (nlin - base) : 32u);
     if (live) {
+      float f_r = 0.0f, f_mu = 0.0f, f_sig = 0.0f;  // adjoint terms of these (up to) 32 lineages
       for (uint32_t ii = 0; ii < n; ++ii) {
-        float f_r = 0.0f, f_mu = 0.0f, f_sig = 0.0f;  // this lineage's adjoint terms
         if (quiescent) {
           // quiescent type: a leaf at generation 0 (cell.cu:69-75)
           if constexpr (Backward) {
-            f_r = my_ag[0];
-          } else {
-            kahan_add(fmy, w_hi);
-            fmy[kThreads] = __fsub_rn(fmy[kThreads], w_lo);
+            f_r += my_ag[0];
+          } else if (walks) {
+            kahan_add(fmy, 1.0f);
           }
         } else if (walks) {
           const uint32_t li = warp * 32u + ii;
           if (grid)
-            walk<Backward>(zbuf + ii, u_age[li], u_one[li], u_one_lo[li], inv_h, steps, stop, rg, fixed_tau, w_hi,
-                           w_lo, fmy, my_ag, f_r, f_mu, f_sig);
+            walk<Backward>(zbuf + ii, u_age[li], u_one[li], u_one_lo[li], inv_h, steps, stop, rg, fixed_tau, fmy,
+                           my_ag, f_r, f_mu, f_sig);
           else {
             const float3 f = walk_fp64<Backward>(zbuf + ii, u_age[li], u_one[li], u_one_lo[li], inv_h, steps, stop,
-                                                 rd, fixed_tau, w_hi, w_lo, fmy, my_ag);
-            f_r = f.x;
-            f_mu = f.y;
-            f_sig = f.z;
+                                                 rd, fixed_tau, fmy, my_ag);
+            f_r += f.x;
+            f_mu += f.y;
+            f_sig += f.z;
           }
         }
-        if constexpr (Backward) {
-          // per-thread compensated FP32 sums (terms of either sign cancel); scaled by
-          // ratio / paths once, at the end
-          kahan_add(fmy, f_r);
-          kahan_add(fmy + 2 * kThreads, f_mu);
-          kahan_add(fmy + 4 * kThreads, f_sig);
-        }
+      }
+      if constexpr (Backward) {
+        // per-thread compensated FP32 sums over the batches of 32 lineages (terms of either
+        // sign cancel); scaled by ratio / paths once, at the end
+        kahan_add(fmy, f_r);
+        kahan_add(fmy + 2 * kThreads, f_mu);
+        kahan_add(fmy + 4 * kThreads, f_sig);
       }
     }
     __syncwarp();
   }
   __syncthreads();
-  // sums over the warps in warp order (adjoint rows scaled by 1 / paths, and those of mean
-  // and sd by the ratio); lane l of every warp holds candidate 32 * group + l, so the warps
-  // split the rows
+  // sums over the warps in warp order (forward row g scaled by ratio / paths * 2^g, adjoint
+  // rows by 1 / paths, and those of mean and sd by the ratio); lane l of every warp holds
+  // candidate 32 * group + l, so the warps split the rows
   if (!live) return;
   const double inv_paths = 1.0 / (double)A.paths, ratio = my_prm[0];
   const uint32_t nrows = Backward ? 3u : A.rows;
@@ -569,7 +550,10 @@ __global__ void __launch_bounds__(kThreads, PC_SMOOTH_MIN_BLOCKS) k_smooth(const
 #pragma unroll
     for (uint32_t w = 0; w < kWarps; ++w)
       v += (double)facc[2 * q * kThreads + w * 32u + lane] - (double)facc[(2 * q + 1) * kThreads + w * 32u + lane];
-    if constexpr (Backward) v *= (q == 0u ? 1.0 : ratio) * inv_paths;
+    if constexpr (Backward)
+      v *= (q == 0u ? 1.0 : ratio) * inv_paths;
+    else
+      v *= ldexp(ratio * inv_paths, (int)q);
     o[q] = v;
   }
 }
