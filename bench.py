@@ -800,7 +800,41 @@ def measure_calibration(eng, local, steps, warmup, cpu_seconds, pso_seconds, ext
         g, L = step(theta)
     e1.record(stream)
     torch.cuda.synchronize()
-    elapsed_ms = e0.elapsed_time(e1)
+    eager_ms = e0.elapsed_time(e1)
+    # the same step captured once into a CUDA graph and replayed, as the Levenberg-Marquardt
+    # harness runs its iterations: the library's six kernels and the loss arithmetic without
+    # a host launch each (checked bit for bit against the eager step)
+    th_static = theta.clone()
+    graph, graph_note = None, None
+    try:
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            step(th_static)  # library scratch allocated outside the capture
+        torch.cuda.current_stream().wait_stream(side)
+        cg = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(cg):
+            g_static, L_static = step(th_static)
+        cg.replay()
+        g_ref, L_ref = step(th_static)
+        torch.cuda.synchronize()
+        if torch.equal(g_static, g_ref) and torch.equal(L_static, L_ref):
+            graph = cg
+        else:
+            graph_note = "graph replay differs from the eager step; eager timings reported"
+    except Exception as ex:  # capture unavailable: the eager loop stands
+        graph_note = "no graph: " + repr(ex)[:200]
+    elapsed_ms = eager_ms
+    if graph is not None:
+        for _ in range(warmup):
+            graph.replay()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(steps):
+            graph.replay()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        elapsed_ms = e0.elapsed_time(e1)
     # end to end: parameters from pinned host memory, gradients and losses back to the host
     host_theta = theta.cpu().pin_memory()
     out_g = torch.empty((C, prob.n_types, 3), dtype=torch.float64).pin_memory()
@@ -808,8 +842,13 @@ def measure_calibration(eng, local, steps, warmup, cpu_seconds, pso_seconds, ext
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(steps):
-        th = host_theta.to("cuda", non_blocking=True)
-        g, L = step(th)
+        if graph is not None:
+            th_static.copy_(host_theta, non_blocking=True)
+            graph.replay()
+            g, L = g_static, L_static
+        else:
+            th = host_theta.to("cuda", non_blocking=True)
+            g, L = step(th)
         out_g.copy_(g, non_blocking=True)
         out_l.copy_(L, non_blocking=True)
     torch.cuda.synchronize()
@@ -886,7 +925,11 @@ def measure_calibration(eng, local, steps, warmup, cpu_seconds, pso_seconds, ext
         "config": {"workload": "calibration: 256 bins, 1e5 cells, 3 types, %d candidates, t_max 168, h 0.5, "
                                "%d lineages per cell; a step = smoothed forward + loss gradient + adjoint"
                                % (C, prob.smooth_paths),
+                   "launch": ("the step replayed from a CUDA graph captured once (bit-identical to the eager "
+                              "step)" if graph is not None else "eager: " + str(graph_note)),
                    "l2": "inputs (bins, parameters) are a few MB; the kernels are compute bound"},
+        "eager": {"ms_per_step": eager_ms / steps, "grads_per_s": C * steps / (eager_ms * 1e-3),
+                  "what": "the same step launched call by call (library calls and torch operations)"},
         "calibration": comp,
         "calibration_other_seeds": {
             "swarm_seconds": extra_pso_seconds, "results": others,
