@@ -52,6 +52,7 @@ struct pc_context {
   int opt_config = kDefaultSweepConfig;  // sweep configuration (narrow key layout)
   int opt_driver = 0;                    // 0: one launch per sweep, 1: persistent launch
   int opt_graph = 0;                     // persistent driver: replay a captured CUDA graph
+  int opt_smooth_predraw = 1;            // smoothed plans keep their lineages' draws in HBM
   // resident blocks per SM of each configuration's kernels: [narrow][batched][config]
   int occ[2][2][kNumSweepConfigs][3] = {};
   uint32_t* persist_ctl = nullptr;       // [2] barrier + [8] run totals (u64 [4])
@@ -500,6 +501,8 @@ int pc_set_option(pc_context* ctx, const char* name, double value) {
     ctx->opt_driver = (int)value;
   } else if (n == "graph") {
     ctx->opt_graph = value != 0.0 ? 1 : 0;
+  } else if (n == "smooth_predraw") {
+    ctx->opt_smooth_predraw = value != 0.0 ? 1 : 0;
   } else if (n == "fail_nth_call") {
     // counted from the calls made so far: the n-th call after this one fails (0: none)
     ctx->fail_at = value >= 1.0 ? ctx->cuda_calls + (uint64_t)value : 0;
@@ -2025,6 +2028,9 @@ struct pc_smooth {
   uint32_t jac_cap = 0;
   uint32_t* order_dev = nullptr;  // [ntypes][order_cap]: candidates by mean, per type
   uint32_t order_cap = 0;
+  float* lin_z_dev = nullptr;      // [lineages][zrow]: every lineage's normals (null: drawn per pass)
+  LineageU* lin_u_dev = nullptr;   // [lineages]: every lineage's initial age
+  uint32_t zrow = 0;
 };
 
 namespace {
@@ -2047,6 +2053,9 @@ SmoothArgs smooth_args(const pc_context* ctx, const pc_smooth* s) {
   A.zig = ctx->zig_dev;
   A.error = ctx->error_dev;
   A.order = s->order_dev;
+  A.lin_z = s->lin_z_dev;
+  A.lin_u = s->lin_u_dev;
+  A.zrow = s->zrow;
   return A;
 }
 
@@ -2171,6 +2180,18 @@ int pc_smooth_create(pc_context* ctx, const pc_bin* bins, uint64_t n_bins, uint3
     e = pc_cuda_copy(s->inv_off_dev, cnt.data(), cnt.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess && !inv.empty())
     e = pc_cuda_copy(s->inv_idx_dev, inv.data(), inv.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
+  // Every lineage's draws (normals and initial age depend on the seed and the bins, not on
+  // the parameters), made once here when they fit in 1 GB: every pass then reads them back
+  // instead of drawing them again in each of its (bin, candidate group, type) blocks.
+  const uint64_t nlin = s->I.roots * s->paths;
+  const uint32_t zrow = (s->rows + 3u) & ~3u;
+  const uint64_t lin_bytes = nlin * zrow * sizeof(float) + nlin * sizeof(LineageU);
+  if (e == cudaSuccess && ctx->opt_smooth_predraw && nlin > 0 && lin_bytes <= (uint64_t(1) << 30)) {
+    s->zrow = zrow;
+    e = pc_cuda_malloc(&s->lin_z_dev, nlin * zrow * sizeof(float));
+    if (e == cudaSuccess) e = pc_cuda_malloc(&s->lin_u_dev, nlin * sizeof(LineageU));
+    if (e == cudaSuccess) e = PC_LAUNCH(launch_smooth_draws(smooth_args(ctx, s), s->lin_z_dev, s->lin_u_dev, st));
+  }
   if (e == cudaSuccess) e = pc_cuda_sync(st);
   if (e != cudaSuccess) {
     pc_smooth_destroy(s);
@@ -2295,6 +2316,8 @@ void pc_smooth_destroy(pc_smooth* s) {
   pc_cuda_free(s->part_dev);
   pc_cuda_free(s->jac_raw_dev);
   pc_cuda_free(s->order_dev);
+  pc_cuda_free(s->lin_z_dev);
+  pc_cuda_free(s->lin_u_dev);
   delete s;
 }
 

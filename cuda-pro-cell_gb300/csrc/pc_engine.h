@@ -188,6 +188,12 @@ int launch_barrier_probe(uint32_t* bar, unsigned long long timeout_ns, unsigned 
 constexpr int kSmoothMaxTypes = 8;
 constexpr int kSmoothMaxRows = 64;  // generations per bin (cap + 1)
 
+// A sampled lineage's initial age: U (FP64 form) and 1 + U as a pair of floats hi + lo.
+struct LineageU {
+  double u;
+  float hi, lo;
+};
+
 struct SmoothArgs {
   uint32_t k0, k1;            // seed
   uint32_t nbins, rows;       // rows = max cap + 1 (generation rows per bin)
@@ -200,8 +206,16 @@ struct SmoothArgs {
   const ZigTables* zig;
   uint32_t* error;            // bit 1: sampler round budget exhausted
   uint32_t* order;            // [ntypes][ncand] scratch: the candidates of each type by mean
+  // the lineages' draws, made once per smoothed plan (null: drawn in every pass):
+  // lin_z[L * zrow + j], j < the bin's cap + 1, and lin_u[L] for lineage L = first initial
+  // cell of its bin x paths + its index in the bin
+  const float* lin_z;
+  const LineageU* lin_u;
+  uint32_t zrow;              // floats per lineage in lin_z, a multiple of 4
 };
 
+// Every lineage's draws into lin_z / lin_u (params-independent: once per smoothed plan).
+int launch_smooth_draws(const SmoothArgs& A, float* lin_z, LineageU* lin_u, void* stream);
 // e_raw[c][k][b][g] (FP64) for params[c][k][3] = (ratio, mean, sd): type k's part.
 int launch_smooth_forward(const SmoothArgs& A, const double* params, uint32_t ncand, double* e_raw,
                           void* stream);

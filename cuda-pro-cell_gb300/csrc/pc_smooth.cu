@@ -28,10 +28,12 @@
 //
 // Work layout: one block per (bin, group of 32 candidates, type); lane l of every warp is
 // candidate 32 * group + l, and the block's 4 warps take the bin's lineages 32 at a time:
-// first each lane draws one lineage's normals (one Philox block and ziggurat draw per
-// generation) into shared memory, then every lane walks all 32 lineages for its own
-// candidate, reading the shared draws. Each normal is thus drawn once per 32 candidates and
-// type. Remaining time R = T - S is carried on the FP32 pipe as a float on a fixed grid plus
+// first each lane stages one lineage's normals into shared memory, then every lane walks all
+// 32 lineages for its own candidate, reading the shared draws. The draws depend on the seed
+// and the bins only: a smoothed plan makes them once (k_smooth_draws: one Philox block and
+// ziggurat draw per generation) and keeps them in device memory, so a pass only reads them
+// back (plans too large for that draw them in every block, once per 32 candidates and type).
+// Remaining time R = T - S is carried on the FP32 pipe as a float on a fixed grid plus
 // a float remainder (RemGrid: exact grid sums, 11 FP32 operations per step; GB300's FP64
 // pipe has 2 lanes per clock per SM), or in FP64 where that form's error bound would exceed
 // 2^-22 h (RemFp64). Per-thread partial sums
@@ -110,6 +112,15 @@ __device__ __forceinline__ void sig_pair(float x, float& s, float& one_m_s) {
   const float eq = e * q;
   s = x >= 0.0f ? q : eq;
   one_m_s = x >= 0.0f ? eq : q;
+}
+
+// x == 0.0 and x < 0.0 (for x not NaN) on the integer pipes.
+__device__ __forceinline__ bool zero_bits(double x) {
+  return ((unsigned long long)__double_as_longlong(x) << 1) == 0ull;
+}
+__device__ __forceinline__ bool neg_nonzero(double x) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  return (u >> 63) != 0ull && (u << 1) != 0ull;
 }
 
 // A double rounded toward zero to float on the integer pipes (GB300 runs FP64<->FP32
@@ -225,9 +236,9 @@ constexpr float kFar = 24.0f;
 // Lineage i of a bin whose initial cells start at r0 (initial cell r0 + i / paths, replica
 // i % paths, which draws as initial cell r + replica * ncells): its initial age, and the
 // normals of the nodes it visits (heap nodes 1, 2 + b_1, ..., b_j the path bits) into
-// z[j * 32], j < steps.
+// z[j * zstride], j < steps.
 __device__ __forceinline__ void draw_lineage(const SmoothArgs& A, const ZigTables& Z, uint64_t r0, uint64_t i,
-                                             uint32_t steps, float* z, double& u_age) {
+                                             uint32_t steps, float* z, uint32_t zstride, double& u_age) {
   const uint32_t m = (uint32_t)(i % A.paths);
   const uint32_t root = (uint32_t)(r0 + i / A.paths) + m * A.ncells;
   const u32x4 R = philox(u32x4{0u, 0u, root, kPurposeRoot}, A.k0, A.k1);
@@ -236,19 +247,47 @@ __device__ __forceinline__ void draw_lineage(const SmoothArgs& A, const ZigTable
   const uint64_t bits = (uint64_t)B.x | ((uint64_t)B.y << 32);
   uint64_t node = 1;
   for (uint32_t j = 0; j < steps; ++j) {
-    z[j * 32u] = node_z(node, root, A.k0, A.k1, Z, A.error);
+    z[j * zstride] = node_z(node, root, A.k0, A.k1, Z, A.error);
     node = 2ull * node + ((bits >> j) & 1ull);
   }
 }
 
 // A lineage's initial age U for the walks of all 32 candidates: U itself (FP64 form) and
 // 1 + U as a pair of floats hi + lo (grid form; hi is also the FP32 dS_1/dmean).
-__device__ __forceinline__ void store_lineage_u(double u, double* u_age, float* hi, float* lo) {
+__device__ __forceinline__ LineageU lineage_u(double u) {
   const double one = 1.0 + u;
   const float h = __double2float_rn(one);
-  *u_age = u;
-  *hi = h;
-  *lo = __double2float_rn(one - (double)h);
+  return LineageU{u, h, __double2float_rn(one - (double)h)};
+}
+
+// Lineage base + lane of a bin (initial cells from r0) into the warp's shared-memory draws
+// zbuf[j * 32 + lane] and the block's u tables: read back from the plan's lineage tables
+// (Kept), or drawn here when the plan keeps none. The kernels are instantiated for both, so
+// neither path's code (the draw's FP64 set-up in particular) runs predicated in the other.
+template <bool Kept>
+__device__ __forceinline__ void stage_lineage(const SmoothArgs& A, const ZigTables& Z, uint64_t r0, uint64_t i,
+                                              uint32_t steps, float* zlane, double* u_age, float* u_one,
+                                              float* u_one_lo) {
+  LineageU lu;
+  if constexpr (Kept) {
+    const uint64_t L = r0 * A.paths + i;
+    const float4* zr = reinterpret_cast<const float4*>(A.lin_z + L * A.zrow);
+    for (uint32_t j = 0; j < steps; j += 4u) {
+      const float4 q = __ldg(zr + j / 4u);
+      zlane[j * 32u] = q.x;
+      if (j + 1u < steps) zlane[(j + 1u) * 32u] = q.y;
+      if (j + 2u < steps) zlane[(j + 2u) * 32u] = q.z;
+      if (j + 3u < steps) zlane[(j + 3u) * 32u] = q.w;
+    }
+    lu = A.lin_u[L];
+  } else {
+    double u;
+    draw_lineage(A, Z, r0, i, steps, zlane, 32u, u);
+    lu = lineage_u(u);
+  }
+  *u_age = lu.u;
+  *u_one = lu.hi;
+  *u_one_lo = lu.lo;
 }
 
 // One lineage (its normals z[j * 32], j = 0.., and initial age U; 1 + U = u1 + u1_lo) for one
@@ -364,6 +403,7 @@ __device__ __noinline__ void walk_jacobian_fp64(const float* z, double u_age, fl
 // = (sum 2^g w_g / paths, ratio_k / paths * sum 2^g dw_g/dmean, the same for sd), i.e.
 // d E_{b,g} / d(ratio_k, mean_k, sd_k); every block draws its bin's lineages itself (the
 // draws are shared by the 32 candidates of a warp, not across types).
+template <bool Kept>
 __global__ void __launch_bounds__(kThreads, PC_SMOOTH_MIN_BLOCKS) k_smooth_jacobian(const SmoothArgs A, const double* __restrict__ params,
                                                               uint32_t ncand, double* __restrict__ out) {
   // dynamic: per-thread sums [3 * rows][kThreads], then the lineage draws [kWarps][rows][32]
@@ -388,7 +428,7 @@ __global__ void __launch_bounds__(kThreads, PC_SMOOTH_MIN_BLOCKS) k_smooth_jacob
     mu = params[(uint64_t)c * KQ + 3u * k + 1u];
     sd = params[(uint64_t)c * KQ + 3u * k + 2u];
   }
-  const bool quiescent = mu < 0.0, fixed_tau = mu == 0.0;
+  const bool quiescent = neg_nonzero(mu), fixed_tau = zero_bits(mu);
   __syncthreads();
   const uint32_t steps = __ldg(A.bin_cap + b) + 1u;
   const uint64_t r0 = __ldg(A.bin_start + b), r1 = __ldg(A.bin_start + b + 1);
@@ -400,11 +440,9 @@ __global__ void __launch_bounds__(kThreads, PC_SMOOTH_MIN_BLOCKS) k_smooth_jacob
   const float stop = stop_level(steps);  // once per block: the walks' stopping threshold
   const uint64_t nlin = (r1 - r0) * A.paths;
   for (uint64_t base = (uint64_t)warp * 32u; base < nlin; base += 32u * kWarps) {
-    if (base + lane < nlin) {
-      double u;
-      draw_lineage(A, Z, r0, base + lane, steps, zbuf + lane, u);
-      store_lineage_u(u, u_age + threadIdx.x, u_one + threadIdx.x, u_one_lo + threadIdx.x);
-    }
+    if (base + lane < nlin)
+      stage_lineage<Kept>(A, Z, r0, base + lane, steps, zbuf + lane, u_age + threadIdx.x, u_one + threadIdx.x,
+                          u_one_lo + threadIdx.x);
     __syncwarp();
     const uint32_t n = (uint32_t)((nlin - base) < 32u ? (nlin - base) : 32u);
     if (live) {
@@ -438,7 +476,7 @@ __global__ void __launch_bounds__(kThreads, PC_SMOOTH_MIN_BLOCKS) k_smooth_jacob
 // Forward (e_raw[c][k][b][g] = ratio_k / paths * sum 2^g w_g over the bin's lineages) and
 // adjoint (part[c][b][3k + q] = d(sum_g A_g E_g)/d(ratio_k, mean_k, sd_k)) of one type: block
 // (bin, group of 32 candidates, type k). Every block draws its bin's lineages itself.
-template <bool Backward>
+template <bool Backward, bool Kept>
 __global__ void __launch_bounds__(kThreads, PC_SMOOTH_MIN_BLOCKS) k_smooth(const SmoothArgs A, const double* __restrict__ params,
                                                      uint32_t ncand, const double* __restrict__ grad_expected,
                                                      uint32_t nvalues, const int32_t* __restrict__ vidx,
@@ -479,9 +517,11 @@ __global__ void __launch_bounds__(kThreads, PC_SMOOTH_MIN_BLOCKS) k_smooth(const
   }
   const double* my_prm = params + (uint64_t)(live ? c : 0u) * KQ + 3u * k;
   const double mu = live ? my_prm[1] : 0.0, sd = live ? my_prm[2] : 0.0;
-  const bool quiescent = mu < 0.0, fixed_tau = mu == 0.0;
+  // per-block flags from the parameters' bits (integer tests: nothing for the FP64 pipe to
+  // redo inside the lineage loops)
+  const bool quiescent = neg_nonzero(mu), fixed_tau = zero_bits(mu);
   // a type of ratio 0 adds nothing to the expected counts (its adjoint rows still count)
-  const bool walks = Backward || (live && my_prm[0] != 0.0);
+  const bool walks = Backward || (live && !zero_bits(my_prm[0]));
   __syncthreads();
   const uint64_t r0 = __ldg(A.bin_start + b), r1 = __ldg(A.bin_start + b + 1);
   float* fmy = facc + threadIdx.x;
@@ -494,12 +534,10 @@ __global__ void __launch_bounds__(kThreads, PC_SMOOTH_MIN_BLOCKS) k_smooth(const
   // lineage i of the bin: initial cell r0 + i / paths, replica i % paths
   const uint64_t nlin = (r1 - r0) * A.paths;
   for (uint64_t base = (uint64_t)warp * 32u; base < nlin; base += 32u * kWarps) {
-    // this lane draws lineage base + lane
-    if (base + lane < nlin) {
-      double u;
-      draw_lineage(A, Z, r0, base + lane, steps, zbuf + lane, u);
-      store_lineage_u(u, u_age + threadIdx.x, u_one + threadIdx.x, u_one_lo + threadIdx.x);
-    }
+    // this lane stages lineage base + lane
+    if (base + lane < nlin)
+      stage_lineage<Kept>(A, Z, r0, base + lane, steps, zbuf + lane, u_age + threadIdx.x, u_one + threadIdx.x,
+                          u_one_lo + threadIdx.x);
     __syncwarp();
     const uint32_t n = (uint32_t)((nlin - base) < 32u ? (nlin - base) : 32u);
     if (live) {
@@ -555,6 +593,26 @@ __global__ void __launch_bounds__(kThreads, PC_SMOOTH_MIN_BLOCKS) k_smooth(const
     else
       v *= ldexp(ratio * inv_paths, (int)q);
     o[q] = v;
+  }
+}
+
+// Every lineage's draws (normals of its path, initial age), which depend on the seed and the
+// bins but not on the parameters: block b takes bin b's lineages.
+__global__ void __launch_bounds__(256) k_smooth_draws(const SmoothArgs A, float* __restrict__ lin_z,
+                                                      LineageU* __restrict__ lin_u) {
+  __shared__ ZigTables Z;
+  for (uint32_t i = threadIdx.x; i < sizeof(ZigTables) / 4; i += blockDim.x)
+    reinterpret_cast<uint32_t*>(&Z)[i] = __ldg(reinterpret_cast<const uint32_t*>(A.zig) + i);
+  __syncthreads();
+  const uint32_t b = blockIdx.x;
+  const uint64_t r0 = __ldg(A.bin_start + b), r1 = __ldg(A.bin_start + b + 1);
+  const uint32_t steps = __ldg(A.bin_cap + b) + 1u;
+  const uint64_t nlin = (r1 - r0) * A.paths;
+  for (uint64_t i = threadIdx.x; i < nlin; i += blockDim.x) {
+    const uint64_t L = r0 * A.paths + i;
+    double u;
+    draw_lineage(A, Z, r0, i, steps, lin_z + L * A.zrow, 1u, u);
+    lin_u[L] = lineage_u(u);
   }
 }
 
@@ -744,21 +802,48 @@ int smem_bytes(uint32_t out_rows, uint32_t rows) {
   return (int)((2u * out_rows + rows) * kThreads * sizeof(float));
 }
 
-template <bool Backward>
-int launch_smooth_t(const SmoothArgs& A, const double* params, uint32_t ncand, const double* grad_expected,
+template <bool Backward, bool Kept>
+int launch_smooth_k(const SmoothArgs& A, const double* params, uint32_t ncand, const double* grad_expected,
                     uint32_t nvalues, const int32_t* vidx, double* out, cudaStream_t st) {
   const int smem = smem_bytes(Backward ? 3u : A.rows, A.rows);
   // static shared memory plus `smem` may exceed the default 48 KB: always opt in
-  const cudaError_t e = cudaFuncSetAttribute(k_smooth<Backward>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  const cudaError_t e =
+      cudaFuncSetAttribute(k_smooth<Backward, Kept>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return (int)e;
   const int eo = launch_order(A, params, ncand, st);
   if (eo != 0) return eo;
   const dim3 grid(A.nbins, (ncand + 31u) / 32u, A.ntypes);
-  k_smooth<Backward><<<grid, kThreads, smem, st>>>(A, params, ncand, grad_expected, nvalues, vidx, out);
+  k_smooth<Backward, Kept><<<grid, kThreads, smem, st>>>(A, params, ncand, grad_expected, nvalues, vidx, out);
+  return (int)cudaGetLastError();
+}
+
+template <bool Backward>
+int launch_smooth_t(const SmoothArgs& A, const double* params, uint32_t ncand, const double* grad_expected,
+                    uint32_t nvalues, const int32_t* vidx, double* out, cudaStream_t st) {
+  return A.lin_z ? launch_smooth_k<Backward, true>(A, params, ncand, grad_expected, nvalues, vidx, out, st)
+                 : launch_smooth_k<Backward, false>(A, params, ncand, grad_expected, nvalues, vidx, out, st);
+}
+
+// The Jacobian kernel of a plan that keeps its lineage draws or not.
+int launch_jacobian_k(const SmoothArgs& A, const double* params, uint32_t ncand, double* jac_raw, cudaStream_t st) {
+  const int smem = (int)(4u * A.rows * kThreads * sizeof(float));
+  auto* k = A.lin_z ? k_smooth_jacobian<true> : k_smooth_jacobian<false>;
+  const cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return (int)e;
+  const int eo = launch_order(A, params, ncand, st);
+  if (eo != 0) return eo;
+  const dim3 grid(A.nbins, (ncand + 31u) / 32u, A.ntypes);
+  k<<<grid, kThreads, smem, st>>>(A, params, ncand, jac_raw);
   return (int)cudaGetLastError();
 }
 
 }  // namespace
+
+int launch_smooth_draws(const SmoothArgs& A, float* lin_z, LineageU* lin_u, void* stream) {
+  if (A.nbins == 0) return 0;
+  k_smooth_draws<<<A.nbins, 256, 0, (cudaStream_t)stream>>>(A, lin_z, lin_u);
+  return (int)cudaGetLastError();
+}
 
 int launch_smooth_forward(const SmoothArgs& A, const double* params, uint32_t ncand, double* e_raw, void* stream) {
   if (ncand == 0 || A.nbins == 0) return 0;
@@ -787,13 +872,8 @@ int launch_smooth_jacobian(const SmoothArgs& A, const double* params, uint32_t n
     if (e == cudaSuccess) e = cudaMemsetAsync(jacobian, 0, n * kq * sizeof(double), st);
     return (int)e;
   }
-  const int smem = (int)(4u * A.rows * kThreads * sizeof(float));
-  const cudaError_t e = cudaFuncSetAttribute(k_smooth_jacobian, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  if (e != cudaSuccess) return (int)e;
-  const int eo = launch_order(A, params, ncand, st);
-  if (eo != 0) return eo;
-  const dim3 grid(A.nbins, (ncand + 31u) / 32u, A.ntypes);
-  k_smooth_jacobian<<<grid, kThreads, smem, st>>>(A, params, ncand, jac_raw);
+  const int ej = launch_jacobian_k(A, params, ncand, jac_raw, st);
+  if (ej != 0) return ej;
   k_smooth_jacobian_merge<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(jac_raw, params, ncand, A.nbins * A.rows, kq,
                                                                       inv_off, inv_idx, nvalues, expected, jacobian);
   return (int)cudaGetLastError();
@@ -811,13 +891,8 @@ int launch_smooth_gauss_newton(const SmoothArgs& A, const double* params, uint32
     if (e == cudaSuccess) e = cudaMemsetAsync(jtr, 0, (size_t)ncand * kq * sizeof(double), st);
     return (int)e;
   }
-  const int smem = (int)(4u * A.rows * kThreads * sizeof(float));
-  const cudaError_t e = cudaFuncSetAttribute(k_smooth_jacobian, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  if (e != cudaSuccess) return (int)e;
-  const int eo = launch_order(A, params, ncand, st);
-  if (eo != 0) return eo;
-  const dim3 grid(A.nbins, (ncand + 31u) / 32u, A.ntypes);
-  k_smooth_jacobian<<<grid, kThreads, smem, st>>>(A, params, ncand, jac_raw);
+  const int ej = launch_jacobian_k(A, params, ncand, jac_raw, st);
+  if (ej != 0) return ej;
   k_smooth_gauss_newton<<<ncand, kGnTile, kGnTile * (kq + 1u) * sizeof(double), st>>>(
       jac_raw, params, A.nbins * A.rows, kq, inv_off, inv_idx, nvalues, target, loss, jtj, jtr);
   return (int)cudaGetLastError();

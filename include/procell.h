@@ -119,6 +119,9 @@ int pc_set_stream(pc_context* ctx, void* stream);
  *                         cooperative launch per run
  *   "graph"               1: the persistent driver captures its run in a CUDA graph once
  *                         per plan and replays it
+ *   "smooth_predraw"      1 (default): pc_smooth_create draws every sampled lineage's
+ *                         normals and initial age once and keeps them in device memory
+ *                         (when they fit in 1 GB); 0: every pass draws them again
  * Failure injection (no counterpart in the reference, which checks no CUDA status):
  *   "fail_nth_call"       n >= 1: the n-th CUDA call the library makes for this context
  *                         from now on (allocation, copy, memset, synchronisation, event

@@ -140,6 +140,29 @@ def test_gaussian_sum_model(engine):
     sm.close()
 
 
+def test_lineage_draws_kept_or_redrawn_give_identical_results(engine, smooth_setup):
+    """A smoothed plan draws its lineages' normals and initial ages once and keeps them in HBM
+    (option smooth_predraw, the default); with the option off every pass draws them again.
+    Forward, adjoint and Jacobian must not change by a single bit."""
+    from procell.smooth import Smooth
+    sm, bins = smooth_setup
+    engine.set_option("smooth_predraw", 0)
+    try:
+        redraw = Smooth(engine, bins, n_types=3, t_max=168.0, phi=None, h=0.5, paths=2, seed=11)
+    finally:
+        engine.set_option("smooth_predraw", 1)
+    try:
+        P = params_tensor(BASE)
+        gE = torch.tensor(np.random.default_rng(3).normal(size=(2, sm.n_values)), device="cuda")
+        for a, b in ((sm.forward(P), redraw.forward(P)), (sm.backward(P, gE), redraw.backward(P, gE))):
+            assert torch.equal(a, b)
+        (Ea, Ja), (Eb, Jb) = sm.jacobian(P), redraw.jacobian(P)
+        assert torch.equal(Ea, Eb) and torch.equal(Ja, Jb)
+        sm.sync()
+    finally:
+        redraw.close()
+
+
 def test_autograd_function_and_determinism(smooth_setup):
     from procell.smooth import expected_counts
     sm, _ = smooth_setup
