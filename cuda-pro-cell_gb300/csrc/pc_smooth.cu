@@ -114,6 +114,16 @@ __device__ __forceinline__ void sig_pair(float x, float& s, float& one_m_s) {
   one_m_s = x >= 0.0f ? eq : q;
 }
 
+// A per-block flag the compiler must keep as it is: passed through an empty asm, it cannot be
+// re-derived inside the lineage loops from the FP64 comparison that produced it (measured:
+// the forward kernel otherwise re-evaluated the grid test about 2.6 times per lineage walk,
+// which kept GB300's slow FP64 pipe 69% busy).
+__device__ __forceinline__ bool opaque(bool f) {
+  uint32_t u = f ? 1u : 0u;
+  asm volatile("" : "+r"(u));
+  return u != 0u;
+}
+
 // x == 0.0 and x < 0.0 (for x not NaN) on the integer pipes.
 __device__ __forceinline__ bool zero_bits(double x) {
   return ((unsigned long long)__double_as_longlong(x) << 1) == 0ull;
@@ -435,7 +445,7 @@ __global__ void __launch_bounds__(kThreads, PC_SMOOTH_MIN_BLOCKS) k_smooth_jacob
   float* fmy = facc + threadIdx.x;
   const float inv_h = (float)A.inv_h;
   RemGrid rg;
-  const bool grid = grid_setup(rg, mu, sd, A.t_max, steps, 1.0 / A.inv_h);
+  const bool grid = opaque(grid_setup(rg, mu, sd, A.t_max, steps, 1.0 / A.inv_h));
   const RemFp64 rd{mu, sd, A.t_max, 0.0};
   const float stop = stop_level(steps);  // once per block: the walks' stopping threshold
   const uint64_t nlin = (r1 - r0) * A.paths;
@@ -528,7 +538,7 @@ __global__ void __launch_bounds__(kThreads, PC_SMOOTH_MIN_BLOCKS) k_smooth(const
   const float inv_h = (float)A.inv_h;
   const float* my_ag = Backward ? Ag2[lane] : nullptr;
   RemGrid rg;
-  const bool grid = grid_setup(rg, mu, sd, A.t_max, steps, 1.0 / A.inv_h);
+  const bool grid = opaque(grid_setup(rg, mu, sd, A.t_max, steps, 1.0 / A.inv_h));
   const RemFp64 rd{mu, sd, A.t_max, 0.0};
   const float stop = stop_level(steps);  // once per block: the walks' stopping threshold
   // lineage i of the bin: initial cell r0 + i / paths, replica i % paths
