@@ -50,12 +50,16 @@ namespace {
 constexpr int kThreads = 128;
 constexpr uint32_t kBudget = 1u << 16;
 // Resident blocks per SM the lineage-walk kernels are compiled for (registers per thread =
-// 65536 / (128 x this)); a compile-time tuning knob, results do not depend on it. Measured on
-// the calibration input: 5 blocks (96 registers) forward 1.91 ms, adjoint 2.62 ms; 6 (80
-// registers, a few more spills) 1.75 / 2.45 ms; 8 (64 registers) 3.04 / 2.45 ms.
-#ifndef PC_SMOOTH_MIN_BLOCKS
-#define PC_SMOOTH_MIN_BLOCKS 6
-#endif
+// 65536 / (128 x this)); compile-time tuning, results do not depend on it. Measured on the
+// calibration input with the draws made in every pass: 5 blocks (96 registers) forward
+// 1.91 ms, adjoint 2.62 ms; 6 (80 registers) 1.75 / 2.45 ms; 8 (64 registers) 3.04 / 2.45 ms:
+// 6 for those kernels. With the plan's draws kept in device memory they need fewer registers:
+// 6 blocks forward 1.170, adjoint 1.321, Jacobian 1.380 ms; 7 (72 registers, no spills) 1.115
+// / 1.267 / 1.301 ms; 8 (64 registers) 1.066 / 1.213 ms, the Jacobian held at 7 by its shared
+// memory (4 floats per generation row and thread).
+constexpr int kBlocksDrawn = 6;
+constexpr int kBlocksKept = 8;
+constexpr int kBlocksKeptJacobian = 7;
 
 __device__ __forceinline__ double f32_to_f64_bits(float z) {
   const uint32_t f = __float_as_uint(z);
@@ -414,7 +418,7 @@ __device__ __noinline__ void walk_jacobian_fp64(const float* z, double u_age, fl
 // d E_{b,g} / d(ratio_k, mean_k, sd_k); every block draws its bin's lineages itself (the
 // draws are shared by the 32 candidates of a warp, not across types).
 template <bool Kept>
-__global__ void __launch_bounds__(kThreads, PC_SMOOTH_MIN_BLOCKS) k_smooth_jacobian(const SmoothArgs A, const double* __restrict__ params,
+__global__ void __launch_bounds__(kThreads, Kept ? kBlocksKeptJacobian : kBlocksDrawn) k_smooth_jacobian(const SmoothArgs A, const double* __restrict__ params,
                                                               uint32_t ncand, double* __restrict__ out) {
   // dynamic: per-thread sums [3 * rows][kThreads], then the lineage draws [kWarps][rows][32]
   extern __shared__ float facc[];
@@ -487,7 +491,7 @@ __global__ void __launch_bounds__(kThreads, PC_SMOOTH_MIN_BLOCKS) k_smooth_jacob
 // adjoint (part[c][b][3k + q] = d(sum_g A_g E_g)/d(ratio_k, mean_k, sd_k)) of one type: block
 // (bin, group of 32 candidates, type k). Every block draws its bin's lineages itself.
 template <bool Backward, bool Kept>
-__global__ void __launch_bounds__(kThreads, PC_SMOOTH_MIN_BLOCKS) k_smooth(const SmoothArgs A, const double* __restrict__ params,
+__global__ void __launch_bounds__(kThreads, Kept ? kBlocksKept : kBlocksDrawn) k_smooth(const SmoothArgs A, const double* __restrict__ params,
                                                      uint32_t ncand, const double* __restrict__ grad_expected,
                                                      uint32_t nvalues, const int32_t* __restrict__ vidx,
                                                      double* __restrict__ out) {
