@@ -728,7 +728,18 @@ void batch_type_tables(const pc_plan* p, std::vector<BatchType>& btypes, std::ve
 
 // Lays the plan's instances out one after another (initial cells, bins, types, histogram
 // classes), fixes the root chunk and key layout, and uploads the tables.
-int finalize_plan(pc_context* ctx, pc_plan* p) {
+std::atomic<uint64_t> g_plan_ids{1};
+
+// Host-side tables of a plan, kept from its host part until its device part uploads them.
+struct PlanTables {
+  std::vector<uint32_t> bin_inst, bin_class;
+  std::vector<BatchType> btypes;
+  std::vector<InstanceDev> idev;
+};
+
+// The layout and host tables of a plan whose instances are prepared. Touches no context
+// state and makes no CUDA call, so it can run on any thread.
+int finalize_host(pc_plan* p, uint64_t max_root_chunk, PlanTables& t, std::string& msg) {
   uint64_t roots = 0, classes = 0;
   uint32_t bins = 0, ntypes_all = 0, gmax = 0;
   for (auto& I : p->inst) {
@@ -741,10 +752,10 @@ int finalize_plan(pc_context* ctx, pc_plan* p) {
     ntypes_all += (uint32_t)I.types.size();
     classes += (uint64_t)I.bin_value.size() * I.types.size();
     gmax = std::max(gmax, I.gmax);
-    if (bins >= (1u << 24)) return fail(ctx, PC_ERR_UNSUPPORTED, "at most 2^24 nonzero bins in one run");
+    if (bins >= (1u << 24)) return msg = "at most 2^24 nonzero bins in one run", PC_ERR_UNSUPPORTED;
   }
-  if (p->batched && ntypes_all > 0xFFFFu) return fail(ctx, PC_ERR_UNSUPPORTED, "at most 65535 cell types in one batch");
-  if (classes > 0xFFFFFFFFull) return fail(ctx, PC_ERR_UNSUPPORTED, "more than 2^32-1 (bin, type) classes in one run");
+  if (p->batched && ntypes_all > 0xFFFFu) return msg = "at most 65535 cell types in one batch", PC_ERR_UNSUPPORTED;
+  if (classes > 0xFFFFFFFFull) return msg = "more than 2^32-1 (bin, type) classes in one run", PC_ERR_UNSUPPORTED;
   p->nbins = bins;
   p->gmax = gmax;
   p->nclass = classes;
@@ -759,7 +770,7 @@ int finalize_plan(pc_context* ctx, pc_plan* p) {
   if (want_bits < 64) chunk = std::min<uint64_t>(chunk, 1ull << want_bits);
   if (gmax <= 32) chunk = std::min<uint64_t>(chunk, 1ull << 32);
   if (p->batched) chunk = std::min<uint64_t>(chunk, 1ull << 28);  // 2 GiB of root records
-  if (ctx->opt_max_root_chunk) chunk = std::min<uint64_t>(chunk, std::max<uint64_t>(1, ctx->opt_max_root_chunk));
+  if (max_root_chunk) chunk = std::min<uint64_t>(chunk, std::max<uint64_t>(1, max_root_chunk));
   p->chunk = chunk;
   const uint32_t rb = bits_for(chunk);
   p->g_store_max = std::min<uint32_t>(62u, 64u - rb);
@@ -767,9 +778,8 @@ int finalize_plan(pc_context* ctx, pc_plan* p) {
 
   // Per-bin tables (first initial cell, cap and flags; in a batch also the instance and first
   // class). Each instance fills its own slice, on host threads when there are many.
-  std::vector<uint32_t> bin_inst, bin_class;
-  std::vector<BatchType> btypes;
-  std::vector<InstanceDev> idev;
+  auto& bin_inst = t.bin_inst;
+  auto& bin_class = t.bin_class;
   p->bin_start.assign((size_t)bins + 1, 0);
   p->bin_info.assign(bins, 0);
   if (p->batched) {
@@ -804,13 +814,21 @@ int finalize_plan(pc_context* ctx, pc_plan* p) {
   } else {
     for (uint32_t i = 0; i < ninst; ++i) fill(i);
   }
-  if (p->batched) batch_type_tables(p, btypes, idev);
+  if (p->batched) batch_type_tables(p, t.btypes, t.idev);
+  return PC_OK;
+}
 
-  // Device copies.
+// The allocations and uploads of a plan whose host part is done (on the context's thread).
+int finalize_device(pc_context* ctx, pc_plan* p, const PlanTables& t) {
+  const auto& bin_inst = t.bin_inst;
+  const auto& bin_class = t.bin_class;
+  const auto& btypes = t.btypes;
+  const auto& idev = t.idev;
+  const uint64_t chunk = p->chunk;
   PC_CUDA(ctx, cudaSetDevice(ctx->device));
   cudaStream_t st = ctx->stream;
-  const size_t nb = bins;
-  p->hist_elems = (size_t)p->hist_gens * std::max<uint64_t>(1, classes);
+  const size_t nb = p->nbins;
+  p->hist_elems = (size_t)p->hist_gens * std::max<uint64_t>(1, p->nclass);
   p->upload_bytes = nb * sizeof(uint32_t) + (nb + 1) * sizeof(uint64_t);
   cudaError_t e = pc_cuda_malloc(&p->bin_info_dev, std::max<size_t>(1, nb) * sizeof(uint32_t));
   if (e == cudaSuccess) e = pc_cuda_malloc(&p->bin_start_dev, (nb + 1) * sizeof(uint64_t));
@@ -851,6 +869,48 @@ int finalize_plan(pc_context* ctx, pc_plan* p) {
   if (e != cudaSuccess)
     return fail(ctx, e == cudaErrorMemoryAllocation ? PC_ERR_NOMEM : PC_ERR_CUDA,
                 std::string("plan upload: ") + cudaGetErrorString(e));
+  return PC_OK;
+}
+
+int finalize_plan(pc_context* ctx, pc_plan* p) {
+  PlanTables t;
+  std::string msg;
+  const int rc = finalize_host(p, ctx->opt_max_root_chunk, t, msg);
+  if (rc != PC_OK) return fail(ctx, rc, msg);
+  return finalize_device(ctx, p, t);
+}
+
+// The host part of a batch: its instances prepared on host threads, then its layout and
+// tables. Touches no context state and makes no CUDA call (runs on any thread); messages
+// number the instances from `first`.
+int prepare_batch(const pc_instance* instances, uint32_t n, uint32_t first, uint64_t max_root_chunk,
+                  pc_batch** out, PlanTables& t, std::string& msg) {
+  *out = nullptr;
+  if (n == 0) return msg = "a batch needs at least one instance", PC_ERR_INVALID;
+  pc_batch* b = new (std::nothrow) pc_batch();
+  if (!b) return msg = "host allocation", PC_ERR_NOMEM;
+  std::memset(&b->stats, 0, sizeof(b->stats));
+  b->id = g_plan_ids.fetch_add(1);
+  b->batched = true;
+  b->inst.resize(n);
+  std::vector<int> codes(n, PC_OK);
+  std::vector<std::string> msgs(n);
+  parallel_for(n, [&](uint32_t i) {
+    const pc_instance& x = instances[i];
+    codes[i] = prepare_instance(x.bins, x.n_bins, x.types, x.n_types, x.t_max, x.phi, x.seed, b->inst[i], msgs[i]);
+  });
+  int rc = PC_OK;
+  for (uint32_t i = 0; i < n && rc == PC_OK; ++i)
+    if (codes[i] != PC_OK) {
+      rc = codes[i];
+      msg = "instance " + std::to_string(first + i) + ": " + msgs[i];
+    }
+  if (rc == PC_OK) rc = finalize_host(b, max_root_chunk, t, msg);
+  if (rc != PC_OK) {
+    delete b;
+    return rc;
+  }
+  *out = b;
   return PC_OK;
 }
 
@@ -902,7 +962,6 @@ int instance_result(const pc_plan* p, const InstanceHost& I, const unsigned long
   return PC_OK;
 }
 
-std::atomic<uint64_t> g_plan_ids{1};
 
 // Device scratch of the result merge above this size is not kept: such plans merge on host
 // threads instead.
@@ -1591,27 +1650,15 @@ int pc_histogram_accumulate(pc_histogram* dst, const pc_histogram* src) {
 int pc_batch_create(pc_context* ctx, const pc_instance* instances, uint32_t n_instances, pc_batch** out) {
   PC_GUARD_BEGIN
   FaultScope fault_scope__(ctx);
-  if (!ctx || !out || (n_instances && !instances)) return fail(ctx, PC_ERR_INVALID, "null argument");
+  if (!ctx || !out) return fail(ctx, PC_ERR_INVALID, "null argument");
   *out = nullptr;
-  if (n_instances == 0) return fail(ctx, PC_ERR_INVALID, "a batch needs at least one instance");
-  pc_batch* b = new (std::nothrow) pc_batch();
-  if (!b) return fail(ctx, PC_ERR_NOMEM, "host allocation");
-  std::memset(&b->stats, 0, sizeof(b->stats));
-  b->id = g_plan_ids.fetch_add(1);
-  b->batched = true;
-  b->inst.resize(n_instances);
-  std::vector<int> codes(n_instances, PC_OK);
-  std::vector<std::string> msgs(n_instances);
-  parallel_for(n_instances, [&](uint32_t i) {
-    const pc_instance& x = instances[i];
-    codes[i] = prepare_instance(x.bins, x.n_bins, x.types, x.n_types, x.t_max, x.phi, x.seed, b->inst[i], msgs[i]);
-  });
-  for (uint32_t i = 0; i < n_instances; ++i)
-    if (codes[i] != PC_OK) {
-      delete b;
-      return fail(ctx, codes[i], "instance " + std::to_string(i) + ": " + msgs[i]);
-    }
-  const int rc = finalize_plan(ctx, b);
+  if (n_instances && !instances) return fail(ctx, PC_ERR_INVALID, "null argument");
+  PlanTables t;
+  std::string msg;
+  pc_batch* b = nullptr;
+  int rc = prepare_batch(instances, n_instances, 0, ctx->opt_max_root_chunk, &b, t, msg);
+  if (rc != PC_OK) return fail(ctx, rc, msg);
+  rc = finalize_device(ctx, b, t);
   if (rc != PC_OK) {
     pc_batch_destroy(b);
     return rc;
@@ -1758,12 +1805,16 @@ int pc_simulate_batch(pc_context* ctx, const pc_instance* instances, uint32_t n_
   PC_GUARD_BEGIN
   FaultScope fault_scope__(ctx);
   if (!ctx || !out) return fail(ctx, PC_ERR_INVALID, "null argument");
+  if (n_instances && !instances) return fail(ctx, PC_ERR_INVALID, "null argument");
   for (uint32_t i = 0; i < n_instances; ++i) std::memset(out + i, 0, sizeof(pc_histogram));
-  // Large batches run as consecutive sub-batches of up to 4 parts: host threads merge one
-  // part's histograms (for 4096 instances about 0.5 GB of host output) while the device runs
-  // the next. Every instance's counts depend on that instance alone, so the split changes no
-  // result.
+  // Large batches run as consecutive sub-batches of up to 4 parts. While the device runs one
+  // part, a host thread prepares the next (its instances, layout and tables: everything but
+  // the uploads) and host threads merge the previous part's histograms (for 4096 instances
+  // about 0.5 GB of host output). Every instance's counts depend on that instance alone, so
+  // the split changes no result.
   const uint32_t parts = std::min<uint32_t>(4u, std::max<uint32_t>(1u, n_instances / 1024u));
+  const uint64_t max_root_chunk = ctx->opt_max_root_chunk;
+  auto first_of = [&](uint32_t part) { return (uint32_t)((uint64_t)n_instances * part / parts); };
   std::vector<int> codes(n_instances, PC_OK);
   std::vector<const char*> msgs(n_instances, "");
   auto merge = [&codes, &msgs, out](pc_batch* b, const unsigned long long* h, uint32_t first) {
@@ -1772,7 +1823,32 @@ int pc_simulate_batch(pc_context* ctx, const pc_instance* instances, uint32_t n_
       out[first + i].stats.roots = b->inst[i].roots;
     });
   };
-  // the part being merged on its own thread; joined (and its batch destroyed) on every path
+  // A part's host preparation; a batch it still owns is destroyed with it.
+  struct Prepared {
+    pc_batch* b = nullptr;
+    PlanTables t;
+    int rc = PC_OK;
+    std::string msg;
+    ~Prepared() { pc_batch_destroy(b); }
+  };
+  auto prepare_part = [&](uint32_t part, Prepared& pr) {
+    try {
+      pr.rc = prepare_batch(instances + first_of(part), first_of(part + 1) - first_of(part), first_of(part),
+                            max_root_chunk, &pr.b, pr.t, pr.msg);
+    } catch (...) {
+      pr.rc = PC_ERR_NOMEM;
+      pr.msg = "host allocation";
+    }
+  };
+  Prepared prep[2];
+  // the thread preparing the next part, and the part being merged on its own thread (its
+  // batch destroyed when the merge is done); both joined on every path
+  struct Joined {
+    std::thread th;
+    ~Joined() {
+      if (th.joinable()) th.join();
+    }
+  } preparer;
   struct Merging {
     std::thread th;
     pc_batch* b = nullptr;
@@ -1783,21 +1859,41 @@ int pc_simulate_batch(pc_context* ctx, const pc_instance* instances, uint32_t n_
     }
     ~Merging() { finish(); }
   } merging;
+  prepare_part(0, prep[0]);
   int rc = PC_OK;
   for (uint32_t part = 0; part < parts && rc == PC_OK; ++part) {
-    const uint32_t first = (uint32_t)((uint64_t)n_instances * part / parts);
-    const uint32_t count = (uint32_t)((uint64_t)n_instances * (part + 1) / parts) - first;
-    pc_batch* b = nullptr;
-    rc = pc_batch_create(ctx, instances + first, count, &b);
+    Prepared& cur = prep[part & 1u];
+    Prepared& nxt = prep[(part + 1u) & 1u];
+    if (cur.rc != PC_OK) {
+      rc = fail(ctx, cur.rc, cur.msg);
+      break;
+    }
+    pc_batch* b = cur.b;
+    cur.b = nullptr;
+    rc = finalize_device(ctx, b, cur.t);
+    if (rc == PC_OK && part + 1 < parts) {
+      pc_batch_destroy(nxt.b);
+      nxt.b = nullptr;
+      nxt.t = PlanTables();
+      nxt.rc = PC_OK;
+      nxt.msg.clear();
+      try {
+        preparer.th = std::thread([&prepare_part, &nxt, part]() { prepare_part(part + 1u, nxt); });
+      } catch (...) {
+        prepare_part(part + 1u, nxt);  // no thread to overlap with: prepare here
+      }
+    }
     if (rc == PC_OK) rc = pc_batch_run(ctx, b);
     const unsigned long long* h = nullptr;
     if (rc == PC_OK) rc = copy_table(ctx, b, (int)(part & 1u), &h);
     merging.finish();  // the previous part's merge read the other stage
+    if (preparer.th.joinable()) preparer.th.join();
     if (rc != PC_OK) {
       pc_batch_destroy(b);
       break;
     }
     merging.b = b;
+    const uint32_t first = first_of(part);
     if (part + 1 == parts) {
       merge(b, h, first);  // nothing left to overlap with
     } else {
@@ -1818,6 +1914,7 @@ int pc_simulate_batch(pc_context* ctx, const pc_instance* instances, uint32_t n_
     }
   }
   merging.finish();
+  if (preparer.th.joinable()) preparer.th.join();
   for (uint32_t i = 0; rc == PC_OK && i < n_instances; ++i)
     if (codes[i] != PC_OK) rc = fail(ctx, codes[i], msgs[i]);
   if (rc != PC_OK)
