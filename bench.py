@@ -785,8 +785,9 @@ def measure_calibration(eng, local, steps, warmup, cpu_seconds, pso_seconds, ext
     def step(th):
         P = prob.params(th)
         E = prob.smooth.forward(P)
-        gE = 2.0 * (torch.log1p(E) - torch.log1p(prob.target)) / (1.0 + E)
-        return prob.smooth.backward(P, gE), ((torch.log1p(E) - torch.log1p(prob.target)) ** 2).sum(dim=1)
+        r = torch.log1p(E) - prob.target_log  # residuals log(1 + E_v) - log(1 + target_v)
+        gE = 2.0 * r / (1.0 + E)
+        return prob.smooth.backward(P, gE), (r * r).sum(dim=1)
 
     for _ in range(warmup):
         step(theta)

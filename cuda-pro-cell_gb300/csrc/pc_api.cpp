@@ -1814,7 +1814,14 @@ int pc_simulate_batch(pc_context* ctx, const pc_instance* instances, uint32_t n_
   // the split changes no result.
   const uint32_t parts = std::min<uint32_t>(4u, std::max<uint32_t>(1u, n_instances / 1024u));
   const uint64_t max_root_chunk = ctx->opt_max_root_chunk;
-  auto first_of = [&](uint32_t part) { return (uint32_t)((uint64_t)n_instances * part / parts); };
+  // the first and the last part, whose preparation and merge overlap nothing, are half the
+  // size of the others (weights 1, 2, ..., 2, 1)
+  auto first_of = [&](uint32_t part) {
+    if (parts == 1) return part == 0 ? 0u : n_instances;
+    const uint64_t total = 2ull * parts - 2ull;
+    const uint64_t w = part == 0 ? 0ull : (part == parts ? total : 2ull * part - 1ull);
+    return (uint32_t)((uint64_t)n_instances * w / total);
+  };
   std::vector<int> codes(n_instances, PC_OK);
   std::vector<const char*> msgs(n_instances, "");
   auto merge = [&codes, &msgs, out](pc_batch* b, const unsigned long long* h, uint32_t first) {
