@@ -53,6 +53,7 @@ struct pc_context {
   int opt_driver = 0;                    // 0: one launch per sweep, 1: persistent launch
   int opt_graph = 0;                     // persistent driver: replay a captured CUDA graph
   int opt_smooth_predraw = 1;            // smoothed plans keep their lineages' draws in HBM
+  int opt_device_merge = 1;              // single-instance results merged on the device
   // resident blocks per SM of each configuration's kernels: [narrow][batched][config]
   int occ[2][2][kNumSweepConfigs][3] = {};
   uint32_t* persist_ctl = nullptr;       // [2] barrier + [8] run totals (u64 [4])
@@ -503,6 +504,8 @@ int pc_set_option(pc_context* ctx, const char* name, double value) {
     ctx->opt_graph = value != 0.0 ? 1 : 0;
   } else if (n == "smooth_predraw") {
     ctx->opt_smooth_predraw = value != 0.0 ? 1 : 0;
+  } else if (n == "device_merge") {
+    ctx->opt_device_merge = value != 0.0 ? 1 : 0;
   } else if (n == "fail_nth_call") {
     // counted from the calls made so far: the n-th call after this one fails (0: none)
     ctx->fail_at = value >= 1.0 ? ctx->cuda_calls + (uint64_t)value : 0;
@@ -1550,13 +1553,14 @@ int pc_plan_result(pc_context* ctx, pc_plan* p, pc_histogram* out) {
   if (!ctx || !p || !out || p->inst.empty()) return PC_ERR_INVALID;
   std::memset(out, 0, sizeof(*out));
   if (!p->ran) return fail(ctx, PC_ERR_INVALID, "plan has not run");
-  int rc = device_result(ctx, p, out);
+  int rc = ctx->opt_device_merge ? device_result(ctx, p, out) : PC_ERR_UNSUPPORTED;
   uint64_t h2d = 0, d2h = 0;
   if (rc == PC_OK) {
     h2d = out->stats.h2d_bytes;
     d2h = out->stats.d2h_bytes;
   } else if (rc == PC_ERR_UNSUPPORTED) {
-    // merge scratch too large for the device: read the count table back, merge on the host
+    // merge scratch too large for the device (or the device merge switched off): read the
+    // count table back, merge on the host
     const unsigned long long* h = nullptr;
     rc = stage_table(ctx, p, &h);
     if (rc != PC_OK) return rc;

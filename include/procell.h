@@ -119,6 +119,10 @@ int pc_set_stream(pc_context* ctx, void* stream);
  *                         cooperative launch per run
  *   "graph"               1: the persistent driver captures its run in a CUDA graph once
  *                         per plan and replays it
+ *   "device_merge"        1 (default): pc_plan_result merges the counts into the value
+ *                         histogram on the device; 0: reads the count table back and
+ *                         merges on the host (as it does anyway for merge scratch above
+ *                         256 MB)
  *   "smooth_predraw"      1 (default): pc_smooth_create draws every sampled lineage's
  *                         normals and initial age once and keeps them in device memory
  *                         (when they fit in 1 GB); 0: every pass draws them again

@@ -140,6 +140,38 @@ def test_shards_add_up(engine):
     assert sum(p.stats["divisions"] for p in parts) == full.stats["divisions"]
 
 
+@pytest.mark.parametrize("name", ["medium", "edge"])
+def test_device_and_host_merge_agree(engine, oracle_lib, name):
+    """pc_plan_result merges the counts into the value histogram on the device and reads back
+    only the merged counts; the host merge (used for plans whose merge scratch would exceed
+    256 MB, forced here by the option device_merge = 0) must give the same histogram, and
+    both the oracle's."""
+    if name == "medium":
+        w = cfg.medium()
+        bins, types, t_max, phi, seed = w.bins, w.types, w.t_max, w.phi, w.seed
+    else:  # duplicate values across bins and generations, a quiescent type, a zero-ratio type
+        bins = [(64.0, 30), (32.0, 20), (16.0, 10), (48.0, 7), (3.0, 0), (24.0, 9)]
+        types = [(0.5, 9.0, 3.0), (0.0, 12.0, 2.0), (0.5, -1.0, -1.0)]
+        t_max, phi, seed = 60.0, 2.0, 77
+    p = engine.plan(bins, types, t_max, phi, seed)
+    try:
+        p.run()
+        dev = p.result()
+        engine.set_option("device_merge", 0)
+        try:
+            host = p.result()
+        finally:
+            engine.set_option("device_merge", 1)
+    finally:
+        p.close()
+    o = oracle_lib.simulate(bins, types, t_max, phi, seed=seed, nthreads=0)
+    for r in (dev, host):
+        assert np.array_equal(r.values, o.values)
+        assert np.array_equal(r.totals, o.totals)
+        assert np.array_equal(r.per_type, o.per_type)
+    assert dev.stats["leaves"] == host.stats["leaves"] == o.stats["leaves"]
+
+
 def test_repeat_runs_identical(engine):
     w = cfg.small()
     p = engine.plan(w.bins, w.types, w.t_max, w.phi, w.seed)
