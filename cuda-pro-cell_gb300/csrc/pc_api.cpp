@@ -233,7 +233,7 @@ cudaError_t pc_cuda_graph_launch(cudaGraphExec_t g, cudaStream_t s) {
 #define PC_LAUNCH(expr) \
   (injected(cudaErrorLaunchOutOfResources) != cudaSuccess ? cudaErrorLaunchOutOfResources : (cudaError_t)(expr))
 
-// Ziggurat tables for f(x) = exp(-x^2/2), 128 layers (Marsaglia & Tsang 2000): the layer
+// Ziggurat tables for f(x) = exp(-x^2/2), kZigLayers layers (Marsaglia & Tsang 2000): the layer
 // edges follow x_{i+1} = sqrt(-2 ln(v/x_i + f(x_i))) from x_1 = r; the base strip's
 // effective width is v/f(r).
 ZigTables build_zig_tables() {

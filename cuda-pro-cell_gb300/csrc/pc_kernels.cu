@@ -33,7 +33,7 @@ __global__ void k_debug_normals(const ZigTables* zig, uint32_t k0, uint32_t k1, 
   const u32x4 P = philox(u32x4{(uint32_t)parent, (uint32_t)(parent >> 32), root, kPurposePair}, k0, k1);
   ChildStream cs = child_stream(2ull * parent + c, root, k0, k1);
   uint32_t budget = kRoundBudget;
-  z[i] = zig_normal(c ? P.y : P.x, (P.z >> (8u * c)) & 255u, true, pair_wedge_bits(P, c), cs, Z, budget);
+  z[i] = zig_normal(c ? P.y : P.x, pair_layer(P, c), true, pair_wedge_bits(P, c), cs, Z, budget);
 }
 
 // Grid barriers of the persistent driver, for the failure-detection tests. mode 0: one

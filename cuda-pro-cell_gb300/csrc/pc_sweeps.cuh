@@ -122,14 +122,14 @@ __device__ __noinline__ float slow_z(uint32_t j, uint32_t layer, uint32_t wedge,
     if (z >= zlo && z <= zhi) return z;
     have_wedge = false;
     j = cs.next();
-    layer = cs.next() & 255u;
+    layer = cs.next() & kZigLayerMask;
     --budget;
   }
   atomicOr(error, 2u);
   return 0.0f;
 }
 
-// First-attempt fast path (about 98.5% of draws): one strip test, one FP32 multiply.
+// First-attempt fast path (about 99.6% of draws): one strip test, one FP32 multiply.
 __device__ __forceinline__ float draw_z(uint32_t j, uint32_t layer, uint32_t wedge, uint64_t node,
                                         uint32_t root, uint32_t k0, uint32_t k1, float zlo, float zhi,
                                         const ZigTables& Z, uint32_t* error) {
@@ -379,7 +379,7 @@ __device__ void root_body(const RunArgs& a, const uint64_t root_base, const uint
       } else {
         const u32x4 P = Batched ? philox(u32x4{0u, 0u, root, kPurposePair}, k0, k1)
                                 : philox_ks(u32x4{0u, 0u, root, kPurposePair}, a.ks);
-        const float z = draw_z(P.y, (P.z >> 8) & 255u, pair_wedge_bits(P, 1u), 1ull, root, k0, k1, T.zlo, T.zhi,
+        const float z = draw_z(P.y, pair_layer(P, 1u), pair_wedge_bits(P, 1u), 1ull, root, k0, k1, T.zlo, T.zhi,
                                s.zig_or(a), a.error);
         const double tau = fma(T.sigma, f32_to_f64(z), T.mu);  // 0 for zero-mean types
         d0 = tau * u_age + tau;  // t = tau * U (cell.cu:124-143), due = t + timer
@@ -423,7 +423,7 @@ __device__ void root_body(const RunArgs& a, const uint64_t root_base, const uint
 // The main loop settles each daughter from its first-attempt normal: a leaf (counted
 // into the histogram, never stored), a vanished cell, or a dividing cell whose exact FP64
 // due time is written to the front of the segment. Daughters whose first attempt is not
-// accepted by the ziggurat strip test (about 1.5%) are written as (birth, key) to the back
+// accepted by the ziggurat strip test (about 0.43%) are written as (birth, key) to the back
 // of the segment and resolved after the main loop, 32 at a time with every lane busy;
 // their first-attempt bits are re-derived from the parent's Philox block. The rejection
 // path thus costs the main loop neither registers nor idle lanes. Resolved cells are
@@ -491,7 +491,7 @@ __device__ __forceinline__ CellDraw classify(const ulonglong2 c, bool act, uint3
   // first attempts of both daughters: strip test and truncation bounds (zero-mean types
   // carry sigma = mu = 0 and unbounded z, so any accepted z gives tau = 0)
   const ZigTables& Z = s.zig_or(a);
-  const uint32_t l0 = P.z & 255u, l1 = (P.z >> 8) & 255u;
+  const uint32_t l0 = pair_layer(P, 0u), l1 = pair_layer(P, 1u);
   float z0 = __fmul_rn((float)(P.x & 0x7FFFFFFFu), Z.w[l0]);
   float z1 = __fmul_rn((float)(P.y & 0x7FFFFFFFu), Z.w[l1]);
   z0 = (P.x >> 31) ? -z0 : z0;
@@ -660,7 +660,7 @@ __device__ void divide_body(const RunArgs& a, const uint64_t root_base, const Le
       const uint64_t parent = node >> 1;
       const uint32_t ch = (uint32_t)(node & 1ull);
       const u32x4 P = philox(u32x4{(uint32_t)parent, (uint32_t)(parent >> 32), root, kPurposePair}, tc.k0, tc.k1);
-      const float z = slow_z(ch ? P.y : P.x, (P.z >> (8u * ch)) & 255u, pair_wedge_bits(P, ch), node, root,
+      const float z = slow_z(ch ? P.y : P.x, pair_layer(P, ch), pair_wedge_bits(P, ch), node, root,
                              tc.k0, tc.k1, tc.zlo, tc.zhi, s.zig_or(a), a.error);
       f = fate(birth, z, tc, g1 < cap, due);
       if (f == kLeaf && !in_bounds((uint32_t)rec < a.nclass && row_ok, a.error)) f = kNone;

@@ -18,6 +18,8 @@ import numpy as np
 from . import _lib
 from ._lib import ProcellError
 
+ZIG_LAYERS = 1024  # layers of the normal sampler's ziggurat (pc_rng.h kZigLayers)
+
 __all__ = ["Engine", "Batch", "Result", "log_space", "rebin", "ProcellError", "format_histogram"]
 
 
@@ -271,9 +273,9 @@ class Engine:
         return z
 
     def tables(self):
-        k = np.zeros(256, np.uint32)
-        w = np.zeros(256, np.uint32)
-        f = np.zeros(257, np.uint32)
+        k = np.zeros(ZIG_LAYERS, np.uint32)
+        w = np.zeros(ZIG_LAYERS, np.uint32)
+        f = np.zeros(ZIG_LAYERS + 1, np.uint32)
         self._check(self.L.pc_debug_tables(self.ctx, k.ctypes.data_as(_lib.U32P),
                                            w.ctypes.data_as(_lib.U32P), f.ctypes.data_as(_lib.U32P)))
         return k, w.view(np.float32), f.view(np.float32)

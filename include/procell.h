@@ -355,7 +355,7 @@ int pc_simulate_noalloc(const pc_bin* bins, uint64_t n_bins, const pc_cell_type*
  * pc_debug_philox: out[4*i..] = Philox4x32-10(ctr[4*i..], key) for i < n.
  * pc_debug_normals: z[i] = first-attempt normal of child (i & 1) of node first_parent+i/2
  *                   under `root` (no truncation), as the division sweep computes it.
- * pc_debug_tables: the device's ziggurat tables (k[256], w bits[256], f bits[257]). */
+ * pc_debug_tables: the device's ziggurat tables (k[1024], w bits[1024], f bits[1025]). */
 /* Grid barriers of the persistent driver in a cooperative launch of up to 8 blocks, with
  * the wait limited to timeout_ms (failure detection without a GPU fault; the context stays
  * usable). starve = 0: one barrier. starve = 1: the arrival counter is preset so that the

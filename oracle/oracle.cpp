@@ -94,11 +94,14 @@ float o_logf(float u) {
 }
 
 // ------------------------------------------------------------ ziggurat tables ------
-// Marsaglia & Tsang (2000) construction with 256 layers for the normal density
+// Marsaglia & Tsang (2000) construction with 1024 layers for the normal density
 // f(x) = exp(-x^2/2): x_1 = r, x_{i+1} = sqrt(-2 ln(v/x_i + f(x_i))), base width v/f(r),
-// with r = 3.6541528853610088 and v = 4.9286732339746553e-3 (the closure of the 256-layer
-// construction, solved numerically).
-const int kLayers = 256;
+// with r = 4.0388498461095045227 and v = 1.2263246463530880729e-3 (the closure of the
+// 1024-layer construction, solved numerically by bisection; the same solver reproduces the
+// published 256-layer pair r = 3.6541528853610088, v = 4.9286732339746553e-3).
+const int kLayers = 1024;
+const uint32_t kLayerMask = kLayers - 1;
+const double kR = 4.0388498461095045227, kV = 1.2263246463530880729e-3;
 
 struct Tables {
   uint32_t k[kLayers];
@@ -107,7 +110,7 @@ struct Tables {
 };
 
 Tables make_tables() {
-  const double r = 3.6541528853610088, v = 4.9286732339746553e-3, two31 = 2147483648.0;
+  const double r = kR, v = kV, two31 = 2147483648.0;
   double x[kLayers + 1];
   x[1] = r;
   for (int i = 1; i < kLayers - 1; ++i) x[i + 1] = std::sqrt(-2.0 * std::log(v / x[i] + std::exp(-0.5 * x[i] * x[i])));
@@ -164,7 +167,7 @@ float u24_closed_open(uint32_t w) { return (float)(w >> 8) * 5.9604644775390625e
 // uniform comes from the pair block when `have_wedge` is set.
 float ziggurat(uint32_t j, uint32_t layer, bool have_wedge, uint32_t wedge_bits, NodeStream& ns) {
   const Tables& t = tables();
-  const float rf = (float)3.6541528853610088;
+  const float rf = (float)kR;  // the tail starts at r
   bool first = have_wedge;
   while (true) {
     const uint32_t mag = j & 0x7FFFFFFFu;
@@ -183,12 +186,13 @@ float ziggurat(uint32_t j, uint32_t layer, bool have_wedge, uint32_t wedge_bits,
       return sign * x;
     first = false;
     j = ns.next();
-    layer = ns.next() & 255u;
+    layer = ns.next() & kLayerMask;
   }
 }
 
-// Pair block of node `parent`: child c's magnitude word, layer byte and wedge bits
-// (child 0: low 24 bits of word 3; child 1: top byte of word 3, top half of word 2).
+// Pair block of node `parent`: child c's magnitude word, layer (bits 10c..10c+9 of word 2)
+// and 22 wedge bits in the top of a word (child 0: low 22 bits of word 3; child 1: top 10
+// bits of word 3 above the top 12 bits of word 2).
 struct PairDraw {
   uint32_t j, layer, wedge;
 };
@@ -199,8 +203,8 @@ PairDraw pair_draw(uint64_t parent, uint32_t c, uint32_t root, uint32_t k0, uint
   philox_block(pc, k0, k1, pw);
   PairDraw d;
   d.j = pw[c];
-  d.layer = (pw[2] >> (8 * c)) & 255u;
-  d.wedge = c == 0 ? (pw[3] << 8) : ((pw[3] & 0xFF000000u) | ((pw[2] >> 16) << 8));
+  d.layer = (pw[2] >> (10 * c)) & kLayerMask;
+  d.wedge = c == 0 ? (pw[3] << 10) : (((pw[3] >> 22) << 22) | ((pw[2] >> 20) << 10));
   return d;
 }
 
@@ -218,7 +222,7 @@ double draw_tau(uint64_t parent, uint32_t c, uint32_t root, uint32_t k0, uint32_
     if (tau > 0.0) return tau;
     have_wedge = false;
     j = ns.next();
-    layer = ns.next() & 255u;
+    layer = ns.next() & kLayerMask;
   }
 }
 

@@ -15,6 +15,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "build", "liboracle.so")
+ZIG_LAYERS = 1024  # layers of the ziggurat (oracle.cpp kLayers)
 
 _lib = None
 
@@ -151,9 +152,9 @@ def philox(ctr, key):
 
 def tables():
     L = lib()
-    k = np.zeros(256, np.uint32)
-    w = np.zeros(256, np.uint32)
-    f = np.zeros(257, np.uint32)
+    k = np.zeros(ZIG_LAYERS, np.uint32)
+    w = np.zeros(ZIG_LAYERS, np.uint32)
+    f = np.zeros(ZIG_LAYERS + 1, np.uint32)
     L.oracle_tables(_ptr(k, ctypes.c_uint32), _ptr(w, ctypes.c_uint32), _ptr(f, ctypes.c_uint32))
     return k, w.view(np.float32), f.view(np.float32)
 

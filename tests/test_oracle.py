@@ -27,8 +27,8 @@ def test_philox_known_answers(oracle_lib):
 def test_ziggurat_tables(oracle_lib):
     k, w, f = oracle_lib.tables()
     n = len(k)
-    assert n == 256 and len(f) == n + 1
-    r, v = 3.6541528853610088, 4.9286732339746553e-3
+    assert n == 1024 and len(f) == n + 1
+    r, v = 4.0388498461095045227, 1.2263246463530880729e-3
     x = w.astype(np.float64) * 2.0 ** 31
     # layer 1's right edge is r, edges shrink towards the top layer
     assert abs(x[1] - r) < 1e-6
@@ -38,7 +38,10 @@ def test_ziggurat_tables(oracle_lib):
     fx = np.exp(-0.5 * x[1:] ** 2)
     fnext = np.append(fx[1:], 1.0)
     areas = x[1:] * (fnext - fx)
-    assert np.allclose(areas[:-1], v, rtol=5e-5), areas  # w is FP32-rounded
+    # x_i is rebuilt from the FP32-rounded w, and the difference f(x_{i+1}) - f(x_i) of a thin
+    # layer amplifies that rounding: up to 8.5e-5 relative with 1024 layers (the tables are
+    # built in FP64, where the construction closes to 4e-9)
+    assert np.allclose(areas[:-1], v, rtol=2e-4), areas
     assert abs(areas[-1] - v) < 1e-3 * v
     # the base strip: rectangle [0, r] x [0, f(r)] plus the tail, area v
     tail = math.sqrt(math.pi / 2) * math.erfc(r / math.sqrt(2))
@@ -47,10 +50,11 @@ def test_ziggurat_tables(oracle_lib):
     assert np.allclose(f[1:n], fx, rtol=1e-6)
     ratio = np.append(x[2:n] / x[1:n - 1], 0.0)
     assert np.allclose(k[1:n] / 2.0 ** 31, ratio, atol=1e-9)
-    # about 98.5% of first attempts are accepted by the strip test alone (97.2% with 128
-    # layers); the proposals rejected overall are the area above the curve, N v - sqrt(pi/2)
-    assert 0.984 < k.astype(np.float64).mean() / 2.0 ** 31 < 0.986
-    assert abs((n * v - math.sqrt(math.pi / 2)) / (n * v) - 0.00668) < 1e-4
+    # about 99.57% of first attempts are accepted by the strip test alone (98.5% with 256
+    # layers, 97.2% with 128); the proposals rejected overall are the area above the curve,
+    # N v - sqrt(pi/2)
+    assert 0.9955 < k.astype(np.float64).mean() / 2.0 ** 31 < 0.9960
+    assert abs((n * v - math.sqrt(math.pi / 2)) / (n * v) - 0.001945) < 1e-5
 
 
 def test_normal_statistics(oracle_lib):
