@@ -575,62 +575,22 @@ int prepare_types(const pc_cell_type* types, uint32_t n_types, InstanceHost& I, 
   return PC_OK;
 }
 
-int prepare_instance(const pc_bin* bins, uint64_t n_bins, const pc_cell_type* types, uint32_t n_types,
-                     double t_max, double phi, uint64_t seed, InstanceHost& I, std::string& msg) {
-  if ((n_bins && !bins) || (n_types && !types)) return msg = "null argument", PC_ERR_INVALID;
-  if (!(t_max >= 0.0) || std::isinf(t_max)) return msg = "t_max must be finite and >= 0", PC_ERR_INVALID;
-  if (!(phi >= 0.0) || std::isinf(phi)) return msg = "phi must be finite and > 0 (0 = automatic)", PC_ERR_INVALID;
-  if (n_types == 0)
-    return msg = "ERROR: proportion distribution of cell types does not sum to 1, aborting.", PC_ERR_INVALID;
-  if (n_types > (uint32_t)kMaxTypes) return msg = "at most 64 cell types are supported", PC_ERR_UNSUPPORTED;
-
-  // Threshold (parser.cu:80-96: with no threshold given, the smallest value with a
-  // nonzero frequency; the `threshold == 0.0 ||` test is the reference's).
-  double threshold = phi;
-  if (threshold == 0.0) {
-    for (uint64_t i = 0; i < n_bins; ++i)
-      if (bins[i].frequency > 0 && (threshold == 0.0 || bins[i].value < threshold)) threshold = bins[i].value;
-  }
-  if (!(threshold > 0.0) || std::isinf(threshold)) return msg = "phi must be finite and > 0", PC_ERR_INVALID;
-  I.phi = threshold;
-  I.t_max = (t_max == 0.0) ? 0.0 : t_max;  // normalise -0
-  I.seed = seed;
-
-  // Bins with a nonzero frequency, in file order; output value set (parser.cu:98-151):
-  // every bin's halving chain v, v/2, ... while >= phi, sorted and deduplicated, together
-  // with the (bin, generation) -> value index map of the result merge.
-  uint64_t total = 0;
-  std::vector<uint32_t> chain_len;  // chain length per nonzero bin
+// Output value set of a prepared instance (parser.cu:98-151): every nonzero bin's halving
+// chain v, v/2, ... while >= phi, sorted and deduplicated, together with the
+// (bin, generation) -> value index map of the result merge. Reads the instance's bins and
+// phi, writes only values, vidx and vidx_stride (the run reads none of the three).
+void build_value_set(InstanceHost& I) {
+  const double threshold = I.phi;
+  const size_t nb = I.bin_value.size();
+  std::vector<uint32_t> chain_len(nb);  // chain length per nonzero bin
   uint64_t chain_total = 0;
   uint32_t longest = 0;
-  bool normal = threshold >= 0x1p-1000;  // halving a normal double only lowers its exponent
-  for (uint64_t i = 0; i < n_bins; ++i) {
-    if (bins[i].frequency == 0) continue;
-    const double v = bins[i].value;
-    if (!std::isfinite(v)) return msg = "histogram values must be finite", PC_ERR_INVALID;
-    if (bins[i].frequency > 0xFFFFFFFFull - total) return msg = "more than 2^32-1 initial cells", PC_ERR_UNSUPPORTED;
-    if (I.bin_value.size() + 1 >= (1u << 24)) return msg = "at most 2^24 nonzero bins", PC_ERR_UNSUPPORTED;
-    total += bins[i].frequency;
-    I.bin_value.push_back(v);
-    I.bin_freq.push_back(bins[i].frequency);
+  for (size_t b = 0; b < nb; ++b) {
     uint32_t g = 0;
-    for (double cur = v; cur >= threshold; cur = cur / 2) ++g;
-    chain_len.push_back(g);
+    for (double cur = I.bin_value[b]; cur >= threshold; cur = cur / 2) ++g;
+    chain_len[b] = g;
     chain_total += g;
     longest = std::max(longest, g);
-  }
-  I.roots = total;
-
-  // Phi cap per bin: a cell of generation g divides only while its fluorescence, the bin
-  // value halved g times, still satisfies `f / 2 > phi` (proliferation.cu:323).
-  const size_t nb = I.bin_value.size();
-  I.cap.resize(nb);
-  I.gmax = 0;
-  for (size_t b = 0; b < nb; ++b) {
-    uint32_t c = 0;
-    for (double f = I.bin_value[b]; f / 2 > threshold && c < 4096; f = f / 2) ++c;
-    I.cap[b] = c;
-    I.gmax = std::max(I.gmax, c);
   }
   // Every generation a leaf can have (<= gmax) has a row; chains are never longer.
   I.vidx_stride = std::max(I.gmax, longest) + 1;
@@ -638,8 +598,10 @@ int prepare_instance(const pc_bin* bins, uint64_t n_bins, const pc_cell_type* ty
   I.values.clear();
 
   // The chain of a normal value keeps its mantissa and lowers its exponent by one per
-  // halving, so the value set is enumerated exponent by exponent, each exponent's values in
-  // mantissa order. Used when that grid is dense; otherwise all chain values are sorted.
+  // halving (phi >= 2^-1000 keeps every chain value normal), so the value set is enumerated
+  // exponent by exponent, each exponent's values in mantissa order. Used when that grid is
+  // dense; otherwise all chain values are sorted.
+  bool normal = threshold >= 0x1p-1000;
   struct Chain {
     uint64_t mant;
     int32_t e_hi, len;
@@ -695,8 +657,60 @@ int prepare_instance(const pc_bin* bins, uint64_t n_bins, const pc_cell_type* ty
       I.vidx[(size_t)chain[i].bin * I.vidx_stride + chain[i].gen] = (int32_t)(I.values.size() - 1);
     }
   }
+}
 
-  return prepare_types(types, n_types, I, msg);
+// An instance's bins, phi caps and types from the caller's arrays; with_values also builds
+// its output value set (build_value_set), which only the result merge reads.
+int prepare_instance(const pc_bin* bins, uint64_t n_bins, const pc_cell_type* types, uint32_t n_types,
+                     double t_max, double phi, uint64_t seed, InstanceHost& I, std::string& msg,
+                     bool with_values = true) {
+  if ((n_bins && !bins) || (n_types && !types)) return msg = "null argument", PC_ERR_INVALID;
+  if (!(t_max >= 0.0) || std::isinf(t_max)) return msg = "t_max must be finite and >= 0", PC_ERR_INVALID;
+  if (!(phi >= 0.0) || std::isinf(phi)) return msg = "phi must be finite and > 0 (0 = automatic)", PC_ERR_INVALID;
+  if (n_types == 0)
+    return msg = "ERROR: proportion distribution of cell types does not sum to 1, aborting.", PC_ERR_INVALID;
+  if (n_types > (uint32_t)kMaxTypes) return msg = "at most 64 cell types are supported", PC_ERR_UNSUPPORTED;
+
+  // Threshold (parser.cu:80-96: with no threshold given, the smallest value with a
+  // nonzero frequency; the `threshold == 0.0 ||` test is the reference's).
+  double threshold = phi;
+  if (threshold == 0.0) {
+    for (uint64_t i = 0; i < n_bins; ++i)
+      if (bins[i].frequency > 0 && (threshold == 0.0 || bins[i].value < threshold)) threshold = bins[i].value;
+  }
+  if (!(threshold > 0.0) || std::isinf(threshold)) return msg = "phi must be finite and > 0", PC_ERR_INVALID;
+  I.phi = threshold;
+  I.t_max = (t_max == 0.0) ? 0.0 : t_max;  // normalise -0
+  I.seed = seed;
+
+  // Bins with a nonzero frequency, in file order.
+  uint64_t total = 0;
+  for (uint64_t i = 0; i < n_bins; ++i) {
+    if (bins[i].frequency == 0) continue;
+    const double v = bins[i].value;
+    if (!std::isfinite(v)) return msg = "histogram values must be finite", PC_ERR_INVALID;
+    if (bins[i].frequency > 0xFFFFFFFFull - total) return msg = "more than 2^32-1 initial cells", PC_ERR_UNSUPPORTED;
+    if (I.bin_value.size() + 1 >= (1u << 24)) return msg = "at most 2^24 nonzero bins", PC_ERR_UNSUPPORTED;
+    total += bins[i].frequency;
+    I.bin_value.push_back(v);
+    I.bin_freq.push_back(bins[i].frequency);
+  }
+  I.roots = total;
+
+  // Phi cap per bin: a cell of generation g divides only while its fluorescence, the bin
+  // value halved g times, still satisfies `f / 2 > phi` (proliferation.cu:323).
+  const size_t nb = I.bin_value.size();
+  I.cap.resize(nb);
+  I.gmax = 0;
+  for (size_t b = 0; b < nb; ++b) {
+    uint32_t c = 0;
+    for (double f = I.bin_value[b]; f / 2 > threshold && c < 4096; f = f / 2) ++c;
+    I.cap[b] = c;
+    I.gmax = std::max(I.gmax, c);
+  }
+  const int rc = prepare_types(types, n_types, I, msg);
+  if (rc == PC_OK && with_values) build_value_set(I);
+  return rc;
 }
 
 // The batched form's per-type and per-instance device tables (instances already placed).
@@ -1084,6 +1098,32 @@ int copy_table(pc_context* ctx, pc_plan* p, int which, const unsigned long long*
   return PC_OK;
 }
 
+// A single-instance plan; without its output value set when with_values is false (the
+// caller then builds it with build_value_set before the result merge).
+int plan_create(pc_context* ctx, const pc_bin* bins, uint64_t n_bins, const pc_cell_type* types, uint32_t n_types,
+                double t_max, double phi, uint64_t seed, bool with_values, pc_plan** out) {
+  if (!ctx || !out) return fail(ctx, PC_ERR_INVALID, "null argument");
+  *out = nullptr;
+  pc_plan* p = new (std::nothrow) pc_plan();
+  if (!p) return fail(ctx, PC_ERR_NOMEM, "host allocation");
+  std::memset(&p->stats, 0, sizeof(p->stats));
+  p->id = g_plan_ids.fetch_add(1);
+  p->inst.resize(1);
+  std::string msg;
+  int rc = prepare_instance(bins, n_bins, types, n_types, t_max, phi, seed, p->inst[0], msg, with_values);
+  if (rc != PC_OK) {
+    delete p;
+    return fail(ctx, rc, msg);
+  }
+  rc = finalize_plan(ctx, p);
+  if (rc != PC_OK) {
+    pc_plan_destroy(p);
+    return rc;
+  }
+  *out = p;
+  return PC_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1109,26 +1149,7 @@ int pc_plan_create(pc_context* ctx, const pc_bin* bins, uint64_t n_bins, const p
                    uint32_t n_types, double t_max, double phi, uint64_t seed, pc_plan** out) {
   PC_GUARD_BEGIN
   FaultScope fault_scope__(ctx);
-  if (!ctx || !out) return fail(ctx, PC_ERR_INVALID, "null argument");
-  *out = nullptr;
-  pc_plan* p = new (std::nothrow) pc_plan();
-  if (!p) return fail(ctx, PC_ERR_NOMEM, "host allocation");
-  std::memset(&p->stats, 0, sizeof(p->stats));
-  p->id = g_plan_ids.fetch_add(1);
-  p->inst.resize(1);
-  std::string msg;
-  int rc = prepare_instance(bins, n_bins, types, n_types, t_max, phi, seed, p->inst[0], msg);
-  if (rc != PC_OK) {
-    delete p;
-    return fail(ctx, rc, msg);
-  }
-  rc = finalize_plan(ctx, p);
-  if (rc != PC_OK) {
-    pc_plan_destroy(p);
-    return rc;
-  }
-  *out = p;
-  return PC_OK;
+  return plan_create(ctx, bins, n_bins, types, n_types, t_max, phi, seed, true, out);
   PC_GUARD_END(ctx)
 }
 
@@ -1460,6 +1481,54 @@ int run_persistent(pc_context* ctx, pc_plan* p, const SweepKernels& K, const int
   return PC_OK;
 }
 
+// Bins from which simulate_one builds the output value set on a helper thread.
+constexpr size_t kValueSetThreadBins = 256;
+
+// pc_simulate and pc_simulate_shard: one plan created, run and merged. The output value set,
+// which only the merge reads, is built on a helper thread while the calling thread runs the
+// plan (the run reads none of the instance's value-set fields); small inputs build it first.
+int simulate_one(pc_context* ctx, const pc_bin* bins, uint64_t n_bins, const pc_cell_type* types, uint32_t n_types,
+                 double t_max, double phi, uint64_t seed, const uint64_t* roots, pc_histogram* out) {
+  if (!out) return fail(ctx, PC_ERR_INVALID, "null argument");
+  std::memset(out, 0, sizeof(*out));
+  pc_plan* p = nullptr;
+  int rc = plan_create(ctx, bins, n_bins, types, n_types, t_max, phi, seed, false, &p);
+  if (rc != PC_OK) return rc;
+  if (roots) rc = pc_plan_set_roots(ctx, p, roots[0], roots[1]);
+  if (rc != PC_OK) {
+    pc_plan_destroy(p);
+    return rc;
+  }
+  InstanceHost& I = p->inst[0];
+  std::atomic<bool> built{false};
+  std::thread helper;
+  if (I.bin_value.size() >= kValueSetThreadBins) {
+    try {
+      helper = std::thread([&I, &built] {
+        try {
+          build_value_set(I);
+          built = true;
+        } catch (...) {
+        }
+      });
+    } catch (...) {  // no thread: build it here
+    }
+  }
+  if (!helper.joinable()) {
+    try {
+      build_value_set(I);
+      built = true;
+    } catch (...) {
+    }
+  }
+  rc = pc_plan_run(ctx, p);
+  if (helper.joinable()) helper.join();
+  if (rc == PC_OK && !built) rc = fail(ctx, PC_ERR_NOMEM, "host allocation");
+  if (rc == PC_OK) rc = pc_plan_result(ctx, p, out);
+  pc_plan_destroy(p);
+  return rc;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1595,13 +1664,7 @@ int pc_simulate(pc_context* ctx, const pc_bin* bins, uint64_t n_bins, const pc_c
                 uint32_t n_types, double t_max, double phi, uint64_t seed, pc_histogram* out) {
   PC_GUARD_BEGIN
   FaultScope fault_scope__(ctx);
-  pc_plan* p = nullptr;
-  int rc = pc_plan_create(ctx, bins, n_bins, types, n_types, t_max, phi, seed, &p);
-  if (rc != PC_OK) return rc;
-  rc = pc_plan_run(ctx, p);
-  if (rc == PC_OK) rc = pc_plan_result(ctx, p, out);
-  pc_plan_destroy(p);
-  return rc;
+  return simulate_one(ctx, bins, n_bins, types, n_types, t_max, phi, seed, nullptr, out);
   PC_GUARD_END(ctx)
 }
 
@@ -1610,14 +1673,8 @@ int pc_simulate_shard(pc_context* ctx, const pc_bin* bins, uint64_t n_bins, cons
                       uint64_t root_end, pc_histogram* out) {
   PC_GUARD_BEGIN
   FaultScope fault_scope__(ctx);
-  pc_plan* p = nullptr;
-  int rc = pc_plan_create(ctx, bins, n_bins, types, n_types, t_max, phi, seed, &p);
-  if (rc != PC_OK) return rc;
-  rc = pc_plan_set_roots(ctx, p, root_begin, root_end);
-  if (rc == PC_OK) rc = pc_plan_run(ctx, p);
-  if (rc == PC_OK) rc = pc_plan_result(ctx, p, out);
-  pc_plan_destroy(p);
-  return rc;
+  const uint64_t roots[2] = {root_begin, root_end};
+  return simulate_one(ctx, bins, n_bins, types, n_types, t_max, phi, seed, roots, out);
   PC_GUARD_END(ctx)
 }
 
