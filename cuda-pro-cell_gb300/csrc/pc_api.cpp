@@ -41,6 +41,12 @@ struct LevelBuf {
 };
 
 struct pc_context {
+  // a device buffer kept for reuse
+  struct Spare {
+    void* p = nullptr;
+    size_t bytes = 0;
+  };
+  static constexpr int kSpares = 2;
   int device = 0;
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;
@@ -54,15 +60,14 @@ struct pc_context {
   int opt_graph = 0;                     // persistent driver: replay a captured CUDA graph
   int opt_smooth_predraw = 1;            // smoothed plans keep their lineages' draws in HBM
   int opt_device_merge = 1;              // single-instance results merged on the device
+  uint32_t opt_batch_parts = 4;          // pc_simulate_batch: sub-batches at most
   // resident blocks per SM of each configuration's kernels: [narrow][batched][config]
   int occ[2][2][kNumSweepConfigs][3] = {};
   uint32_t* persist_ctl = nullptr;       // [2] barrier + [8] run totals (u64 [4])
   // the two large per-plan device buffers (root records, count table) of destroyed plans,
-  // kept for the next plan of this context (one of each, the largest)
-  void* spare_rec = nullptr;
-  size_t spare_rec_bytes = 0;
-  void* spare_hist = nullptr;
-  size_t spare_hist_bytes = 0;
+  // kept for the next plans of this context: two of each kind, the largest (the consecutive
+  // sub-batches of pc_simulate_batch alternate between two live plans)
+  Spare spare_rec[kSpares], spare_hist[kSpares];
   std::vector<pc_plan*> live;  // plans created on this context and not yet destroyed
   // pinned host copy of the last count table read back (plan id and run number it holds)
   unsigned long long* stage = nullptr;
@@ -333,28 +338,42 @@ int grid_for(const pc_context* ctx, uint64_t n, int per_sm, int threads) {
 
 // A device buffer of at least `need` bytes: the context's spare one when it is large enough,
 // else a new allocation.
-cudaError_t take_spare(void** spare, size_t* spare_bytes, size_t need, void** out, size_t* out_bytes) {
-  if (*spare && *spare_bytes >= need) {
-    *out = *spare;
-    *out_bytes = *spare_bytes;
-    *spare = nullptr;
-    *spare_bytes = 0;
+// The smallest spare of at least `need` bytes, else a new allocation of `need` bytes.
+using Spare = pc_context::Spare;
+constexpr int kSpares = pc_context::kSpares;
+
+cudaError_t take_spare(Spare* spare, size_t need, void** out, size_t* out_bytes) {
+  int best = -1;
+  for (int i = 0; i < kSpares; ++i)
+    if (spare[i].p && spare[i].bytes >= need && (best < 0 || spare[i].bytes < spare[best].bytes)) best = i;
+  if (best >= 0) {
+    *out = spare[best].p;
+    *out_bytes = spare[best].bytes;
+    spare[best] = Spare();
     return cudaSuccess;
   }
   *out_bytes = need;
   return pc_cuda_malloc(out, need);
 }
 
-// Keep the larger of `buf` and the context's spare, free the other.
-void give_spare(void** spare, size_t* spare_bytes, void* buf, size_t bytes) {
+// Keep the kSpares largest of `buf` and the spares, free the rest.
+void give_spare(Spare* spare, void* buf, size_t bytes) {
   if (!buf) return;
-  if (*spare && *spare_bytes >= bytes) {
+  int slot = 0;  // an empty slot, else the smallest spare
+  for (int i = 0; i < kSpares; ++i) {
+    if (!spare[i].p) {
+      slot = i;
+      break;
+    }
+    if (spare[i].bytes < spare[slot].bytes) slot = i;
+  }
+  if (spare[slot].p && spare[slot].bytes >= bytes) {
     pc_cuda_free(buf);
     return;
   }
-  pc_cuda_free(*spare);
-  *spare = buf;
-  *spare_bytes = bytes;
+  pc_cuda_free(spare[slot].p);
+  spare[slot].p = buf;
+  spare[slot].bytes = bytes;
 }
 
 // f(i) for i in [0, n) on up to `threads` host threads (0 = all cores), the calling thread
@@ -454,8 +473,10 @@ void pc_destroy(pc_context* ctx) {
   if (ctx->stream) pc_cuda_sync(ctx->stream);
   free_pool(ctx);
   for (pc_plan* p : ctx->live) p->owner = nullptr;  // plans outliving their context free their own buffers
-  pc_cuda_free(ctx->spare_rec);
-  pc_cuda_free(ctx->spare_hist);
+  for (int i = 0; i < kSpares; ++i) {
+    pc_cuda_free(ctx->spare_rec[i].p);
+    pc_cuda_free(ctx->spare_hist[i].p);
+  }
   pc_cuda_free(ctx->merge_dev);
   cudaFreeHost(ctx->merge_host);
   pc_cuda_free(ctx->zig_dev);
@@ -506,6 +527,9 @@ int pc_set_option(pc_context* ctx, const char* name, double value) {
     ctx->opt_smooth_predraw = value != 0.0 ? 1 : 0;
   } else if (n == "device_merge") {
     ctx->opt_device_merge = value != 0.0 ? 1 : 0;
+  } else if (n == "batch_parts") {
+    if (value < 1 || value > 64) return fail(ctx, PC_ERR_INVALID, "batch_parts must be 1..64");
+    ctx->opt_batch_parts = (uint32_t)value;
   } else if (n == "fail_nth_call") {
     // counted from the calls made so far: the n-th call after this one fails (0: none)
     ctx->fail_at = value >= 1.0 ? ctx->cuda_calls + (uint64_t)value : 0;
@@ -852,10 +876,10 @@ int finalize_device(pc_context* ctx, pc_plan* p, const PlanTables& t) {
   p->owner = ctx;
   ctx->live.push_back(p);
   if (e == cudaSuccess)
-    e = take_spare(&ctx->spare_rec, &ctx->spare_rec_bytes, std::max<uint64_t>(1, chunk) * sizeof(unsigned long long),
+    e = take_spare(ctx->spare_rec, std::max<uint64_t>(1, chunk) * sizeof(unsigned long long),
                    reinterpret_cast<void**>(&p->root_rec_dev), &p->rec_bytes);
   if (e == cudaSuccess)
-    e = take_spare(&ctx->spare_hist, &ctx->spare_hist_bytes, p->hist_elems * sizeof(unsigned long long),
+    e = take_spare(ctx->spare_hist, p->hist_elems * sizeof(unsigned long long),
                    reinterpret_cast<void**>(&p->hist_dev), &p->hist_bytes);
   if (e == cudaSuccess && nb)
     e = pc_cuda_copy(p->bin_info_dev, p->bin_info.data(), nb * sizeof(uint32_t), cudaMemcpyHostToDevice, st);
@@ -1178,8 +1202,8 @@ void pc_plan_destroy(pc_plan* p) {
   if (p->owner) {
     pc_context* ctx = p->owner;
     ctx->live.erase(std::remove(ctx->live.begin(), ctx->live.end(), p), ctx->live.end());
-    give_spare(&ctx->spare_rec, &ctx->spare_rec_bytes, p->root_rec_dev, p->rec_bytes);
-    give_spare(&ctx->spare_hist, &ctx->spare_hist_bytes, p->hist_dev, p->hist_bytes);
+    give_spare(ctx->spare_rec, p->root_rec_dev, p->rec_bytes);
+    give_spare(ctx->spare_hist, p->hist_dev, p->hist_bytes);
   } else {
     pc_cuda_free(p->root_rec_dev);
     pc_cuda_free(p->hist_dev);
@@ -1868,12 +1892,12 @@ int pc_simulate_batch(pc_context* ctx, const pc_instance* instances, uint32_t n_
   if (!ctx || !out) return fail(ctx, PC_ERR_INVALID, "null argument");
   if (n_instances && !instances) return fail(ctx, PC_ERR_INVALID, "null argument");
   for (uint32_t i = 0; i < n_instances; ++i) std::memset(out + i, 0, sizeof(pc_histogram));
-  // Large batches run as consecutive sub-batches of up to 4 parts. While the device runs one
-  // part, a host thread prepares the next (its instances, layout and tables: everything but
-  // the uploads) and host threads merge the previous part's histograms (for 4096 instances
-  // about 0.5 GB of host output). Every instance's counts depend on that instance alone, so
-  // the split changes no result.
-  const uint32_t parts = std::min<uint32_t>(4u, std::max<uint32_t>(1u, n_instances / 1024u));
+  // Large batches run as consecutive sub-batches of up to batch_parts parts (at least 256
+  // instances each). While the device runs one part, a host thread prepares the next (its
+  // instances, layout and tables: everything but the uploads) and host threads merge the
+  // previous part's histograms (for 4096 instances about 0.5 GB of host output). Every
+  // instance's counts depend on that instance alone, so the split changes no result.
+  const uint32_t parts = std::min<uint32_t>(ctx->opt_batch_parts, std::max<uint32_t>(1u, n_instances / 256u));
   const uint64_t max_root_chunk = ctx->opt_max_root_chunk;
   // the first and the last part, whose preparation and merge overlap nothing, are half the
   // size of the others (weights 1, 2, ..., 2, 1)
