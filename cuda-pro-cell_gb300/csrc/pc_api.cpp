@@ -68,6 +68,7 @@ struct pc_context {
   // kept for the next plans of this context: two of each kind, the largest (the consecutive
   // sub-batches of pc_simulate_batch alternate between two live plans)
   Spare spare_rec[kSpares], spare_hist[kSpares];
+  Spare spare_tables[kSpares];  // ... and of their small tables (one allocation per plan)
   std::vector<pc_plan*> live;  // plans created on this context and not yet destroyed
   // pinned host copy of the last count table read back (plan id and run number it holds)
   unsigned long long* stage = nullptr;
@@ -131,6 +132,8 @@ struct pc_plan {
   uint32_t* bin_class_dev = nullptr;
   uint32_t* bin_info_dev = nullptr;
   uint64_t* bin_start_dev = nullptr;
+  void* tables_dev = nullptr;           // the tables above, one allocation
+  size_t tables_bytes = 0;
   unsigned long long* root_rec_dev = nullptr;
   unsigned long long* hist_dev = nullptr;
   size_t hist_elems = 0;
@@ -476,6 +479,7 @@ void pc_destroy(pc_context* ctx) {
   for (int i = 0; i < kSpares; ++i) {
     pc_cuda_free(ctx->spare_rec[i].p);
     pc_cuda_free(ctx->spare_hist[i].p);
+    pc_cuda_free(ctx->spare_tables[i].p);
   }
   pc_cuda_free(ctx->merge_dev);
   cudaFreeHost(ctx->merge_host);
@@ -871,10 +875,36 @@ int finalize_device(pc_context* ctx, pc_plan* p, const PlanTables& t) {
   const size_t nb = p->nbins;
   p->hist_elems = (size_t)p->hist_gens * std::max<uint64_t>(1, p->nclass);
   p->upload_bytes = nb * sizeof(uint32_t) + (nb + 1) * sizeof(uint64_t);
-  cudaError_t e = pc_cuda_malloc(&p->bin_info_dev, std::max<size_t>(1, nb) * sizeof(uint32_t));
-  if (e == cudaSuccess) e = pc_cuda_malloc(&p->bin_start_dev, (nb + 1) * sizeof(uint64_t));
+  // The plan's small tables share one device allocation (a spare of the context when one is
+  // large enough), each at a 16-byte boundary: no allocator call per table on creation or
+  // destruction.
+  size_t tables = 0;
+  auto place = [&tables](size_t bytes) {
+    const size_t at = tables;
+    tables += (std::max<size_t>(1, bytes) + 15) & ~size_t(15);
+    return at;
+  };
+  const size_t nt = p->batched ? 0 : p->inst[0].types.size();
+  const size_t o_info = place(nb * sizeof(uint32_t)), o_start = place((nb + 1) * sizeof(uint64_t));
+  const size_t o_types = place(nt * sizeof(TypeDev)), o_btypes = place(btypes.size() * sizeof(BatchType));
+  const size_t o_inst = place(idev.size() * sizeof(InstanceDev));
+  const size_t o_binst = place(p->batched ? nb * sizeof(uint32_t) : 0), o_bclass = place(p->batched ? nb * sizeof(uint32_t) : 0);
   p->owner = ctx;
   ctx->live.push_back(p);
+  cudaError_t e = take_spare(ctx->spare_tables, tables, &p->tables_dev, &p->tables_bytes);
+  if (e == cudaSuccess) {
+    char* base = static_cast<char*>(p->tables_dev);
+    p->bin_info_dev = reinterpret_cast<uint32_t*>(base + o_info);
+    p->bin_start_dev = reinterpret_cast<uint64_t*>(base + o_start);
+    if (!p->batched) {
+      p->types_dev = reinterpret_cast<TypeDev*>(base + o_types);
+    } else {
+      p->btypes_dev = reinterpret_cast<BatchType*>(base + o_btypes);
+      p->inst_dev = reinterpret_cast<InstanceDev*>(base + o_inst);
+      p->bin_inst_dev = reinterpret_cast<uint32_t*>(base + o_binst);
+      p->bin_class_dev = reinterpret_cast<uint32_t*>(base + o_bclass);
+    }
+  }
   if (e == cudaSuccess)
     e = take_spare(ctx->spare_rec, std::max<uint64_t>(1, chunk) * sizeof(unsigned long long),
                    reinterpret_cast<void**>(&p->root_rec_dev), &p->rec_bytes);
@@ -886,16 +916,10 @@ int finalize_device(pc_context* ctx, pc_plan* p, const PlanTables& t) {
   if (e == cudaSuccess)
     e = pc_cuda_copy(p->bin_start_dev, p->bin_start.data(), (nb + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, st);
   if (!p->batched) {
-    const size_t nt = p->inst[0].types.size();
-    if (e == cudaSuccess) e = pc_cuda_malloc(&p->types_dev, nt * sizeof(TypeDev));
     if (e == cudaSuccess)
       e = pc_cuda_copy(p->types_dev, p->inst[0].types.data(), nt * sizeof(TypeDev), cudaMemcpyHostToDevice, st);
     p->upload_bytes += nt * sizeof(TypeDev);
   } else {
-    if (e == cudaSuccess) e = pc_cuda_malloc(&p->btypes_dev, btypes.size() * sizeof(BatchType));
-    if (e == cudaSuccess) e = pc_cuda_malloc(&p->inst_dev, idev.size() * sizeof(InstanceDev));
-    if (e == cudaSuccess) e = pc_cuda_malloc(&p->bin_inst_dev, std::max<size_t>(1, nb) * sizeof(uint32_t));
-    if (e == cudaSuccess) e = pc_cuda_malloc(&p->bin_class_dev, std::max<size_t>(1, nb) * sizeof(uint32_t));
     if (e == cudaSuccess)
       e = pc_cuda_copy(p->btypes_dev, btypes.data(), btypes.size() * sizeof(BatchType), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess)
@@ -1122,6 +1146,15 @@ int copy_table(pc_context* ctx, pc_plan* p, int which, const unsigned long long*
   return PC_OK;
 }
 
+// Frees a plan's host tables once its results are merged (for a sub-batch of thousands of
+// instances, tens of thousands of vectors: milliseconds that pc_simulate_batch spends on a
+// merge thread rather than on the thread that feeds the device). Touches no device state.
+void release_host_tables(pc_plan* p) {
+  std::vector<InstanceHost>().swap(p->inst);
+  std::vector<uint64_t>().swap(p->bin_start);
+  std::vector<uint32_t>().swap(p->bin_info);
+}
+
 // A single-instance plan; without its output value set when with_values is false (the
 // caller then builds it with build_value_set before the result merge).
 int plan_create(pc_context* ctx, const pc_bin* bins, uint64_t n_bins, const pc_cell_type* types, uint32_t n_types,
@@ -1192,19 +1225,14 @@ int pc_plan_set_roots(pc_context* ctx, pc_plan* p, uint64_t root_begin, uint64_t
 void pc_plan_destroy(pc_plan* p) {
   if (!p) return;
   if (p->graph) cudaGraphExecDestroy(p->graph);
-  pc_cuda_free(p->types_dev);
-  pc_cuda_free(p->btypes_dev);
-  pc_cuda_free(p->inst_dev);
-  pc_cuda_free(p->bin_inst_dev);
-  pc_cuda_free(p->bin_class_dev);
-  pc_cuda_free(p->bin_info_dev);
-  pc_cuda_free(p->bin_start_dev);
   if (p->owner) {
     pc_context* ctx = p->owner;
     ctx->live.erase(std::remove(ctx->live.begin(), ctx->live.end(), p), ctx->live.end());
+    give_spare(ctx->spare_tables, p->tables_dev, p->tables_bytes);
     give_spare(ctx->spare_rec, p->root_rec_dev, p->rec_bytes);
     give_spare(ctx->spare_hist, p->hist_dev, p->hist_bytes);
   } else {
+    pc_cuda_free(p->tables_dev);
     pc_cuda_free(p->root_rec_dev);
     pc_cuda_free(p->hist_dev);
   }
@@ -1892,19 +1920,18 @@ int pc_simulate_batch(pc_context* ctx, const pc_instance* instances, uint32_t n_
   if (!ctx || !out) return fail(ctx, PC_ERR_INVALID, "null argument");
   if (n_instances && !instances) return fail(ctx, PC_ERR_INVALID, "null argument");
   for (uint32_t i = 0; i < n_instances; ++i) std::memset(out + i, 0, sizeof(pc_histogram));
-  // Large batches run as consecutive sub-batches of up to batch_parts parts (at least 256
-  // instances each). While the device runs one part, a host thread prepares the next (its
+  // Large batches run as min(batch_parts, n / 256) consecutive sub-batches. While the device runs one part, a host thread prepares the next (its
   // instances, layout and tables: everything but the uploads) and host threads merge the
   // previous part's histograms (for 4096 instances about 0.5 GB of host output). Every
   // instance's counts depend on that instance alone, so the split changes no result.
   const uint32_t parts = std::min<uint32_t>(ctx->opt_batch_parts, std::max<uint32_t>(1u, n_instances / 256u));
   const uint64_t max_root_chunk = ctx->opt_max_root_chunk;
-  // the first and the last part, whose preparation and merge overlap nothing, are half the
-  // size of the others (weights 1, 2, ..., 2, 1)
+  // the first and the last part, whose preparation and merge overlap nothing, are a quarter
+  // of the size of the others (weights 1, 4, ..., 4, 1)
   auto first_of = [&](uint32_t part) {
     if (parts == 1) return part == 0 ? 0u : n_instances;
-    const uint64_t total = 2ull * parts - 2ull;
-    const uint64_t w = part == 0 ? 0ull : (part == parts ? total : 2ull * part - 1ull);
+    const uint64_t total = 4ull * parts - 6ull;
+    const uint64_t w = part == 0 ? 0ull : (part == parts ? total : 4ull * part - 3ull);
     return (uint32_t)((uint64_t)n_instances * w / total);
   };
   std::vector<int> codes(n_instances, PC_OK);
@@ -1993,6 +2020,7 @@ int pc_simulate_batch(pc_context* ctx, const pc_instance* instances, uint32_t n_
         merging.th = std::thread([merge, &codes, &msgs, b, h, first]() {
           try {
             merge(b, h, first);
+            release_host_tables(b);
           } catch (...) {
             for (uint32_t i = 0; i < (uint32_t)b->inst.size(); ++i) {
               codes[first + i] = PC_ERR_NOMEM;

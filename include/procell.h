@@ -123,9 +123,9 @@ int pc_set_stream(pc_context* ctx, void* stream);
  *                         histogram on the device; 0: reads the count table back and
  *                         merges on the host (as it does anyway for merge scratch above
  *                         256 MB)
- *   "batch_parts"         1-64: pc_simulate_batch runs a batch as at most this many
- *                         consecutive sub-batches of >= 256 instances, preparing the next
- *                         and merging the previous on host threads while one runs (default 4)
+ *   "batch_parts"         1-64: pc_simulate_batch runs n instances as min(batch_parts,
+ *                         n / 256) consecutive sub-batches, preparing the next and merging
+ *                         the previous on host threads while one runs (default 4)
  *   "smooth_predraw"      1 (default): pc_smooth_create draws every sampled lineage's
  *                         normals and initial age once and keeps them in device memory
  *                         (when they fit in 1 GB); 0: every pass draws them again
