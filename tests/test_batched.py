@@ -186,13 +186,18 @@ def tiny_instances(n, seed):
     return instances
 
 
-@pytest.mark.parametrize("n", [7, 2100])
-def test_simulate_batch_matches_one_batch(engine, n):
+@pytest.mark.parametrize("n,parts", [(7, 4), (2100, 4), (2100, 3), (2100, 64), (2100, 1)])
+def test_simulate_batch_matches_one_batch(engine, n, parts):
     """pc_simulate_batch (host inputs in, merged histograms out) equals pc_batch_result of one
-    batch run, instance by instance. From 2048 instances on it runs the batch as sub-batches,
-    merging one on host threads while the device runs the next: results must not change."""
+    batch run, instance by instance. It runs n instances as min(batch_parts, n / 256)
+    sub-batches (weights 1, 4, ..., 4, 1), preparing the next and merging the previous on host
+    threads while the device runs one: results must not change with the split."""
     instances = small_uneven(n, seed=5) if n < 100 else tiny_instances(n, seed=77)
-    got = engine.simulate_batch(instances)
+    engine.set_option("batch_parts", parts)
+    try:
+        got = engine.simulate_batch(instances)
+    finally:
+        engine.set_option("batch_parts", 4)
     b = engine.batch(instances)
     try:
         b.run()
@@ -205,6 +210,15 @@ def test_simulate_batch_matches_one_batch(engine, n):
             assert got[i].stats["roots"] == want.stats["roots"], i
     finally:
         b.close()
+
+
+def test_batch_parts_option_bounds(engine):
+    """batch_parts takes 1..64; other values are rejected."""
+    for bad in (0, 65, 0.5):
+        with pytest.raises(ProcellError):
+            engine.set_option("batch_parts", bad)
+    engine.set_option("batch_parts", 64)
+    engine.set_option("batch_parts", 4)
 
 
 def test_set_types_and_totals(engine):
