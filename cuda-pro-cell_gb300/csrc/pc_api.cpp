@@ -567,6 +567,8 @@ int prepare_types(const pc_cell_type* types, uint32_t n_types, InstanceHost& I, 
   for (uint32_t i = 0; i < n_types; ++i) {
     if (!std::isfinite(types[i].ratio) || !std::isfinite(types[i].mean) || !std::isfinite(types[i].sd))
       return msg = "cell type parameters must be finite", PC_ERR_INVALID;
+    if (types[i].mean > 0.0 && !(std::fabs(types[i].sd) < kMaxSigma))
+      return msg = "cell type standard deviations must be below 2^127", PC_ERR_UNSUPPORTED;
     sum += types[i].ratio;
   }
   if (std::fabs(1.0 - sum) > 1.0 / std::pow(10.0, 8.0))
@@ -583,7 +585,7 @@ int prepare_types(const pc_cell_type* types, uint32_t n_types, InstanceHost& I, 
     acc += src.ratio;
     t.cum = acc;
     t.mu = src.mean;
-    t.sigma = src.sd;
+    t.sigma = std::ldexp(src.sd, kSigmaShift);
     t.t_max = I.t_max;
     t.mode = src.mean < 0.0 ? kModeQuiescent : (src.mean == 0.0 ? kModeZeroMean : kModeNormal);
     truncation_bounds(src.mean, src.sd, t.zlo, t.zhi);

@@ -43,10 +43,17 @@ constexpr int kWarpsPerBlock = kBlock / 32;
 
 enum TypeMode : int32_t { kModeNormal = 0, kModeQuiescent = 1, kModeZeroMean = 2 };
 
+// The sweeps keep each type's sd scaled by 2^kSigmaShift and widen a float normal z to the
+// double z x 2^-kSigmaShift by moving its bits (exact, no rebias: widen_scaled in
+// pc_sweeps.cuh); the FMA's product is exact, so the timer is fma(sd, z, mean) bit for bit.
+// |sd| < kMaxSigma keeps the scaled sd finite.
+constexpr int kSigmaShift = 896;
+constexpr double kMaxSigma = 0x1p127;
+
 // One cell type, in the descending-ratio order the reference samples in.
 // The division sweep reads bytes 0-31 (mu, sigma, zlo, zhi, t_max) as two 16-byte loads.
 struct alignas(16) TypeDev {
-  double mu, sigma;  // 0, 8: tau = fma(sigma, z, mu)
+  double mu, sigma;  // 0, 8: mean, sd x 2^kSigmaShift (tau = fma(sd, z, mean))
   float zlo, zhi;    // 16: the FP32 z range for which fma(sigma, z, mu) > 0 (the truncation)
   double t_max;      // 24: its instance's t_max (read by the batched sweeps; plain: RunArgs)
   double cum;        // 32: cumulative ratio in this order

@@ -166,6 +166,8 @@ extern "C" int pc_simulate_noalloc(const pc_bin* bins, uint64_t n_bins, const pc
   for (uint32_t i = 0; i < n_types; ++i) {
     if (!std::isfinite(types[i].ratio) || !std::isfinite(types[i].mean) || !std::isfinite(types[i].sd))
       return fail(err, err_len, PC_ERR_INVALID, "cell type parameters must be finite");
+    if (types[i].mean > 0.0 && !(std::fabs(types[i].sd) < kMaxSigma))
+      return fail(err, err_len, PC_ERR_UNSUPPORTED, "cell type standard deviations must be below 2^127");
     sum += types[i].ratio;
   }
   if (std::fabs(1.0 - sum) > 1.0 / std::pow(10.0, 8.0))
@@ -192,7 +194,7 @@ extern "C" int pc_simulate_noalloc(const pc_bin* bins, uint64_t n_bins, const pc
     acc += src.ratio;
     t.cum = acc;
     t.mu = src.mean;
-    t.sigma = src.sd;
+    t.sigma = std::ldexp(src.sd, kSigmaShift);
     t.t_max = tmax;
     t.mode = src.mean < 0.0 ? kModeQuiescent : (src.mean == 0.0 ? kModeZeroMean : kModeNormal);
     host_truncation_bounds(src.mean, src.sd, t.zlo, t.zhi);

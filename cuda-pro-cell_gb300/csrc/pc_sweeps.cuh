@@ -147,14 +147,17 @@ enum Fate : int { kNone = 0, kLeaf = 1, kEmit = 2, kVanish = 3 };
 // GB300 runs FP64 arithmetic and every FP64<->FP32 conversion on a pipe of 2 lanes per
 // clock per SM, so the conversion and the comparison below are done on the bits instead.
 //
-// Exact float -> double for zero or a normal float (z is never subnormal: |z| >= the
-// smallest ziggurat strip width, about 1e-10): rebias the exponent, widen the mantissa.
-__device__ __forceinline__ double f32_to_f64(float z) {
+// z x 2^-kSigmaShift as a double, exactly, for every finite float (zero and subnormals
+// included): the float's sign, exponent and mantissa move into the double's fields
+// unchanged (an arithmetic shift by 3 carries the sign, the mask clears the three bits it
+// copied into the exponent's top), where the double's bias, 896 larger, reads them. The
+// sweeps pair it with the type's sd stored as sd x 2^kSigmaShift, so fma(sigma, widen(z),
+// mu) is fma(sd, z, mean) bit for bit: two integer operations, no rebias and no zero test.
+__device__ __forceinline__ double widen_scaled(float z) {
   const uint32_t f = __float_as_uint(z);
-  const uint32_t a = f & 0x7FFFFFFFu;
-  const uint32_t hi = (f & 0x80000000u) | (a ? (a >> 3) + (896u << 20) : 0u);
-  return __hiloint2double((int)hi, (int)(f << 29));
+  return __hiloint2double((int)((uint32_t)((int32_t)f >> 3) & 0x8FFFFFFFu), (int)(f << 29));
 }
+static_assert(kSigmaShift == 1023 - 127, "the float's exponent field read with the double's bias");
 
 // a > b for non-negative doubles (IEEE order equals integer order of the bit patterns).
 __device__ __forceinline__ bool gt_nonneg(double a, double b) {
@@ -163,7 +166,7 @@ __device__ __forceinline__ bool gt_nonneg(double a, double b) {
 
 // What a cell's type, and in the batched form its instance, supplies to the sweeps.
 struct TypeCtx {
-  double mu, sigma;     // tau = fma(sigma, z, mu)
+  double mu, sigma;     // mean, sd x 2^kSigmaShift: tau = fma(sigma, widen_scaled(z), mu)
   float zlo, zhi;       // truncation bounds on z
   double t_max;
   uint64_t root_begin;  // batch index of the instance's first initial cell
@@ -207,11 +210,11 @@ __device__ __forceinline__ uint32_t rec_type(unsigned long long r) { return (uin
 __device__ __forceinline__ uint32_t rec_cap(unsigned long long r) { return (uint32_t)(r >> 48) & 0xFFu; }
 __device__ __forceinline__ bool rec_clamped(unsigned long long r) { return ((r >> 57) & 1ull) != 0ull; }
 
-// Fate of one daughter born at `birth` with normal z: due = birth + fma(sigma, z, mu), the
+// Fate of one daughter born at `birth` with normal z: due = birth + fma(sd, z, mean), the
 // reference's t + timer; a leaf if due > t_max (proliferation.cu:404-410), else it divides
 // again when its phi cap allows and vanishes when not.
 __device__ __forceinline__ int fate(double birth, float z, const TypeCtx& c, bool can_divide, double& due) {
-  due = birth + fma(c.sigma, f32_to_f64(z), c.mu);
+  due = birth + fma(c.sigma, widen_scaled(z), c.mu);
   if (gt_nonneg(due, c.t_max)) return kLeaf;
   return can_divide ? kEmit : kVanish;
 }
@@ -381,7 +384,7 @@ __device__ void root_body(const RunArgs& a, const uint64_t root_base, const uint
                                 : philox_ks(u32x4{0u, 0u, root, kPurposePair}, a.ks);
         const float z = draw_z(P.y, pair_layer(P, 1u), pair_wedge_bits(P, 1u), 1ull, root, k0, k1, T.zlo, T.zhi,
                                s.zig_or(a), a.error);
-        const double tau = fma(T.sigma, f32_to_f64(z), T.mu);  // 0 for zero-mean types
+        const double tau = fma(T.sigma, widen_scaled(z), T.mu);  // 0 for zero-mean types
         d0 = tau * u_age + tau;  // t = tau * U (cell.cu:124-143), due = t + timer
         leaf = gt_nonneg(d0, t_max);
       }
@@ -494,15 +497,15 @@ __device__ __forceinline__ CellDraw classify(const ulonglong2 c, bool act, uint3
   const uint32_t l0 = pair_layer(P, 0u), l1 = pair_layer(P, 1u);
   float z0 = __fmul_rn((float)(P.x & 0x7FFFFFFFu), Z.w[l0]);
   float z1 = __fmul_rn((float)(P.y & 0x7FFFFFFFu), Z.w[l1]);
-  z0 = (P.x >> 31) ? -z0 : z0;
-  z1 = (P.y >> 31) ? -z1 : z1;
+  z0 = __uint_as_float(__float_as_uint(z0) ^ (P.x & 0x80000000u));  // the sign bit of j
+  z1 = __uint_as_float(__float_as_uint(z1) ^ (P.y & 0x80000000u));
   const float zlo = tc.zlo, zhi = tc.zhi;
   const bool ok0 = act && (P.x & 0x7FFFFFFFu) < Z.k[l0] && z0 >= zlo && z0 <= zhi;
   const bool ok1 = act && (P.y & 0x7FFFFFFFu) < Z.k[l1] && z1 >= zlo && z1 <= zhi;
   // exact FP64 due times (the reference's t + timer): they decide leaves and are what an
   // emitted daughter stores
-  r.due0 = d + fma(tc.sigma, f32_to_f64(z0), tc.mu);
-  r.due1 = d + fma(tc.sigma, f32_to_f64(z1), tc.mu);
+  r.due0 = d + fma(tc.sigma, widen_scaled(z0), tc.mu);
+  r.due1 = d + fma(tc.sigma, widen_scaled(z1), tc.mu);
   const bool leaf0 = ok0 && gt_nonneg(r.due0, tc.t_max);
   const bool leaf1 = ok1 && gt_nonneg(r.due1, tc.t_max);
   r.em0 = ok0 && !leaf0 && can_divide;
