@@ -810,17 +810,20 @@ int finalize_host(pc_plan* p, uint64_t max_root_chunk, PlanTables& t, std::strin
   p->root_begin = 0;
   p->root_end = roots;
 
-  // Root chunk and key layout: key = root_local * 2^g + path must fit 64 bits; the narrow
-  // layout (root_local << 32 | heap node) needs root_local < 2^32.
+  // Root chunk and key layout: key = root_local * 2^g + path must fit 64 bits for every
+  // generation a key can have: the stored cells (g < cap <= gmax) and the daughters of the
+  // deepest of them, one generation further, which are parked with a key when their first
+  // draw is not settled. So gmax path bits; the narrow layout (root_local << 32 | heap node
+  // 2^g + path) holds generations up to 31 and needs root_local < 2^32.
   uint64_t chunk = std::max<uint64_t>(1, roots);
-  const uint32_t want_bits = gmax >= 45 ? 20u : 65u - gmax;  // room for gmax - 1 path bits
+  const uint32_t want_bits = gmax >= 45 ? 20u : 64u - gmax;
   if (want_bits < 64) chunk = std::min<uint64_t>(chunk, 1ull << want_bits);
-  if (gmax <= 32) chunk = std::min<uint64_t>(chunk, 1ull << 32);
+  if (gmax <= kNarrowMaxGen) chunk = std::min<uint64_t>(chunk, 1ull << 32);
   if (p->batched) chunk = std::min<uint64_t>(chunk, 1ull << 28);  // 2 GiB of root records
   if (max_root_chunk) chunk = std::min<uint64_t>(chunk, std::max<uint64_t>(1, max_root_chunk));
   p->chunk = chunk;
   const uint32_t rb = bits_for(chunk);
-  p->g_store_max = std::min<uint32_t>(62u, 64u - rb);
+  p->g_store_max = std::min<uint32_t>(62u, 63u - rb);  // its daughters' keys fit as well
   p->hist_gens = std::min(gmax, p->g_store_max + 1) + 1;
 
   // Per-bin tables (first initial cell, cap and flags; in a batch also the instance and first
@@ -1601,7 +1604,7 @@ int pc_plan_run(pc_context* ctx, pc_plan* p) {
   p->stats.roots = nroots;
   p->ran = true;
   ++p->run_id;
-  const bool narrow = p->gmax <= 32;
+  const bool narrow = p->gmax <= kNarrowMaxGen;
   const int config = narrow ? ctx->opt_config : kDefaultSweepConfig;
   const SweepKernels& K = sweep_kernels(narrow, p->batched, config);
   int occ[3];
@@ -2051,7 +2054,7 @@ int pc_autotune(pc_context* ctx, pc_plan* p, uint32_t repeats, pc_tuning* out) {
   if (!ctx || !p || !out) return PC_ERR_INVALID;
   std::memset(out, 0, sizeof(*out));
   repeats = std::max<uint32_t>(1, repeats);
-  const bool narrow = p->gmax <= 32;
+  const bool narrow = p->gmax <= kNarrowMaxGen;
   const int saved[3] = {ctx->opt_config, ctx->opt_driver, ctx->opt_graph};
   double best = 1e300, dflt = 0.0, best_persist = 1e300;
   int best_cfg = kDefaultSweepConfig, best_drv = 0, n = 0, persist_cfg = kDefaultSweepConfig;

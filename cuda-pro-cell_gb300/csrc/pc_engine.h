@@ -9,9 +9,12 @@
 //   names the tree node: its root (chunk-local index) and its heap index
 //   node = 2^g + path for a cell of generation g, path being its g left/right choices
 //   from the root (the Philox node address). Two layouts:
-//     narrow (every stored generation <= 31): key = root_local << 32 | node, so the
-//            daughters' keys are key + node + c with 32-bit arithmetic;
-//     wide   (deeper trees):                   key = root_local * 2^g + path.
+//     narrow (gmax <= 31, so that every key, a stored cell's or a parked daughter's one
+//            generation below the deepest stored one, has g <= 31):
+//            key = root_local << 32 | node, so the daughters' keys are key + node + c
+//            with no carry out of the node's 32 bits;
+//     wide   (deeper trees):                   key = root_local * 2^g + path, with
+//            root bits + g <= 64 for every g up to gmax (chunk and g_store_max sized so).
 //   Fluorescence is never stored: it is the bin value halved g times.
 // * A level buffer holds the cells of one generation that will divide. It is split into
 //   one segment per warp of the kernel that produced it; segment s holds count[s]
@@ -48,6 +51,9 @@ enum TypeMode : int32_t { kModeNormal = 0, kModeQuiescent = 1, kModeZeroMean = 2
 // pc_sweeps.cuh); the FMA's product is exact, so the timer is fma(sd, z, mean) bit for bit.
 // |sd| < kMaxSigma keeps the scaled sd finite.
 constexpr int kSigmaShift = 896;
+
+// Deepest phi cap (gmax) the narrow key layout serves.
+constexpr uint32_t kNarrowMaxGen = 31;
 constexpr double kMaxSigma = 0x1p127;
 
 // One cell type, in the descending-ratio order the reference samples in.

@@ -208,9 +208,9 @@ extern "C" int pc_simulate_noalloc(const pc_bin* bins, uint64_t n_bins, const pc
 
   // key layout (as pc_plan_create): the generation limit follows the full root count
   uint64_t key_chunk = std::max<uint64_t>(1, total);
-  const uint32_t want_bits = gmax >= 45 ? 20u : 65u - gmax;
+  const uint32_t want_bits = gmax >= 45 ? 20u : 64u - gmax;
   if (want_bits < 64) key_chunk = std::min<uint64_t>(key_chunk, 1ull << want_bits);
-  const uint32_t g_store_max = std::min<uint32_t>(62u, 64u - bits_for(key_chunk));
+  const uint32_t g_store_max = std::min<uint32_t>(62u, 63u - bits_for(key_chunk));
   const uint32_t hist_gens = std::min(gmax, g_store_max + 1) + 1;
   const uint64_t hist_elems = (uint64_t)hist_gens * nb * n_types;
   dims[0] = hist_gens;
@@ -338,7 +338,7 @@ extern "C" int pc_simulate_noalloc(const pc_bin* bins, uint64_t n_bins, const pc
   a.hist = (unsigned long long*)(S + hist_off);
   a.stats = stats_dev;
   a.error = error_dev;
-  const bool narrow = gmax <= 32;
+  const bool narrow = gmax <= kNarrowMaxGen;
 
   // --- root chunks, then generation slices depth-first (as pc_plan_run) ---------------
   struct Entry {

@@ -100,6 +100,10 @@ EDGE_CASES = {
     "ratio_ties": ([(300.0, 3000)], [(0.25, 10.0, 3.0), (0.25, 20.0, 3.0), (0.5, 15.0, 2.0)], 80.0, 1.0),
     "zero_ratio_type": ([(300.0, 3000)], [(0.0, 10.0, 3.0), (1.0, 20.0, 3.0)], 80.0, 1.0),
     "deep_tree": ([(2.0 ** 40, 3)], [(1.0, 1.0, 0.05)], 30.0, 1.0),
+    # phi cap exactly 32 and lineages through generation 31: the daughters of generation-31
+    # cells (generation 32, never stored) are parked with a key when their first draw is
+    # not settled, so keys of generation 32 must fit the layout (about 1e7 divisions)
+    "narrow_boundary": ([(2.0 ** 32.5, 3)], [(1.0, 1.0, 0.5)], 22.0, 1.0),
     "tiny_phi": ([(1e-3, 50)], [(1.0, 2.0, 0.4)], 24.0, 1e-9),
     "huge_t": ([(1e5, 200)], [(1.0, 3.0, 1.0)], 1e9, 1.0),
 }

@@ -86,8 +86,11 @@ CASES = {
     # phi cap above 32 generations: the wide key layout
     "wide_keys": ([(2.0 ** 40, 5), (2.0 ** 36, 3), (5.0, 4)], [(0.6, 10.0, 2.0), (0.4, 12.0, 3.0)],
                   200.0, 1.0, 7),
+    # phi cap exactly 32 with lineages through generation 31: parked generation-32 daughters
+    # carry keys one generation deeper than any stored cell
+    "narrow_boundary": ([(2.0 ** 32.5, 3)], [(1.0, 1.0, 0.5)], 22.0, 1.0, 12345),
 }
-ORACLE_CASES = ("medium", "medium_types_ascending", "wide_keys")
+ORACLE_CASES = ("medium", "medium_types_ascending", "wide_keys", "narrow_boundary")
 
 
 @pytest.mark.parametrize("name", sorted(CASES))
