@@ -237,15 +237,24 @@ class Engine:
         return out
 
     def simulate(self, bins, types, t_max, phi=None, seed=0, root_begin=None, root_end=None) -> Result:
-        p = self.plan(bins, types, t_max, phi, seed)
+        """pc_simulate (pc_simulate_shard for a range of initial cells): one input's merged
+        histogram, host arrays in and out, in one library call."""
+        b, t = _lib.bins_numpy(bins), _lib.types_numpy(types)
+        h = _lib.Histogram()
+        args = (self.ctx, b.ctypes.data_as(ctypes.POINTER(_lib.Bin)), len(b),
+                t.ctypes.data_as(ctypes.POINTER(_lib.CellType)), len(t), float(t_max),
+                0.0 if phi is None else float(phi), int(seed))
+        if root_begin is not None or root_end is not None:
+            total = int(b["frequency"].sum())
+            rc = self.L.pc_simulate_shard(*args, int(root_begin or 0), total if root_end is None else int(root_end),
+                                          ctypes.byref(h))
+        else:
+            rc = self.L.pc_simulate(*args, ctypes.byref(h))
         try:
-            if root_begin is not None or root_end is not None:
-                total = int(_lib.bins_numpy(bins)["frequency"].sum())
-                p.set_roots(root_begin or 0, total if root_end is None else root_end)
-            p.run()
-            return p.result()
+            self._check(rc)
+            return Result(*_lib.histogram_to_numpy(h))
         finally:
-            p.close()
+            self.L.pc_histogram_free(ctypes.byref(h))
 
     def get_option(self, name: str) -> float:
         v = ctypes.c_double()
