@@ -640,8 +640,8 @@ __device__ void divide_body(const RunArgs& a, const uint64_t root_base, const Le
 
   // Resolve the parked daughters, 32 at a time: re-derive the first attempt from the
   // parent's pair block, draw with the rejection path, settle exactly, append to the front.
-  // Rounds take the records nearest the front first (the last parked): front + pending
-  // <= 2n, so a round's writes, at most one per record resolved so far, stay below every
+  // Passes take the records nearest the front first (the last parked): front + pending
+  // <= 2n, so a pass's writes, at most one per record resolved so far, stay below every
   // record not yet read.
   __syncwarp();
   for (uint32_t hi = pending; hi > 0u;) {
@@ -678,7 +678,7 @@ __device__ void divide_body(const RunArgs& a, const uint64_t root_base, const Le
         if (!Narrow && rec_clamped(rec) && g1 == cap) depth_error = 1u;
       }
     }
-    __syncwarp();  // every parked record of this round is read before the front grows
+    __syncwarp();  // every parked record of this pass is read before the front grows
     const uint32_t em = __ballot_sync(kFull, f == kEmit);
     if (f == kEmit && in_bounds(front + __popc(em & lt) < 2u * n, a.error))
       ob[front + __popc(em & lt)] = make_ulonglong2((unsigned long long)__double_as_longlong(due), key);
