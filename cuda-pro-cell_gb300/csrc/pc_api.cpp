@@ -93,6 +93,9 @@ struct pc_context {
   uint32_t* error_dev = nullptr;
   unsigned long long* pinned = nullptr;     // host staging for small reads
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  // pc_simulate_batch: count tables copied back on a second stream while the next part runs
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t copy_done[2] = {nullptr, nullptr};
   uint64_t free_at_start = 0;
   // host-side fault injection (option fail_nth_call): CUDA calls the library made for this
   // context, the call number that fails next (0: none) and the failures injected so far
@@ -474,6 +477,7 @@ void pc_destroy(pc_context* ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
   if (ctx->stream) pc_cuda_sync(ctx->stream);
+  if (ctx->copy_stream) pc_cuda_sync(ctx->copy_stream);
   free_pool(ctx);
   for (pc_plan* p : ctx->live) p->owner = nullptr;  // plans outliving their context free their own buffers
   for (int i = 0; i < kSpares; ++i) {
@@ -492,6 +496,9 @@ void pc_destroy(pc_context* ctx) {
   cudaFreeHost(ctx->stage2);
   for (auto& ev : ctx->ev)
     if (ev) cudaEventDestroy(ev);
+  for (auto& ev : ctx->copy_done)
+    if (ev) cudaEventDestroy(ev);
+  if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   delete ctx;
 }
@@ -1133,7 +1140,8 @@ int stage_table(pc_context* ctx, pc_plan* p, const unsigned long long** out) {
 
 // The count table of a run into pinned stage `which` (0: the stage stage_table caches, whose
 // cache this clears; 1: the second stage), without caching.
-int copy_table(pc_context* ctx, pc_plan* p, int which, const unsigned long long** out) {
+int copy_table(pc_context* ctx, pc_plan* p, int which, const unsigned long long** out,
+               cudaEvent_t* async_done = nullptr) {
   unsigned long long** buf = which ? &ctx->stage2 : &ctx->stage;
   size_t* cap = which ? &ctx->stage2_elems : &ctx->stage_elems;
   if (!which) ctx->stage_plan = 0;
@@ -1144,10 +1152,21 @@ int copy_table(pc_context* ctx, pc_plan* p, int which, const unsigned long long*
     PC_CUDA(ctx, pc_cuda_malloc_host(buf, p->hist_elems * sizeof(unsigned long long)));
     *cap = p->hist_elems;
   }
-  PC_CUDA(ctx, pc_cuda_copy(*buf, p->hist_dev, p->hist_elems * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
-                            ctx->stream));
-  PC_CUDA(ctx, pc_cuda_sync(ctx->stream));
   *out = *buf;
+  const size_t bytes = p->hist_elems * sizeof(unsigned long long);
+  if (!async_done) {
+    PC_CUDA(ctx, pc_cuda_copy(*buf, p->hist_dev, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    PC_CUDA(ctx, pc_cuda_sync(ctx->stream));
+    return PC_OK;
+  }
+  // the run that wrote the table has completed (pc_plan_run returns after it): the copy goes
+  // on the second stream and `*async_done` completes with it, while the caller's stream runs on
+  if (!ctx->copy_stream) PC_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+  cudaEvent_t& ev = ctx->copy_done[which];
+  if (!ev) PC_CUDA(ctx, cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  PC_CUDA(ctx, pc_cuda_copy(*buf, p->hist_dev, bytes, cudaMemcpyDeviceToHost, ctx->copy_stream));
+  PC_CUDA(ctx, pc_cuda_event_record(ev, ctx->copy_stream));
+  *async_done = ev;
   return PC_OK;
 }
 
@@ -2009,7 +2028,11 @@ int pc_simulate_batch(pc_context* ctx, const pc_instance* instances, uint32_t n_
     }
     if (rc == PC_OK) rc = pc_batch_run(ctx, b);
     const unsigned long long* h = nullptr;
-    if (rc == PC_OK) rc = copy_table(ctx, b, (int)(part & 1u), &h);
+    // every part but the last has its count table copied back while the next part runs;
+    // its merge waits for that copy
+    const bool last = part + 1 == parts;
+    cudaEvent_t copied = nullptr;
+    if (rc == PC_OK) rc = copy_table(ctx, b, (int)(part & 1u), &h, last ? nullptr : &copied);
     merging.finish();  // the previous part's merge read the other stage
     if (preparer.th.joinable()) preparer.th.join();
     if (rc != PC_OK) {
@@ -2018,14 +2041,26 @@ int pc_simulate_batch(pc_context* ctx, const pc_instance* instances, uint32_t n_
     }
     merging.b = b;
     const uint32_t first = first_of(part);
-    if (part + 1 == parts) {
+    // a part's merge once its count table is on the host (false: the copy failed)
+    auto merge_copied = [merge, &codes, &msgs](pc_batch* pb, const unsigned long long* ph, uint32_t pfirst,
+                                               cudaEvent_t ev) {
+      if (ev && cudaEventSynchronize(ev) != cudaSuccess) {
+        for (uint32_t i = 0; i < (uint32_t)pb->inst.size(); ++i) {
+          codes[pfirst + i] = PC_ERR_CUDA;
+          msgs[pfirst + i] = "count table copy failed";
+        }
+        return false;
+      }
+      merge(pb, ph, pfirst);
+      return true;
+    };
+    if (last) {
       merge(b, h, first);  // nothing left to overlap with
     } else {
       try {
-        merging.th = std::thread([merge, &codes, &msgs, b, h, first]() {
+        merging.th = std::thread([merge_copied, &codes, &msgs, b, h, first, copied]() {
           try {
-            merge(b, h, first);
-            release_host_tables(b);
+            if (merge_copied(b, h, first, copied)) release_host_tables(b);
           } catch (...) {
             for (uint32_t i = 0; i < (uint32_t)b->inst.size(); ++i) {
               codes[first + i] = PC_ERR_NOMEM;
@@ -2034,7 +2069,7 @@ int pc_simulate_batch(pc_context* ctx, const pc_instance* instances, uint32_t n_
           }
         });
       } catch (...) {
-        merge(b, h, first);  // no thread to overlap with: merge here
+        merge_copied(b, h, first, copied);  // no thread to overlap with: merge here
       }
     }
   }
