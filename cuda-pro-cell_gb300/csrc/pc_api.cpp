@@ -420,6 +420,23 @@ uint32_t bits_for(uint64_t n) {  // bits needed for values in [0, n)
 namespace pc {
 // Host helpers shared with the allocation-free entry point (pc_noalloc.cu).
 ZigTables host_zig_tables() { return build_zig_tables(); }
+
+KeyLayout key_layout(uint64_t roots, uint32_t gmax, bool batched, uint64_t max_root_chunk) {
+  // key = root_local * 2^g + path must fit 64 bits for every generation a key can have,
+  // gmax path bits; the narrow layout (root_local << 32 | heap node 2^g + path) holds
+  // generations up to 31 and needs root_local < 2^32
+  uint64_t chunk = std::max<uint64_t>(1, roots);
+  const uint32_t want_bits = gmax >= 45 ? 20u : 64u - gmax;
+  if (want_bits < 64) chunk = std::min<uint64_t>(chunk, 1ull << want_bits);
+  if (gmax <= kNarrowMaxGen) chunk = std::min<uint64_t>(chunk, 1ull << 32);
+  if (batched) chunk = std::min<uint64_t>(chunk, 1ull << 28);  // 2 GiB of root records
+  if (max_root_chunk) chunk = std::min<uint64_t>(chunk, std::max<uint64_t>(1, max_root_chunk));
+  KeyLayout k;
+  k.chunk = chunk;
+  k.g_store_max = std::min<uint32_t>(62u, 63u - bits_for(chunk));  // its daughters' keys fit as well
+  k.narrow = gmax <= kNarrowMaxGen;
+  return k;
+}
 void host_truncation_bounds(double mu, double sigma, float& zlo, float& zhi) {
   truncation_bounds(mu, sigma, zlo, zhi);
 }
@@ -817,20 +834,11 @@ int finalize_host(pc_plan* p, uint64_t max_root_chunk, PlanTables& t, std::strin
   p->root_begin = 0;
   p->root_end = roots;
 
-  // Root chunk and key layout: key = root_local * 2^g + path must fit 64 bits for every
-  // generation a key can have: the stored cells (g < cap <= gmax) and the daughters of the
-  // deepest of them, one generation further, which are parked with a key when their first
-  // draw is not settled. So gmax path bits; the narrow layout (root_local << 32 | heap node
-  // 2^g + path) holds generations up to 31 and needs root_local < 2^32.
-  uint64_t chunk = std::max<uint64_t>(1, roots);
-  const uint32_t want_bits = gmax >= 45 ? 20u : 64u - gmax;
-  if (want_bits < 64) chunk = std::min<uint64_t>(chunk, 1ull << want_bits);
-  if (gmax <= kNarrowMaxGen) chunk = std::min<uint64_t>(chunk, 1ull << 32);
-  if (p->batched) chunk = std::min<uint64_t>(chunk, 1ull << 28);  // 2 GiB of root records
-  if (max_root_chunk) chunk = std::min<uint64_t>(chunk, std::max<uint64_t>(1, max_root_chunk));
-  p->chunk = chunk;
-  const uint32_t rb = bits_for(chunk);
-  p->g_store_max = std::min<uint32_t>(62u, 63u - rb);  // its daughters' keys fit as well
+  // Root chunk and key layout (key_layout): every key, a stored cell's or a parked
+  // daughter's one generation below the deepest stored one, fits 64 bits.
+  const KeyLayout kl = key_layout(roots, gmax, p->batched, max_root_chunk);
+  p->chunk = kl.chunk;
+  p->g_store_max = kl.g_store_max;
   p->hist_gens = std::min(gmax, p->g_store_max + 1) + 1;
 
   // Per-bin tables (first initial cell, cap and flags; in a batch also the instance and first

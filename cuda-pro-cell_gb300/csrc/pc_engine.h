@@ -261,4 +261,16 @@ int launch_smooth_gauss_newton(const SmoothArgs& A, const double* params, uint32
 ZigTables host_zig_tables();
 void host_truncation_bounds(double mu, double sigma, float& zlo, float& zhi);
 
+// Root chunk and key layout of a run with `roots` initial cells and deepest phi cap gmax:
+// at most `chunk` initial cells per root sweep; keys for every generation up to
+// min(gmax, g_store_max + 1) (the stored cells, g <= g_store_max, and the daughters of the
+// deepest of them, parked with a key when their first draw is not settled) fit in
+// bits_for(chunk) + g <= 64 bits; the narrow layout when gmax <= kNarrowMaxGen.
+struct KeyLayout {
+  uint64_t chunk;
+  uint32_t g_store_max;
+  bool narrow;
+};
+KeyLayout key_layout(uint64_t roots, uint32_t gmax, bool batched, uint64_t max_root_chunk);
+
 }  // namespace pc

@@ -58,12 +58,6 @@ int fail_cuda(char* err, size_t len, const char* what, cudaError_t e) {
 
 uint64_t align256(uint64_t x) { return (x + 255u) & ~uint64_t(255u); }
 
-uint32_t bits_for(uint64_t n) {
-  uint32_t b = 0;
-  while (b < 64 && (n - 1) >> b) ++b;
-  return n <= 1 ? 0 : b;
-}
-
 // Per-bin tables from the caller's rows, on the device (one block): the nonzero rows in
 // file order become bins with their phi cap, countability and first root, exactly as
 // pc_plan_create derives them on the host.
@@ -207,10 +201,8 @@ extern "C" int pc_simulate_noalloc(const pc_bin* bins, uint64_t n_bins, const pc
   }
 
   // key layout (as pc_plan_create): the generation limit follows the full root count
-  uint64_t key_chunk = std::max<uint64_t>(1, total);
-  const uint32_t want_bits = gmax >= 45 ? 20u : 64u - gmax;
-  if (want_bits < 64) key_chunk = std::min<uint64_t>(key_chunk, 1ull << want_bits);
-  const uint32_t g_store_max = std::min<uint32_t>(62u, 63u - bits_for(key_chunk));
+  const KeyLayout kl = key_layout(total, gmax, false, 0);
+  const uint32_t g_store_max = kl.g_store_max;
   const uint32_t hist_gens = std::min(gmax, g_store_max + 1) + 1;
   const uint64_t hist_elems = (uint64_t)hist_gens * nb * n_types;
   dims[0] = hist_gens;
@@ -281,7 +273,7 @@ extern "C" int pc_simulate_noalloc(const pc_bin* bins, uint64_t n_bins, const pc
                   (unsigned)PC_NOALLOC_SCRATCH_BYTES, (unsigned long long)fixed);
     return fail(err, err_len, PC_ERR_NOMEM, b);
   }
-  const uint64_t chunk = std::min<uint64_t>(std::max<uint64_t>(1, total), std::min<uint64_t>(key_chunk, cells - segs));
+  const uint64_t chunk = std::min<uint64_t>(std::max<uint64_t>(1, total), std::min<uint64_t>(kl.chunk, cells - segs));
   const uint64_t rec_off = align256(fixed);
   uint64_t boff = align256(rec_off + 8ull * chunk);
   Buf bufs[kMaxBufs];
@@ -338,7 +330,7 @@ extern "C" int pc_simulate_noalloc(const pc_bin* bins, uint64_t n_bins, const pc
   a.hist = (unsigned long long*)(S + hist_off);
   a.stats = stats_dev;
   a.error = error_dev;
-  const bool narrow = gmax <= kNarrowMaxGen;
+  const bool narrow = kl.narrow;
 
   // --- root chunks, then generation slices depth-first (as pc_plan_run) ---------------
   struct Entry {
