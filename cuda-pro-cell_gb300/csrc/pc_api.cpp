@@ -1215,6 +1215,23 @@ int plan_create(pc_context* ctx, const pc_bin* bins, uint64_t n_bins, const pc_c
 
 }  // namespace
 
+namespace pc {
+
+int host_value_set(const pc_bin* bins, uint64_t n_bins, double phi, double* values, uint64_t capacity,
+                   uint64_t* n_values) {
+  InstanceHost I;
+  std::string msg;
+  const pc_cell_type one{1.0, 1.0, 0.0};
+  const int rc = prepare_instance(bins, n_bins, &one, 1, 0.0, phi, 0, I, msg);
+  if (rc != PC_OK) return rc;
+  *n_values = I.values.size();
+  if (I.values.size() > capacity) return PC_ERR_INVALID;
+  std::copy(I.values.begin(), I.values.end(), values);
+  return PC_OK;
+}
+
+}  // namespace pc
+
 extern "C" {
 
 int pc_get_option(pc_context* ctx, const char* name, double* value) {

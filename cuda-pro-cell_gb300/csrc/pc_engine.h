@@ -38,6 +38,8 @@
 
 #include "pc_rng.h"
 
+struct pc_bin;  // include/procell.h
+
 namespace pc {
 
 constexpr int kMaxTypes = 64;
@@ -260,6 +262,11 @@ int launch_smooth_gauss_newton(const SmoothArgs& A, const double* params, uint32
 // Host helpers (pc_api.cpp).
 ZigTables host_zig_tables();
 void host_truncation_bounds(double mu, double sigma, float& zlo, float& zhi);
+
+// The output value set a plan builds for this histogram and phi (0: automatic), ascending,
+// into values[capacity]; PC_ERR_INVALID (with *n_values set) when it does not fit.
+int host_value_set(const ::pc_bin* bins, uint64_t n_bins, double phi, double* values, uint64_t capacity,
+                   uint64_t* n_values);
 
 // Root chunk and key layout of a run with `roots` initial cells and deepest phi cap gmax:
 // at most `chunk` initial cells per root sweep; keys for every generation up to

@@ -25,18 +25,24 @@ def layout(built, tmp_path_factory):
     from procell import _lib
     out = str(tmp_path_factory.mktemp("layout") / "libkey_layout.so")
     libdir = os.path.dirname(_lib.LIB_PATH)
-    subprocess.run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", os.path.join(ROOT, "tests", "key_layout.cpp"),
-                    "-o", out, "-L" + libdir, "-lprocell", "-Wl,-rpath," + libdir], check=True)
+    subprocess.run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-I" + os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "key_layout.cpp"), "-o", out, "-L" + libdir, "-lprocell",
+                    "-Wl,-rpath," + libdir], check=True)
     ctypes.CDLL(_lib.LIB_PATH, mode=ctypes.RTLD_GLOBAL)
     lib = ctypes.CDLL(out)
     lib.layout.restype = None
     lib.layout.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_int, ctypes.c_uint64,
                            ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_int)]
 
+    lib.value_set.restype = ctypes.c_int
+    lib.value_set.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_double, ctypes.c_void_p, ctypes.c_uint64,
+                              ctypes.POINTER(ctypes.c_uint64)]
+
     def call(roots, gmax, batched=False, max_root_chunk=0):
         c, g, n = ctypes.c_uint64(), ctypes.c_uint32(), ctypes.c_int()
         lib.layout(roots, gmax, int(batched), max_root_chunk, ctypes.byref(c), ctypes.byref(g), ctypes.byref(n))
         return c.value, g.value, bool(n.value)
+    call.lib = lib
     return call
 
 
@@ -73,3 +79,38 @@ def test_boundary_inputs(layout):
     # gmax 40 with 2^25 roots: the chunk keeps 24 root bits, so generation-40 keys fit
     chunk, gsm, _ = layout(2 ** 25, 40)
     assert bits_for(chunk) + 40 <= 64 and gsm >= 39
+
+
+def test_value_set_equals_the_oracle(layout, oracle_lib):
+    """The output value set (the halving chains v, v/2, ... >= phi of the nonzero bins, sorted
+    and deduplicated; parser.cu:98-151) as the engine builds it on the host, against the
+    oracle's, on histograms with duplicate values, shared mantissas, automatic phi and a
+    wide range of exponents."""
+    import numpy as np
+    from procell import _lib
+    rng = np.random.default_rng(11)
+    for trial in range(60):
+        nb = int(rng.integers(1, 400))
+        kind = trial % 4
+        if kind == 0:
+            v = np.exp(rng.uniform(0.0, np.log(1e6), nb))
+        elif kind == 1:
+            v = np.ldexp(1.0 + rng.integers(0, 8, nb) / 8.0, rng.integers(0, 30, nb))
+        elif kind == 2:
+            v = rng.integers(1, 50, nb).astype(np.float64)
+        else:
+            v = np.exp(rng.uniform(np.log(1e-30), np.log(1e30), nb))
+        f = rng.integers(0, 4, nb)
+        bins = list(zip(v.tolist(), f.tolist()))
+        phi = [None, 1.0, 1e-6][trial % 3]
+        b = _lib.bins_numpy(bins)
+        cap = 1 << 20
+        out = np.zeros(cap, np.float64)
+        n = ctypes.c_uint64()
+        rc = layout.lib.value_set(b.ctypes.data, len(b), 0.0 if phi is None else phi, out.ctypes.data, cap,
+                                  ctypes.byref(n))
+        o = oracle_lib.simulate(bins, [(1.0, 1.0, 0.0)], 0.0, phi, seed=1, nthreads=1)
+        if f.sum() == 0:
+            continue
+        assert rc == 0, (trial, rc)
+        assert np.array_equal(out[:n.value], o.values), trial
